@@ -1,0 +1,120 @@
+"""CPU oracle for the NeRF field (density MLP, SH encoding, colour MLP).  TEST INFRASTRUCTURE ONLY.
+
+NumPy restatement of ``make_nerf_ngp`` (models/nerfs.py:422-454) / ``NeRF.__call__``
+(nerfs.py:39-86) / ``CoordinateBasedMLP`` (nerfs.py:89-128), the truncated exponential
+(nerfs.py:216-238), ``SphericalHarmonicsEncoder`` degree 4 (models/encoders.py:360-406), with the
+hand-derived backward that JAX's autodiff computes for it.  All layers are bias-free Dense layers
+(kernel ``[in, out]``):
+
+    density:  h1 = relu(enc @ W0)  (32->64);   x = h1 @ W1  (64->16);   sigma = exp(x[:, 0])
+    colour:   h2 = relu([x, SH4(dir)] @ W2)  (32->64);   h3 = relu(h2 @ W3)  (64->64)
+              rgb = sigmoid(h3 @ W4)  (64->3)
+    output:   drgb = [sigma, rgb]
+
+The backward of sigma uses exp(clip(x0, -15, 15)) (nerfs.py:230-234); relu passes gradient where
+its input is > 0.
+"""
+from __future__ import annotations
+
+from typing import Dict
+
+import numpy as np
+
+SHAPES = {"W0": (32, 64), "W1": (64, 16), "W2": (32, 64), "W3": (64, 64), "W4": (64, 3)}
+
+
+def glorot_uniform(rng: np.random.Generator, shape, dtype=np.float32) -> np.ndarray:
+    lim = np.sqrt(6.0 / (shape[0] + shape[1]))
+    return rng.uniform(-lim, lim, size=shape).astype(dtype)
+
+
+def init_weights(seed: int = 0, dtype=np.float32) -> Dict[str, np.ndarray]:
+    rng = np.random.default_rng(seed)
+    return {k: glorot_uniform(rng, s, dtype) for k, s in SHAPES.items()}
+
+
+def to_flax_params(w: Dict[str, np.ndarray]) -> dict:
+    """The reference's parameter tree for these weights (flax names Dense_i/kernel)."""
+    return {
+        "density_mlp": {"Dense_0": {"kernel": w["W0"]}, "Dense_1": {"kernel": w["W1"]}},
+        "rgb_mlp": {"Dense_0": {"kernel": w["W2"]}, "Dense_1": {"kernel": w["W3"]},
+                    "Dense_2": {"kernel": w["W4"]}},
+    }
+
+
+def sh4(d: np.ndarray) -> np.ndarray:
+    """encoders.py:375-406, degrees 0..3 (16 outputs), in the input's dtype."""
+    d = np.asarray(d)
+    t = d.dtype.type
+    x, y, z = d[..., 0], d[..., 1], d[..., 2]
+    xy, xz, yz = x * y, x * z, y * z
+    x2, y2, z2 = x * x, y * y, z * z
+    out = np.empty(d.shape[:-1] + (16,), d.dtype)
+    out[..., 0] = t(0.28209479177387814)
+    out[..., 1] = t(-0.48860251190291987) * y
+    out[..., 2] = t(0.48860251190291987) * z
+    out[..., 3] = t(-0.48860251190291987) * x
+    out[..., 4] = t(1.0925484305920792) * xy
+    out[..., 5] = t(-1.0925484305920792) * yz
+    out[..., 6] = t(0.94617469575755997) * z2 - t(0.31539156525251999)
+    out[..., 7] = t(-1.0925484305920792) * xz
+    out[..., 8] = t(0.54627421529603959) * x2 - t(0.54627421529603959) * y2
+    out[..., 9] = t(0.59004358992664352) * y * (t(-3.0) * x2 + y2)
+    out[..., 10] = t(2.8906114426405538) * xy * z
+    out[..., 11] = t(0.45704579946446572) * y * (t(1.0) - t(5.0) * z2)
+    out[..., 12] = t(0.3731763325901154) * z * (t(5.0) * z2 - t(3.0))
+    out[..., 13] = t(0.45704579946446572) * x * (t(1.0) - t(5.0) * z2)
+    out[..., 14] = t(1.4453057213202769) * z * (x2 - y2)
+    out[..., 15] = t(0.59004358992664352) * x * (-x2 + t(3.0) * y2)
+    return out
+
+
+def forward(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray], dtype=np.float32):
+    """Returns (drgb [S,4], cache) in `dtype`."""
+    w = {k: np.asarray(v, dtype) for k, v in w.items()}
+    enc = np.asarray(enc, dtype)
+    a1 = enc @ w["W0"]
+    h1 = np.maximum(a1, 0)
+    x = h1 @ w["W1"]
+    sigma = np.exp(x[:, :1])
+    sh = sh4(np.asarray(dirs, dtype))
+    c = np.concatenate([x, sh], axis=-1)
+    a2 = c @ w["W2"]
+    h2 = np.maximum(a2, 0)
+    a3 = h2 @ w["W3"]
+    h3 = np.maximum(a3, 0)
+    a4 = h3 @ w["W4"]
+    rgb = 1 / (1 + np.exp(-a4))
+    drgb = np.concatenate([sigma, rgb], axis=-1).astype(dtype)
+    cache = dict(enc=enc, a1=a1, h1=h1, x=x, c=c, a2=a2, h2=h2, a3=a3, h3=h3, rgb=rgb)
+    return drgb, cache
+
+
+def backward(dL_ddrgb: np.ndarray, cache, w: Dict[str, np.ndarray], dtype=np.float64):
+    """Returns (dL_denc [S,32], dict of dL_dW)."""
+    w = {k: np.asarray(v, dtype) for k, v in w.items()}
+    c = {k: np.asarray(v, dtype) for k, v in cache.items()}
+    g = np.asarray(dL_ddrgb, dtype)
+    dx0 = g[:, 0] * np.exp(np.clip(c["x"][:, 0], -15, 15))
+    rgb = c["rgb"]
+    da4 = g[:, 1:] * rgb * (1 - rgb)
+    grads = {"W4": c["h3"].T @ da4}
+    da3 = (da4 @ w["W4"].T) * (c["a3"] > 0)
+    grads["W3"] = c["h2"].T @ da3
+    da2 = (da3 @ w["W3"].T) * (c["a2"] > 0)
+    grads["W2"] = c["c"].T @ da2
+    dc = da2 @ w["W2"].T
+    dx = dc[:, :16].copy()
+    dx[:, 0] += dx0
+    grads["W1"] = c["h1"].T @ dx
+    da1 = (dx @ w["W1"].T) * (c["a1"] > 0)
+    grads["W0"] = c["enc"].T @ da1
+    denc = da1 @ w["W0"].T
+    return denc, grads
+
+
+def density_only(enc: np.ndarray, w: Dict[str, np.ndarray], dtype=np.float32) -> np.ndarray:
+    """NeRF.__call__ with dir=None (nerfs.py:71-72): sigma [S]."""
+    w = {k: np.asarray(v, dtype) for k, v in w.items()}
+    h1 = np.maximum(np.asarray(enc, dtype) @ w["W0"], 0)
+    return np.exp((h1 @ w["W1"])[:, 0])
