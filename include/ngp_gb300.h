@@ -1,0 +1,328 @@
+/*
+ * libngp_gb300: GB300-native (sm_103a) kernels for the NeRF hot path of jaxngp, behind a C ABI.
+ *
+ * Every entry point takes the caller's CUDA stream, enqueues work on it and returns without
+ * blocking the host.  Nothing allocates device memory except where noted (scratch is passed in).
+ * Buffers are device pointers owned by the caller.
+ *
+ * Two signatures per op:
+ *   void NAME(cudaStream_t, void **buffers, const char *opaque, size_t opaque_len)
+ *       The XLA custom-call signature of the reference's volrendjax targets (registered there by
+ *       deps/volume-rendering-jax/lib/ffi.cc:25-51).  `buffers` holds the operands in declaration
+ *       order followed by the results, exactly as in volrendjax's per-op lowering.py; `opaque` holds
+ *       the raw bytes of the op's descriptor struct.  Errors are recorded for ngp_last_status()
+ *       instead of thrown (the reference throws std::runtime_error across the C boundary).
+ *   int  NAME_status(same arguments)
+ *       Same work; returns the status code directly.
+ */
+#ifndef NGP_GB300_H_
+#define NGP_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------ status codes */
+#define NGP_OK 0
+#define NGP_ERR_OPAQUE_SIZE 1      /* opaque length differs from sizeof(descriptor) */
+#define NGP_ERR_INVALID_ARGUMENT 2 /* a descriptor field or pointer is out of contract */
+#define NGP_ERR_CUDA 3             /* a CUDA runtime call or kernel launch failed */
+#define NGP_ERR_DEVICE 4           /* a kernel reported an error through its status word */
+#define NGP_ERR_CAPACITY 5         /* a size exceeds a fixed capacity of the entry point */
+
+/* Status and message of the last call made on this host thread. */
+int ngp_last_status(void);
+const char *ngp_last_status_message(void);
+/* ABI version of this library (bumped on any signature or descriptor change). */
+int ngp_abi_version(void);
+
+/* ------------------------------------------------------- volrendjax descriptors (byte-exact) */
+/* deps/volume-rendering-jax/lib/impl/volrend.h:23-29 */
+typedef struct IntegratingDescriptor {
+    uint32_t n_rays;
+    uint32_t total_samples;
+} IntegratingDescriptor;
+
+/* volrend.h:32-42 */
+typedef struct IntegratingBackwardDescriptor {
+    uint32_t n_rays;
+    uint32_t total_samples;
+    float near_distance;
+} IntegratingBackwardDescriptor;
+
+/* volrend.h:45-54 */
+typedef struct IntegratingInferenceDescriptor {
+    uint32_t n_total_rays;
+    uint32_t n_rays;
+    uint32_t march_steps_cap;
+} IntegratingInferenceDescriptor;
+
+/* volrend.h:57-86 */
+typedef struct MarchingDescriptor {
+    uint32_t n_rays;
+    uint32_t total_samples;
+    uint32_t diagonal_n_steps;
+    uint32_t K;
+    uint32_t G;
+    float bound;
+    float stepsize_portion;
+} MarchingDescriptor;
+
+/* volrend.h:89-108 */
+typedef struct MarchingInferenceDescriptor {
+    uint32_t n_total_rays;
+    uint32_t n_rays;
+    uint32_t diagonal_n_steps, K, G;
+    uint32_t march_steps_cap;
+    float bound;
+    float stepsize_portion;
+} MarchingInferenceDescriptor;
+
+/* volrend.h:110-113 */
+typedef struct Morton3DDescriptor {
+    uint32_t length;
+} Morton3DDescriptor;
+
+/* volrend.h:116-118 */
+typedef struct PackbitsDescriptor {
+    uint32_t n_bytes;
+} PackbitsDescriptor;
+
+/* ------------------------------------------------------------------ volrendjax entry points */
+/* Replaces volrendjax::pack_density_into_bits (volrend.h:121-126; packbits.cu:76-83).
+ * buffers: density_threshold f32[n], density_grid f32[n] -> occupied_mask bool[n],
+ * occupancy_bitfield u8[n/8]; opaque: PackbitsDescriptor.  n_bytes == 0 is an error
+ * (ffi.cc:57-59).  density and threshold 16-byte aligned, mask 8-byte aligned. */
+void pack_density_into_bits(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int pack_density_into_bits_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::march_rays (volrend.h:128-133; marching.cu:669-676).
+ * buffers: rays_o f32[R,3], rays_d f32[R,3], t_starts f32[R], t_ends f32[R], noises f32[R],
+ * occupancy_bitfield u8[K*G^3/8] -> next_sample_write_location u32[1],
+ * number_of_exceeded_samples u32[1], ray_is_valid bool[R], rays_n_samples u32[R],
+ * rays_sample_startidx u32[R], idcs u32[S], xyzs f32[S,3], dirs f32[S,3], dss f32[S],
+ * z_vals f32[S]; opaque: MarchingDescriptor. */
+void march_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int march_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::march_rays_inference (volrend.h:135-140; marching.cu:678-685), without
+ * the host-blocking stream synchronisation of marching.cu:562.
+ * buffers: rays_o f32[N,3], rays_d f32[N,3], t_starts f32[N], t_ends f32[N],
+ * occupancy_bitfield u8[K*G^3/8], next_ray_index_in u32[1], terminated bool[n],
+ * indices_in u32[n] -> next_ray_index u32[1], indices_out u32[n], n_samples u32[n],
+ * t_starts_out f32[n], xyzs f32[n,cap,3], dss f32[n,cap], z_vals f32[n,cap];
+ * opaque: MarchingInferenceDescriptor. */
+void march_rays_inference(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int march_rays_inference_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::morton3d (volrend.h:143-148; marching.cu:687-694).
+ * buffers: xyzs u32[N,3] -> idcs u32[N]; opaque: Morton3DDescriptor. */
+void morton3d(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int morton3d_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::morton3d_invert (volrend.h:149-154; marching.cu:696-703).
+ * buffers: idcs u32[N] -> xyzs u32[N,3]; opaque: Morton3DDescriptor. */
+void morton3d_invert(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int morton3d_invert_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::integrate_rays (volrend.h:156-161; integrating.cu:512-519).
+ * buffers: rays_sample_startidx u32[R], rays_n_samples u32[R], bgs f32[R,3], dss f32[S],
+ * z_vals f32[S], drgbs f32[S,4] -> measured_batch_size u32[1], final_rgbds f32[R,4],
+ * final_opacities f32[R]; opaque: IntegratingDescriptor.  drgbs/final_rgbds 16-byte aligned. */
+void integrate_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int integrate_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::integrate_rays_backward (volrend.h:163-168; integrating.cu:521-528).
+ * buffers: rays_sample_startidx, rays_n_samples, bgs, dss, z_vals, drgbs, final_rgbds,
+ * final_opacities, dL_dfinal_rgbds f32[R,4] -> dL_dbgs f32[R,3], dL_dz_vals f32[S],
+ * dL_ddrgbs f32[S,4]; opaque: IntegratingBackwardDescriptor. */
+void integrate_rays_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int integrate_rays_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces volrendjax::integrate_rays_inference (volrend.h:170-175; integrating.cu:530-537).
+ * buffers: rays_bg f32[N,3], rays_rgbd f32[N,4], rays_T f32[N], n_samples u32[n],
+ * indices u32[n], dss f32[n,cap], z_vals f32[n,cap], drgbs f32[n,cap,4] -> terminate_cnt u32[1],
+ * terminated bool[n], rays_rgbd_out f32[n,4], rays_T_out f32[n];
+ * opaque: IntegratingInferenceDescriptor. */
+void integrate_rays_inference(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int integrate_rays_inference_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* march_rays' measured_batch_size_before_compaction on the device (marching/__init__.py:91):
+ * buffers: next_sample_write_location u32[1], number_of_exceeded_samples u32[1] -> count u32[1].
+ * opaque: none (length 0).  The result is the number of leading sample slots that hold samples. */
+void ngp_march_count(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_march_count_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* -------------------------------------------------------------------- hash-grid encoder */
+#define NGP_MAX_LEVELS 32
+
+/* Static description of a HashGridEncoder (models/encoders.py:58-114): the per-level table the
+ * flax module computes on the host in float64 (scale_l = N_min * b^l - 1, cast to float32;
+ * res_l = ceil(scale_l) + 1; offsets = prefix sums of the level sizes). */
+typedef struct NgpHashGridDescriptor {
+    uint32_t n_coords;          /* number of query points */
+    uint32_t L, F, T;           /* levels, features per level (2), max entries per level */
+    uint32_t first_hash_level;  /* levels [0, first_hash_level) are dense */
+    uint32_t n_params;          /* P = offsets[L], rows of the latent table */
+    float bound;                /* positions are in [-bound, bound]^3 */
+    float two_bound;            /* float32(2 * bound) */
+    float scales[NGP_MAX_LEVELS];
+    uint32_t resolutions[NGP_MAX_LEVELS];
+    uint32_t offsets[NGP_MAX_LEVELS + 1];
+} NgpHashGridDescriptor;
+
+/* Replaces HashGridEncoder.__call__ without the TV term (models/encoders.py:83-233).
+ * buffers: pos f32[N,3], latents f32[P,F], active_count u32[1] or NULL -> encodings f32[N,L*F]
+ * (level-major columns).  With an active count, only the first min(N, *count) rows are
+ * computed.  opaque: NgpHashGridDescriptor. */
+void ngp_hashgrid_forward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_hashgrid_forward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Replaces the gradient JAX derives for the gather of encoders.py:226 (a scatter-add).
+ * buffers: pos f32[N,3], dL_denc f32[N,L*F], active_count u32[1] or NULL -> dL_dlatents f32[P,F].
+ * The output is zero-filled first.  opaque: NgpHashGridDescriptor. */
+void ngp_hashgrid_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_hashgrid_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* ------------------------------------------------------------------------- field MLP */
+#define NGP_MLP_WEIGHTS 9408 /* W0[32,64] W1[64,16] W2[32,64] W3[64,64] W4[64,3], packed */
+
+typedef struct NgpMlpDescriptor {
+    uint32_t n_samples;
+    uint32_t accumulate; /* backward only: add into dL_dweights instead of overwriting */
+} NgpMlpDescriptor;
+
+/* Replaces the XLA computation of NeRF.__call__ after the encoder (models/nerfs.py:64-86 with
+ * make_nerf_ngp, nerfs.py:422-454): density MLP, truncated exp, SH degree 4, colour MLP, sigmoid.
+ * buffers: encodings f32[S,32], dirs f32[S,3], weights f32[9408], active_count u32[1] or NULL
+ * -> drgbs f32[S,4].  opaque: NgpMlpDescriptor. */
+void ngp_field_forward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_forward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Density only (NeRF.__call__ with dir=None, nerfs.py:71-72).
+ * buffers: encodings f32[S,32], weights f32[9408] -> sigma f32[S]. */
+void ngp_field_density(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_density_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Backward of ngp_field_forward (JAX autodiff of nerfs.py:39-128, with the truncated-exp
+ * gradient of nerfs.py:230-234), recomputing the activations from the encodings.
+ * buffers: encodings, dirs, weights, dL_ddrgbs f32[S,4], active_count u32[1] or NULL,
+ * grad_scale f32[1] or NULL (multiplies dL_ddrgbs), scratch f32[ngp_field_backward_scratch_floats()]
+ * -> dL_dencodings f32[S,32], dL_dweights f32[9408].  opaque: NgpMlpDescriptor. */
+void ngp_field_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+size_t ngp_field_backward_scratch_floats(void);
+
+/* --------------------------------------------------------------- training-step kernels */
+/* Camera of the training set: pinhole intrinsics plus one 3x4 camera-to-world matrix per view
+ * (utils/types.py Camera; app/nerf/_utils.py:97-115 builds rays from them). */
+typedef struct NgpTrainRaysDescriptor {
+    uint32_t n_rays;       /* rays in the batch */
+    uint32_t width, height, n_views;
+    float fx, fy, cx, cy;
+    float bound;           /* scene AABB half-width */
+    uint32_t perturb;      /* jitter each ray's start by a uniform fraction of a step */
+    uint32_t random_bg;    /* uniform random background colour per ray, else `bg` */
+    float bg[3];
+    uint64_t seed;         /* counter-based RNG seed for this step */
+} NgpTrainRaysDescriptor;
+
+/* Builds one training batch: for each ray, a pixel index (from `perm` when given, else drawn
+ * uniformly), its world-space origin/direction (_utils.py:97-115), AABB near/far
+ * (renderers/cuda.py:56-97), start jitter, background colour, and the ground-truth colour
+ * blended over that background (utils/data.py:443-465).
+ * buffers: transforms f32[V,12] (row-major 3x4 camera-to-world), rgbas u8[V*H*W,4],
+ * perm u32[R] or NULL -> rays_o f32[R,3], rays_d f32[R,3], t_starts f32[R], t_ends f32[R],
+ * noises f32[R], bgs f32[R,3], gt_rgbs f32[R,3].  opaque: NgpTrainRaysDescriptor. */
+void ngp_train_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_train_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+typedef struct NgpIntegrateLossDescriptor {
+    uint32_t n_rays;
+    uint32_t total_samples;
+    float near_distance;
+    float huber_delta;     /* 0.1 (app/nerf/_utils.py:154) */
+} NgpIntegrateLossDescriptor;
+
+/* integrate_rays forward, the masked Huber loss of app/nerf/_utils.py:151-156 and
+ * integrate_rays_backward in one pass per ray.  The loss is sum over valid rays of
+ * mean_c huber(pred - gt) / n_valid; dL_ddrgbs are written unnormalised and `grad_scale`
+ * receives 1/n_valid for the field backward.
+ * buffers: ray_is_valid bool[R], rays_sample_startidx, rays_n_samples, bgs f32[R,3],
+ * gt_rgbs f32[R,3], dss, z_vals, drgbs, active_count u32[1], scratch f32[3] -> dL_ddrgbs f32[S,4],
+ * stats f32[4] (loss, n_valid_rays, measured_batch_size, samples before compaction),
+ * grad_scale f32[1].  opaque: NgpIntegrateLossDescriptor. */
+void ngp_integrate_loss_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_integrate_loss_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+typedef struct NgpAdamDescriptor {
+    uint32_t n;            /* parameters in this group */
+    uint32_t step;         /* 1-based step count after this update */
+    float lr, beta1, beta2, eps, eps_root;
+    float weight_decay;    /* decoupled, added to the update (optax.add_decayed_weights) */
+    uint32_t zero_grad;    /* write zeros into the gradient after reading it */
+} NgpAdamDescriptor;
+
+/* optax.adam(b1, b2, eps, eps_root) chained with add_decayed_weights (app/nerf/_utils.py:19-77)
+ * for one parameter group, updating params and moments in place.
+ * buffers: params f32[n], grads f32[n], m f32[n], v f32[n]; opaque: NgpAdamDescriptor. */
+void ngp_adam(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_adam_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* ------------------------------------------------------------- occupancy-grid maintenance */
+typedef struct NgpOgridDescriptor {
+    uint32_t K, G;          /* cascades, grid resolution */
+    uint32_t cascade;       /* cascade being updated */
+    uint32_t n_points;      /* M: cells updated this round */
+    uint32_t update_all;    /* point j is in cell j (the first 256 steps, types.py:1166-1169) */
+    float bound;            /* scene AABB half-width */
+    float decay;            /* 0.95 (types.py:1161) */
+    float threshold_step;   /* 0.01 * diag / (2 min(bound,1) sqrt3) (types.py:1385-1386) */
+    uint64_t seed;
+    /* camera data for ngp_ogrid_mark_untrained */
+    uint32_t n_views, width, height;
+    float fx, fy, cx, cy;
+} NgpOgridDescriptor;
+
+/* types.py:1161-1162: density *= decay for the live cells (>= 0) of `cascade`.
+ * buffers: density f32[K*G^3] (updated in place, passed as the result). */
+void ngp_ogrid_decay(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_ogrid_decay_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* types.py:1164-1204: pick n_points cells of `cascade` and a uniform point in each (world space).
+ * buffers: density f32[K*G^3], occupancy_bitfield u8[K*G^3/8] -> cells u32[M] (0xFFFFFFFF for a
+ * dead cell), xyzs f32[M,3]. */
+void ngp_ogrid_sample(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_ogrid_sample_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* types.py:1218-1220: density[cell] = max(density[cell], sigma).
+ * buffers: cells u32[M], sigma f32[M] -> density f32[K*G^3] (in place). */
+void ngp_ogrid_max(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_ogrid_max_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* types.py:1227-1231: threshold = min(threshold_step, mean live density of cascade 0).
+ * buffers: density f32[K*G^3], scratch f32[2] -> threshold f32[1]. */
+void ngp_ogrid_threshold(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_ogrid_threshold_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* types.py:1241-1362 (pinhole cameras): cells no training camera sees get density -1.
+ * buffers: transforms f32[V,12] -> density f32[K*G^3] (in place). */
+void ngp_ogrid_mark_untrained(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_ogrid_mark_untrained_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* packbits with one device-scalar threshold (no materialised per-cell threshold array).
+ * buffers: threshold f32[1], density f32[n] -> occupied_mask bool[n], bitfield u8[n/8];
+ * opaque: PackbitsDescriptor. */
+void ngp_packbits_scalar(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_packbits_scalar_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NGP_GB300_H_ */

@@ -1,0 +1,258 @@
+// The C ABI of libngp_gb300: descriptor decoding, buffer unpacking and status handling for every
+// entry point declared in include/ngp_gb300.h.  Buffer order follows volrendjax's lowering rules
+// (deps/volume-rendering-jax/src/volrendjax/*/lowering.py): operands, then results.
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace ngp {
+
+int launch_march_rays(cudaStream_t, const MarchingDescriptor &, const float *, const float *, const float *,
+                      const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *,
+                      bool *, std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, float *, float *);
+int launch_march_rays_inference(cudaStream_t, const MarchingInferenceDescriptor &, const float *, const float *,
+                                const float *, const float *, const std::uint8_t *, const std::uint32_t *,
+                                const bool *, const std::uint32_t *, std::uint32_t *, std::uint32_t *,
+                                std::uint32_t *, float *, float *, float *, float *);
+int launch_morton3d(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t *);
+int launch_morton3d_invert(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t *);
+int launch_integrate_rays(cudaStream_t, const IntegratingDescriptor &, const std::uint32_t *, const std::uint32_t *,
+                          const float *, const float *, const float *, const float *, std::uint32_t *, float *, float *);
+int launch_integrate_rays_backward(cudaStream_t, const IntegratingBackwardDescriptor &, const std::uint32_t *,
+                                   const std::uint32_t *, const float *, const float *, const float *, const float *,
+                                   const float *, const float *, const float *, float *, float *, float *);
+int launch_integrate_rays_inference(cudaStream_t, const IntegratingInferenceDescriptor &, const float *, const float *,
+                                    const float *, const std::uint32_t *, const std::uint32_t *, const float *,
+                                    const float *, const float *, std::uint32_t *, bool *, float *, float *);
+int launch_packbits(cudaStream_t, std::uint32_t, const float *, const float *, bool *, std::uint8_t *, bool);
+int launch_hashgrid_forward(cudaStream_t, const NgpHashGridDescriptor &, const std::uint32_t *, const float *,
+                            const float *, float *);
+int launch_hashgrid_backward(cudaStream_t, const NgpHashGridDescriptor &, const std::uint32_t *, const float *,
+                             const float *, float *, bool);
+int launch_mlp_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                       const float *, float *);
+int launch_mlp_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
+int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                        const float *, const float *, const float *, float *, float *, float *, bool);
+std::size_t mlp_partials_floats();
+int launch_train_rays(cudaStream_t, const NgpTrainRaysDescriptor &, const float *, const std::uint8_t *,
+                      const std::uint32_t *, float *, float *, float *, float *, float *, float *, float *);
+int launch_integrate_loss_backward(cudaStream_t, const NgpIntegrateLossDescriptor &, const bool *,
+                                   const std::uint32_t *, const std::uint32_t *, const float *, const float *,
+                                   const float *, const float *, const float *, const std::uint32_t *, float *,
+                                   float *, float *, float *);
+int launch_adam(cudaStream_t, const NgpAdamDescriptor &, float *, float *, float *, float *);
+int launch_ogrid_decay(cudaStream_t, std::uint32_t, float, float *);
+int launch_ogrid_sample(cudaStream_t, std::uint32_t, bool, std::uint32_t, std::uint32_t, float, std::uint64_t,
+                        const float *, const std::uint8_t *, std::uint32_t *, float *);
+int launch_ogrid_max(cudaStream_t, std::uint32_t, std::uint32_t, std::uint32_t, const std::uint32_t *,
+                     const float *, float *);
+int launch_ogrid_threshold(cudaStream_t, std::uint32_t, float, const float *, float *, float *);
+int launch_ogrid_mark_untrained(cudaStream_t, std::uint32_t, std::uint32_t, float, std::uint32_t, const float *,
+                                float, float, float, float, std::uint32_t, std::uint32_t, float *);
+
+namespace {
+thread_local int t_status = NGP_OK;
+thread_local char t_message[256] = "ok";
+
+__global__ void march_count_kernel(const std::uint32_t *__restrict__ next_loc, const std::uint32_t *__restrict__ exceeded,
+                                   std::uint32_t *__restrict__ count) {
+    *count = *next_loc - *exceeded;
+}
+}  // namespace
+
+void set_last_status(int status, const char *msg) {
+    t_status = status;
+    std::snprintf(t_message, sizeof(t_message), "%s", msg ? msg : "");
+}
+
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cached[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+}  // namespace ngp
+
+using namespace ngp;
+
+#define U32(i) static_cast<std::uint32_t *>(buffers[i])
+#define CU32(i) static_cast<const std::uint32_t *>(buffers[i])
+#define F32(i) static_cast<float *>(buffers[i])
+#define CF32(i) static_cast<const float *>(buffers[i])
+#define U8(i) static_cast<std::uint8_t *>(buffers[i])
+#define CU8(i) static_cast<const std::uint8_t *>(buffers[i])
+#define B8(i) static_cast<bool *>(buffers[i])
+#define CB8(i) static_cast<const bool *>(buffers[i])
+
+#define NGP_ENTRY(name)                                                                              \
+    int name##_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);   \
+    void name(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len) {          \
+        name##_status(stream, buffers, opaque, opaque_len);                                          \
+    }                                                                                                \
+    int name##_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len)
+
+#define NGP_DESC(T, var)                                                                             \
+    T var;                                                                                           \
+    do {                                                                                             \
+        if (buffers == nullptr) {                                                                    \
+            set_last_status(NGP_ERR_INVALID_ARGUMENT, "buffers is NULL");                            \
+            return NGP_ERR_INVALID_ARGUMENT;                                                         \
+        }                                                                                            \
+        int st_ = read_descriptor(opaque, opaque_len, &var);                                         \
+        if (st_ != NGP_OK) return st_;                                                               \
+    } while (0)
+
+extern "C" {
+
+int ngp_last_status(void) { return t_status; }
+const char *ngp_last_status_message(void) { return t_message; }
+int ngp_abi_version(void) { return 1; }
+
+NGP_ENTRY(pack_density_into_bits) {
+    NGP_DESC(PackbitsDescriptor, d);
+    return launch_packbits(stream, d.n_bytes, CF32(0), CF32(1), B8(2), U8(3), false);
+}
+
+NGP_ENTRY(ngp_packbits_scalar) {
+    NGP_DESC(PackbitsDescriptor, d);
+    return launch_packbits(stream, d.n_bytes, CF32(0), CF32(1), B8(2), U8(3), true);
+}
+
+NGP_ENTRY(march_rays) {
+    NGP_DESC(MarchingDescriptor, d);
+    return launch_march_rays(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
+                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15));
+}
+
+NGP_ENTRY(march_rays_inference) {
+    NGP_DESC(MarchingInferenceDescriptor, d);
+    return launch_march_rays_inference(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CU8(4), CU32(5), CB8(6),
+                                       CU32(7), U32(8), U32(9), U32(10), F32(11), F32(12), F32(13), F32(14));
+}
+
+NGP_ENTRY(morton3d) {
+    NGP_DESC(Morton3DDescriptor, d);
+    return launch_morton3d(stream, d.length, CU32(0), U32(1));
+}
+
+NGP_ENTRY(morton3d_invert) {
+    NGP_DESC(Morton3DDescriptor, d);
+    return launch_morton3d_invert(stream, d.length, CU32(0), U32(1));
+}
+
+static bool misaligned16(const void *p) { return ((std::uintptr_t)p & 15u) != 0; }
+
+NGP_ENTRY(integrate_rays) {
+    NGP_DESC(IntegratingDescriptor, d);
+    NGP_CHECK_ARG(!misaligned16(buffers[5]) && !misaligned16(buffers[7]), "integrate_rays: drgbs and final_rgbds must be 16-byte aligned");
+    return launch_integrate_rays(stream, d, CU32(0), CU32(1), CF32(2), CF32(3), CF32(4), CF32(5), U32(6), F32(7), F32(8));
+}
+
+NGP_ENTRY(integrate_rays_backward) {
+    NGP_DESC(IntegratingBackwardDescriptor, d);
+    NGP_CHECK_ARG(!misaligned16(buffers[5]) && !misaligned16(buffers[6]) && !misaligned16(buffers[8]) && !misaligned16(buffers[11]),
+                  "integrate_rays_backward: drgbs, final_rgbds, dL_dfinal_rgbds and dL_ddrgbs must be 16-byte aligned");
+    return launch_integrate_rays_backward(stream, d, CU32(0), CU32(1), CF32(2), CF32(3), CF32(4), CF32(5), CF32(6),
+                                          CF32(7), CF32(8), F32(9), F32(10), F32(11));
+}
+
+NGP_ENTRY(integrate_rays_inference) {
+    NGP_DESC(IntegratingInferenceDescriptor, d);
+    NGP_CHECK_ARG(!misaligned16(buffers[1]) && !misaligned16(buffers[7]) && !misaligned16(buffers[10]),
+                  "integrate_rays_inference: rays_rgbd, drgbs and rays_rgbd_out must be 16-byte aligned");
+    return launch_integrate_rays_inference(stream, d, CF32(0), CF32(1), CF32(2), CU32(3), CU32(4), CF32(5), CF32(6),
+                                           CF32(7), U32(8), B8(9), F32(10), F32(11));
+}
+
+NGP_ENTRY(ngp_march_count) {
+    (void)opaque;
+    (void)opaque_len;
+    NGP_CHECK_ARG(buffers != nullptr, "buffers is NULL");
+    march_count_kernel<<<1, 1, 0, stream>>>(CU32(0), CU32(1), U32(2));
+    return launch_status();
+}
+
+NGP_ENTRY(ngp_hashgrid_forward) {
+    NGP_DESC(NgpHashGridDescriptor, d);
+    return launch_hashgrid_forward(stream, d, CU32(2), CF32(0), CF32(1), F32(3));
+}
+
+NGP_ENTRY(ngp_hashgrid_backward) {
+    NGP_DESC(NgpHashGridDescriptor, d);
+    return launch_hashgrid_backward(stream, d, CU32(2), CF32(0), CF32(1), F32(3), false);
+}
+
+NGP_ENTRY(ngp_field_forward) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_mlp_forward(stream, d.n_samples, CU32(3), CF32(0), CF32(1), CF32(2), F32(4));
+}
+
+NGP_ENTRY(ngp_field_density) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_mlp_density(stream, d.n_samples, CF32(0), CF32(1), F32(2));
+}
+
+NGP_ENTRY(ngp_field_backward) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_mlp_backward(stream, d.n_samples, CU32(4), CF32(0), CF32(1), CF32(2), CF32(3), CF32(5), F32(7),
+                               F32(8), F32(6), d.accumulate != 0);
+}
+
+size_t ngp_field_backward_scratch_floats(void) { return mlp_partials_floats(); }
+
+NGP_ENTRY(ngp_train_rays) {
+    NGP_DESC(NgpTrainRaysDescriptor, d);
+    return launch_train_rays(stream, d, CF32(0), CU8(1), CU32(2), F32(3), F32(4), F32(5), F32(6), F32(7), F32(8),
+                             F32(9));
+}
+
+NGP_ENTRY(ngp_integrate_loss_backward) {
+    NGP_DESC(NgpIntegrateLossDescriptor, d);
+    return launch_integrate_loss_backward(stream, d, CB8(0), CU32(1), CU32(2), CF32(3), CF32(4), CF32(5), CF32(6),
+                                          CF32(7), CU32(8), F32(10), F32(11), F32(12), F32(9));
+}
+
+NGP_ENTRY(ngp_adam) {
+    NGP_DESC(NgpAdamDescriptor, d);
+    return launch_adam(stream, d, F32(0), F32(1), F32(2), F32(3));
+}
+
+NGP_ENTRY(ngp_ogrid_decay) {
+    NGP_DESC(NgpOgridDescriptor, d);
+    NGP_CHECK_ARG(d.cascade < d.K, "ogrid: cascade out of range");
+    const std::uint32_t G3 = d.G * d.G * d.G;
+    return launch_ogrid_decay(stream, G3, d.decay, F32(0) + (std::size_t)d.cascade * G3);
+}
+
+NGP_ENTRY(ngp_ogrid_sample) {
+    NGP_DESC(NgpOgridDescriptor, d);
+    NGP_CHECK_ARG(d.cascade < d.K && d.G > 1, "ogrid: cascade out of range");
+    NGP_CHECK_ARG(!d.update_all || d.n_points == d.G * d.G * d.G, "ogrid: update_all needs one point per cell");
+    return launch_ogrid_sample(stream, d.n_points, d.update_all != 0, d.cascade, d.G, d.bound, d.seed, CF32(0), CU8(1),
+                               U32(2), F32(3));
+}
+
+NGP_ENTRY(ngp_ogrid_max) {
+    NGP_DESC(NgpOgridDescriptor, d);
+    return launch_ogrid_max(stream, d.n_points, d.cascade, d.G * d.G * d.G, CU32(0), CF32(1), F32(2));
+}
+
+NGP_ENTRY(ngp_ogrid_threshold) {
+    NGP_DESC(NgpOgridDescriptor, d);
+    return launch_ogrid_threshold(stream, d.G * d.G * d.G, d.threshold_step, CF32(0), F32(1), F32(2));
+}
+
+NGP_ENTRY(ngp_ogrid_mark_untrained) {
+    NGP_DESC(NgpOgridDescriptor, d);
+    return launch_ogrid_mark_untrained(stream, d.K, d.G, d.bound, d.n_views, CF32(0), d.fx, d.fy, d.cx, d.cy, d.width,
+                                       d.height, F32(1));
+}
+
+}  // extern "C"

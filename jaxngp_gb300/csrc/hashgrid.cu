@@ -1,0 +1,148 @@
+// Multiresolution hash-grid encoder for sm_103a: forward gather and gradient scatter.
+//
+// Replaces HashGridEncoder.__call__ (models/encoders.py:83-256) and the scatter-add that JAX's
+// autodiff makes of its gather (encoders.py:226).  One thread handles one (point, level) pair, a
+// warp covers two points x sixteen levels, so the level-major output row of a point
+// (column l*F + f, encoders.py:233) is written by consecutive lanes in one 256-byte burst.
+//
+// The index and weight arithmetic uses explicitly rounded intrinsics, one rounding per
+// operation in the reference's order, so corner indices are bit-identical to the reference and
+// encodings agree bit for bit with its float32 evaluation:
+//   pos01  = (pos + bound) / (2*bound)                      encoders.py:87
+//   ps     = pos01 * float32(scale_l) + 0.5                 encoders.py:216-218
+//   corner = floor(ps) + {0,1}^3 as uint32                  encoders.py:116-123
+//   index  = x + y*res + z*res^2           (dense levels)   encoders.py:134-155
+//          = x ^ y*2654435761 ^ z*805459861 (hashed levels) encoders.py:157-177
+//            then mod T, + offsets[l]; clamped to the table  encoders.py:179-189
+//   weight = prod_d (o_d ? frac_d : 1 - frac_d)             encoders.py:191-213
+//   enc    = sum over corners in corner order               encoders.py:231
+#include "common.cuh"
+
+namespace ngp {
+namespace {
+
+struct Corner8 {
+    std::uint32_t idx[8];
+    float w[8];
+};
+
+__device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, std::uint32_t l,
+                                              float px, float py, float pz, Corner8 &c) {
+    const float b = d.bound;
+    const float two_b = d.two_bound;
+    // (pos + bound) / (2 * bound)
+    const float ux = __fdiv_rn(__fadd_rn(px, b), two_b);
+    const float uy = __fdiv_rn(__fadd_rn(py, b), two_b);
+    const float uz = __fdiv_rn(__fadd_rn(pz, b), two_b);
+    const float s = d.scales[l];
+    const float sx = __fadd_rn(__fmul_rn(ux, s), 0.5f);
+    const float sy = __fadd_rn(__fmul_rn(uy, s), 0.5f);
+    const float sz = __fadd_rn(__fmul_rn(uz, s), 0.5f);
+    const float fx = floorf(sx), fy = floorf(sy), fz = floorf(sz);
+    const std::uint32_t bx = (std::uint32_t)(int)fx, by = (std::uint32_t)(int)fy, bz = (std::uint32_t)(int)fz;
+    const float rx = __fsub_rn(sx, fx), ry = __fsub_rn(sy, fy), rz = __fsub_rn(sz, fz);
+    const float wx[2] = {__fsub_rn(1.f, rx), rx};
+    const float wy[2] = {__fsub_rn(1.f, ry), ry};
+    const float wz[2] = {__fsub_rn(1.f, rz), rz};
+    const bool dense = l < d.first_hash_level;
+    const std::uint32_t res = d.resolutions[l], res2 = res * res;
+    const std::uint32_t off = d.offsets[l], last = d.n_params - 1u, T = d.T;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const std::uint32_t ox = (k >> 2) & 1, oy = (k >> 1) & 1, oz = k & 1;
+        const std::uint32_t x = bx + ox, y = by + oy, z = bz + oz;
+        const std::uint32_t h = dense ? (x + y * res + z * res2) : (x ^ (y * 2654435761u) ^ (z * 805459861u));
+        std::uint32_t idx = h % T + off;
+        c.idx[k] = idx < last ? idx : last;
+        c.w[k] = __fmul_rn(__fmul_rn(wx[ox], wy[oy]), wz[oz]);
+    }
+}
+
+// enc[n, l*2 + f] for n < n_points (n_points read from `count` when given).
+__global__ void __launch_bounds__(256) hashgrid_forward_kernel(
+    NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
+    const float *__restrict__ pos, const float2 *__restrict__ latents, float2 *__restrict__ enc) {
+    std::uint32_t n_active = n_points;
+    if (count != nullptr) n_active = min(n_active, *count);
+    const std::size_t total = (std::size_t)n_active * d.L;
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    for (std::size_t t = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const std::uint32_t n = (std::uint32_t)(t / d.L), l = (std::uint32_t)(t % d.L);
+        Corner8 c;
+        level_corners(d, l, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
+        float2 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(latents + c.idx[k]);
+        float a0 = __fmul_rn(v[0].x, c.w[0]), a1 = __fmul_rn(v[0].y, c.w[0]);
+#pragma unroll
+        for (int k = 1; k < 8; ++k) {
+            a0 = __fadd_rn(a0, __fmul_rn(v[k].x, c.w[k]));
+            a1 = __fadd_rn(a1, __fmul_rn(v[k].y, c.w[k]));
+        }
+        enc[t] = make_float2(a0, a1);
+    }
+}
+
+// dL/dlatents[idx_k] += w_k * dL/denc[n, l]: the transpose of the gather.  Levels whose incoming
+// gradient is exactly zero (samples past a ray's termination) issue no atomics.
+__global__ void __launch_bounds__(256) hashgrid_backward_kernel(
+    NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
+    const float *__restrict__ pos, const float2 *__restrict__ dL_denc, float2 *__restrict__ dL_dlat) {
+    std::uint32_t n_active = n_points;
+    if (count != nullptr) n_active = min(n_active, *count);
+    const std::size_t total = (std::size_t)n_active * d.L;
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    for (std::size_t t = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const float2 g = dL_denc[t];
+        if (g.x == 0.f && g.y == 0.f) continue;
+        const std::uint32_t n = (std::uint32_t)(t / d.L), l = (std::uint32_t)(t % d.L);
+        Corner8 c;
+        level_corners(d, l, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) atomicAdd(dL_dlat + c.idx[k], make_float2(c.w[k] * g.x, c.w[k] * g.y));
+    }
+}
+
+}  // namespace
+
+int check_hashgrid_descriptor(const NgpHashGridDescriptor &d) {
+    NGP_CHECK_ARG(d.F == 2, "hashgrid: only F = 2 features per level is supported");
+    NGP_CHECK_ARG(d.L >= 1 && d.L <= NGP_MAX_LEVELS, "hashgrid: L must be in [1, 32]");
+    NGP_CHECK_ARG(d.T > 0 && d.n_params > 0 && d.first_hash_level <= d.L, "hashgrid: bad table sizes");
+    NGP_CHECK_ARG(d.offsets[d.L] == d.n_params, "hashgrid: offsets[L] must equal n_params");
+    NGP_CHECK_ARG(d.bound > 0.f && d.two_bound > 0.f, "hashgrid: bound must be positive");
+    return NGP_OK;
+}
+
+int launch_hashgrid_forward(cudaStream_t stream, const NgpHashGridDescriptor &d,
+                            const std::uint32_t *count, const float *pos, const float *latents,
+                            float *enc) {
+    int st = check_hashgrid_descriptor(d);
+    if (st != NGP_OK) return st;
+    NGP_CHECK_ARG(((std::uintptr_t)latents & 7u) == 0 && ((std::uintptr_t)enc & 7u) == 0,
+                  "hashgrid: latents and encodings must be 8-byte aligned");
+    const std::size_t items = (std::size_t)d.n_coords * d.L;
+    if (items > 0) {
+        hashgrid_forward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
+            d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(latents), reinterpret_cast<float2 *>(enc));
+    }
+    return launch_status();
+}
+
+int launch_hashgrid_backward(cudaStream_t stream, const NgpHashGridDescriptor &d,
+                             const std::uint32_t *count, const float *pos, const float *dL_denc,
+                             float *dL_dlatents, bool accumulate) {
+    int st = check_hashgrid_descriptor(d);
+    if (st != NGP_OK) return st;
+    NGP_CHECK_ARG(((std::uintptr_t)dL_denc & 7u) == 0 && ((std::uintptr_t)dL_dlatents & 7u) == 0,
+                  "hashgrid: gradients must be 8-byte aligned");
+    if (!accumulate) NGP_CUDA_TRY(cudaMemsetAsync(dL_dlatents, 0, (std::size_t)d.n_params * 2 * sizeof(float), stream));
+    const std::size_t items = (std::size_t)d.n_coords * d.L;
+    if (items > 0) {
+        hashgrid_backward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
+            d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(dL_denc), reinterpret_cast<float2 *>(dL_dlatents));
+    }
+    return launch_status();
+}
+
+}  // namespace ngp

@@ -1,0 +1,456 @@
+// Fused density/colour MLP of the NeRF field for sm_103a, FP32: forward, density-only forward,
+// and backward with recomputation.
+//
+// Replaces what XLA generates for NeRF.__call__ (models/nerfs.py:39-86) with the NGP layout of
+// make_nerf_ngp (nerfs.py:422-454): CoordinateBasedMLP layers without bias (nerfs.py:89-128),
+// truncated exponential on density (nerfs.py:221-238), degree-4 spherical harmonics of the view
+// direction (models/encoders.py:375-406), sigmoid on colour:
+//
+//   h1 = relu(enc @ W0)  [32->64]     x = h1 @ W1  [64->16]       sigma = exp(x[0])
+//   h2 = relu([x, SH4(dir)] @ W2)  [32->64]   h3 = relu(h2 @ W3)  [64->64]
+//   rgb = sigmoid(h3 @ W4)  [64->3]           drgb = [sigma, rgb]
+//
+// Weights are one packed array of 9408 floats, each kernel in flax's [in, out] row-major layout:
+// W0 @0, W1 @2048, W2 @3072, W3 @5120, W4 @9216.
+//
+// Design: a CTA of 256 threads loops over tiles of 64 samples.  The weights (and, for the
+// backward, their transposes) sit in shared memory for the CTA's lifetime; per-tile activations
+// sit in shared memory; every layer is a small register-blocked SIMT GEMM (each thread owns a
+// 4-column strip, float4 weight loads, broadcast activation loads).  The backward recomputes the
+// forward activations of its tile from the encodings (nothing per-layer is stored in HBM),
+// accumulates each thread's share of dL/dW in registers across all its tiles, and writes one
+// partial per CTA; a second kernel sums the partials in a fixed order, so weight gradients are
+// deterministic.  FP32 throughout (the parity path); the BF16 tensor-core path is separate.
+#include "common.cuh"
+
+namespace ngp {
+namespace {
+
+constexpr int kTile = 64;
+constexpr int kThreads = 256;
+constexpr int kW0 = 0, kW1 = 2048, kW2 = 3072, kW3 = 5120, kW4 = 9216, kNW = 9408;
+// transposed copies (backward only)
+constexpr int kT0 = 0;      // W0^T [64][32]
+constexpr int kT1 = 2048;   // W1^T [16][64]
+constexpr int kT2 = 3072;   // W2[:16]^T [64][16]
+constexpr int kT3 = 4096;   // W3^T [64][64]
+constexpr int kT4 = 8192;   // W4^T [3][64]
+constexpr int kNT = 8384;
+constexpr int kLd = 68;     // activation row stride (floats): 16-byte aligned rows
+
+__device__ __forceinline__ void sh4(float x, float y, float z, float *o) {
+    const float xy = x * y, xz = x * z, yz = y * z, x2 = x * x, y2 = y * y, z2 = z * z;
+    o[0] = 0.28209479177387814f;
+    o[1] = -0.48860251190291987f * y;
+    o[2] = 0.48860251190291987f * z;
+    o[3] = -0.48860251190291987f * x;
+    o[4] = 1.0925484305920792f * xy;
+    o[5] = -1.0925484305920792f * yz;
+    o[6] = 0.94617469575755997f * z2 - 0.31539156525251999f;
+    o[7] = -1.0925484305920792f * xz;
+    o[8] = 0.54627421529603959f * x2 - 0.54627421529603959f * y2;
+    o[9] = 0.59004358992664352f * y * (-3.0f * x2 + y2);
+    o[10] = 2.8906114426405538f * xy * z;
+    o[11] = 0.45704579946446572f * y * (1.0f - 5.0f * z2);
+    o[12] = 0.3731763325901154f * z * (5.0f * z2 - 3.0f);
+    o[13] = 0.45704579946446572f * x * (1.0f - 5.0f * z2);
+    o[14] = 1.4453057213202769f * z * (x2 - y2);
+    o[15] = 0.59004358992664352f * x * (-x2 + 3.0f * y2);
+}
+
+// C[s][n] = act(sum_k A[s][k] * B[k][n]) for s < kTile, n < N (N % 4 == 0).  Each thread owns a
+// 4-wide column strip and kTile/R rows spaced R apart.
+template <int K, int N, bool kRelu>
+__device__ __forceinline__ void mm(const float *A, int lda, const float *B, float *C, int ldc) {
+    constexpr int G = N / 4, R = kThreads / G, RPT = kTile / R;
+    static_assert(kThreads % G == 0 && kTile % R == 0, "tile shape");
+    const int t = threadIdx.x, c0 = (t % G) * 4, r0 = t / G;
+    float acc[RPT][4];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < K; ++k) {
+        const float4 b = *reinterpret_cast<const float4 *>(B + k * N + c0);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            const float a = A[(r0 + q * R) * lda + k];
+            acc[q][0] += a * b.x;
+            acc[q][1] += a * b.y;
+            acc[q][2] += a * b.z;
+            acc[q][3] += a * b.w;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+        float4 v = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
+        if (kRelu) v = make_float4(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f), fmaxf(v.z, 0.f), fmaxf(v.w, 0.f));
+        *reinterpret_cast<float4 *>(C + (r0 + q * R) * ldc + c0) = v;
+    }
+}
+
+// Like mm, but the result is multiplied elementwise by (M[s][n] > 0) and written over M (the
+// relu adjoint: M holds the layer's post-activation values).
+template <int K, int N>
+__device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const float *B, float *M, int ldm) {
+    constexpr int G = N / 4, R = kThreads / G, RPT = kTile / R;
+    const int t = threadIdx.x, c0 = (t % G) * 4, r0 = t / G;
+    float acc[RPT][4];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < K; ++k) {
+        const float4 b = *reinterpret_cast<const float4 *>(B + k * N + c0);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            const float a = A[(r0 + q * R) * lda + k];
+            acc[q][0] += a * b.x;
+            acc[q][1] += a * b.y;
+            acc[q][2] += a * b.z;
+            acc[q][3] += a * b.w;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+        float4 *p = reinterpret_cast<float4 *>(M + (r0 + q * R) * ldm + c0);
+        const float4 m = *p;
+        *p = make_float4(m.x > 0.f ? acc[q][0] : 0.f, m.y > 0.f ? acc[q][1] : 0.f,
+                         m.z > 0.f ? acc[q][2] : 0.f, m.w > 0.f ? acc[q][3] : 0.f);
+    }
+}
+
+// acc[m][n] += sum_s A[s][m] * D[s][n] over the tile's rows (the weight-gradient GEMM).
+template <int M, int N>
+struct WGrad {
+    static constexpr int G = N / 4, R = kThreads / G, RPT = M / R;
+    float acc[RPT][4];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+    }
+    __device__ __forceinline__ void add(const float *A, int lda, const float *D, int ldd, int rows) {
+        const int t = threadIdx.x, c0 = (t % G) * 4, m0 = t / G;
+#pragma unroll 4
+        for (int s = 0; s < rows; ++s) {
+            const float4 d = *reinterpret_cast<const float4 *>(D + s * ldd + c0);
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                const float a = A[s * lda + m0 + q * R];
+                acc[q][0] += a * d.x;
+                acc[q][1] += a * d.y;
+                acc[q][2] += a * d.z;
+                acc[q][3] += a * d.w;
+            }
+        }
+    }
+    __device__ __forceinline__ void store(float *out) const {  // out: [M][N] row-major
+        const int t = threadIdx.x, c0 = (t % G) * 4, m0 = t / G;
+#pragma unroll
+        for (int q = 0; q < RPT; ++q)
+            *reinterpret_cast<float4 *>(out + (m0 + q * R) * N + c0) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
+    }
+};
+
+__device__ __forceinline__ std::uint32_t active_count(std::uint32_t n, const std::uint32_t *count) {
+    return count != nullptr ? min(n, *count) : n;
+}
+
+// Stage the packed weights (and optionally their transposes) into shared memory.
+__device__ __forceinline__ void load_weights(const float *__restrict__ w, float *sW, float *sT) {
+    for (int i = threadIdx.x; i < kNW / 4; i += kThreads)
+        reinterpret_cast<float4 *>(sW)[i] = reinterpret_cast<const float4 *>(w)[i];
+    if (sT != nullptr) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 2048; i += kThreads) {  // W0 [32][64] -> [64][32]
+            const int r = i / 64, c = i % 64;
+            sT[kT0 + c * 32 + r] = sW[kW0 + i];
+        }
+        for (int i = threadIdx.x; i < 1024; i += kThreads) {  // W1 [64][16] -> [16][64]
+            const int r = i / 16, c = i % 16;
+            sT[kT1 + c * 64 + r] = sW[kW1 + i];
+        }
+        for (int i = threadIdx.x; i < 1024; i += kThreads) {  // W2[:16] [16][64] -> [64][16]
+            const int r = i / 64, c = i % 64;
+            sT[kT2 + c * 16 + r] = sW[kW2 + i];
+        }
+        for (int i = threadIdx.x; i < 4096; i += kThreads) {  // W3 [64][64] -> [64][64]
+            const int r = i / 64, c = i % 64;
+            sT[kT3 + c * 64 + r] = sW[kW3 + i];
+        }
+        for (int i = threadIdx.x; i < 192; i += kThreads) {  // W4 [64][3] -> [3][64]
+            const int r = i / 3, c = i % 3;
+            sT[kT4 + c * 64 + r] = sW[kW4 + i];
+        }
+    }
+    __syncthreads();
+}
+
+// Loads the tile's encodings into X[:, 0:32] (zero rows past `rows`).
+__device__ __forceinline__ void load_enc(const float *__restrict__ enc, std::size_t s0, int rows, float *X) {
+    for (int i = threadIdx.x; i < kTile * 8; i += kThreads) {
+        const int r = i / 8, c = (i % 8) * 4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r < rows) v = *reinterpret_cast<const float4 *>(enc + (s0 + r) * 32 + c);
+        *reinterpret_cast<float4 *>(X + r * kLd + c) = v;
+    }
+}
+
+// XC[s][16:32] = SH4(dir_s); rows past `rows` get a unit +z direction.
+__device__ __forceinline__ void load_sh(const float *__restrict__ dirs, std::size_t s0, int rows, float *XC) {
+    for (int r = threadIdx.x; r < kTile; r += kThreads) {
+        float dx = 0.f, dy = 0.f, dz = 1.f;
+        if (r < rows) {
+            dx = dirs[(s0 + r) * 3 + 0];
+            dy = dirs[(s0 + r) * 3 + 1];
+            dz = dirs[(s0 + r) * 3 + 2];
+        }
+        float o[16];
+        sh4(dx, dy, dz, o);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) XC[r * kLd + 16 + j] = o[j];
+    }
+}
+
+// Forward through the tile; leaves X0=enc, H1, XC=[x, sh], H2, H3 in shared memory and writes
+// sigma/rgb into O (O[s][0] = x0 (pre-activation), O[s][1..3] = rgb).
+__device__ __forceinline__ void tile_forward(const float *sW, float *X0, float *H1, float *XC, float *H2,
+                                             float *H3, float *O) {
+    mm<32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
+    __syncthreads();
+    mm<64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
+    __syncthreads();
+    mm<32, 64, true>(XC, kLd, sW + kW2, H2, kLd);
+    __syncthreads();
+    mm<64, 64, true>(H2, kLd, sW + kW3, H3, kLd);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kTile * 3; i += kThreads) {
+        const int r = i / 3, c = i % 3;
+        float a = 0.f;
+#pragma unroll 16
+        for (int k = 0; k < 64; ++k) a += H3[r * kLd + k] * sW[kW4 + k * 3 + c];
+        O[r * 4 + 1 + c] = 1.f / (1.f + expf(-a));
+    }
+    for (int r = threadIdx.x; r < kTile; r += kThreads) O[r * 4] = XC[r * kLd];
+    __syncthreads();
+}
+
+constexpr int kActFloats = 5 * kTile * kLd + kTile * 4;
+
+__global__ void __launch_bounds__(kThreads) mlp_forward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb) {
+    extern __shared__ __align__(16) float smem[];
+    float *sW = smem;
+    float *X0 = sW + kNW, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd, *H2 = XC + kTile * kLd;
+    float *H3 = H2 + kTile * kLd, *O = H3 + kTile * kLd;
+    load_weights(weights, sW, nullptr);
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::size_t s0 = (std::size_t)tile * kTile;
+        const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
+        load_enc(enc, s0, rows, X0);
+        load_sh(dirs, s0, rows, XC);
+        __syncthreads();
+        tile_forward(sW, X0, H1, XC, H2, H3, O);
+        for (int i = threadIdx.x; i < rows; i += kThreads) {
+            const float4 o = *reinterpret_cast<const float4 *>(O + i * 4);
+            reinterpret_cast<float4 *>(drgb)[s0 + i] = make_float4(expf(o.x), o.y, o.z, o.w);
+        }
+        __syncthreads();
+    }
+}
+
+// sigma only (NeRF.__call__ with dir=None, nerfs.py:71-72), used by the occupancy-grid refresh.
+__global__ void __launch_bounds__(kThreads) mlp_density_kernel(
+    std::uint32_t n, const float *__restrict__ enc, const float *__restrict__ weights, float *__restrict__ sigma) {
+    extern __shared__ __align__(16) float smem[];
+    float *sW = smem;
+    float *X0 = sW + kNW, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd;
+    load_weights(weights, sW, nullptr);
+    const std::uint32_t n_tiles = (n + kTile - 1) / kTile;
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::size_t s0 = (std::size_t)tile * kTile;
+        const int rows = (int)min((std::uint32_t)kTile, n - (std::uint32_t)s0);
+        load_enc(enc, s0, rows, X0);
+        __syncthreads();
+        mm<32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
+        __syncthreads();
+        mm<64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
+        __syncthreads();
+        for (int i = threadIdx.x; i < rows; i += kThreads) sigma[s0 + i] = expf(XC[i * kLd]);
+        __syncthreads();
+    }
+}
+
+// Backward.  dL_ddrgb rows past the active count are ignored; dL_denc rows past it are zeroed.
+// `grad_scale` multiplies the incoming gradient (loss normalisation); `partials` receives one
+// [9408] dL/dW partial per CTA.
+__global__ void __launch_bounds__(kThreads) mlp_backward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ dirs, const float *__restrict__ weights,
+    const float *__restrict__ dL_ddrgb, const float *__restrict__ grad_scale,
+    float *__restrict__ dL_denc, float *__restrict__ partials) {
+    extern __shared__ __align__(16) float smem[];
+    float *sW = smem, *sT = sW + kNW;
+    float *X0 = sT + kNT, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd, *H2 = XC + kTile * kLd;
+    float *H3 = H2 + kTile * kLd, *O = H3 + kTile * kLd;
+    load_weights(weights, sW, sT);
+    const float gs = grad_scale != nullptr ? *grad_scale : 1.f;
+
+    WGrad<32, 64> g0;  // dW0 = enc^T dA1
+    WGrad<64, 16> g1;  // dW1 = h1^T dx
+    WGrad<32, 64> g2;  // dW2 = [x, sh]^T dA2
+    WGrad<64, 64> g3;  // dW3 = h2^T dA3
+    float g4 = 0.f;    // dW4 = h3^T dA4: thread t < 192 owns element t
+    g0.zero();
+    g1.zero();
+    g2.zero();
+    g3.zero();
+
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::size_t s0 = (std::size_t)tile * kTile;
+        const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
+        load_enc(enc, s0, rows, X0);
+        load_sh(dirs, s0, rows, XC);
+        __syncthreads();
+        tile_forward(sW, X0, H1, XC, H2, H3, O);
+
+        // O[s] <- [dL/dx0, dL/da4 (3)]; rows past `rows` get zero gradient
+        for (int r = threadIdx.x; r < kTile; r += kThreads) {
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < rows) g = reinterpret_cast<const float4 *>(dL_ddrgb)[s0 + r];
+            const float4 o = *reinterpret_cast<const float4 *>(O + r * 4);
+            const float x0 = fminf(fmaxf(o.x, -15.f), 15.f);
+            *reinterpret_cast<float4 *>(O + r * 4) =
+                make_float4(gs * g.x * expf(x0), gs * g.y * o.y * (1.f - o.y), gs * g.z * o.z * (1.f - o.z),
+                            gs * g.w * o.w * (1.f - o.w));
+        }
+        __syncthreads();
+        if (threadIdx.x < 192) {  // dW4[m][c] += sum_s h3[s][m] * dA4[s][c]
+            const int m = threadIdx.x / 3, c = threadIdx.x % 3;
+            float a = 0.f;
+            for (int s = 0; s < kTile; ++s) a += H3[s * kLd + m] * O[s * 4 + 1 + c];
+            g4 += a;
+        }
+        __syncthreads();
+        // dA3 = (dA4 @ W4^T) * (h3 > 0), over H3
+        for (int i = threadIdx.x; i < kTile * 64; i += kThreads) {
+            const int r = i / 64, c = i % 64;
+            const float h = H3[r * kLd + c];
+            const float v = O[r * 4 + 1] * sT[kT4 + c] + O[r * 4 + 2] * sT[kT4 + 64 + c] + O[r * 4 + 3] * sT[kT4 + 128 + c];
+            H3[r * kLd + c] = h > 0.f ? v : 0.f;
+        }
+        __syncthreads();
+        g3.add(H2, kLd, H3, kLd, kTile);
+        __syncthreads();
+        mm_mask_inplace<64, 64>(H3, kLd, sT + kT3, H2, kLd);  // dA2 over H2
+        __syncthreads();
+        g2.add(XC, kLd, H2, kLd, kTile);
+        __syncthreads();
+        // dx = dA2 @ W2[:16]^T (+ dL/dx0 on column 0), over XC[:, 0:16]
+        mm<64, 16, false>(H2, kLd, sT + kT2, XC, kLd);
+        __syncthreads();
+        for (int r = threadIdx.x; r < kTile; r += kThreads) XC[r * kLd] += O[r * 4];
+        __syncthreads();
+        g1.add(H1, kLd, XC, kLd, kTile);
+        __syncthreads();
+        mm_mask_inplace<16, 64>(XC, kLd, sT + kT1, H1, kLd);  // dA1 over H1
+        __syncthreads();
+        g0.add(X0, kLd, H1, kLd, kTile);
+        __syncthreads();
+        mm<64, 32, false>(H1, kLd, sT + kT0, X0, kLd);  // dL/denc over X0
+        __syncthreads();
+        for (int i = threadIdx.x; i < kTile * 8; i += kThreads) {
+            const int r = i / 8, c = (i % 8) * 4;
+            if (r < rows) *reinterpret_cast<float4 *>(dL_denc + (s0 + r) * 32 + c) = *reinterpret_cast<const float4 *>(X0 + r * kLd + c);
+        }
+        __syncthreads();
+    }
+    float *p = partials + (std::size_t)blockIdx.x * kNW;
+    g0.store(p + kW0);
+    g1.store(p + kW1);
+    g2.store(p + kW2);
+    g3.store(p + kW3);
+    if (threadIdx.x < 192) p[kW4 + threadIdx.x] = g4;
+}
+
+// dW[j] = sum over CTAs c (in order) of partials[c][j]; accumulate into dW when requested.
+__global__ void reduce_partials_kernel(std::uint32_t n_parts, const float *__restrict__ partials,
+                                       float *__restrict__ dW, int accumulate) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= kNW) return;
+    float a = 0.f;
+    for (std::uint32_t c = 0; c < n_parts; ++c) a += partials[(std::size_t)c * kNW + j];
+    dW[j] = accumulate ? dW[j] + a : a;
+}
+
+// zero dL/denc rows in [active, n)
+__global__ void zero_rows_kernel(std::uint32_t n, const std::uint32_t *__restrict__ count, float *__restrict__ x, int width) {
+    const std::uint32_t a = active_count(n, count);
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    for (std::size_t i = (std::size_t)a * width + (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (std::size_t)n * width; i += stride)
+        x[i] = 0.f;
+}
+
+constexpr std::size_t kFwdSmem = (std::size_t)(kNW + kActFloats) * sizeof(float);
+constexpr std::size_t kBwdSmem = (std::size_t)(kNW + kNT + kActFloats) * sizeof(float);
+constexpr std::size_t kDensSmem = (std::size_t)(kNW + 3 * kTile * kLd) * sizeof(float);
+
+}  // namespace
+
+int mlp_partials_count() { return sm_count(); }
+std::size_t mlp_partials_floats() { return (std::size_t)mlp_partials_count() * kNW; }
+
+static bool aligned16(const void *p) { return ((std::uintptr_t)p & 15u) == 0; }
+
+int launch_mlp_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
+                       const float *enc, const float *dirs, const float *weights, float *drgb) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp: enc, weights and drgb must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        attr = true;
+    }
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kTile - 1) / kTile;
+    const unsigned grid = tiles < (unsigned)sm_count() * 2 ? tiles : (unsigned)sm_count() * 2;
+    mlp_forward_kernel<<<grid, kThreads, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
+    return launch_status();
+}
+
+int launch_mlp_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp: enc and weights must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_density_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDensSmem));
+        attr = true;
+    }
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kTile - 1) / kTile;
+    const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
+    mlp_density_kernel<<<grid, kThreads, kDensSmem, stream>>>(n, enc, weights, sigma);
+    return launch_status();
+}
+
+// `partials` must hold mlp_partials_floats() floats (scratch).
+int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
+                        const float *enc, const float *dirs, const float *weights,
+                        const float *dL_ddrgb, const float *grad_scale, float *dL_denc,
+                        float *dL_dweights, float *partials, bool accumulate) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
+                  "mlp: buffers must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        attr = true;
+    }
+    const unsigned grid = (unsigned)mlp_partials_count();
+    mlp_backward_kernel<<<grid, kThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
+    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(grid, partials, dL_dweights, accumulate ? 1 : 0);
+    if (count != nullptr && n > 0) zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
+    return launch_status();
+}
+
+}  // namespace ngp

@@ -1,0 +1,468 @@
+// Training-step kernels around the drop-in ops: batch construction, the fused
+// integrate -> loss -> integrate-backward pass, Adam, and occupancy-grid maintenance.
+//
+// They restate, as single kernels, what the reference does with several XLA ops per step:
+//   ray batch:       app/nerf/_utils.py:93-115 (rays from pixel indices), models/renderers/
+//                    cuda.py:56-97 (AABB near/far), :118-121 (start jitter), _utils.py:134-137
+//                    (random background), utils/data.py:443-465 (RGBA over background)
+//   loss:            app/nerf/_utils.py:149-160 (Huber, delta 0.1, masked by ray_is_valid)
+//   optimiser:       app/nerf/_utils.py:19-77 (optax adam + add_decayed_weights)
+//   occupancy grid:  utils/types.py:1149-1225 (decay, sampling, density max), :1227-1239
+//                    (threshold), :1241-1362 (marking cells no camera sees), :1385-1392
+#include "common.cuh"
+
+namespace ngp {
+namespace {
+
+// SplitMix64-based counter RNG: uniform floats in [0, 1) keyed by (seed, stream, index).
+__device__ __forceinline__ std::uint64_t mix64(std::uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ std::uint64_t rng_u64(std::uint64_t seed, std::uint32_t stream, std::uint64_t i) {
+    return mix64(seed ^ mix64(((std::uint64_t)stream << 48) ^ i));
+}
+__device__ __forceinline__ float rng_uniform(std::uint64_t seed, std::uint32_t stream, std::uint64_t i) {
+    return (float)(rng_u64(seed, stream, i) >> 40) * (1.0f / 16777216.0f);
+}
+
+__global__ void __launch_bounds__(256) train_rays_kernel(
+    NgpTrainRaysDescriptor d, const float *__restrict__ transforms, const std::uint8_t *__restrict__ rgbas,
+    const std::uint32_t *__restrict__ perm, float *__restrict__ rays_o, float *__restrict__ rays_d,
+    float *__restrict__ t_starts, float *__restrict__ t_ends, float *__restrict__ noises,
+    float *__restrict__ bgs, float *__restrict__ gt) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n_rays) return;
+    const std::uint64_t n_pix = (std::uint64_t)d.width * d.height;
+    std::uint64_t p;
+    const std::uint64_t n_all = n_pix * d.n_views;
+    if (perm != nullptr) {
+        p = perm[i];
+        if (p >= n_all) p = n_all - 1;  // out-of-range pixel indices are clamped
+    } else {
+        p = (std::uint64_t)(((unsigned __int128)rng_u64(d.seed, 0, i) * n_all) >> 64);
+    }
+    const std::uint32_t view = (std::uint32_t)(p / n_pix);
+    const std::uint32_t pix = (std::uint32_t)(p % n_pix);
+    const float px = (float)(pix % d.width), py = (float)(pix / d.width);
+    // camera-space direction, CV -> CG axis flip (utils/types.py:417-439)
+    float cx = ((px + 0.5f) - d.cx) / d.fx;
+    float cy = -(((py + 0.5f) - d.cy) / d.fy);
+    float cz = -1.0f;
+    const float inv = rsqrtf(cx * cx + cy * cy + cz * cz);
+    cx *= inv;
+    cy *= inv;
+    cz *= inv;
+    const float *T = transforms + (std::size_t)view * 12;
+    const float dx = cx * T[0] + cy * T[1] + cz * T[2];
+    const float dy = cx * T[3] + cy * T[4] + cz * T[5];
+    const float dz = cx * T[6] + cy * T[7] + cz * T[8];
+    const float ox = T[9], oy = T[10], oz = T[11];
+    rays_o[i * 3 + 0] = ox;
+    rays_o[i * 3 + 1] = oy;
+    rays_o[i * 3 + 2] = oz;
+    rays_d[i * 3 + 0] = dx;
+    rays_d[i * 3 + 1] = dy;
+    rays_d[i * 3 + 2] = dz;
+    // AABB intersection (renderers/cuda.py:56-97)
+    const float eps = 1e-15f, b = d.bound;
+    const float ex = signbit(dx) ? fminf(dx, -eps) : fmaxf(dx, eps);
+    const float ey = signbit(dy) ? fminf(dy, -eps) : fmaxf(dy, eps);
+    const float ez = signbit(dz) ? fminf(dz, -eps) : fmaxf(dz, eps);
+    const float tx0 = (-b - ox) / ex, tx1 = (b - ox) / ex;
+    const float ty0 = (-b - oy) / ey, ty1 = (b - oy) / ey;
+    const float tz0 = (-b - oz) / ez, tz1 = (b - oz) / ez;
+    const float ts = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+    const float te = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    t_starts[i] = fmaxf(0.f, ts);
+    t_ends[i] = te;
+    noises[i] = d.perturb ? rng_uniform(d.seed, 1, i) : 0.f;
+    float bg[3] = {d.bg[0], d.bg[1], d.bg[2]};
+    if (d.random_bg) {
+        bg[0] = rng_uniform(d.seed, 2, i);
+        bg[1] = rng_uniform(d.seed, 3, i);
+        bg[2] = rng_uniform(d.seed, 4, i);
+    }
+    const uchar4 px4 = reinterpret_cast<const uchar4 *>(rgbas)[p];
+    const float a = px4.w / 255.f;
+    const float rgb[3] = {px4.x / 255.f, px4.y / 255.f, px4.z / 255.f};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        bgs[i * 3 + c] = bg[c];
+        gt[i * 3 + c] = rgb[c] * a + bg[c] * (1.f - a);
+    }
+}
+
+// Per ray: integrate_rays forward (integrating.cu:24-104), Huber loss against the target, and
+// integrate_rays_backward (integrating.cu:106-240) with dL/dfinal_rgbd from the loss; dL/ddepth
+// is zero (the loss ignores depth).  Gradients are unnormalised; 1/n_valid is applied by the
+// field backward through `grad_scale`.
+__global__ void __launch_bounds__(256) integrate_loss_backward_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, float near_distance, float delta, const bool *__restrict__ valid,
+    const std::uint32_t *__restrict__ startidx, const std::uint32_t *__restrict__ n_samples,
+    const float *__restrict__ bgs, const float *__restrict__ gt, const float *__restrict__ dss,
+    const float *__restrict__ z_vals, const float *__restrict__ drgbs,
+    float *__restrict__ dL_ddrgbs, float *__restrict__ acc /* [loss, n_valid, measured] */) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float loss = 0.f, nv = 0.f, used_f = 0.f;
+    if (i < n_rays) {
+        const std::uint32_t s = startidx[i];
+        const std::uint32_t n = s >= total_samples ? 0u : min(n_samples[i], total_samples - s);
+        const float *rd = dss + s, *rz = z_vals + s;
+        const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + s;
+        float4 *gc = reinterpret_cast<float4 *>(dL_ddrgbs) + s;
+        const float bg0 = bgs[i * 3 + 0], bg1 = bgs[i * 3 + 1], bg2 = bgs[i * 3 + 2];
+        // forward
+        float T = 1.f, r = 0.f, g = 0.f, b = 0.f, dep = 0.f;
+        std::uint32_t k = 0;
+        for (; T > kTThreshold && k < n; ++k) {
+            const float4 c = rc[k];
+            const float alpha = 1.f - __expf(-c.x * rd[k]);
+            const float w = T * alpha;
+            r += w * c.y;
+            g += w * c.z;
+            b += w * c.w;
+            dep += w * rz[k];
+            T *= 1.f - alpha;
+        }
+        const std::uint32_t used = k;
+        const float fo = 1.f - T;
+        float4 fr;
+        if (T <= kTThreshold) {
+            const float id = 1.f / fo;
+            fr = make_float4(r * id, g * id, b * id, dep * id);
+        } else {
+            fr = make_float4(r + T * bg0, g + T * bg1, b + T * bg2, dep);
+        }
+        // loss and its gradient (mean over channels, sum over valid rays)
+        float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid[i]) {
+            nv = 1.f;
+            const float e[3] = {fr.x - gt[i * 3 + 0], fr.y - gt[i * 3 + 1], fr.z - gt[i * 3 + 2]};
+            float gg[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float ae = fabsf(e[c]);
+                loss += ae <= delta ? 0.5f * e[c] * e[c] : delta * (ae - 0.5f * delta);
+                gg[c] = (ae <= delta ? e[c] : copysignf(delta, e[c])) * (1.f / 3.f);
+            }
+            loss *= 1.f / 3.f;
+            go = make_float4(gg[0], gg[1], gg[2], 0.f);
+        }
+        // backward (recomputes the forward, as integrating.cu:177-233 does)
+        const bool terminated = fo >= 1.f - kTThreshold;
+        const float bgterm = terminated ? 0.f : 1.f - fo;
+        T = 1.f;
+        float cr = 0.f, cg = 0.f, cb = 0.f, cd = 0.f;
+        for (k = 0; T > kTThreshold && k < n; ++k) {
+            const float4 c = rc[k];
+            const float z = rz[k], dt = rd[k];
+            const float alpha = 1.f - __expf(-c.x * dt);
+            const float w = T * alpha;
+            cr += w * c.y;
+            cg += w * c.z;
+            cb += w * c.w;
+            cd += w * z;
+            T *= 1.f - alpha;
+            const float dsig = dt * (go.x * (T * c.y - (fr.x - cr) - bg0 * bgterm)
+                                   + go.y * (T * c.z - (fr.y - cg) - bg1 * bgterm)
+                                   + go.z * (T * c.w - (fr.z - cb) - bg2 * bgterm)
+                                   + go.w * (T * z - (fr.w - cd)));
+            const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
+            gc[k] = make_float4(fminf(z * z, 1.f) * dsig + reg, w * go.x, w * go.y, w * go.z);
+        }
+        for (; k < n; ++k) gc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        used_f = (float)used;
+    }
+    loss = warp_sum(loss);
+    nv = warp_sum(nv);
+    used_f = warp_sum(used_f);
+    if (lane_id() == 0) {
+        if (loss != 0.f) atomicAdd(acc + 0, loss);
+        if (nv != 0.f) atomicAdd(acc + 1, nv);
+        if (used_f != 0.f) atomicAdd(acc + 2, used_f);
+    }
+}
+
+// stats = [loss / n_valid, n_valid, measured_batch_size, samples before compaction];
+// grad_scale = 1 / n_valid.  `count` holds the active-sample count from the marcher.
+__global__ void finalize_loss_kernel(const float *__restrict__ acc, const std::uint32_t *__restrict__ count,
+                                     float *__restrict__ stats, float *__restrict__ grad_scale) {
+    const float nv = acc[1];
+    const float inv = nv > 0.f ? 1.f / nv : 0.f;
+    stats[0] = acc[0] * inv;
+    stats[1] = nv;
+    stats[2] = acc[2];
+    stats[3] = (float)*count;
+    *grad_scale = inv;
+}
+
+// zero dL_ddrgbs slots in [count, total) (slots no ray owns)
+__global__ void zero_tail4_kernel(std::uint32_t total, const std::uint32_t *__restrict__ count, float4 *__restrict__ x) {
+    const std::uint32_t a = min(total, *count);
+    for (std::size_t s = a + (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; s < total; s += (std::size_t)gridDim.x * blockDim.x)
+        x[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// optax.adam (scale_by_adam, then scale by -lr) chained with add_decayed_weights, in that order
+// (app/nerf/_utils.py:45-77), then optax.apply_updates:
+//   m = b1 m + (1-b1) g;  v = b2 v + (1-b2) g^2;  mh = m / (1-b1^t);  vh = v / (1-b2^t)
+//   update = -lr * mh / (sqrt(vh + eps_root) + eps) + wd * p;  p = p + update
+// (the decay term is added after the learning-rate scaling, exactly as the reference chains it).
+__global__ void __launch_bounds__(256) adam_kernel(NgpAdamDescriptor d, float bc1, float bc2,
+                                                   float *__restrict__ p, float *__restrict__ g,
+                                                   float *__restrict__ m, float *__restrict__ v) {
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    const std::size_t n4 = d.n / 4;
+    for (std::size_t i = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        float4 pp = reinterpret_cast<float4 *>(p)[i];
+        float4 gg = reinterpret_cast<float4 *>(g)[i];
+        float4 mm = reinterpret_cast<float4 *>(m)[i];
+        float4 vv = reinterpret_cast<float4 *>(v)[i];
+        float *pa = &pp.x, *ga = &gg.x, *ma = &mm.x, *va = &vv.x;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            ma[c] = d.beta1 * ma[c] + (1.f - d.beta1) * ga[c];
+            va[c] = d.beta2 * va[c] + (1.f - d.beta2) * ga[c] * ga[c];
+            const float mh = ma[c] / bc1, vh = va[c] / bc2;
+            const float upd = -d.lr * (mh / (sqrtf(vh + d.eps_root) + d.eps)) + d.weight_decay * pa[c];
+            pa[c] = pa[c] + upd;
+        }
+        reinterpret_cast<float4 *>(p)[i] = pp;
+        reinterpret_cast<float4 *>(m)[i] = mm;
+        reinterpret_cast<float4 *>(v)[i] = vv;
+        if (d.zero_grad) reinterpret_cast<float4 *>(g)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (std::size_t i = n4 * 4 + (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += stride) {
+        float mm = d.beta1 * m[i] + (1.f - d.beta1) * g[i];
+        float vv = d.beta2 * v[i] + (1.f - d.beta2) * g[i] * g[i];
+        const float upd = -d.lr * ((mm / bc1) / (sqrtf(vv / bc2 + d.eps_root) + d.eps)) + d.weight_decay * p[i];
+        p[i] = p[i] + upd;
+        m[i] = mm;
+        v[i] = vv;
+        if (d.zero_grad) g[i] = 0.f;
+    }
+}
+
+__device__ __forceinline__ std::uint32_t morton_decode(std::uint32_t x) {
+    x = x & 0x49249249u;
+    x = (x | (x >> 2)) & 0xc30c30c3u;
+    x = (x | (x >> 4)) & 0x0f00f00fu;
+    x = (x | (x >> 8)) & 0xff0000ffu;
+    x = (x | (x >> 16)) & 0x0000ffffu;
+    return x;
+}
+
+// types.py:1161-1162: decay the cascade's live cells (cells marked untrainable hold -1).
+__global__ void ogrid_decay_kernel(std::uint32_t n, float decay, float *__restrict__ density) {
+    for (std::size_t i = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (std::size_t)gridDim.x * blockDim.x) {
+        const float v = density[i];
+        if (v >= 0.f) density[i] = v * decay;
+    }
+}
+
+// types.py:1164-1204: choose cells and a random point inside each.  With update_all, point j is
+// in cell j; otherwise the first half of the points go to cells drawn uniformly among live cells
+// and the second half to cells drawn uniformly among occupied live cells (rejection sampling on
+// the bitfield, as the paper describes; a draw that keeps failing falls back to a uniform cell).
+// Dead cells get index 0xFFFFFFFF and are skipped downstream.
+__global__ void ogrid_sample_kernel(std::uint32_t M, std::uint32_t update_all, std::uint32_t cas, std::uint32_t G,
+                                    float bound, std::uint64_t seed, const float *__restrict__ density,
+                                    const std::uint8_t *__restrict__ bits, std::uint32_t *__restrict__ cells,
+                                    float *__restrict__ xyz) {
+    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= M) return;
+    const std::uint32_t G3 = G * G * G;
+    const float *dcas = density + (std::size_t)cas * G3;
+    std::uint32_t c;
+    if (update_all) {
+        c = j;
+    } else {
+        const bool want_occupied = j >= M / 2;
+        c = (std::uint32_t)(rng_u64(seed, 5, j) % G3);
+        for (int tries = 0; tries < 64; ++tries) {
+            const std::uint32_t cand = (std::uint32_t)(rng_u64(seed, 6 + tries, j) % G3);
+            const std::uint32_t gi = cas * G3 + cand;
+            const bool live = dcas[cand] >= 0.f;
+            const bool occ = (bits[gi >> 3] >> (gi & 7u)) & 1u;
+            if (live && (!want_occupied || occ)) {
+                c = cand;
+                break;
+            }
+        }
+    }
+    if (dcas[c] < 0.f) {
+        cells[j] = 0xFFFFFFFFu;
+        xyz[j * 3 + 0] = xyz[j * 3 + 1] = xyz[j * 3 + 2] = 0.f;
+        return;
+    }
+    cells[j] = c;
+    const float mip_bound = fminf(bound, (float)(1u << cas));
+    const float hcw = mip_bound / (float)G;
+    const std::uint32_t g[3] = {morton_decode(c), morton_decode(c >> 1), morton_decode(c >> 2)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float v = (float)g[a] / (float)(G - 1) * 2.f - 1.f;
+        v *= mip_bound - hcw;
+        v += (rng_uniform(seed, 100 + a, j) * 2.f - 1.f) * hcw;
+        xyz[j * 3 + a] = v;
+    }
+}
+
+// types.py:1218-1220: density = max(density, new) at the chosen cells.  Non-negative floats order
+// like their bit patterns, so an integer atomicMax gives the float max.
+__global__ void ogrid_max_kernel(std::uint32_t M, std::uint32_t cas, std::uint32_t G3,
+                                 const std::uint32_t *__restrict__ cells, const float *__restrict__ sigma,
+                                 float *__restrict__ density) {
+    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= M) return;
+    const std::uint32_t c = cells[j];
+    if (c >= G3) return;  // dead cell marker (or an out-of-range index)
+    const float s = fmaxf(sigma[j], 0.f);
+    atomicMax(reinterpret_cast<int *>(density + (std::size_t)cas * G3 + c), __float_as_int(s));
+}
+
+// types.py:1227-1231 and :1385-1386: threshold = min(0.01 * diag / (2 min(bound,1) sqrt3),
+// mean density over the live cells of cascade 0).
+__global__ void ogrid_mean_kernel(std::uint32_t n, const float *__restrict__ density, float *__restrict__ acc) {
+    float s = 0.f, c = 0.f;
+    for (std::size_t i = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (std::size_t)gridDim.x * blockDim.x) {
+        const float v = density[i];
+        if (v >= 0.f) {
+            s += v;
+            c += 1.f;
+        }
+    }
+    s = warp_sum(s);
+    c = warp_sum(c);
+    if (lane_id() == 0) {
+        atomicAdd(acc, s);
+        atomicAdd(acc + 1, c);
+    }
+}
+__global__ void ogrid_threshold_kernel(float thr_step, const float *__restrict__ acc, float *__restrict__ thr) {
+    const float mean = acc[1] > 0.f ? acc[0] / acc[1] : 0.f;
+    *thr = fminf(thr_step, mean);
+}
+
+// types.py:1241-1362 for pinhole cameras: a cell stays trainable if any of its 8 corners lies in
+// front of some training camera and projects inside its image; other cells get density -1.
+__global__ void ogrid_mark_untrained_kernel(std::uint32_t K, std::uint32_t G, float bound, std::uint32_t n_views,
+                                            const float *__restrict__ transforms, float fx, float fy, float cx,
+                                            float cy, std::uint32_t width, std::uint32_t height,
+                                            float *__restrict__ density) {
+    const std::uint32_t G3 = G * G * G;
+    const std::size_t n = (std::size_t)K * G3;
+    for (std::size_t i = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (std::size_t)gridDim.x * blockDim.x) {
+        const std::uint32_t level = (std::uint32_t)(i / G3), c = (std::uint32_t)(i % G3);
+        const float mip_bound = fminf((float)(1u << level), bound);
+        const float cw = 2.f * mip_bound / (float)G;
+        const float gx = ((float)morton_decode(c) / (float)G - 0.5f) * 2.f * mip_bound;
+        const float gy = ((float)morton_decode(c >> 1) / (float)G - 0.5f) * 2.f * mip_bound;
+        const float gz = ((float)morton_decode(c >> 2) / (float)G - 0.5f) * 2.f * mip_bound;
+        bool alive = false;
+        for (std::uint32_t v = 0; v < n_views && !alive; ++v) {
+            const float *T = transforms + (std::size_t)v * 12;
+            for (int k = 0; k < 8 && !alive; ++k) {
+                const float px = gx + cw * ((k >> 2) & 1) - T[9];
+                const float py = gy + cw * ((k >> 1) & 1) - T[10];
+                const float pz = gz + cw * (k & 1) - T[11];
+                // p_cam = R^T p
+                const float qx = px * T[0] + py * T[3] + pz * T[6];
+                const float qy = px * T[1] + py * T[4] + pz * T[7];
+                const float qz = px * T[2] + py * T[5] + pz * T[8];
+                if (!(qz < 0.f)) continue;
+                const float u = (qx / -qz * fx + cx) / (float)width;
+                const float w = (qy / -qz * fy + cy) / (float)height;
+                alive = u >= 0.f && u < 1.f && w >= 0.f && w < 1.f;
+            }
+        }
+        if (!alive) density[i] = -1.f;
+    }
+}
+
+}  // namespace
+
+int launch_ogrid_decay(cudaStream_t stream, std::uint32_t n, float decay, float *density) {
+    if (n > 0) ogrid_decay_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, decay, density);
+    return launch_status();
+}
+
+int launch_ogrid_sample(cudaStream_t stream, std::uint32_t M, bool update_all, std::uint32_t cas, std::uint32_t G,
+                        float bound, std::uint64_t seed, const float *density, const std::uint8_t *bits,
+                        std::uint32_t *cells, float *xyz) {
+    NGP_CHECK_ARG(G >= 2 && G <= 1024 && (G & (G - 1)) == 0, "ogrid: G must be a power of two in [2, 1024]");
+    if (M > 0)
+        ogrid_sample_kernel<<<(M + 255) / 256, 256, 0, stream>>>(M, update_all ? 1u : 0u, cas, G, bound, seed, density,
+                                                                bits, cells, xyz);
+    return launch_status();
+}
+
+int launch_ogrid_max(cudaStream_t stream, std::uint32_t M, std::uint32_t cas, std::uint32_t G3,
+                     const std::uint32_t *cells, const float *sigma, float *density) {
+    if (M > 0) ogrid_max_kernel<<<(M + 255) / 256, 256, 0, stream>>>(M, cas, G3, cells, sigma, density);
+    return launch_status();
+}
+
+// `acc` is a 2-float scratch accumulator.
+int launch_ogrid_threshold(cudaStream_t stream, std::uint32_t n_cas0, float thr_step, const float *density,
+                           float *acc, float *thr) {
+    NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(float), stream));
+    ogrid_mean_kernel<<<grid_for(n_cas0, 256, 4), 256, 0, stream>>>(n_cas0, density, acc);
+    ogrid_threshold_kernel<<<1, 1, 0, stream>>>(thr_step, acc, thr);
+    return launch_status();
+}
+
+int launch_ogrid_mark_untrained(cudaStream_t stream, std::uint32_t K, std::uint32_t G, float bound,
+                                std::uint32_t n_views, const float *transforms, float fx, float fy, float cx,
+                                float cy, std::uint32_t width, std::uint32_t height, float *density) {
+    NGP_CHECK_ARG(G >= 2 && G <= 1024 && (G & (G - 1)) == 0 && K >= 1 && K <= 16, "ogrid: bad K or G");
+    ogrid_mark_untrained_kernel<<<grid_for((std::size_t)K * G * G * G, 256, 8), 256, 0, stream>>>(
+        K, G, bound, n_views, transforms, fx, fy, cx, cy, width, height, density);
+    return launch_status();
+}
+
+int launch_train_rays(cudaStream_t stream, const NgpTrainRaysDescriptor &d, const float *transforms,
+                      const std::uint8_t *rgbas, const std::uint32_t *perm, float *rays_o, float *rays_d,
+                      float *t_starts, float *t_ends, float *noises, float *bgs, float *gt) {
+    NGP_CHECK_ARG(d.width > 0 && d.height > 0 && d.n_views > 0 && d.bound > 0.f, "train_rays: bad camera");
+    NGP_CHECK_ARG(((std::uintptr_t)rgbas & 3u) == 0, "train_rays: rgbas must be 4-byte aligned");
+    if (d.n_rays > 0)
+        train_rays_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(d, transforms, rgbas, perm, rays_o, rays_d,
+                                                                     t_starts, t_ends, noises, bgs, gt);
+    return launch_status();
+}
+
+// `acc` is a 3-float scratch accumulator.
+int launch_integrate_loss_backward(cudaStream_t stream, const NgpIntegrateLossDescriptor &d, const bool *valid,
+                                   const std::uint32_t *startidx, const std::uint32_t *n_samples,
+                                   const float *bgs, const float *gt, const float *dss, const float *z_vals,
+                                   const float *drgbs, const std::uint32_t *count, float *dL_ddrgbs,
+                                   float *stats, float *grad_scale, float *acc) {
+    NGP_CHECK_ARG(((std::uintptr_t)drgbs & 15u) == 0 && ((std::uintptr_t)dL_ddrgbs & 15u) == 0,
+                  "integrate_loss_backward: drgbs and dL_ddrgbs must be 16-byte aligned");
+    NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, 3 * sizeof(float), stream));
+    if (d.n_rays > 0)
+        integrate_loss_backward_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
+            d.n_rays, d.total_samples, d.near_distance, d.huber_delta, valid, startidx, n_samples, bgs, gt, dss, z_vals, drgbs,
+            dL_ddrgbs, acc);
+    if (d.total_samples > 0)
+        zero_tail4_kernel<<<grid_for(d.total_samples, 256, 4), 256, 0, stream>>>(
+            d.total_samples, count, reinterpret_cast<float4 *>(dL_ddrgbs));
+    finalize_loss_kernel<<<1, 1, 0, stream>>>(acc, count, stats, grad_scale);
+    return launch_status();
+}
+
+int launch_adam(cudaStream_t stream, const NgpAdamDescriptor &d, float *p, float *g, float *m, float *v) {
+    NGP_CHECK_ARG(d.step >= 1, "adam: step is 1-based");
+    NGP_CHECK_ARG((((std::uintptr_t)p | (std::uintptr_t)g | (std::uintptr_t)m | (std::uintptr_t)v) & 15u) == 0,
+                  "adam: buffers must be 16-byte aligned");
+    const float bc1 = 1.f - powf(d.beta1, (float)d.step);
+    const float bc2 = 1.f - powf(d.beta2, (float)d.step);
+    if (d.n > 0) adam_kernel<<<grid_for(d.n / 4 + 1, 256, 8), 256, 0, stream>>>(d, bc1, bc2, p, g, m, v);
+    return launch_status();
+}
+
+}  // namespace ngp

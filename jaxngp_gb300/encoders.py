@@ -1,0 +1,147 @@
+"""HashGridEncoder on the GPU kernels, with the interface of the reference's flax module.
+
+Mirrors ``HashGridEncoder`` of models/encoders.py:58-256: fields (L, T, F, N_min, N_max,
+tv_scale, param_dtype), the parameter named "latent codes stored on grid vertices" of shape
+[offsets[-1], F] initialised ~U(-1e-4, 1e-4) (encoders.py:105-114), and
+``__call__(pos, bound) -> (encodings [N, L*F], tv)``.  The gradient w.r.t. the table is the
+scatter-add of the gather's transpose; positions get no gradient (the reference never
+differentiates w.r.t. sample positions: they come from march_rays, which has no JVP).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import List, Optional
+
+import torch
+
+from . import _lib as L
+
+PARAM_NAME = "latent codes stored on grid vertices"
+
+
+@dataclass(frozen=True)
+class LevelTable:
+    """encoders.py:77-103, computed on the host in float64 as the reference does."""
+    L: int
+    T: int
+    F: int
+    N_min: int
+    N_max: int
+    per_level_scale: Optional[float] = None
+    dim: int = 3
+
+    @property
+    def b(self) -> float:
+        if self.per_level_scale is not None:
+            return float(self.per_level_scale)
+        return math.exp((math.log(self.N_max) - math.log(self.N_min)) / (self.L - 1))
+
+    def levels(self):
+        scales: List[float] = []
+        res: List[int] = []
+        offsets = [0]
+        first_hash = 0
+        for i in range(self.L):
+            s = self.N_min * (self.b ** i) - 1
+            scales.append(s)
+            r = math.ceil(s) + 1
+            res.append(r)
+            n = (r ** self.dim + 7) // 8 * 8
+            if n <= self.T:
+                first_hash += 1
+            else:
+                n = self.T
+            offsets.append(offsets[-1] + n)
+        return scales, res, offsets, first_hash
+
+    @property
+    def n_params(self) -> int:
+        return self.levels()[2][-1]
+
+    def descriptor(self, n_coords: int, bound: float) -> L.NgpHashGridDescriptor:
+        if self.L > L.MAX_LEVELS:
+            raise ValueError(f"at most {L.MAX_LEVELS} levels are supported")
+        if self.F != 2:
+            raise NotImplementedError("the GPU encoder supports F = 2 features per level")
+        scales, res, offsets, first_hash = self.levels()
+        if offsets[-1] >= 2 ** 32:
+            raise ValueError("table too large for 32-bit indices")
+        d = L.NgpHashGridDescriptor()
+        d.n_coords = n_coords
+        d.L, d.F, d.T = self.L, self.F, self.T
+        d.first_hash_level = first_hash
+        d.n_params = offsets[-1]
+        d.bound = bound
+        d.two_bound = 2 * bound
+        for i in range(self.L):
+            d.scales[i] = scales[i]           # float64 -> float32, as jnp.asarray(scales, float32)
+            d.resolutions[i] = res[i] & 0xFFFFFFFF
+        for i in range(self.L + 1):
+            d.offsets[i] = offsets[i]
+        return d
+
+
+def hashgrid_forward(table: LevelTable, pos: torch.Tensor, latents: torch.Tensor, bound: float,
+                     count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    pos = pos.contiguous()
+    n = pos.shape[0]
+    if out is None:
+        out = torch.empty(n, table.L * table.F, dtype=torch.float32, device=pos.device)
+    L.call("ngp_hashgrid_forward", [pos, latents, count, out], table.descriptor(n, bound))
+    return out
+
+
+def hashgrid_backward(table: LevelTable, pos: torch.Tensor, dL_denc: torch.Tensor, bound: float,
+                      count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    n = pos.shape[0]
+    if out is None:
+        out = torch.empty(table.n_params, table.F, dtype=torch.float32, device=pos.device)
+    L.call("ngp_hashgrid_backward", [pos.contiguous(), dL_denc.contiguous(), count, out], table.descriptor(n, bound))
+    return out
+
+
+class _HashGridFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pos, latents, table, bound):
+        ctx.table, ctx.bound = table, bound
+        ctx.save_for_backward(pos)
+        return hashgrid_forward(table, pos, latents, bound)
+
+    @staticmethod
+    def backward(ctx, g):
+        (pos,) = ctx.saved_tensors
+        return None, hashgrid_backward(ctx.table, pos, g.contiguous(), ctx.bound), None, None
+
+
+class HashGridEncoder(torch.nn.Module):
+    """models/encoders.py:58-256 on libngp_gb300."""
+
+    def __init__(self, L: int, T: int, F: int, N_min: int, N_max: int, tv_scale: float = 0.0,
+                 param_dtype: torch.dtype = torch.float32, per_level_scale: Optional[float] = None,
+                 device="cuda", generator: Optional[torch.Generator] = None):
+        super().__init__()
+        if param_dtype != torch.float32:
+            raise NotImplementedError("the FP32 encoder stores float32 latents")
+        self.table = LevelTable(L, T, F, N_min, N_max, per_level_scale)
+        self.L, self.T, self.F, self.N_min, self.N_max = L, T, F, N_min, N_max
+        self.tv_scale = tv_scale
+        lat = torch.empty(self.table.n_params, F, dtype=torch.float32, device=device)
+        lat.uniform_(-1e-4, 1e-4, generator=generator)
+        self.register_parameter(PARAM_NAME, torch.nn.Parameter(lat))
+
+    @property
+    def latents(self) -> torch.nn.Parameter:
+        return getattr(self, PARAM_NAME)
+
+    @property
+    def b(self) -> float:
+        return self.table.b
+
+    def forward(self, pos: torch.Tensor, bound: float):
+        if self.tv_scale > 0:
+            raise NotImplementedError("the total-variation term (tv_scale > 0) is not implemented on the GPU")
+        if pos.dtype != torch.float32 or pos.dim() != 2 or pos.shape[-1] != 3:
+            raise ValueError("pos must be float32 [N, 3]")
+        enc = _HashGridFn.apply(pos, self.latents, self.table, float(bound))
+        return enc, 0.0
