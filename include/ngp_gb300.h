@@ -171,6 +171,7 @@ typedef struct NgpHashGridDescriptor {
     uint32_t n_params;          /* P = offsets[L], rows of the latent table */
     float bound;                /* positions are in [-bound, bound]^3 */
     float two_bound;            /* float32(2 * bound) */
+    uint32_t accumulate;        /* backward: add into dL_dlatents instead of zero-filling it first */
     float scales[NGP_MAX_LEVELS];
     uint32_t resolutions[NGP_MAX_LEVELS];
     uint32_t offsets[NGP_MAX_LEVELS + 1];
@@ -185,7 +186,7 @@ int ngp_hashgrid_forward_status(cudaStream_t stream, void **buffers, const char 
 
 /* Replaces the gradient JAX derives for the gather of encoders.py:226 (a scatter-add).
  * buffers: pos f32[N,3], dL_denc f32[N,L*F], active_count u32[1] or NULL -> dL_dlatents f32[P,F].
- * The output is zero-filled first.  opaque: NgpHashGridDescriptor. */
+ * The output is zero-filled first unless `accumulate` is set.  opaque: NgpHashGridDescriptor. */
 void ngp_hashgrid_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_hashgrid_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
@@ -273,6 +274,27 @@ typedef struct NgpAdamDescriptor {
  * buffers: params f32[n], grads f32[n], m f32[n], v f32[n]; opaque: NgpAdamDescriptor. */
 void ngp_adam(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_adam_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* ------------------------------------------------------------------ synthetic scene data */
+typedef struct NgpRenderBlobsDescriptor {
+    uint32_t n_rays;       /* pixels to render: view0 * H * W onwards, n_rays of them */
+    uint32_t n_blobs;
+    uint32_t n_steps;      /* quadrature steps across the scene box */
+    uint32_t width, height, n_views;
+    uint32_t view0;        /* first view rendered */
+    uint32_t n_shells;
+    float fx, fy, cx, cy;
+    float bound;
+} NgpRenderBlobsDescriptor;
+
+/* Ground truth for the synthetic scenes: midpoint quadrature of the emission-absorption integral
+ * through a sum of isotropic Gaussian density blobs (and thin spherical shells), colour the
+ * density-weighted blend of the blob colours.  Output RGBA u8 with alpha = opacity and straight
+ * (not premultiplied) colour, as an RGBA photograph of the object.
+ * buffers: transforms f32[V,12], blobs f32[B,8] (cx, cy, cz, sigma, peak, r, g, b),
+ * shells f32[S,8] (cx, cy, cz, radius, thickness, peak, c0, c1; colour (c0, c0, c1)) -> rgba u8[n_rays,4]. */
+void ngp_render_blobs(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_render_blobs_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
 /* ------------------------------------------------------------- occupancy-grid maintenance */
 typedef struct NgpOgridDescriptor {

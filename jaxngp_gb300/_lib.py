@@ -68,7 +68,8 @@ class PackbitsDescriptor(_Desc):
 
 class NgpHashGridDescriptor(_Desc):
     _fields_ = [("n_coords", c_u32), ("L", c_u32), ("F", c_u32), ("T", c_u32), ("first_hash_level", c_u32),
-                ("n_params", c_u32), ("bound", c_f32), ("two_bound", c_f32), ("scales", c_f32 * MAX_LEVELS),
+                ("n_params", c_u32), ("bound", c_f32), ("two_bound", c_f32), ("accumulate", c_u32),
+                ("scales", c_f32 * MAX_LEVELS),
                 ("resolutions", c_u32 * MAX_LEVELS), ("offsets", c_u32 * (MAX_LEVELS + 1))]
 
 

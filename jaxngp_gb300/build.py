@@ -22,7 +22,8 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", 
 # Per-file flags.  The marcher is compiled without multiply-add contraction so that its float
 # arithmetic is the reference's, one rounding per operation.
 EXTRA = {"marching.cu": ["--fmad=false"]}
-SOURCES = ["abi.cu", "marching.cu", "integrating.cu", "packbits.cu", "hashgrid.cu", "mlp.cu", "train.cu"]
+SOURCES = ["abi.cu", "marching.cu", "integrating.cu", "packbits.cu", "hashgrid.cu", "mlp.cu", "train.cu",
+           "scene.cu"]
 
 
 def nvcc() -> str:

@@ -1,6 +1,7 @@
 // The C ABI of libngp_gb300: descriptor decoding, buffer unpacking and status handling for every
 // entry point declared in include/ngp_gb300.h.  Buffer order follows volrendjax's lowering rules
 // (deps/volume-rendering-jax/src/volrendjax/*/lowering.py): operands, then results.
+#include <atomic>
 #include <cstdio>
 
 #include "common.cuh"
@@ -35,6 +36,8 @@ int launch_mlp_density(cudaStream_t, std::uint32_t, const float *, const float *
 int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                         const float *, const float *, const float *, float *, float *, float *, bool);
 std::size_t mlp_partials_floats();
+int launch_render_blobs(cudaStream_t, const NgpRenderBlobsDescriptor &, const float *, const float *, const float *,
+                        std::uint8_t *);
 int launch_train_rays(cudaStream_t, const NgpTrainRaysDescriptor &, const float *, const std::uint8_t *,
                       const std::uint32_t *, float *, float *, float *, float *, float *, float *, float *);
 int launch_integrate_loss_backward(cudaStream_t, const NgpIntegrateLossDescriptor &, const bool *,
@@ -60,6 +63,9 @@ __global__ void march_count_kernel(const std::uint32_t *__restrict__ next_loc, c
     *count = *next_loc - *exceeded;
 }
 }  // namespace
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_last_status(int status, const char *msg) {
     t_status = status;
@@ -114,6 +120,7 @@ extern "C" {
 int ngp_last_status(void) { return t_status; }
 const char *ngp_last_status_message(void) { return t_message; }
 int ngp_abi_version(void) { return 1; }
+unsigned long long ngp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 NGP_ENTRY(pack_density_into_bits) {
     NGP_DESC(PackbitsDescriptor, d);
@@ -176,6 +183,7 @@ NGP_ENTRY(ngp_march_count) {
     (void)opaque_len;
     NGP_CHECK_ARG(buffers != nullptr, "buffers is NULL");
     march_count_kernel<<<1, 1, 0, stream>>>(CU32(0), CU32(1), U32(2));
+    count_launches(1);
     return launch_status();
 }
 
@@ -186,7 +194,12 @@ NGP_ENTRY(ngp_hashgrid_forward) {
 
 NGP_ENTRY(ngp_hashgrid_backward) {
     NGP_DESC(NgpHashGridDescriptor, d);
-    return launch_hashgrid_backward(stream, d, CU32(2), CF32(0), CF32(1), F32(3), false);
+    return launch_hashgrid_backward(stream, d, CU32(2), CF32(0), CF32(1), F32(3), d.accumulate != 0);
+}
+
+NGP_ENTRY(ngp_render_blobs) {
+    NGP_DESC(NgpRenderBlobsDescriptor, d);
+    return launch_render_blobs(stream, d, CF32(0), CF32(1), CF32(2), U8(3));
 }
 
 NGP_ENTRY(ngp_field_forward) {

@@ -27,6 +27,9 @@ inline unsigned grid_for(std::size_t n, unsigned block, unsigned per_sm) {
     return want == 0 ? 1u : (unsigned)want;
 }
 
+// Process-wide count of kernel launches made by this library (ngp_kernel_launches()).
+void count_launches(unsigned n);
+
 // Status of the last legacy-signature call on this host thread (the legacy signatures return
 // void, as XLA custom calls do).
 void set_last_status(int status, const char *msg);

@@ -125,6 +125,7 @@ int launch_hashgrid_forward(cudaStream_t stream, const NgpHashGridDescriptor &d,
     if (items > 0) {
         hashgrid_forward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
             d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(latents), reinterpret_cast<float2 *>(enc));
+        count_launches(1);
     }
     return launch_status();
 }
@@ -141,6 +142,7 @@ int launch_hashgrid_backward(cudaStream_t stream, const NgpHashGridDescriptor &d
     if (items > 0) {
         hashgrid_backward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
             d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(dL_denc), reinterpret_cast<float2 *>(dL_dlatents));
+        count_launches(1);
     }
     return launch_status();
 }

@@ -172,6 +172,7 @@ int launch_integrate_rays(cudaStream_t stream, const IntegratingDescriptor &d,
     if (d.n_rays > 0) {
         integrate_rays_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_rays, d.total_samples, startidx, n_samples, bgs, dss, z_vals, drgbs, measured, final_rgbds, final_opacities);
+        count_launches(1);
     }
     return launch_status();
 }
@@ -191,6 +192,7 @@ int launch_integrate_rays_backward(cudaStream_t stream, const IntegratingBackwar
         integrate_rays_backward_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_rays, d.total_samples, d.near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs, final_rgbds,
             final_opacities, dL_dfinal_rgbds, dL_dbgs, dL_dz_vals, dL_ddrgbs);
+        count_launches(1);
     }
     return launch_status();
 }
@@ -207,6 +209,7 @@ int launch_integrate_rays_inference(cudaStream_t stream, const IntegratingInfere
         integrate_rays_inference_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_total_rays, d.n_rays, d.march_steps_cap, rays_bg, rays_rgbd, rays_T, n_samples,
             indices, dss, z_vals, drgbs, terminate_cnt, terminated, rgbd_out, T_out);
+        count_launches(1);
     }
     return launch_status();
 }

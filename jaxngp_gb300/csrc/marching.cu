@@ -370,10 +370,12 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
         march_rays_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
             n_exceeded, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals);
+        count_launches(1);
     }
     if (d.total_samples > 0) {
         zero_sample_tail_kernel<<<grid_for(d.total_samples, 256, 8), 256, 0, stream>>>(
             d.total_samples, next_loc, n_exceeded, idcs, xyzs, dirs, dss, z_vals);
+        count_launches(1);
     }
     return launch_status();
 }
@@ -390,23 +392,31 @@ int launch_march_rays_inference(cudaStream_t stream, const MarchingInferenceDesc
     NGP_CHECK_ARG(d.K <= 16, "march_rays_inference: at most 16 cascades");
     NGP_CHECK_ARG(d.bound > 0.f && d.stepsize_portion >= 0.f, "march_rays_inference: bound must be positive");
     copy_counter_kernel<<<1, 1, 0, stream>>>(next_ray_index_in, next_ray_index);
+    count_launches(1);
     const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
     if (d.n_rays > 0) {
         march_rays_inference_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_total_rays, d.n_rays, d.march_steps_cap, m, rays_o, rays_d, t_starts, t_ends, bits,
             terminated, indices_in, next_ray_index, indices_out, n_samples, t_starts_out, xyzs, dss,
             z_vals);
+        count_launches(1);
     }
     return launch_status();
 }
 
 int launch_morton3d(cudaStream_t stream, std::uint32_t n, const std::uint32_t *xyz, std::uint32_t *idcs) {
-    if (n > 0) morton3d_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, xyz, idcs);
+    if (n > 0) {
+        morton3d_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, xyz, idcs);
+        count_launches(1);
+    }
     return launch_status();
 }
 
 int launch_morton3d_invert(cudaStream_t stream, std::uint32_t n, const std::uint32_t *idcs, std::uint32_t *xyz) {
-    if (n > 0) morton3d_invert_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, idcs, xyz);
+    if (n > 0) {
+        morton3d_invert_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, idcs, xyz);
+        count_launches(1);
+    }
     return launch_status();
 }
 

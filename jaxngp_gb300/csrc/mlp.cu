@@ -417,6 +417,7 @@ int launch_mlp_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 2 ? tiles : (unsigned)sm_count() * 2;
     mlp_forward_kernel<<<grid, kThreads, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
+    count_launches(1);
     return launch_status();
 }
 
@@ -431,6 +432,7 @@ int launch_mlp_density(cudaStream_t stream, std::uint32_t n, const float *enc, c
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
     mlp_density_kernel<<<grid, kThreads, kDensSmem, stream>>>(n, enc, weights, sigma);
+    count_launches(1);
     return launch_status();
 }
 
@@ -448,8 +450,13 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
     }
     const unsigned grid = (unsigned)mlp_partials_count();
     mlp_backward_kernel<<<grid, kThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
+    count_launches(1);
     reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(grid, partials, dL_dweights, accumulate ? 1 : 0);
-    if (count != nullptr && n > 0) zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
+    count_launches(1);
+    if (count != nullptr && n > 0) {
+        zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
+        count_launches(1);
+    }
     return launch_status();
 }
 

@@ -44,10 +44,14 @@ int launch_packbits(cudaStream_t stream, std::uint32_t n_bytes, const float *thr
                       (scalar_threshold || ((std::uintptr_t)thr & 15u) == 0),
                   "packbits: density/threshold must be 16-byte aligned and the mask 8-byte aligned");
     const unsigned grid = grid_for(n_bytes, 256, 8);
-    if (scalar_threshold)
+    if (scalar_threshold) {
         pack_bits_kernel<true><<<grid, 256, 0, stream>>>(n_bytes, thr, density, mask, bits);
-    else
+        count_launches(1);
+    }
+    else {
         pack_bits_kernel<false><<<grid, 256, 0, stream>>>(n_bytes, thr, density, mask, bits);
+        count_launches(1);
+    }
     return launch_status();
 }
 

@@ -386,7 +386,10 @@ __global__ void ogrid_mark_untrained_kernel(std::uint32_t K, std::uint32_t G, fl
 }  // namespace
 
 int launch_ogrid_decay(cudaStream_t stream, std::uint32_t n, float decay, float *density) {
-    if (n > 0) ogrid_decay_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, decay, density);
+    if (n > 0) {
+        ogrid_decay_kernel<<<grid_for(n, 256, 8), 256, 0, stream>>>(n, decay, density);
+        count_launches(1);
+    }
     return launch_status();
 }
 
@@ -394,15 +397,20 @@ int launch_ogrid_sample(cudaStream_t stream, std::uint32_t M, bool update_all, s
                         float bound, std::uint64_t seed, const float *density, const std::uint8_t *bits,
                         std::uint32_t *cells, float *xyz) {
     NGP_CHECK_ARG(G >= 2 && G <= 1024 && (G & (G - 1)) == 0, "ogrid: G must be a power of two in [2, 1024]");
-    if (M > 0)
+    if (M > 0) {
         ogrid_sample_kernel<<<(M + 255) / 256, 256, 0, stream>>>(M, update_all ? 1u : 0u, cas, G, bound, seed, density,
                                                                 bits, cells, xyz);
+        count_launches(1);
+    }
     return launch_status();
 }
 
 int launch_ogrid_max(cudaStream_t stream, std::uint32_t M, std::uint32_t cas, std::uint32_t G3,
                      const std::uint32_t *cells, const float *sigma, float *density) {
-    if (M > 0) ogrid_max_kernel<<<(M + 255) / 256, 256, 0, stream>>>(M, cas, G3, cells, sigma, density);
+    if (M > 0) {
+        ogrid_max_kernel<<<(M + 255) / 256, 256, 0, stream>>>(M, cas, G3, cells, sigma, density);
+        count_launches(1);
+    }
     return launch_status();
 }
 
@@ -411,7 +419,9 @@ int launch_ogrid_threshold(cudaStream_t stream, std::uint32_t n_cas0, float thr_
                            float *acc, float *thr) {
     NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(float), stream));
     ogrid_mean_kernel<<<grid_for(n_cas0, 256, 4), 256, 0, stream>>>(n_cas0, density, acc);
+    count_launches(1);
     ogrid_threshold_kernel<<<1, 1, 0, stream>>>(thr_step, acc, thr);
+    count_launches(1);
     return launch_status();
 }
 
@@ -421,6 +431,7 @@ int launch_ogrid_mark_untrained(cudaStream_t stream, std::uint32_t K, std::uint3
     NGP_CHECK_ARG(G >= 2 && G <= 1024 && (G & (G - 1)) == 0 && K >= 1 && K <= 16, "ogrid: bad K or G");
     ogrid_mark_untrained_kernel<<<grid_for((std::size_t)K * G * G * G, 256, 8), 256, 0, stream>>>(
         K, G, bound, n_views, transforms, fx, fy, cx, cy, width, height, density);
+    count_launches(1);
     return launch_status();
 }
 
@@ -429,9 +440,11 @@ int launch_train_rays(cudaStream_t stream, const NgpTrainRaysDescriptor &d, cons
                       float *t_starts, float *t_ends, float *noises, float *bgs, float *gt) {
     NGP_CHECK_ARG(d.width > 0 && d.height > 0 && d.n_views > 0 && d.bound > 0.f, "train_rays: bad camera");
     NGP_CHECK_ARG(((std::uintptr_t)rgbas & 3u) == 0, "train_rays: rgbas must be 4-byte aligned");
-    if (d.n_rays > 0)
+    if (d.n_rays > 0) {
         train_rays_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(d, transforms, rgbas, perm, rays_o, rays_d,
                                                                      t_starts, t_ends, noises, bgs, gt);
+        count_launches(1);
+    }
     return launch_status();
 }
 
@@ -444,14 +457,19 @@ int launch_integrate_loss_backward(cudaStream_t stream, const NgpIntegrateLossDe
     NGP_CHECK_ARG(((std::uintptr_t)drgbs & 15u) == 0 && ((std::uintptr_t)dL_ddrgbs & 15u) == 0,
                   "integrate_loss_backward: drgbs and dL_ddrgbs must be 16-byte aligned");
     NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, 3 * sizeof(float), stream));
-    if (d.n_rays > 0)
+    if (d.n_rays > 0) {
         integrate_loss_backward_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_rays, d.total_samples, d.near_distance, d.huber_delta, valid, startidx, n_samples, bgs, gt, dss, z_vals, drgbs,
             dL_ddrgbs, acc);
-    if (d.total_samples > 0)
+        count_launches(1);
+    }
+    if (d.total_samples > 0) {
         zero_tail4_kernel<<<grid_for(d.total_samples, 256, 4), 256, 0, stream>>>(
             d.total_samples, count, reinterpret_cast<float4 *>(dL_ddrgbs));
+        count_launches(1);
+    }
     finalize_loss_kernel<<<1, 1, 0, stream>>>(acc, count, stats, grad_scale);
+    count_launches(1);
     return launch_status();
 }
 
@@ -461,7 +479,10 @@ int launch_adam(cudaStream_t stream, const NgpAdamDescriptor &d, float *p, float
                   "adam: buffers must be 16-byte aligned");
     const float bc1 = 1.f - powf(d.beta1, (float)d.step);
     const float bc2 = 1.f - powf(d.beta2, (float)d.step);
-    if (d.n > 0) adam_kernel<<<grid_for(d.n / 4 + 1, 256, 8), 256, 0, stream>>>(d, bc1, bc2, p, g, m, v);
+    if (d.n > 0) {
+        adam_kernel<<<grid_for(d.n / 4 + 1, 256, 8), 256, 0, stream>>>(d, bc1, bc2, p, g, m, v);
+        count_launches(1);
+    }
     return launch_status();
 }
 

@@ -59,7 +59,7 @@ class LevelTable:
     def n_params(self) -> int:
         return self.levels()[2][-1]
 
-    def descriptor(self, n_coords: int, bound: float) -> L.NgpHashGridDescriptor:
+    def descriptor(self, n_coords: int, bound: float, accumulate: bool = False) -> L.NgpHashGridDescriptor:
         if self.L > L.MAX_LEVELS:
             raise ValueError(f"at most {L.MAX_LEVELS} levels are supported")
         if self.F != 2:
@@ -74,6 +74,7 @@ class LevelTable:
         d.n_params = offsets[-1]
         d.bound = bound
         d.two_bound = 2 * bound
+        d.accumulate = 1 if accumulate else 0
         for i in range(self.L):
             d.scales[i] = scales[i]           # float64 -> float32, as jnp.asarray(scales, float32)
             d.resolutions[i] = res[i] & 0xFFFFFFFF
@@ -93,11 +94,13 @@ def hashgrid_forward(table: LevelTable, pos: torch.Tensor, latents: torch.Tensor
 
 
 def hashgrid_backward(table: LevelTable, pos: torch.Tensor, dL_denc: torch.Tensor, bound: float,
-                      count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+                      count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None,
+                      accumulate: bool = False) -> torch.Tensor:
     n = pos.shape[0]
     if out is None:
         out = torch.empty(table.n_params, table.F, dtype=torch.float32, device=pos.device)
-    L.call("ngp_hashgrid_backward", [pos.contiguous(), dL_denc.contiguous(), count, out], table.descriptor(n, bound))
+    L.call("ngp_hashgrid_backward", [pos.contiguous(), dL_denc.contiguous(), count, out],
+           table.descriptor(n, bound, accumulate))
     return out
 
 

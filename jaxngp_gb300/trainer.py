@@ -1,0 +1,286 @@
+"""The plain NGP training step on libngp_gb300 (the path `train_step` takes in the reference).
+
+One step (app/nerf/_utils.py:80-170 with models/renderers/cuda.py:100-162):
+    ray batch (pixel indices -> rays, near/far, jitter, background, target colour)   ngp_train_rays
+    march_rays over the occupancy bitfield                                           march_rays
+    hash-grid encoding of the samples                                                ngp_hashgrid_forward
+    density/colour MLP                                                               ngp_field_forward
+    integrate_rays + masked Huber loss + integrate_rays_backward                     ngp_integrate_loss_backward
+    MLP backward (recomputing activations)                                           ngp_field_backward
+    table-gradient scatter                                                           ngp_hashgrid_backward
+    Adam on the table and on the MLP (+ decayed weights)                             ngp_adam
+then, on the reference's cadence (utils/types.py:1378-1392), the occupancy-grid refresh
+(decay, sample, density query, max, threshold, packbits).
+
+Everything is enqueued on the current CUDA stream with preallocated buffers; a step never
+synchronises with the host (metrics stay on the device until read).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .encoders import LevelTable
+from .field import SHAPES, glorot_uniform, pack_weights
+from .scene import SceneData
+
+
+@dataclass
+class TrainConfig:
+    total_samples: int = 1 << 18       # sample budget per step (the reference's batch size)
+    n_rays: Optional[int] = None       # rays per step; the reference uses total_samples (train.py:48)
+    diagonal_n_steps: int = 1024
+    G: int = 128
+    perturb: bool = True
+    random_bg: bool = True
+    lr: float = 1e-2
+    L: int = 16
+    T: int = 1 << 19
+    N_min: int = 16
+    N_max: Optional[int] = None        # 2048 * bound (nerfs.py:322-331)
+    per_level_scale: Optional[float] = None
+    near: float = 0.3
+    huber_delta: float = 0.1
+    seed: int = 0
+
+
+def cascades_for(bound: float) -> int:
+    """SceneMeta.cascades (utils/types.py:858-860)."""
+    return max(1, int(1 + math.ceil(math.log2(bound))))
+
+
+def stepsize_portion_for(bound: float) -> float:
+    """SceneMeta.stepsize_portion (utils/types.py:874-886)."""
+    if bound >= 64:
+        return 1 / 128
+    if bound >= 16:
+        return 6e-3
+    if bound >= 4:
+        return 5e-3
+    if bound > 1:
+        return 1 / 256
+    return 0.0
+
+
+def lr_at(lr: float, count: int) -> float:
+    """optax.exponential_decay(lr, 10k, 1/3, staircase, begin 10k, end lr/100) (_utils.py:20-27)."""
+    p = math.floor(max(count - 10_000, 0) / 10_000)
+    return max(lr * (1 / 3) ** p, lr / 100)
+
+
+class NGPTrainer:
+    def __init__(self, data: SceneData, cfg: TrainConfig = TrainConfig(), device="cuda"):
+        L.require_cuda()
+        self.data, self.cfg = data, cfg
+        self.dev = torch.device(device)
+        bound = float(data.bound)
+        self.bound = bound
+        self.K = cascades_for(bound)
+        self.sp = stepsize_portion_for(bound)
+        self.R = cfg.n_rays or cfg.total_samples
+        self.S = cfg.total_samples
+        self.table = LevelTable(cfg.L, cfg.T, 2, cfg.N_min, cfg.N_max or int(2 ** 11 * bound), cfg.per_level_scale)
+        P = self.table.n_params
+        g = torch.Generator(device=self.dev)
+        g.manual_seed(cfg.seed)
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        i32 = dict(dtype=torch.int32, device=self.dev)
+        # parameters and optimiser state (_utils.py:19-77: one Adam for the field)
+        self.latents = torch.empty(P, 2, **f32).uniform_(-1e-4, 1e-4, generator=g)
+        self.weights = pack_weights({k: glorot_uniform(s, g, self.dev) for k, s in SHAPES})
+        self.g_lat = torch.zeros(P, 2, **f32)
+        self.g_w = torch.zeros(L.MLP_WEIGHTS, **f32)
+        self.m_lat, self.v_lat = torch.zeros(P, 2, **f32), torch.zeros(P, 2, **f32)
+        self.m_w, self.v_w = torch.zeros(L.MLP_WEIGHTS, **f32), torch.zeros(L.MLP_WEIGHTS, **f32)
+        # occupancy grid (OccupancyDensityGrid.create, utils/types.py:111-140)
+        G3 = cfg.G ** 3
+        self.G3 = G3
+        self.density = torch.zeros(self.K * G3, **f32)
+        self.occ_mask = torch.zeros(self.K * G3, dtype=torch.bool, device=self.dev)
+        self.bitfield = torch.full((self.K * G3 // 8,), 255, dtype=torch.uint8, device=self.dev)
+        self.threshold = torch.zeros(1, **f32)
+        self.thr_scratch = torch.zeros(2, **f32)
+        self.thr_step = 0.01 * cfg.diagonal_n_steps / (2 * min(bound, 1) * 3 ** 0.5)
+        # batch buffers
+        R, S = self.R, self.S
+        self.rays_o, self.rays_d = torch.empty(R, 3, **f32), torch.empty(R, 3, **f32)
+        self.t0, self.t1, self.noise = torch.empty(R, **f32), torch.empty(R, **f32), torch.empty(R, **f32)
+        self.bgs, self.gt = torch.empty(R, 3, **f32), torch.empty(R, 3, **f32)
+        self.counters = torch.zeros(2, **i32)
+        self.count = torch.zeros(1, **i32)
+        self.valid = torch.empty(R, dtype=torch.bool, device=self.dev)
+        self.n_samples, self.startidx = torch.empty(R, **i32), torch.empty(R, **i32)
+        self.idcs = torch.empty(S, **i32)
+        self.xyzs, self.dirs = torch.empty(S, 3, **f32), torch.empty(S, 3, **f32)
+        self.dss, self.z_vals = torch.empty(S, **f32), torch.empty(S, **f32)
+        self.enc = torch.empty(S, 32, **f32)
+        self.drgbs = torch.empty(S, 4, **f32)
+        self.g_drgbs = torch.empty(S, 4, **f32)
+        self.g_enc = torch.empty(S, 32, **f32)
+        self.stats = torch.zeros(4, **f32)
+        self.grad_scale = torch.zeros(1, **f32)
+        self.loss_scratch = torch.zeros(3, **f32)
+        self.mlp_scratch = torch.empty(L.field_backward_scratch_floats(), **f32)
+        self.step_count = 0
+        self._seed = np.random.SeedSequence(cfg.seed)
+        # descriptors that do not change between steps
+        self._d_march = L.MarchingDescriptor(R, S, cfg.diagonal_n_steps, self.K, cfg.G, bound, self.sp)
+        self._d_hg = self.table.descriptor(S, bound)
+        self._d_hg_acc = self.table.descriptor(S, bound, accumulate=True)
+        self._d_mlp = L.NgpMlpDescriptor(S, 0)
+        self._d_loss = L.NgpIntegrateLossDescriptor(R, S, data.camera.near if hasattr(data.camera, "near") else cfg.near,
+                                                    cfg.huber_delta)
+        self._n_alive = None
+        self.mark_untrained_grid()
+
+    # ---------------------------------------------------------------------------- helpers
+    def _next_seed(self) -> int:
+        return int(self._seed.spawn(1)[0].generate_state(1, np.uint64)[0])
+
+    def _ogrid_desc(self, cascade=0, n_points=0, update_all=False, seed=0) -> L.NgpOgridDescriptor:
+        c = self.data.camera
+        return L.NgpOgridDescriptor(self.K, self.cfg.G, cascade, n_points, 1 if update_all else 0, self.bound, 0.95,
+                                    self.thr_step, seed, self.data.n_views, c.width, c.height, c.fx, c.fy, c.cx, c.cy)
+
+    def mark_untrained_grid(self):
+        """utils/types.py:1241-1362 followed by the step-0 packbits with threshold -0.5."""
+        L.call("ngp_ogrid_mark_untrained", [self.data.transforms, self.density], self._ogrid_desc())
+        thr = torch.full((1,), -0.5, dtype=torch.float32, device=self.dev)
+        L.call("ngp_packbits_scalar", [thr, self.density, self.occ_mask, self.bitfield],
+               L.PackbitsDescriptor(self.K * self.G3 // 8))
+        self._n_alive = [int((self.density[c * self.G3:(c + 1) * self.G3] >= 0).sum().item()) for c in range(self.K)]
+
+    def ogrid_due(self, step: int) -> bool:
+        """NeRFState.should_call_update_ogrid (utils/types.py:1378-1388)."""
+        interval = min(16, step // 16 + 1)
+        return step > 0 and step % interval == 0
+
+    def update_ogrid(self):
+        """update_ogrid_density for every cascade (types.py:1149-1225), then threshold_ogrid
+        (types.py:1227-1239)."""
+        update_all = self.step_count < 256
+        chunk = 1 << 20
+        for cas in range(self.K):
+            M = self.G3 if update_all else max(1, self._n_alive[cas] // 2)
+            d = self._ogrid_desc(cas, M, update_all, self._next_seed())
+            L.call("ngp_ogrid_decay", [self.density], d)
+            cells = torch.empty(M, dtype=torch.int32, device=self.dev)
+            xyz = torch.empty(M, 3, dtype=torch.float32, device=self.dev)
+            L.call("ngp_ogrid_sample", [self.density, self.bitfield, cells, xyz], d)
+            sigma = torch.empty(M, dtype=torch.float32, device=self.dev)
+            for s in range(0, M, chunk):
+                n = min(chunk, M - s)
+                enc = self.enc[:n] if n <= self.S else torch.empty(n, 32, dtype=torch.float32, device=self.dev)
+                L.call("ngp_hashgrid_forward", [xyz[s:s + n], self.latents, None, enc], self.table.descriptor(n, self.bound))
+                L.call("ngp_field_density", [enc, self.weights, sigma[s:s + n]], L.NgpMlpDescriptor(n, 0))
+            L.call("ngp_ogrid_max", [cells, sigma, self.density], d)
+        L.call("ngp_ogrid_threshold", [self.density, self.thr_scratch, self.threshold], self._ogrid_desc())
+        L.call("ngp_packbits_scalar", [self.threshold, self.density, self.occ_mask, self.bitfield],
+               L.PackbitsDescriptor(self.K * self.G3 // 8))
+
+    # ------------------------------------------------------------------------------- step
+    def step(self, perm: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """One training step.  `perm`: int32 pixel indices [n_rays] on the device (as the
+        reference's `perm`), or None to draw them on the device.  Returns the device tensor
+        [loss, n_valid_rays, measured_batch_size, measured_batch_size_before_compaction]."""
+        cfg, c = self.cfg, self.data.camera
+        seed = self._next_seed()
+        d_rays = L.NgpTrainRaysDescriptor(self.R, c.width, c.height, self.data.n_views, c.fx, c.fy, c.cx, c.cy,
+                                          self.bound, int(cfg.perturb), int(cfg.random_bg), (L.c_f32 * 3)(1, 1, 1), seed)
+        L.call("ngp_train_rays", [self.data.transforms, self.data.rgbas, perm, self.rays_o, self.rays_d, self.t0,
+                                  self.t1, self.noise, self.bgs, self.gt], d_rays)
+        L.call("march_rays", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
+                              self.counters[0:1], self.counters[1:2], self.valid, self.n_samples, self.startidx,
+                              self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals], self._d_march)
+        L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
+        L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, self.count, self.enc], self._d_hg)
+        L.call("ngp_field_forward", [self.enc, self.dirs, self.weights, self.count, self.drgbs], self._d_mlp)
+        L.call("ngp_integrate_loss_backward", [self.valid, self.startidx, self.n_samples, self.bgs, self.gt, self.dss,
+                                               self.z_vals, self.drgbs, self.count, self.loss_scratch, self.g_drgbs,
+                                               self.stats, self.grad_scale], self._d_loss)
+        L.call("ngp_field_backward", [self.enc, self.dirs, self.weights, self.g_drgbs, self.count, self.grad_scale,
+                                      self.mlp_scratch, self.g_enc, self.g_w], self._d_mlp)
+        L.call("ngp_hashgrid_backward", [self.xyzs, self.g_enc, self.count, self.g_lat], self._d_hg_acc)
+        count = self.step_count
+        lr = lr_at(cfg.lr, count)
+        L.call("ngp_adam", [self.latents, self.g_lat, self.m_lat, self.v_lat],
+               L.NgpAdamDescriptor(self.latents.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 0.0, 1))
+        L.call("ngp_adam", [self.weights, self.g_w, self.m_w, self.v_w],
+               L.NgpAdamDescriptor(self.weights.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 1e-6, 1))
+        self.step_count += 1
+        if self.ogrid_due(self.step_count):
+            self.update_ogrid()
+        return self.stats
+
+    # -------------------------------------------------------------------------- rendering
+    @torch.no_grad()
+    def render_rays(self, rays_o: torch.Tensor, rays_d: torch.Tensor, bg=(1.0, 1.0, 1.0),
+                    chunk: int = 1 << 16, max_samples: int = 1 << 22) -> torch.Tensor:
+        """Colours [N, 3] of arbitrary rays (no jitter), marching in chunks."""
+        out = torch.empty(rays_o.shape[0], 3, dtype=torch.float32, device=self.dev)
+        bgt = torch.tensor(bg, dtype=torch.float32, device=self.dev)
+        for s in range(0, rays_o.shape[0], chunk):
+            o, d = rays_o[s:s + chunk].contiguous(), rays_d[s:s + chunk].contiguous()
+            n = o.shape[0]
+            t0, t1 = near_far(self.bound, o, d)
+            dm = L.MarchingDescriptor(n, max_samples, self.cfg.diagonal_n_steps, self.K, self.cfg.G, self.bound, self.sp)
+            i32 = dict(dtype=torch.int32, device=self.dev)
+            cnt, count = torch.zeros(2, **i32), torch.zeros(1, **i32)
+            valid = torch.empty(n, dtype=torch.bool, device=self.dev)
+            ns, st, idc = torch.empty(n, **i32), torch.empty(n, **i32), torch.empty(max_samples, **i32)
+            xyz = torch.empty(max_samples, 3, device=self.dev)
+            dirs = torch.empty(max_samples, 3, device=self.dev)
+            dss, zs = torch.empty(max_samples, device=self.dev), torch.empty(max_samples, device=self.dev)
+            zero = torch.zeros(n, device=self.dev)
+            L.call("march_rays", [o, d, t0, t1, zero, self.bitfield, cnt[0:1], cnt[1:2], valid, ns, st, idc, xyz, dirs,
+                                  dss, zs], dm)
+            L.call("ngp_march_count", [cnt[0:1], cnt[1:2], count])
+            enc = torch.empty(max_samples, 32, device=self.dev)
+            L.call("ngp_hashgrid_forward", [xyz, self.latents, count, enc], self.table.descriptor(max_samples, self.bound))
+            drgb = torch.zeros(max_samples, 4, device=self.dev)
+            L.call("ngp_field_forward", [enc, dirs, self.weights, count, drgb], L.NgpMlpDescriptor(max_samples, 0))
+            m = torch.empty(1, **i32)
+            rgbd = torch.empty(n, 4, device=self.dev)
+            opac = torch.empty(n, device=self.dev)
+            bgs = bgt.expand(n, 3).contiguous()
+            L.call("integrate_rays", [st, ns, bgs, dss, zs, drgb, m, rgbd, opac], L.IntegratingDescriptor(n, max_samples))
+            out[s:s + n] = rgbd[:, :3]
+        return out
+
+    @torch.no_grad()
+    def render_view(self, view: int, transforms: Optional[torch.Tensor] = None, bg=(1.0, 1.0, 1.0)) -> torch.Tensor:
+        """RGB u8 [H, W, 3] of a view (of the training poses unless `transforms` is given)."""
+        tr = self.data.transforms if transforms is None else transforms
+        o, d = camera_rays(self.data.camera, tr[view])
+        rgb = self.render_rays(o, d, bg)
+        return (rgb.clamp(0, 1) * 255).round().to(torch.uint8).view(self.data.camera.height, self.data.camera.width, 3)
+
+
+def camera_rays(cam, transform: torch.Tensor):
+    """Pixel-centre rays of one view (models/renderers/cuda.py:21-53, utils/types.py:400-439)."""
+    dev = transform.device
+    idx = torch.arange(cam.n_pixels, device=dev)
+    x = (idx % cam.width).float()
+    y = torch.div(idx, cam.width, rounding_mode="floor").float()
+    d = torch.stack([((x + 0.5) - cam.cx) / cam.fx, -(((y + 0.5) - cam.cy) / cam.fy), -torch.ones_like(x)], -1)
+    d = d / d.norm(dim=-1, keepdim=True)
+    R = transform[:9].view(3, 3)
+    d_world = (d @ R.T).contiguous()
+    o = transform[9:12].expand_as(d_world).contiguous()
+    return o, d_world
+
+
+def near_far(bound: float, o: torch.Tensor, d: torch.Tensor):
+    """make_near_far_from_bound (models/renderers/cuda.py:56-97)."""
+    eps = 1e-15
+    d = torch.where(torch.signbit(d), torch.clamp(d, max=-eps), torch.clamp(d, min=eps))
+    t0 = (-bound - o) / d
+    t1 = (bound - o) / d
+    ts = torch.maximum(torch.minimum(t0, t1).amax(-1), torch.zeros((), device=o.device))
+    te = torch.maximum(t0, t1).amin(-1)
+    return ts.contiguous(), te.contiguous()

@@ -118,3 +118,16 @@ def density_only(enc: np.ndarray, w: Dict[str, np.ndarray], dtype=np.float32) ->
     w = {k: np.asarray(v, dtype) for k, v in w.items()}
     h1 = np.maximum(np.asarray(enc, dtype) @ w["W0"], 0)
     return np.exp((h1 @ w["W1"])[:, 0])
+
+
+def kink_distance(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray]) -> np.ndarray:
+    """Per sample, the smallest |pre-activation| of the three ReLU layers relative to that layer's
+    largest |pre-activation| over the batch (FP64).  Samples near 0 sit on a ReLU kink, where
+    float32 evaluations may take either side and the gradient jumps; parity tests of gradients
+    leave them out."""
+    _, c = forward(enc, dirs, w, dtype=np.float64)
+    out = np.full(np.asarray(enc).shape[0], np.inf)
+    for k in ("a1", "a2", "a3"):
+        a = np.abs(c[k])
+        out = np.minimum(out, (a / a.max()).min(axis=1))
+    return out

@@ -4,6 +4,10 @@ Bar: encodings bit-exact against the reference's HashGridEncoder (golden fixture
 models/encoders.py) and the float32 oracle; table gradients, MLP outputs and MLP gradients within
 1e-5 relative error against the FP64 oracle, measured column-wise as
 max|gpu - fp64| / max|fp64| (atomics and matmul blocking reorder float32 sums).
+
+MLP gradients are compared on samples whose ReLU pre-activations are all at least KINK * max|a|
+away from zero: closer than that, a float32 evaluation (the reference's as much as ours) may land
+on the other side of the kink than FP64 and the gradient jumps there.
 """
 import numpy as np
 import pytest
@@ -17,6 +21,7 @@ from tests.golden_util import load
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-5
+KINK = 1e-4
 
 
 def rel_err(a, b, axis=0):
@@ -107,6 +112,9 @@ def test_field_backward_vs_fp64(n):
     dirs = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
     w = Fd.init_weights(4)
     g = rng.normal(size=(n, 4)).astype(np.float32)
+    keep = Fd.kink_distance(enc, dirs, w) > KINK
+    assert keep.mean() > 0.9
+    enc, dirs, g = enc[keep], dirs[keep], g[keep]
     _, cache = Fd.forward(enc, dirs, w, dtype=np.float64)
     denc_ref, gw_ref = Fd.backward(g, cache, w, dtype=np.float64)
     wt = pack_weights({k: torch.from_numpy(v) for k, v in w.items()}).cuda()
@@ -147,11 +155,13 @@ def test_field_module_autograd():
     d = rng.normal(size=(n, 3))
     dirs = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
     gout = rng.normal(size=(n, 4)).astype(np.float32)
-    drgb = f(cu(pos), cu(dirs))
-    (drgb * cu(gout)).sum().backward()
     tab = H.LevelTable(16, 2 ** 14, 2, 16, 2048)
     lat = f.position_encoder.latents.detach().cpu().numpy()
     w = {k: v.cpu().numpy() for k, v in unpack_weights(f.weights.detach()).items()}
+    keep = Fd.kink_distance(H.encode(pos, lat, 1.0, tab, dtype=np.float64), dirs, w) > KINK
+    pos, dirs, gout = pos[keep], dirs[keep], gout[keep]
+    drgb = f(cu(pos), cu(dirs))
+    (drgb * cu(gout)).sum().backward()
     enc64 = H.encode(pos, lat, 1.0, tab, dtype=np.float64)
     _, cache = Fd.forward(enc64, dirs, w, dtype=np.float64)
     denc, gw = Fd.backward(gout, cache, w, dtype=np.float64)
