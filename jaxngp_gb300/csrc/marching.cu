@@ -247,9 +247,10 @@ __global__ void __launch_bounds__(256) march_rays_inference_kernel(
     const bool refill = in_range && terminated[i];
     // marching.cu:300: finished slots take fresh rays, one atomic per warp, slot order in a warp
     const unsigned ballot = __ballot_sync(0xffffffffu, refill);
+    const int leader = ballot != 0 ? __ffs(ballot) - 1 : 0;  // lowest refilling lane
     std::uint32_t base = 0;
-    if (ballot != 0 && lane_id() == (unsigned)(__ffs(ballot) - 1)) base = atomicAdd(next_ray_index, (unsigned)__popc(ballot));
-    base = __shfl_sync(0xffffffffu, base, __ffs(ballot | 1u) - 1);
+    if (ballot != 0 && (int)lane_id() == leader) base = atomicAdd(next_ray_index, (unsigned)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, leader);
     if (!in_range) return;
     const std::uint32_t r = refill ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : indices_in[i];
     indices_out[i] = r;

@@ -136,6 +136,7 @@ class NGPTrainer:
         self._d_loss = L.NgpIntegrateLossDescriptor(R, S, data.camera.near if hasattr(data.camera, "near") else cfg.near,
                                                     cfg.huber_delta)
         self._n_alive = None
+        self.cadence_offset = 0   # added to step_count for the occupancy-grid cadence only
         self.mark_untrained_grid()
 
     # ---------------------------------------------------------------------------- helpers
@@ -155,6 +156,34 @@ class NGPTrainer:
                L.PackbitsDescriptor(self.K * self.G3 // 8))
         self._n_alive = [int((self.density[c * self.G3:(c + 1) * self.G3] >= 0).sum().item()) for c in range(self.K)]
 
+    @torch.no_grad()
+    def init_occupancy_analytic(self, scene=None, steady_state: bool = True):
+        """Fill the density grid from the scene's analytic density at cell centres (a stand-in for
+        a converged grid), threshold it as threshold_ogrid does, and, with `steady_state`, run the
+        grid refresh on the cadence of a run past its first 256 steps (partial updates every 16
+        steps).  Cells marked untrainable keep density -1."""
+        from .volrendjax import morton3d_invert
+        scene = scene or self.data.scene
+        G, G3 = self.cfg.G, self.G3
+        xyz = morton3d_invert(torch.arange(G3, dtype=torch.int32, device=self.dev)).float()
+        blobs = torch.from_numpy(scene.blobs).to(self.dev).double()
+        for c in range(self.K):
+            mb = min(2.0 ** c, self.bound)
+            centres = (((xyz.double() + 0.5) / G - 0.5) * 2 * mb)
+            dens = torch.zeros(G3, dtype=torch.float64, device=self.dev)
+            for s0 in range(0, G3, 1 << 18):
+                x = centres[s0:s0 + (1 << 18)]
+                r2 = ((x[:, None, :] - blobs[None, :, :3]) ** 2).sum(-1)
+                dens[s0:s0 + (1 << 18)] = (blobs[None, :, 4] * torch.exp(-r2 / (2 * blobs[None, :, 3] ** 2))).sum(-1)
+            cur = self.density[c * G3:(c + 1) * G3]
+            cur.copy_(torch.where(cur < 0, cur, dens.float()))
+        live0 = self.density[:G3][self.density[:G3] >= 0]
+        self.threshold.fill_(min(self.thr_step, float(live0.mean().item())))
+        L.call("ngp_packbits_scalar", [self.threshold, self.density, self.occ_mask, self.bitfield],
+               L.PackbitsDescriptor(self.K * self.G3 // 8))
+        if steady_state:
+            self.cadence_offset = 256
+
     def ogrid_due(self, step: int) -> bool:
         """NeRFState.should_call_update_ogrid (utils/types.py:1378-1388)."""
         interval = min(16, step // 16 + 1)
@@ -163,7 +192,7 @@ class NGPTrainer:
     def update_ogrid(self):
         """update_ogrid_density for every cascade (types.py:1149-1225), then threshold_ogrid
         (types.py:1227-1239)."""
-        update_all = self.step_count < 256
+        update_all = self.step_count + self.cadence_offset < 256
         chunk = 1 << 20
         for cas in range(self.K):
             M = self.G3 if update_all else max(1, self._n_alive[cas] // 2)
@@ -213,7 +242,7 @@ class NGPTrainer:
         L.call("ngp_adam", [self.weights, self.g_w, self.m_w, self.v_w],
                L.NgpAdamDescriptor(self.weights.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 1e-6, 1))
         self.step_count += 1
-        if self.ogrid_due(self.step_count):
+        if self.ogrid_due(self.step_count + self.cadence_offset):
             self.update_ogrid()
         return self.stats
 

@@ -231,3 +231,33 @@ def test_empty_inputs(vr):
     m, rgbd, opac = vr.integrate_rays(0.3, ei, ei, torch.zeros(0, 3, device="cuda"), e1, e1,
                                       torch.zeros(0, 4, device="cuda"))
     assert int(host(m)) == 0 and rgbd.shape == (0, 4)
+
+
+def test_march_rays_inference_multiwarp_vs_oracle(vr):
+    """Many warps, a mix of finished and running slots, several refill rounds: the set of rays in
+    flight and each ray's samples and advanced t match the oracle ray by ray."""
+    rng = np.random.default_rng(11)
+    n_total, n_slots, cap, G = 6000, 1024, 8, 64
+    o, d, t0, t1 = make_rays(rng, n_total, 1.0)
+    bits = random_bitfield(rng, 1, G, 0.15)
+    term_h = np.ones(n_slots, bool)
+    idx_h = np.zeros(n_slots, np.uint32)
+    nri_h = np.zeros(1, np.uint32)
+    t_h = t0.copy()
+    for it in range(4):
+        ref = V.march_rays_inference(1024, 1, G, cap, 1.0, 0.0, o, d, t_h, t1, bits, nri_h, term_h, idx_h)
+        r = vr.march_rays_inference(1024, 1, G, cap, 1.0, 0.0, dev(o), dev(d), dev(t_h), dev(t1), dev(bits),
+                                    dev(nri_h), dev(term_h), dev(idx_h))
+        nri, idx, ns, t_new, xyzs, dss, zs = [host(x) for x in r]
+        assert np.array_equal(nri, ref[0])
+        assert np.array_equal(t_new, ref[3])
+        assert sorted(idx.tolist()) == sorted(ref[1].tolist())
+        pos = {int(v): s for s, v in enumerate(ref[1])}
+        for s, v in enumerate(idx):
+            q = pos[int(v)]
+            assert ns[s] == ref[2][q]
+            assert np.array_equal(xyzs[s], ref[4][q]) and np.array_equal(zs[s], ref[6][q])
+        # follow the oracle's state into the next round
+        term_h = ref[2] < cap
+        term_h[rng.uniform(size=n_slots) < 0.2] = True
+        idx_h, nri_h, t_h = ref[1], ref[0], ref[3]
