@@ -34,8 +34,8 @@ WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 f
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=50)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--pretrain", type=int, default=300, help="untimed training steps before warm-up")
     p.add_argument("--samples", type=int, default=1 << 18)
@@ -62,7 +62,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -203,16 +203,17 @@ def run_ours(args) -> dict:
     tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
         tr.step()
-    for _ in range(args.warmup):
-        tr.step()
     torch.cuda.synchronize()
 
     # ---- timed region: device-resident inputs (pixel indices drawn on the device)
     acc = torch.zeros(4, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches0 = L.lib().ngp_kernel_launches()
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):   # warm-up runs while the clock sampler starts
+            tr.step()
+        torch.cuda.synchronize()
+        launches0 = L.lib().ngp_kernel_launches()
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()

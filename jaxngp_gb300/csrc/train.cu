@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256) integrate_loss_backward_kernel(
         std::uint32_t k = 0;
         for (; T > kTThreshold && k < n; ++k) {
             const float4 c = rc[k];
-            const float alpha = 1.f - __expf(-c.x * rd[k]);
+            const float alpha = 1.f - expf(-c.x * rd[k]);
             const float w = T * alpha;
             r += w * c.y;
             g += w * c.z;
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) integrate_loss_backward_kernel(
         for (k = 0; T > kTThreshold && k < n; ++k) {
             const float4 c = rc[k];
             const float z = rz[k], dt = rd[k];
-            const float alpha = 1.f - __expf(-c.x * dt);
+            const float alpha = 1.f - expf(-c.x * dt);
             const float w = T * alpha;
             cr += w * c.y;
             cg += w * c.z;
