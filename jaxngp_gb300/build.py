@@ -19,9 +19,10 @@ LIB = os.path.join(HERE, "libngp_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
                  "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-# Per-file flags.  The marcher is compiled without multiply-add contraction so that its float
-# arithmetic is the reference's, one rounding per operation.
-EXTRA = {"marching.cu": ["--fmad=false"]}
+# Per-file flags.  The marcher and the integrators are compiled without multiply-add contraction
+# so that their float arithmetic is the reference's source arithmetic, one rounding per operation
+# (sample counts and early-termination steps then agree exactly with the reference built that way).
+EXTRA = {"marching.cu": ["--fmad=false"], "integrating.cu": ["--fmad=false"], "train.cu": ["--fmad=false"]}
 SOURCES = ["abi.cu", "marching.cu", "integrating.cu", "packbits.cu", "hashgrid.cu", "mlp.cu", "train.cu",
            "scene.cu"]
 
