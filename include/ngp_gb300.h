@@ -219,6 +219,23 @@ void ngp_field_backward(cudaStream_t stream, void **buffers, const char *opaque,
 int ngp_field_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 size_t ngp_field_backward_scratch_floats(void);
 
+/* No counterpart in the reference.  ngp_field_backward for callers that cannot allocate device
+ * memory: an XLA custom call bound through the legacy signature receives only its operand and
+ * result buffers, and an embedder running inside a fixed, pre-reserved memory budget may not call
+ * cudaMalloc or any allocating library routine.  The per-CTA dL/dW partials live in a static
+ * array inside the library (9.6 MB, held by every GPU that loads the library until exit) instead
+ * of a caller-provided scratch buffer, so the batch is bounded by
+ * NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES; larger batches return NGP_ERR_CAPACITY.  The first call
+ * on each device looks up the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU (different
+ * streams) race on it and must be ordered by the caller.  Nothing has to be cleared between calls.
+ * buffers: encodings f32[S,32], dirs f32[S,3], weights f32[9408], dL_ddrgbs f32[S,4],
+ * active_count u32[1] or NULL, grad_scale f32[1] or NULL -> dL_dencodings f32[S,32],
+ * dL_dweights f32[9408].  opaque: NgpMlpDescriptor. */
+#define NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES 524288
+void ngp_field_backward_noalloc(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_backward_noalloc_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* --------------------------------------------------------------- training-step kernels */
 /* Camera of the training set: pinhole intrinsics plus one 3x4 camera-to-world matrix per view
  * (utils/types.py Camera; app/nerf/_utils.py:97-115 builds rays from them). */

@@ -36,6 +36,8 @@ int launch_mlp_density(cudaStream_t, std::uint32_t, const float *, const float *
 int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                         const float *, const float *, const float *, float *, float *, float *, bool);
 std::size_t mlp_partials_floats();
+int launch_mlp_backward_noalloc(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                                const float *, const float *, const float *, float *, float *, bool);
 int launch_render_blobs(cudaStream_t, const NgpRenderBlobsDescriptor &, const float *, const float *, const float *,
                         std::uint8_t *);
 int launch_train_rays(cudaStream_t, const NgpTrainRaysDescriptor &, const float *, const std::uint8_t *,
@@ -219,6 +221,12 @@ NGP_ENTRY(ngp_field_backward) {
 }
 
 size_t ngp_field_backward_scratch_floats(void) { return mlp_partials_floats(); }
+
+NGP_ENTRY(ngp_field_backward_noalloc) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_mlp_backward_noalloc(stream, d.n_samples, CU32(4), CF32(0), CF32(1), CF32(2), CF32(3), CF32(5),
+                                       F32(6), F32(7), d.accumulate != 0);
+}
 
 NGP_ENTRY(ngp_train_rays) {
     NGP_DESC(NgpTrainRaysDescriptor, d);

@@ -21,6 +21,8 @@
 // accumulates each thread's share of dL/dW in registers across all its tiles, and writes one
 // partial per CTA; a second kernel sums the partials in a fixed order, so weight gradients are
 // deterministic.  FP32 throughout (the parity path); the BF16 tensor-core path is separate.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace ngp {
@@ -400,6 +402,23 @@ constexpr std::size_t kDensSmem = (std::size_t)(kNW + 3 * kTile * kLd) * sizeof(
 
 }  // namespace
 
+// ------------------------------------------------------------- allocation-free backward
+//
+// ngp_field_backward needs one dL/dW partial per CTA in a caller-provided scratch buffer.  Callers
+// that cannot allocate device memory -- an XLA custom call bound through the legacy signature
+// receives only its operand and result buffers, and embedders that run with a fixed,
+// pre-reserved memory budget may not call cudaMalloc or any allocating library routine -- use
+// ngp_field_backward_noalloc instead, whose partials live in the array below.  Every CTA owns a
+// fixed span of kNoAllocSamplesPerPart samples, so the number of partials, and therefore the
+// batch, is bounded: at most kNoAllocMaxParts * kNoAllocSamplesPerPart = 524288 samples, and the
+// array is 256 * 9408 floats = 9.6 MB, held by every GPU that loads the library until the process
+// exits.  Each call overwrites every partial it later reads, so nothing has to be cleared between
+// calls; but all calls share the one array, so calls that overlap on the GPU (on different
+// streams) race on it and must be ordered by the caller.
+constexpr std::uint32_t kNoAllocSamplesPerPart = 2048;
+constexpr std::uint32_t kNoAllocMaxParts = 256;
+__device__ __align__(256) float g_noalloc_partials[kNoAllocMaxParts * kNW];
+
 int mlp_partials_count() { return sm_count(); }
 std::size_t mlp_partials_floats() { return (std::size_t)mlp_partials_count() * kNW; }
 
@@ -452,6 +471,60 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
     mlp_backward_kernel<<<grid, kThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
     count_launches(1);
     reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(grid, partials, dL_dweights, accumulate ? 1 : 0);
+    count_launches(1);
+    if (count != nullptr && n > 0) {
+        zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+// Device address of g_noalloc_partials on the current device, looked up once per device (the
+// array's host-side name is only a stand-in and must never be handed to a kernel).
+static int noalloc_scratch(float **out) {
+    static std::mutex mu;
+    static float *ptrs[64] = {nullptr};
+    int dev = 0;
+    NGP_CUDA_TRY(cudaGetDevice(&dev));
+    NGP_CHECK_ARG(dev >= 0 && dev < 64, "field backward (no-alloc): device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (ptrs[dev] == nullptr) {
+        void *p = nullptr;
+        NGP_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+        ptrs[dev] = static_cast<float *>(p);
+    }
+    *out = ptrs[dev];
+    return NGP_OK;
+}
+
+int launch_mlp_backward_noalloc(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
+                                const float *enc, const float *dirs, const float *weights,
+                                const float *dL_ddrgb, const float *grad_scale, float *dL_denc,
+                                float *dL_dweights, bool accumulate) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc),
+                  "mlp: buffers must be 16-byte aligned");
+    const std::uint64_t parts = ((std::uint64_t)n + kNoAllocSamplesPerPart - 1) / kNoAllocSamplesPerPart;
+    if (parts > kNoAllocMaxParts) {
+        set_last_status(NGP_ERR_CAPACITY,
+                        "ngp_field_backward_noalloc: n_samples exceeds 524288, the capacity of its static scratch; "
+                        "use ngp_field_backward with a caller-provided scratch buffer");
+        return NGP_ERR_CAPACITY;
+    }
+    float *scratch = nullptr;
+    int st = noalloc_scratch(&scratch);
+    if (st != NGP_OK) return st;
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        attr = true;
+    }
+    if (parts > 0) {
+        mlp_backward_kernel<<<(unsigned)parts, kThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
+                                                                             grad_scale, dL_denc, scratch);
+        count_launches(1);
+    }
+    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>((std::uint32_t)parts, scratch, dL_dweights,
+                                                                  accumulate ? 1 : 0);
     count_launches(1);
     if (count != nullptr && n > 0) {
         zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
