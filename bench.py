@@ -315,6 +315,7 @@ def run_ours(args) -> dict:
                       "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,
                       "occupancy_init": "analytic scene density, then learned updates",
                       "mean_samples_per_step": round(samples_used, 1),
+                      "mean_composited_samples_per_step": round(float(a[2]) / args.steps, 1),
                       "mean_samples_per_valid_ray": round(samples_used / max(rays / args.steps, 1), 2),
                       "valid_rays_per_step": round(rays / args.steps, 1),
                       "l2": "per-step working set (table 46.5 MB + 2^18-sample buffers ~70 MB) is touched once per step; "

@@ -120,6 +120,26 @@ int march_rays_status(cudaStream_t stream, void **buffers, const char *opaque, s
 void march_rays_inference(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int march_rays_inference_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* march_rays_inference for a device-resident render loop (the host loop of
+ * models/renderers/cuda.py:326-361 without its per-iteration synchronisation): slot indices and the
+ * next-ray counter are updated in place, the advanced t is written straight into t_starts (the
+ * scatter of marching/__init__.py:156), and every sample also receives its ray's direction.
+ * buffers: rays_o f32[N,3], rays_d f32[N,3], t_starts f32[N] (in/out), t_ends f32[N],
+ * occupancy_bitfield u8[K*G^3/8], terminated bool[n], indices u32[n] (in/out),
+ * next_ray_index u32[1] (in/out) -> n_samples u32[n], xyzs f32[n,cap,3], dirs f32[n,cap,3],
+ * dss f32[n,cap], z_vals f32[n,cap].  opaque: MarchingInferenceDescriptor. */
+void ngp_march_rays_inference_inplace(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_march_rays_inference_inplace_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* integrate_rays_inference for a device-resident render loop: each slot continues its ray directly
+ * in rays_rgbd / rays_T (the scatter of integrating/__init__.py:108-109), and the number of rays
+ * that terminated is added to terminate_total (not reset), so the host polls it only now and then.
+ * buffers: rays_bg f32[N,3], rays_rgbd f32[N,4] (in/out), rays_T f32[N] (in/out), n_samples u32[n],
+ * indices u32[n], dss f32[n,cap], z_vals f32[n,cap], drgbs f32[n,cap,4], terminate_total u32[1]
+ * (in/out) -> terminated bool[n].  opaque: IntegratingInferenceDescriptor. */
+void ngp_integrate_rays_inference_inplace(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_integrate_rays_inference_inplace_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* Replaces volrendjax::morton3d (volrend.h:143-148; marching.cu:687-694).
  * buffers: xyzs u32[N,3] -> idcs u32[N]; opaque: Morton3DDescriptor. */
 void morton3d(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
@@ -151,6 +171,16 @@ int integrate_rays_backward_status(cudaStream_t stream, void **buffers, const ch
  * opaque: IntegratingInferenceDescriptor. */
 void integrate_rays_inference(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int integrate_rays_inference_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* march_rays for the training step: the same per-ray outputs as march_rays for every ray that
+ * fits the sample budget, with every sample-less ray valid and every ray that does not fit
+ * invalid; but a ray that meets its first occupied sample after the budget is full stops there
+ * (it could only overflow) and is left out of both counters, whose difference -- the samples
+ * written -- stays exact.  Rays are taken from a work queue in index order.
+ * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call).
+ * opaque: MarchingDescriptor. */
+void ngp_march_rays_train(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_march_rays_train_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
 /* march_rays' measured_batch_size_before_compaction on the device (marching/__init__.py:91):
  * buffers: next_sample_write_location u32[1], number_of_exceeded_samples u32[1] -> count u32[1].

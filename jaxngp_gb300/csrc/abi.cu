@@ -10,11 +10,18 @@ namespace ngp {
 
 int launch_march_rays(cudaStream_t, const MarchingDescriptor &, const float *, const float *, const float *,
                       const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *,
-                      bool *, std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, float *, float *);
+                      bool *, std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, float *, float *,
+                      std::uint32_t *, bool);
 int launch_march_rays_inference(cudaStream_t, const MarchingInferenceDescriptor &, const float *, const float *,
                                 const float *, const float *, const std::uint8_t *, const std::uint32_t *,
                                 const bool *, const std::uint32_t *, std::uint32_t *, std::uint32_t *,
                                 std::uint32_t *, float *, float *, float *, float *);
+int launch_march_rays_inference_inplace(cudaStream_t, const MarchingInferenceDescriptor &, const float *, const float *,
+                                        float *, const float *, const std::uint8_t *, const bool *, std::uint32_t *,
+                                        std::uint32_t *, std::uint32_t *, float *, float *, float *, float *);
+int launch_integrate_rays_inference_inplace(cudaStream_t, const IntegratingInferenceDescriptor &, const float *, float *,
+                                            float *, const std::uint32_t *, const std::uint32_t *, const float *,
+                                            const float *, const float *, std::uint32_t *, bool *);
 int launch_morton3d(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t *);
 int launch_morton3d_invert(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t *);
 int launch_integrate_rays(cudaStream_t, const IntegratingDescriptor &, const std::uint32_t *, const std::uint32_t *,
@@ -137,13 +144,32 @@ NGP_ENTRY(ngp_packbits_scalar) {
 NGP_ENTRY(march_rays) {
     NGP_DESC(MarchingDescriptor, d);
     return launch_march_rays(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
-                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15));
+                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), nullptr, false);
+}
+
+NGP_ENTRY(ngp_march_rays_train) {
+    NGP_DESC(MarchingDescriptor, d);
+    NGP_CHECK_ARG(buffers[16] != nullptr, "ngp_march_rays_train: the queue counter (buffer 16) is required");
+    return launch_march_rays(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
+                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), U32(16), true);
 }
 
 NGP_ENTRY(march_rays_inference) {
     NGP_DESC(MarchingInferenceDescriptor, d);
     return launch_march_rays_inference(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CU8(4), CU32(5), CB8(6),
                                        CU32(7), U32(8), U32(9), U32(10), F32(11), F32(12), F32(13), F32(14));
+}
+
+NGP_ENTRY(ngp_march_rays_inference_inplace) {
+    NGP_DESC(MarchingInferenceDescriptor, d);
+    return launch_march_rays_inference_inplace(stream, d, CF32(0), CF32(1), F32(2), CF32(3), CU8(4), CB8(5), U32(6),
+                                               U32(7), U32(8), F32(9), F32(10), F32(11), F32(12));
+}
+
+NGP_ENTRY(ngp_integrate_rays_inference_inplace) {
+    NGP_DESC(IntegratingInferenceDescriptor, d);
+    return launch_integrate_rays_inference_inplace(stream, d, CF32(0), F32(1), F32(2), CU32(3), CU32(4), CF32(5),
+                                                   CF32(6), CF32(7), U32(8), B8(9));
 }
 
 NGP_ENTRY(morton3d) {

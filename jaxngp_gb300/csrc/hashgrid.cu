@@ -83,23 +83,65 @@ __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
     }
 }
 
-// dL/dlatents[idx_k] += w_k * dL/denc[n, l]: the transpose of the gather.  Levels whose incoming
-// gradient is exactly zero (samples past a ray's termination) issue no atomics.
+// dL/dlatents[idx_k] += w_k * dL/denc[n, l]: the transpose of the gather.
+//
+// A warp takes 32 consecutive points at one level.  Consecutive points of a training batch walk
+// along one ray, so at coarse levels runs of lanes share a corner; those runs are summed with a
+// segmented warp reduction and their last lane issues the one float2 atomic for the run.  Levels
+// where no two neighbouring lanes share a corner issue one atomic per lane.  Points whose incoming
+// gradient is zero at that level (samples past a ray's termination) contribute nothing.
 __global__ void __launch_bounds__(256) hashgrid_backward_kernel(
     NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
     const float *__restrict__ pos, const float2 *__restrict__ dL_denc, float2 *__restrict__ dL_dlat) {
     std::uint32_t n_active = n_points;
     if (count != nullptr) n_active = min(n_active, *count);
-    const std::size_t total = (std::size_t)n_active * d.L;
-    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
-    for (std::size_t t = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        const float2 g = dL_denc[t];
-        if (g.x == 0.f && g.y == 0.f) continue;
-        const std::uint32_t n = (std::uint32_t)(t / d.L), l = (std::uint32_t)(t % d.L);
+    const unsigned lane = lane_id();
+    const std::size_t n_groups = (std::size_t)((n_active + 31) / 32) * d.L;   // (32 points, level) per warp
+    const std::size_t warp0 = ((std::size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const std::size_t n_warps = ((std::size_t)gridDim.x * blockDim.x) >> 5;
+    for (std::size_t wg = warp0; wg < n_groups; wg += n_warps) {
+        const std::uint32_t l = (std::uint32_t)(wg % d.L);
+        const std::uint32_t n = (std::uint32_t)(wg / d.L) * 32u + lane;
+        const bool in = n < n_active;
+        float2 g = make_float2(0.f, 0.f);
         Corner8 c;
-        level_corners(d, l, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
+        if (in) {
+            g = dL_denc[(std::size_t)n * d.L + l];
+            level_corners(d, l, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
+        } else {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) atomicAdd(dL_dlat + c.idx[k], make_float2(c.w[k] * g.x, c.w[k] * g.y));
+            for (int k = 0; k < 8; ++k) {
+                c.idx[k] = 0xFFFFFFFFu;
+                c.w[k] = 0.f;
+            }
+        }
+        const bool live = in && (g.x != 0.f || g.y != 0.f);
+        if (__ballot_sync(0xffffffffu, live) == 0u) continue;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const std::uint32_t idx = live ? c.idx[k] : 0xFFFFFFFFu;
+            float vx = live ? c.w[k] * g.x : 0.f, vy = live ? c.w[k] * g.y : 0.f;
+            const std::uint32_t prev = __shfl_up_sync(0xffffffffu, idx, 1);
+            const bool head = lane == 0 || idx != prev;
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            if (heads == 0xffffffffu) {  // no two neighbours share this corner
+                if (live) atomicAdd(dL_dlat + idx, make_float2(vx, vy));
+                continue;
+            }
+            // segmented inclusive sum over runs of equal indices (runs start at head lanes)
+            const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float tx = __shfl_up_sync(0xffffffffu, vx, o);
+                const float ty = __shfl_up_sync(0xffffffffu, vy, o);
+                if ((int)lane - o >= seg_start) {
+                    vx += tx;
+                    vy += ty;
+                }
+            }
+            const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+            if (tail && idx != 0xFFFFFFFFu) atomicAdd(dL_dlat + idx, make_float2(vx, vy));
+        }
     }
 }
 
@@ -138,7 +180,7 @@ int launch_hashgrid_backward(cudaStream_t stream, const NgpHashGridDescriptor &d
     NGP_CHECK_ARG(((std::uintptr_t)dL_denc & 7u) == 0 && ((std::uintptr_t)dL_dlatents & 7u) == 0,
                   "hashgrid: gradients must be 8-byte aligned");
     if (!accumulate) NGP_CUDA_TRY(cudaMemsetAsync(dL_dlatents, 0, (std::size_t)d.n_params * 2 * sizeof(float), stream));
-    const std::size_t items = (std::size_t)d.n_coords * d.L;
+    const std::size_t items = (std::size_t)((d.n_coords + 31) / 32) * 32 * d.L;
     if (items > 0) {
         hashgrid_backward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
             d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(dL_denc), reinterpret_cast<float2 *>(dL_dlatents));

@@ -165,6 +165,58 @@ __global__ void __launch_bounds__(256) integrate_rays_inference_kernel(
     if (lane_id() == 0 && cnt > 0) atomicAdd(terminate_cnt, cnt);
 }
 
+// In-place form for the device-resident renderer: each slot continues its ray straight in the
+// full-frame arrays (what integrating/__init__.py:108-109 does with .at[].set), and the number of
+// terminated rays is added to a running total instead of reset, so the host can poll it rarely.
+__global__ void __launch_bounds__(256) integrate_rays_inference_inplace_kernel(
+    std::uint32_t n_total_rays, std::uint32_t n_rays, std::uint32_t cap,
+    const float *__restrict__ rays_bg, float *__restrict__ rays_rgbd, float *__restrict__ rays_T,
+    const std::uint32_t *__restrict__ n_samples, const std::uint32_t *__restrict__ indices,
+    const float *__restrict__ dss, const float *__restrict__ z_vals, const float *__restrict__ drgbs,
+    std::uint32_t *__restrict__ terminate_total, bool *__restrict__ terminated) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool term = false;
+    if (i < n_rays) {
+        const std::uint32_t n = min(n_samples[i], cap), r = indices[i];
+        if (r < n_total_rays) {
+            const float *rd = dss + (std::size_t)i * cap, *rz = z_vals + (std::size_t)i * cap;
+            const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + (std::size_t)i * cap;
+            float T = rays_T[r];
+            const float4 acc = reinterpret_cast<const float4 *>(rays_rgbd)[r];
+            float cr = acc.x, cg = acc.y, cb = acc.z, cd = acc.w;
+            for (std::uint32_t k = 0; T > kTThreshold && k < n; ++k) {
+                const float4 c = rc[k];
+                const float alpha = 1.f - expf(-c.x * rd[k]);
+                const float w = T * alpha;
+                cr += w * c.y;
+                cg += w * c.z;
+                cb += w * c.w;
+                cd += w * rz[k];
+                T *= (1.f - alpha);
+            }
+            float4 out;
+            float Tw;
+            if (T <= kTThreshold) {
+                const float id = 1.f / (1.f - T);
+                term = true;
+                Tw = 0.f;
+                out = make_float4(cr * id, cg * id, cb * id, cd * id);
+            } else {
+                term = n < cap;
+                Tw = T;
+                out = term ? make_float4(cr + T * rays_bg[(std::size_t)r * 3 + 0], cg + T * rays_bg[(std::size_t)r * 3 + 1],
+                                         cb + T * rays_bg[(std::size_t)r * 3 + 2], cd)
+                           : make_float4(cr, cg, cb, cd);
+            }
+            reinterpret_cast<float4 *>(rays_rgbd)[r] = out;
+            rays_T[r] = Tw;
+        }
+        terminated[i] = term;
+    }
+    const std::uint32_t cnt = warp_sum(term ? 1u : 0u);
+    if (lane_id() == 0 && cnt > 0) atomicAdd(terminate_total, cnt);
+}
+
 }  // namespace
 
 int launch_integrate_rays(cudaStream_t stream, const IntegratingDescriptor &d,
@@ -218,4 +270,22 @@ int launch_integrate_rays_inference(cudaStream_t stream, const IntegratingInfere
     return launch_status();
 }
 
+}  // namespace ngp
+
+namespace ngp {
+int launch_integrate_rays_inference_inplace(cudaStream_t stream, const IntegratingInferenceDescriptor &d,
+                                            const float *rays_bg, float *rays_rgbd, float *rays_T,
+                                            const std::uint32_t *n_samples, const std::uint32_t *indices,
+                                            const float *dss, const float *z_vals, const float *drgbs,
+                                            std::uint32_t *terminate_total, bool *terminated) {
+    NGP_CHECK_ARG(((std::uintptr_t)rays_rgbd & 15u) == 0 && ((std::uintptr_t)drgbs & 15u) == 0,
+                  "integrate_rays_inference: rays_rgbd and drgbs must be 16-byte aligned");
+    if (d.n_rays > 0) {
+        integrate_rays_inference_inplace_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
+            d.n_total_rays, d.n_rays, d.march_steps_cap, rays_bg, rays_rgbd, rays_T, n_samples, indices, dss, z_vals,
+            drgbs, terminate_total, terminated);
+        count_launches(1);
+    }
+    return launch_status();
+}
 }  // namespace ngp

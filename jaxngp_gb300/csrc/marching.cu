@@ -25,9 +25,10 @@ struct V3 {
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
-// marching.cu:15-23
-__device__ __forceinline__ float calc_ds(float t, float sp, float bound, float inv_G, std::uint32_t dns) {
-    return clampf(t * sp, 2.0f * kSqrt3 * fminf(bound, 1.0f) / (float)dns, 2.0f * kSqrt3 * bound * inv_G);
+// marching.cu:15-23.  The clamp bounds do not depend on t: MarchParams holds them, computed once
+// with the same float operations (so every ds is bit-identical to evaluating them per call).
+__device__ __forceinline__ float calc_ds_bounds(float t, float sp, float ds_lo, float ds_hi) {
+    return clampf(t * sp, ds_lo, ds_hi);
 }
 
 // marching.cu:25-39
@@ -67,7 +68,14 @@ __device__ __forceinline__ std::uint32_t morton3_invert(std::uint32_t x) {
 struct MarchParams {
     std::uint32_t dns, K, G;
     float bound, sp, inv_G;
+    float ds_lo, ds_hi;   // calc_ds clamp bounds: 2 sqrt3 min(bound,1) / dns and 2 sqrt3 bound / G
 };
+
+__device__ __forceinline__ float calc_ds(float t, const MarchParams &m) { return calc_ds_bounds(t, m.sp, m.ds_lo, m.ds_hi); }
+
+// x / mb where mb = min(2^cascade, bound).  When mb is a power of two the quotient is the product
+// with its exact reciprocal, bit for bit (both are the exact value rounded once); otherwise divide.
+__device__ __forceinline__ float div_mb(float x, float mb, float inv_mb, bool pow2) { return pow2 ? x * inv_mb : x / mb; }
 
 // Loop caps.  A ray whose t_end is infinite (or so large that t + ds rounds back to t) would
 // march forever; valid rays stay far below these caps (samples <= diagonal_n_steps * bound, empty
@@ -82,10 +90,12 @@ __device__ __forceinline__ bool occupied_at(const MarchParams &m, V3 pos, float 
     std::uint32_t c0 = mip_from_xyz(pos, m.K), c1 = mip_from_ds(ds, m.G, m.K);
     std::uint32_t cascade = c0 > c1 ? c0 : c1;
     mb = fminf(scalbnf(1.0f, (int)cascade), m.bound);
+    const bool pow2 = (__float_as_uint(mb) & 0x007FFFFFu) == 0u && mb >= 1.17549435e-38f;
+    const float inv_mb = pow2 ? __uint_as_float(0x7F000000u - __float_as_uint(mb)) : 0.f;  // 2^-e for mb = 2^e
     float Gf = (float)m.G;
-    g.x = ((pos.x / mb + 1.0f) * 0.5f) * Gf;
-    g.y = ((pos.y / mb + 1.0f) * 0.5f) * Gf;
-    g.z = ((pos.z / mb + 1.0f) * 0.5f) * Gf;
+    g.x = ((div_mb(pos.x, mb, inv_mb, pow2) + 1.0f) * 0.5f) * Gf;
+    g.y = ((div_mb(pos.y, mb, inv_mb, pow2) + 1.0f) * 0.5f) * Gf;
+    g.z = ((div_mb(pos.z, mb, inv_mb, pow2) + 1.0f) * 0.5f) * Gf;
     int Gi = (int)m.G - 1;
     std::uint32_t gx = (std::uint32_t)clampi((int)floorf(g.x), 0, Gi);
     std::uint32_t gy = (std::uint32_t)clampi((int)floorf(g.y), 0, Gi);
@@ -97,7 +107,7 @@ __device__ __forceinline__ bool occupied_at(const MarchParams &m, V3 pos, float 
 // marching.cu:182-189: advance past the empty voxel in whole steps.
 __device__ __forceinline__ float skip_empty(const MarchParams &m, float t, V3 g, float mb, V3 pos,
                                             V3 d, V3 inv_d) {
-    float nt = t + calc_ds(t, m.sp, m.bound, m.inv_G, m.dns);
+    float nt = t + calc_ds(t, m);
     float nx = floorf((g.x + 0.5f) + 0.5f * copysignf(1.0f, d.x));
     float ny = floorf((g.y + 0.5f) + 0.5f * copysignf(1.0f, d.y));
     float nz = floorf((g.z + 0.5f) + 0.5f * copysignf(1.0f, d.z));
@@ -105,7 +115,7 @@ __device__ __forceinline__ float skip_empty(const MarchParams &m, float t, V3 g,
     float dy = (((ny * m.inv_G - 0.5f) * 2.0f) * mb - pos.y) * inv_d.y;
     float dz = (((nz * m.inv_G - 0.5f) * 2.0f) * mb - pos.z) * inv_d.z;
     float next_t = t + fmaxf(0.0f, fminf(dx, fminf(dy, dz)));
-    for (std::uint32_t it = 0; nt < next_t && it < kMaxSkipIters; ++it) nt += calc_ds(nt, m.sp, m.bound, m.inv_G, m.dns);
+    for (std::uint32_t it = 0; nt < next_t && it < kMaxSkipIters; ++it) nt += calc_ds(nt, m);
     return nt;
 }
 
@@ -113,96 +123,178 @@ __device__ __forceinline__ V3 at(V3 o, V3 d, float t) { return {o.x + t * d.x, o
 
 // ------------------------------------------------------------------------------- march_rays
 
-// One thread per ray.  Pass 1 counts the ray's samples; the warp then allocates one contiguous
-// slot range with a single atomic; pass 2 re-marches the ray writing its samples.
-__global__ void __launch_bounds__(256) march_rays_kernel(
+constexpr int kMarchBlock = 128;
+constexpr int kMarchBlocksPerSm = 6;
+
+enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
+
+// Marches rays with lane refill: every lane of a warp carries one ray and advances it by one
+// march iteration per trip of the loop; a lane whose ray is finished takes the next ray at once,
+// so a warp keeps all 32 lanes busy until the rays run out (one thread per ray, as in the
+// reference, leaves most lanes of a warp idle behind the warp's longest ray).
+//
+// Rays come from a global queue counter when `queue` is given, else from a fixed interleaving:
+// warp w takes 32-ray chunks w, w + n_warps, w + 2 n_warps, ...
+//
+// Per ray the arithmetic and the two passes (count, then write) are the reference's
+// (marching.cu:162-192, :224-267).  Slots are allocated once per trip for all lanes that finished
+// counting in it (one atomic).  A ray with no sample is valid (marching.cu:196-199); a ray that
+// does not fit the budget is not (:206-209).  The reference also drops a ray whose thread starts
+// after the buffer filled (:135), which only happens when its grid does not fit on the GPU at
+// once; here every ray is treated as started before that.
+//
+// kProbe (training): a ray that finds the sample budget already full while counting (checked at
+// its first occupied sample and every 16 after) stops there -- it can only overflow -- and adds
+// nothing to the counters, so
+// next_sample_write_location - number_of_exceeded_samples (the samples written) is exact while
+// the two counters themselves leave out such rays.
+template <bool kProbe>
+__global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
     std::uint32_t n_rays, std::uint32_t total_samples, MarchParams m,
     const float *__restrict__ rays_o, const float *__restrict__ rays_d,
     const float *__restrict__ t_starts, const float *__restrict__ t_ends,
     const float *__restrict__ noises, const std::uint8_t *__restrict__ bits,
     std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded,
-    bool *__restrict__ ray_is_valid, std::uint32_t *__restrict__ rays_n_samples,
-    std::uint32_t *__restrict__ rays_startidx, std::uint32_t *__restrict__ idcs,
-    float *__restrict__ xyzs, float *__restrict__ dirs, float *__restrict__ dss,
-    float *__restrict__ z_vals) {
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in_range = i < n_rays;
-    // marching.cu:135: a ray that starts after the sample buffer filled up is dropped.
-    bool live = in_range && *((volatile std::uint32_t *)next_loc) < total_samples;
-    V3 o{0, 0, 0}, d{1, 1, 1};
-    float t0 = 0.f, t1 = 0.f, noise = 0.f;
-    if (live) {
-        o = {rays_o[i * 3 + 0], rays_o[i * 3 + 1], rays_o[i * 3 + 2]};
-        d = {rays_d[i * 3 + 0], rays_d[i * 3 + 1], rays_d[i * 3 + 2]};
-        t0 = t_starts[i];
-        t1 = t_ends[i];
-        noise = noises[i];
-        live = t1 > t0;  // marching.cu:151
-    }
-    const V3 inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-    const float t_first = t0 + calc_ds(t0, m.sp, m.bound, m.inv_G, m.dns) * noise;
+    std::uint32_t *__restrict__ queue, bool *__restrict__ ray_is_valid,
+    std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
+    std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
+    float *__restrict__ dss, float *__restrict__ z_vals) {
+    const unsigned lane = lane_id();
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const std::uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const std::uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    const float n_cap = (float)m.dns * m.bound;
 
-    std::uint32_t n = 0;
-    if (live) {
-        const float n_cap = (float)m.dns * m.bound;
-        float t = t_first;
-        for (std::uint32_t it = 0; (float)n < n_cap && t < t1 && it < kMaxMarchIters; ++it) {
-            V3 pos = at(o, d, t);
-            float ds = calc_ds(t, m.sp, m.bound, m.inv_G, m.dns);
+    int phase = kIdle;
+    std::uint32_t ray = 0, n = 0, k = 0, start = 0, it = 0;
+    V3 o{0.f, 0.f, 0.f}, d{1.f, 1.f, 1.f}, inv_d{1.f, 1.f, 1.f};
+    float t = 0.f, t1 = 0.f, t_first = 0.f;
+    std::uint32_t cursor = 0;   // static interleaving: rays handed out so far by this warp
+    bool exhausted = false;     // warp-uniform
+
+    for (;;) {
+        // ---- hand the next rays to idle lanes until all lanes march or the rays run out
+        for (;;) {
+            const unsigned idle = __ballot_sync(0xffffffffu, phase == kIdle);
+            if (idle == 0u || exhausted) break;
+            const unsigned cnt = (unsigned)__popc(idle);
+            std::uint32_t base = 0;
+            if (queue != nullptr) {
+                if (lane == 0) base = atomicAdd(queue, cnt);
+                base = __shfl_sync(0xffffffffu, base, 0);
+            } else {
+                base = cursor;
+                cursor += cnt;
+            }
+            if (phase == kIdle) {
+                const std::uint32_t q = base + (unsigned)__popc(idle & lt_mask);
+                const std::uint32_t r = queue != nullptr ? q : (((q >> 5) * n_warps + warp) << 5) + (q & 31u);
+                if (r < n_rays) {
+                    ray = r;
+                    o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
+                    d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
+                    const float t0 = t_starts[r];
+                    t1 = t_ends[r];
+                    if (t1 > t0) {  // marching.cu:151
+                        inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                        t_first = t0 + calc_ds(t0, m) * noises[r];
+                        t = t_first;
+                        n = 0;
+                        it = 0;
+                        phase = kCount;
+                    } else {
+                        ray_is_valid[r] = false;
+                        rays_n_samples[r] = 0;
+                        rays_startidx[r] = 0;
+                    }
+                }
+            }
+            // no rays left for this warp: the queue is drained, or the warp's interleaved
+            // sequence (increasing in its index) has passed the last ray
+            if (queue != nullptr)
+                exhausted = (std::uint64_t)base + cnt >= n_rays;
+            else
+                exhausted = ((((cursor >> 5) * n_warps + warp) << 5) + (cursor & 31u)) >= n_rays;
+        }
+        const bool active = phase != kIdle;
+        if (__ballot_sync(0xffffffffu, active) == 0u) break;
+
+        // ---- one march iteration (marching.cu:166-191 / :231-266)
+        bool first_hit = false;
+        if (active) {
+            const V3 pos = at(o, d, t);
+            const float ds = calc_ds(t, m);
             V3 g;
             float mb;
             if (occupied_at(m, pos, ds, bits, g, mb)) {
-                ++n;
+                if (phase == kWrite) {
+                    const std::uint32_t s = start + k;
+                    idcs[s] = ray;
+                    xyzs[(std::size_t)s * 3 + 0] = pos.x;
+                    xyzs[(std::size_t)s * 3 + 1] = pos.y;
+                    xyzs[(std::size_t)s * 3 + 2] = pos.z;
+                    dirs[(std::size_t)s * 3 + 0] = d.x;
+                    dirs[(std::size_t)s * 3 + 1] = d.y;
+                    dirs[(std::size_t)s * 3 + 2] = d.z;
+                    dss[s] = ds;
+                    z_vals[s] = t;
+                    ++k;
+                } else {
+                    ++n;
+                    first_hit = (n & 15u) == 1u;  // at the first occupied sample and every 16 after
+                }
                 t = t + ds;
             } else {
                 t = skip_empty(m, t, g, mb, pos, d, inv_d);
             }
+            ++it;
         }
-    }
 
-    // warp-aggregated slot allocation (marching.cu:205 does one atomic per ray)
-    const std::uint32_t incl = warp_inclusive_scan(n);
-    const std::uint32_t warp_total = __shfl_sync(0xffffffffu, incl, 31);
-    std::uint32_t base = 0;
-    if (lane_id() == 31 && warp_total > 0) base = atomicAdd(next_loc, warp_total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    const std::uint32_t start = base + incl - n;
-    const bool fits = n > 0 && (std::uint64_t)start + n <= total_samples;
-    const std::uint32_t over = warp_sum((n > 0 && !fits) ? n : 0u);
-    if (lane_id() == 0 && over > 0) atomicAdd(n_exceeded, over);
-
-    if (in_range) {
-        ray_is_valid[i] = live && (n == 0 || fits);
-        rays_n_samples[i] = fits ? n : 0u;
-        rays_startidx[i] = fits ? start : 0u;
-    }
-    if (!fits) return;
-
-    std::uint32_t *ri = idcs + start;
-    float *rx = xyzs + (std::size_t)start * 3, *rd = dirs + (std::size_t)start * 3;
-    float *rs = dss + start, *rz = z_vals + start;
-    std::uint32_t k = 0;
-    float t = t_first;
-    for (std::uint32_t it = 0; k < n && t < t1 && it < kMaxMarchIters; ++it) {
-        V3 pos = at(o, d, t);
-        float ds = calc_ds(t, m.sp, m.bound, m.inv_G, m.dns);
-        V3 g;
-        float mb;
-        if (occupied_at(m, pos, ds, bits, g, mb)) {
-            ri[k] = i;
-            rx[k * 3 + 0] = pos.x;
-            rx[k * 3 + 1] = pos.y;
-            rx[k * 3 + 2] = pos.z;
-            rd[k * 3 + 0] = d.x;
-            rd[k * 3 + 1] = d.y;
-            rd[k * 3 + 2] = d.z;
-            rs[k] = ds;
-            rz[k] = t;
-            ++k;
-            t = t + ds;
-        } else {
-            t = skip_empty(m, t, g, mb, pos, d, inv_d);
+        // ---- phase changes
+        bool count_done = phase == kCount && !((float)n < n_cap && t < t1 && it < kMaxMarchIters);
+        if (kProbe && phase == kCount && first_hit && !count_done &&
+            *((volatile std::uint32_t *)next_loc) >= total_samples) {
+            ray_is_valid[ray] = false;  // can only overflow: decided without finishing the count
+            rays_n_samples[ray] = 0;
+            rays_startidx[ray] = 0;
+            phase = kIdle;
         }
+        if (count_done && n == 0) {  // marching.cu:196-199
+            ray_is_valid[ray] = true;
+            rays_n_samples[ray] = 0;
+            rays_startidx[ray] = 0;
+            phase = kIdle;
+            count_done = false;
+        }
+        const bool want = count_done;  // n > 0
+        const unsigned wm = __ballot_sync(0xffffffffu, want);
+        if (wm != 0u) {
+            const std::uint32_t incl = warp_inclusive_scan(want ? n : 0u);
+            const std::uint32_t total_w = __shfl_sync(0xffffffffu, incl, 31);
+            const int leader = __ffs(wm) - 1;
+            std::uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(next_loc, total_w);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            bool fits = false;
+            if (want) {
+                start = base + incl - n;
+                fits = (std::uint64_t)start + n <= total_samples;
+                ray_is_valid[ray] = fits;
+                rays_n_samples[ray] = fits ? n : 0u;
+                rays_startidx[ray] = fits ? start : 0u;
+                if (fits) {  // second pass writes the samples (marching.cu:224-267)
+                    phase = kWrite;
+                    t = t_first;
+                    k = 0;
+                    it = 0;
+                } else {
+                    phase = kIdle;
+                }
+            }
+            const std::uint32_t over = warp_sum((want && !fits) ? n : 0u);
+            if (lane == 0 && over > 0) atomicAdd(n_exceeded, over);
+        }
+        if (phase == kWrite && !(k < n && t < t1 && it < kMaxMarchIters)) phase = kIdle;
     }
 }
 
@@ -271,7 +363,7 @@ __global__ void __launch_bounds__(256) march_rays_inference_kernel(
             t = t0;
             for (std::uint32_t it = 0; steps < cap && t < t1 && it < kMaxMarchIters; ++it) {
                 V3 pos = at(o, d, t);
-                float ds = calc_ds(t, m.sp, m.bound, m.inv_G, m.dns);
+                float ds = calc_ds(t, m);
                 V3 g;
                 float mb;
                 if (occupied_at(m, pos, ds, bits, g, mb)) {
@@ -288,7 +380,7 @@ __global__ void __launch_bounds__(256) march_rays_inference_kernel(
             }
             if (t >= t1) {  // marching.cu:367-394: far-plane sample
                 V3 pos = at(o, d, t1);
-                float ds = calc_ds(t1, m.sp, m.bound, m.inv_G, m.dns);
+                float ds = calc_ds(t1, m);
                 V3 g;
                 float mb;
                 if (occupied_at(m, pos, ds, bits, g, mb)) {
@@ -319,6 +411,96 @@ __global__ void __launch_bounds__(256) march_rays_inference_kernel(
     t_starts_out[i] = wrote_t ? t : 0.f;
 }
 
+// In-place form for the device-resident renderer: the slot indices and the next-ray counter are
+// read and updated in place, the advanced t is scattered straight into t_starts (what
+// marching/__init__.py:156 does with .at[].set on the host side), and each sample also gets its
+// ray's direction (the field needs it; renderers/cuda.py:225 broadcasts rays_d[indices]).
+__global__ void __launch_bounds__(256) march_rays_inference_inplace_kernel(
+    std::uint32_t n_total_rays, std::uint32_t n_rays, std::uint32_t cap, MarchParams m,
+    const float *__restrict__ rays_o, const float *__restrict__ rays_d, float *__restrict__ t_starts,
+    const float *__restrict__ t_ends, const std::uint8_t *__restrict__ bits, const bool *__restrict__ terminated,
+    std::uint32_t *__restrict__ indices, std::uint32_t *__restrict__ next_ray_index,
+    std::uint32_t *__restrict__ n_samples, float *__restrict__ xyzs, float *__restrict__ dirs,
+    float *__restrict__ dss, float *__restrict__ z_vals) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in_range = i < n_rays;
+    const bool refill = in_range && terminated[i];
+    const unsigned ballot = __ballot_sync(0xffffffffu, refill);
+    const int leader = ballot != 0 ? __ffs(ballot) - 1 : 0;
+    std::uint32_t base = 0;
+    if (ballot != 0 && (int)lane_id() == leader) base = atomicAdd(next_ray_index, (unsigned)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!in_range) return;
+    const std::uint32_t r = refill ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : indices[i];
+    indices[i] = r;
+    float *rx = xyzs + (std::size_t)i * cap * 3, *rdir = dirs + (std::size_t)i * cap * 3;
+    float *rs = dss + (std::size_t)i * cap, *rz = z_vals + (std::size_t)i * cap;
+    std::uint32_t steps = 0;
+    if (r < n_total_rays) {
+        const V3 o = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
+        const V3 d = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
+        const float t0 = t_starts[r], t1 = t_ends[r];
+        float t = 0.f;
+        if (!(t1 < t0)) {
+            const V3 inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+            t = t0;
+            for (std::uint32_t it = 0; steps < cap && t < t1 && it < kMaxMarchIters; ++it) {
+                V3 pos = at(o, d, t);
+                float ds = calc_ds(t, m);
+                V3 g;
+                float mb;
+                if (occupied_at(m, pos, ds, bits, g, mb)) {
+                    rx[steps * 3 + 0] = pos.x;
+                    rx[steps * 3 + 1] = pos.y;
+                    rx[steps * 3 + 2] = pos.z;
+                    rs[steps] = ds;
+                    rz[steps] = t;
+                    ++steps;
+                    t = t + ds;
+                } else {
+                    t = skip_empty(m, t, g, mb, pos, d, inv_d);
+                }
+            }
+            if (t >= t1) {
+                V3 pos = at(o, d, t1);
+                float ds = calc_ds(t1, m);
+                V3 g;
+                float mb;
+                if (occupied_at(m, pos, ds, bits, g, mb)) {
+                    if (steps > 0 && rs[steps - 1] + rz[steps - 1] >= t1) rs[steps - 1] = t1 - rz[steps - 1];
+                    if (steps < cap) {
+                        rx[steps * 3 + 0] = pos.x;
+                        rx[steps * 3 + 1] = pos.y;
+                        rx[steps * 3 + 2] = pos.z;
+                        rs[steps] = ds;
+                        rz[steps] = t1;
+                        ++steps;
+                    } else {
+                        t = t1;
+                    }
+                }
+            }
+        }
+        t_starts[r] = t;  // marching.cu:396 + marching/__init__.py:156 (0 for a ray with t_end < t_start)
+        for (std::uint32_t k = 0; k < steps; ++k) {
+            rdir[k * 3 + 0] = d.x;
+            rdir[k * 3 + 1] = d.y;
+            rdir[k * 3 + 2] = d.z;
+        }
+    }
+    for (std::uint32_t k = steps; k < cap; ++k) {
+        rx[k * 3 + 0] = 0.f;
+        rx[k * 3 + 1] = 0.f;
+        rx[k * 3 + 2] = 0.f;
+        rdir[k * 3 + 0] = 0.f;
+        rdir[k * 3 + 1] = 0.f;
+        rdir[k * 3 + 2] = 1.f;
+        rs[k] = 0.f;
+        rz[k] = 0.f;
+    }
+    n_samples[i] = steps;
+}
+
 __global__ void copy_counter_kernel(const std::uint32_t *__restrict__ src, std::uint32_t *__restrict__ dst) {
     *dst = *src;
 }
@@ -347,6 +529,8 @@ MarchParams make_params(std::uint32_t dns, std::uint32_t K, std::uint32_t G, flo
     m.bound = bound;
     m.sp = sp;
     m.inv_G = 1.0f / (float)G;
+    m.ds_lo = 2.0f * kSqrt3 * fminf(bound, 1.0f) / (float)dns;
+    m.ds_hi = 2.0f * kSqrt3 * bound * m.inv_G;
     return m;
 }
 
@@ -359,18 +543,29 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
                       const float *noises, const std::uint8_t *bits, std::uint32_t *next_loc,
                       std::uint32_t *n_exceeded, bool *ray_is_valid, std::uint32_t *rays_n_samples,
                       std::uint32_t *rays_startidx, std::uint32_t *idcs, float *xyzs, float *dirs,
-                      float *dss, float *z_vals) {
+                      float *dss, float *z_vals, std::uint32_t *queue, bool probe) {
     NGP_CHECK_ARG(d.K > 0 && d.G > 0 && d.diagonal_n_steps > 0, "march_rays: K, G and diagonal_n_steps must be positive");
     NGP_CHECK_ARG(d.G <= 1024 && (d.G & (d.G - 1)) == 0, "march_rays: G must be a power of two <= 1024 (Morton codes of other sizes exceed G^3)");
     NGP_CHECK_ARG(d.K <= 16, "march_rays: at most 16 cascades");
     NGP_CHECK_ARG(d.bound > 0.f && d.stepsize_portion >= 0.f, "march_rays: bound must be positive, stepsize_portion non-negative");
     NGP_CUDA_TRY(cudaMemsetAsync(next_loc, 0, sizeof(std::uint32_t), stream));
     NGP_CUDA_TRY(cudaMemsetAsync(n_exceeded, 0, sizeof(std::uint32_t), stream));
+    if (queue != nullptr) NGP_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(std::uint32_t), stream));
     const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
     if (d.n_rays > 0) {
-        march_rays_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
-            d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-            n_exceeded, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals);
+        const unsigned warps_needed = (d.n_rays + 31) / 32;
+        const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
+        const unsigned cap = (unsigned)sm_count() * kMarchBlocksPerSm;
+        const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
+        if (probe) {
+            march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
+                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals);
+        } else {
+            march_rays_kernel<false><<<grid, kMarchBlock, 0, stream>>>(
+                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals);
+        }
         count_launches(1);
     }
     if (d.total_samples > 0) {
@@ -400,6 +595,23 @@ int launch_march_rays_inference(cudaStream_t stream, const MarchingInferenceDesc
             d.n_total_rays, d.n_rays, d.march_steps_cap, m, rays_o, rays_d, t_starts, t_ends, bits,
             terminated, indices_in, next_ray_index, indices_out, n_samples, t_starts_out, xyzs, dss,
             z_vals);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+int launch_march_rays_inference_inplace(cudaStream_t stream, const MarchingInferenceDescriptor &d, const float *rays_o,
+                                        const float *rays_d, float *t_starts, const float *t_ends,
+                                        const std::uint8_t *bits, const bool *terminated, std::uint32_t *indices,
+                                        std::uint32_t *next_ray_index, std::uint32_t *n_samples, float *xyzs,
+                                        float *dirs, float *dss, float *z_vals) {
+    NGP_CHECK_ARG(d.K > 0 && d.K <= 16 && d.G > 0 && d.G <= 1024 && (d.G & (d.G - 1)) == 0 && d.diagonal_n_steps > 0,
+                  "march_rays_inference: bad K, G or diagonal_n_steps");
+    const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
+    if (d.n_rays > 0) {
+        march_rays_inference_inplace_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
+            d.n_total_rays, d.n_rays, d.march_steps_cap, m, rays_o, rays_d, t_starts, t_ends, bits, terminated, indices,
+            next_ray_index, n_samples, xyzs, dirs, dss, z_vals);
         count_launches(1);
     }
     return launch_status();

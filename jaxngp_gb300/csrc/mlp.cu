@@ -29,7 +29,6 @@ namespace ngp {
 namespace {
 
 constexpr int kTile = 64;
-constexpr int kThreads = 256;
 constexpr int kW0 = 0, kW1 = 2048, kW2 = 3072, kW3 = 5120, kW4 = 9216, kNW = 9408;
 // transposed copies (backward only)
 constexpr int kT0 = 0;      // W0^T [64][32]
@@ -60,22 +59,32 @@ __device__ __forceinline__ void sh4(float x, float y, float z, float *o) {
     o[15] = 0.59004358992664352f * x * (-x2 + 3.0f * y2);
 }
 
-// C[s][n] = act(sum_k A[s][k] * B[k][n]) for s < kTile, n < N (N % 4 == 0).  Each thread owns a
-// 4-wide column strip and kTile/R rows spaced R apart.
-template <int K, int N, bool kRelu>
+// Thread layout of a [ROWS x N] result over NT threads: each thread owns a 4-wide column strip
+// and RPT rows spaced R apart; when there are more row groups than rows the extra threads idle.
+template <int NT, int ROWS, int N>
+struct Strip {
+    static constexpr int G = N / 4;
+    static constexpr int R = NT / G;
+    static constexpr int RPT = ROWS >= R ? ROWS / R : 1;
+    static constexpr bool kIdle = R > ROWS;
+    static_assert(NT % G == 0 && (kIdle || ROWS % R == 0), "tile shape");
+};
+
+// C[s][n] = act(sum_k A[s][k] * B[k][n]) for s < kTile, n < N (N % 4 == 0).
+template <int NT, int K, int N, bool kRelu>
 __device__ __forceinline__ void mm(const float *A, int lda, const float *B, float *C, int ldc) {
-    constexpr int G = N / 4, R = kThreads / G, RPT = kTile / R;
-    static_assert(kThreads % G == 0 && kTile % R == 0, "tile shape");
-    const int t = threadIdx.x, c0 = (t % G) * 4, r0 = t / G;
-    float acc[RPT][4];
+    using S = Strip<NT, kTile, N>;
+    const int t = threadIdx.x, c0 = (t % S::G) * 4, r0 = t / S::G;
+    if (S::kIdle && r0 >= kTile) return;
+    float acc[S::RPT][4];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+    for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
 #pragma unroll 8
     for (int k = 0; k < K; ++k) {
         const float4 b = *reinterpret_cast<const float4 *>(B + k * N + c0);
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-            const float a = A[(r0 + q * R) * lda + k];
+        for (int q = 0; q < S::RPT; ++q) {
+            const float a = A[(r0 + q * S::R) * lda + k];
             acc[q][0] += a * b.x;
             acc[q][1] += a * b.y;
             acc[q][2] += a * b.z;
@@ -83,28 +92,29 @@ __device__ __forceinline__ void mm(const float *A, int lda, const float *B, floa
         }
     }
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) {
+    for (int q = 0; q < S::RPT; ++q) {
         float4 v = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
         if (kRelu) v = make_float4(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f), fmaxf(v.z, 0.f), fmaxf(v.w, 0.f));
-        *reinterpret_cast<float4 *>(C + (r0 + q * R) * ldc + c0) = v;
+        *reinterpret_cast<float4 *>(C + (r0 + q * S::R) * ldc + c0) = v;
     }
 }
 
 // Like mm, but the result is multiplied elementwise by (M[s][n] > 0) and written over M (the
 // relu adjoint: M holds the layer's post-activation values).
-template <int K, int N>
+template <int NT, int K, int N>
 __device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const float *B, float *M, int ldm) {
-    constexpr int G = N / 4, R = kThreads / G, RPT = kTile / R;
-    const int t = threadIdx.x, c0 = (t % G) * 4, r0 = t / G;
-    float acc[RPT][4];
+    using S = Strip<NT, kTile, N>;
+    const int t = threadIdx.x, c0 = (t % S::G) * 4, r0 = t / S::G;
+    if (S::kIdle && r0 >= kTile) return;
+    float acc[S::RPT][4];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+    for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
 #pragma unroll 8
     for (int k = 0; k < K; ++k) {
         const float4 b = *reinterpret_cast<const float4 *>(B + k * N + c0);
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-            const float a = A[(r0 + q * R) * lda + k];
+        for (int q = 0; q < S::RPT; ++q) {
+            const float a = A[(r0 + q * S::R) * lda + k];
             acc[q][0] += a * b.x;
             acc[q][1] += a * b.y;
             acc[q][2] += a * b.z;
@@ -112,8 +122,8 @@ __device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const f
         }
     }
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-        float4 *p = reinterpret_cast<float4 *>(M + (r0 + q * R) * ldm + c0);
+    for (int q = 0; q < S::RPT; ++q) {
+        float4 *p = reinterpret_cast<float4 *>(M + (r0 + q * S::R) * ldm + c0);
         const float4 m = *p;
         *p = make_float4(m.x > 0.f ? acc[q][0] : 0.f, m.y > 0.f ? acc[q][1] : 0.f,
                          m.z > 0.f ? acc[q][2] : 0.f, m.w > 0.f ? acc[q][3] : 0.f);
@@ -121,22 +131,24 @@ __device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const f
 }
 
 // acc[m][n] += sum_s A[s][m] * D[s][n] over the tile's rows (the weight-gradient GEMM).
-template <int M, int N>
+template <int NT, int M, int N>
 struct WGrad {
-    static constexpr int G = N / 4, R = kThreads / G, RPT = M / R;
-    float acc[RPT][4];
+    using S = Strip<NT, M, N>;
+    float acc[S::RPT][4];
+    __device__ __forceinline__ bool owner() const { return !S::kIdle || (int)threadIdx.x / S::G < M; }
     __device__ __forceinline__ void zero() {
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+        for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
     }
     __device__ __forceinline__ void add(const float *A, int lda, const float *D, int ldd, int rows) {
-        const int t = threadIdx.x, c0 = (t % G) * 4, m0 = t / G;
+        const int t = threadIdx.x, c0 = (t % S::G) * 4, m0 = t / S::G;
+        if (!owner()) return;
 #pragma unroll 4
         for (int s = 0; s < rows; ++s) {
             const float4 d = *reinterpret_cast<const float4 *>(D + s * ldd + c0);
 #pragma unroll
-            for (int q = 0; q < RPT; ++q) {
-                const float a = A[s * lda + m0 + q * R];
+            for (int q = 0; q < S::RPT; ++q) {
+                const float a = A[s * lda + m0 + q * S::R];
                 acc[q][0] += a * d.x;
                 acc[q][1] += a * d.y;
                 acc[q][2] += a * d.z;
@@ -145,10 +157,11 @@ struct WGrad {
         }
     }
     __device__ __forceinline__ void store(float *out) const {  // out: [M][N] row-major
-        const int t = threadIdx.x, c0 = (t % G) * 4, m0 = t / G;
+        const int t = threadIdx.x, c0 = (t % S::G) * 4, m0 = t / S::G;
+        if (!owner()) return;
 #pragma unroll
-        for (int q = 0; q < RPT; ++q)
-            *reinterpret_cast<float4 *>(out + (m0 + q * R) * N + c0) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
+        for (int q = 0; q < S::RPT; ++q)
+            *reinterpret_cast<float4 *>(out + (m0 + q * S::R) * N + c0) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
     }
 };
 
@@ -157,28 +170,29 @@ __device__ __forceinline__ std::uint32_t active_count(std::uint32_t n, const std
 }
 
 // Stage the packed weights (and optionally their transposes) into shared memory.
+template <int NT>
 __device__ __forceinline__ void load_weights(const float *__restrict__ w, float *sW, float *sT) {
-    for (int i = threadIdx.x; i < kNW / 4; i += kThreads)
+    for (int i = threadIdx.x; i < kNW / 4; i += NT)
         reinterpret_cast<float4 *>(sW)[i] = reinterpret_cast<const float4 *>(w)[i];
     if (sT != nullptr) {
         __syncthreads();
-        for (int i = threadIdx.x; i < 2048; i += kThreads) {  // W0 [32][64] -> [64][32]
+        for (int i = threadIdx.x; i < 2048; i += NT) {  // W0 [32][64] -> [64][32]
             const int r = i / 64, c = i % 64;
             sT[kT0 + c * 32 + r] = sW[kW0 + i];
         }
-        for (int i = threadIdx.x; i < 1024; i += kThreads) {  // W1 [64][16] -> [16][64]
+        for (int i = threadIdx.x; i < 1024; i += NT) {  // W1 [64][16] -> [16][64]
             const int r = i / 16, c = i % 16;
             sT[kT1 + c * 64 + r] = sW[kW1 + i];
         }
-        for (int i = threadIdx.x; i < 1024; i += kThreads) {  // W2[:16] [16][64] -> [64][16]
+        for (int i = threadIdx.x; i < 1024; i += NT) {  // W2[:16] [16][64] -> [64][16]
             const int r = i / 64, c = i % 64;
             sT[kT2 + c * 16 + r] = sW[kW2 + i];
         }
-        for (int i = threadIdx.x; i < 4096; i += kThreads) {  // W3 [64][64] -> [64][64]
+        for (int i = threadIdx.x; i < 4096; i += NT) {  // W3 [64][64] -> [64][64]
             const int r = i / 64, c = i % 64;
             sT[kT3 + c * 64 + r] = sW[kW3 + i];
         }
-        for (int i = threadIdx.x; i < 192; i += kThreads) {  // W4 [64][3] -> [3][64]
+        for (int i = threadIdx.x; i < 192; i += NT) {  // W4 [64][3] -> [3][64]
             const int r = i / 3, c = i % 3;
             sT[kT4 + c * 64 + r] = sW[kW4 + i];
         }
@@ -187,8 +201,9 @@ __device__ __forceinline__ void load_weights(const float *__restrict__ w, float 
 }
 
 // Loads the tile's encodings into X[:, 0:32] (zero rows past `rows`).
+template <int NT>
 __device__ __forceinline__ void load_enc(const float *__restrict__ enc, std::size_t s0, int rows, float *X) {
-    for (int i = threadIdx.x; i < kTile * 8; i += kThreads) {
+    for (int i = threadIdx.x; i < kTile * 8; i += NT) {
         const int r = i / 8, c = (i % 8) * 4;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (r < rows) v = *reinterpret_cast<const float4 *>(enc + (s0 + r) * 32 + c);
@@ -197,8 +212,9 @@ __device__ __forceinline__ void load_enc(const float *__restrict__ enc, std::siz
 }
 
 // XC[s][16:32] = SH4(dir_s); rows past `rows` get a unit +z direction.
+template <int NT>
 __device__ __forceinline__ void load_sh(const float *__restrict__ dirs, std::size_t s0, int rows, float *XC) {
-    for (int r = threadIdx.x; r < kTile; r += kThreads) {
+    for (int r = threadIdx.x; r < kTile; r += NT) {
         float dx = 0.f, dy = 0.f, dz = 1.f;
         if (r < rows) {
             dx = dirs[(s0 + r) * 3 + 0];
@@ -213,48 +229,54 @@ __device__ __forceinline__ void load_sh(const float *__restrict__ dirs, std::siz
 }
 
 // Forward through the tile; leaves X0=enc, H1, XC=[x, sh], H2, H3 in shared memory and writes
-// sigma/rgb into O (O[s][0] = x0 (pre-activation), O[s][1..3] = rgb).
+// sigma/rgb into O (O[s][0] = x0 (pre-activation), O[s][1..3] = rgb).  H3 may alias H1 when the
+// caller does not need H1 afterwards (the forward-only kernel).
+template <int NT>
 __device__ __forceinline__ void tile_forward(const float *sW, float *X0, float *H1, float *XC, float *H2,
                                              float *H3, float *O) {
-    mm<32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
+    mm<NT, 32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
     __syncthreads();
-    mm<64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
+    mm<NT, 64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
     __syncthreads();
-    mm<32, 64, true>(XC, kLd, sW + kW2, H2, kLd);
+    mm<NT, 32, 64, true>(XC, kLd, sW + kW2, H2, kLd);
     __syncthreads();
-    mm<64, 64, true>(H2, kLd, sW + kW3, H3, kLd);
+    mm<NT, 64, 64, true>(H2, kLd, sW + kW3, H3, kLd);
     __syncthreads();
-    for (int i = threadIdx.x; i < kTile * 3; i += kThreads) {
+    for (int i = threadIdx.x; i < kTile * 3; i += NT) {
         const int r = i / 3, c = i % 3;
         float a = 0.f;
 #pragma unroll 16
         for (int k = 0; k < 64; ++k) a += H3[r * kLd + k] * sW[kW4 + k * 3 + c];
         O[r * 4 + 1 + c] = 1.f / (1.f + expf(-a));
     }
-    for (int r = threadIdx.x; r < kTile; r += kThreads) O[r * 4] = XC[r * kLd];
+    for (int r = threadIdx.x; r < kTile; r += NT) O[r * 4] = XC[r * kLd];
     __syncthreads();
 }
 
-constexpr int kActFloats = 5 * kTile * kLd + kTile * 4;
+constexpr int kActFloats = 5 * kTile * kLd + kTile * 4;      // backward: X0, H1, XC, H2, H3, O
+constexpr int kFwdActFloats = 4 * kTile * kLd + kTile * 4;   // forward: H3 reuses H1
+constexpr int kFwdThreads = 256;   // 2 CTAs per SM (108 KB of shared memory each)
+constexpr int kBwdThreads = 256;   // 1 CTA per SM (159 KB of shared memory)
 
-__global__ void __launch_bounds__(kThreads) mlp_forward_kernel(
+template <int NT>
+__global__ void __launch_bounds__(NT) mlp_forward_kernel(
     std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
     const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb) {
     extern __shared__ __align__(16) float smem[];
     float *sW = smem;
     float *X0 = sW + kNW, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd, *H2 = XC + kTile * kLd;
-    float *H3 = H2 + kTile * kLd, *O = H3 + kTile * kLd;
-    load_weights(weights, sW, nullptr);
+    float *H3 = H1, *O = H2 + kTile * kLd;
+    load_weights<NT>(weights, sW, nullptr);
     const std::uint32_t n_act = active_count(n, count);
     const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
     for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const std::size_t s0 = (std::size_t)tile * kTile;
         const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
-        load_enc(enc, s0, rows, X0);
-        load_sh(dirs, s0, rows, XC);
+        load_enc<NT>(enc, s0, rows, X0);
+        load_sh<NT>(dirs, s0, rows, XC);
         __syncthreads();
-        tile_forward(sW, X0, H1, XC, H2, H3, O);
-        for (int i = threadIdx.x; i < rows; i += kThreads) {
+        tile_forward<NT>(sW, X0, H1, XC, H2, H3, O);
+        for (int i = threadIdx.x; i < rows; i += NT) {
             const float4 o = *reinterpret_cast<const float4 *>(O + i * 4);
             reinterpret_cast<float4 *>(drgb)[s0 + i] = make_float4(expf(o.x), o.y, o.z, o.w);
         }
@@ -263,23 +285,24 @@ __global__ void __launch_bounds__(kThreads) mlp_forward_kernel(
 }
 
 // sigma only (NeRF.__call__ with dir=None, nerfs.py:71-72), used by the occupancy-grid refresh.
-__global__ void __launch_bounds__(kThreads) mlp_density_kernel(
+template <int NT>
+__global__ void __launch_bounds__(NT) mlp_density_kernel(
     std::uint32_t n, const float *__restrict__ enc, const float *__restrict__ weights, float *__restrict__ sigma) {
     extern __shared__ __align__(16) float smem[];
     float *sW = smem;
     float *X0 = sW + kNW, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd;
-    load_weights(weights, sW, nullptr);
+    load_weights<NT>(weights, sW, nullptr);
     const std::uint32_t n_tiles = (n + kTile - 1) / kTile;
     for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const std::size_t s0 = (std::size_t)tile * kTile;
         const int rows = (int)min((std::uint32_t)kTile, n - (std::uint32_t)s0);
-        load_enc(enc, s0, rows, X0);
+        load_enc<NT>(enc, s0, rows, X0);
         __syncthreads();
-        mm<32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
+        mm<NT, 32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
         __syncthreads();
-        mm<64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
+        mm<NT, 64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
         __syncthreads();
-        for (int i = threadIdx.x; i < rows; i += kThreads) sigma[s0 + i] = expf(XC[i * kLd]);
+        for (int i = threadIdx.x; i < rows; i += NT) sigma[s0 + i] = expf(XC[i * kLd]);
         __syncthreads();
     }
 }
@@ -287,7 +310,8 @@ __global__ void __launch_bounds__(kThreads) mlp_density_kernel(
 // Backward.  dL_ddrgb rows past the active count are ignored; dL_denc rows past it are zeroed.
 // `grad_scale` multiplies the incoming gradient (loss normalisation); `partials` receives one
 // [9408] dL/dW partial per CTA.
-__global__ void __launch_bounds__(kThreads) mlp_backward_kernel(
+template <int NT>
+__global__ void __launch_bounds__(NT) mlp_backward_kernel(
     std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
     const float *__restrict__ dirs, const float *__restrict__ weights,
     const float *__restrict__ dL_ddrgb, const float *__restrict__ grad_scale,
@@ -296,13 +320,13 @@ __global__ void __launch_bounds__(kThreads) mlp_backward_kernel(
     float *sW = smem, *sT = sW + kNW;
     float *X0 = sT + kNT, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd, *H2 = XC + kTile * kLd;
     float *H3 = H2 + kTile * kLd, *O = H3 + kTile * kLd;
-    load_weights(weights, sW, sT);
+    load_weights<NT>(weights, sW, sT);
     const float gs = grad_scale != nullptr ? *grad_scale : 1.f;
 
-    WGrad<32, 64> g0;  // dW0 = enc^T dA1
-    WGrad<64, 16> g1;  // dW1 = h1^T dx
-    WGrad<32, 64> g2;  // dW2 = [x, sh]^T dA2
-    WGrad<64, 64> g3;  // dW3 = h2^T dA3
+    WGrad<NT, 32, 64> g0;  // dW0 = enc^T dA1
+    WGrad<NT, 64, 16> g1;  // dW1 = h1^T dx
+    WGrad<NT, 32, 64> g2;  // dW2 = [x, sh]^T dA2
+    WGrad<NT, 64, 64> g3;  // dW3 = h2^T dA3
     float g4 = 0.f;    // dW4 = h3^T dA4: thread t < 192 owns element t
     g0.zero();
     g1.zero();
@@ -314,13 +338,13 @@ __global__ void __launch_bounds__(kThreads) mlp_backward_kernel(
     for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const std::size_t s0 = (std::size_t)tile * kTile;
         const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
-        load_enc(enc, s0, rows, X0);
-        load_sh(dirs, s0, rows, XC);
+        load_enc<NT>(enc, s0, rows, X0);
+        load_sh<NT>(dirs, s0, rows, XC);
         __syncthreads();
-        tile_forward(sW, X0, H1, XC, H2, H3, O);
+        tile_forward<NT>(sW, X0, H1, XC, H2, H3, O);
 
         // O[s] <- [dL/dx0, dL/da4 (3)]; rows past `rows` get zero gradient
-        for (int r = threadIdx.x; r < kTile; r += kThreads) {
+        for (int r = threadIdx.x; r < kTile; r += NT) {
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (r < rows) g = reinterpret_cast<const float4 *>(dL_ddrgb)[s0 + r];
             const float4 o = *reinterpret_cast<const float4 *>(O + r * 4);
@@ -338,7 +362,7 @@ __global__ void __launch_bounds__(kThreads) mlp_backward_kernel(
         }
         __syncthreads();
         // dA3 = (dA4 @ W4^T) * (h3 > 0), over H3
-        for (int i = threadIdx.x; i < kTile * 64; i += kThreads) {
+        for (int i = threadIdx.x; i < kTile * 64; i += NT) {
             const int r = i / 64, c = i % 64;
             const float h = H3[r * kLd + c];
             const float v = O[r * 4 + 1] * sT[kT4 + c] + O[r * 4 + 2] * sT[kT4 + 64 + c] + O[r * 4 + 3] * sT[kT4 + 128 + c];
@@ -347,24 +371,24 @@ __global__ void __launch_bounds__(kThreads) mlp_backward_kernel(
         __syncthreads();
         g3.add(H2, kLd, H3, kLd, kTile);
         __syncthreads();
-        mm_mask_inplace<64, 64>(H3, kLd, sT + kT3, H2, kLd);  // dA2 over H2
+        mm_mask_inplace<NT, 64, 64>(H3, kLd, sT + kT3, H2, kLd);  // dA2 over H2
         __syncthreads();
         g2.add(XC, kLd, H2, kLd, kTile);
         __syncthreads();
         // dx = dA2 @ W2[:16]^T (+ dL/dx0 on column 0), over XC[:, 0:16]
-        mm<64, 16, false>(H2, kLd, sT + kT2, XC, kLd);
+        mm<NT, 64, 16, false>(H2, kLd, sT + kT2, XC, kLd);
         __syncthreads();
-        for (int r = threadIdx.x; r < kTile; r += kThreads) XC[r * kLd] += O[r * 4];
+        for (int r = threadIdx.x; r < kTile; r += NT) XC[r * kLd] += O[r * 4];
         __syncthreads();
         g1.add(H1, kLd, XC, kLd, kTile);
         __syncthreads();
-        mm_mask_inplace<16, 64>(XC, kLd, sT + kT1, H1, kLd);  // dA1 over H1
+        mm_mask_inplace<NT, 16, 64>(XC, kLd, sT + kT1, H1, kLd);  // dA1 over H1
         __syncthreads();
         g0.add(X0, kLd, H1, kLd, kTile);
         __syncthreads();
-        mm<64, 32, false>(H1, kLd, sT + kT0, X0, kLd);  // dL/denc over X0
+        mm<NT, 64, 32, false>(H1, kLd, sT + kT0, X0, kLd);  // dL/denc over X0
         __syncthreads();
-        for (int i = threadIdx.x; i < kTile * 8; i += kThreads) {
+        for (int i = threadIdx.x; i < kTile * 8; i += NT) {
             const int r = i / 8, c = (i % 8) * 4;
             if (r < rows) *reinterpret_cast<float4 *>(dL_denc + (s0 + r) * 32 + c) = *reinterpret_cast<const float4 *>(X0 + r * kLd + c);
         }
@@ -396,7 +420,7 @@ __global__ void zero_rows_kernel(std::uint32_t n, const std::uint32_t *__restric
         x[i] = 0.f;
 }
 
-constexpr std::size_t kFwdSmem = (std::size_t)(kNW + kActFloats) * sizeof(float);
+constexpr std::size_t kFwdSmem = (std::size_t)(kNW + kFwdActFloats) * sizeof(float);
 constexpr std::size_t kBwdSmem = (std::size_t)(kNW + kNT + kActFloats) * sizeof(float);
 constexpr std::size_t kDensSmem = (std::size_t)(kNW + 3 * kTile * kLd) * sizeof(float);
 
@@ -429,13 +453,13 @@ int launch_mlp_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp: enc, weights and drgb must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_forward_kernel<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
         attr = true;
     }
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 2 ? tiles : (unsigned)sm_count() * 2;
-    mlp_forward_kernel<<<grid, kThreads, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
+    mlp_forward_kernel<kFwdThreads><<<grid, kFwdThreads, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
     count_launches(1);
     return launch_status();
 }
@@ -444,13 +468,13 @@ int launch_mlp_density(cudaStream_t stream, std::uint32_t n, const float *enc, c
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp: enc and weights must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_density_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDensSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_density_kernel<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDensSmem));
         attr = true;
     }
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
-    mlp_density_kernel<<<grid, kThreads, kDensSmem, stream>>>(n, enc, weights, sigma);
+    mlp_density_kernel<kFwdThreads><<<grid, kFwdThreads, kDensSmem, stream>>>(n, enc, weights, sigma);
     count_launches(1);
     return launch_status();
 }
@@ -464,11 +488,11 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
                   "mlp: buffers must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel<kBwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
         attr = true;
     }
     const unsigned grid = (unsigned)mlp_partials_count();
-    mlp_backward_kernel<<<grid, kThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
+    mlp_backward_kernel<kBwdThreads><<<grid, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
     count_launches(1);
     reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(grid, partials, dL_dweights, accumulate ? 1 : 0);
     count_launches(1);
@@ -515,11 +539,11 @@ int launch_mlp_backward_noalloc(cudaStream_t stream, std::uint32_t n, const std:
     if (st != NGP_OK) return st;
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel<kBwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
         attr = true;
     }
     if (parts > 0) {
-        mlp_backward_kernel<<<(unsigned)parts, kThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
+        mlp_backward_kernel<kBwdThreads><<<(unsigned)parts, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
                                                                              grad_scale, dL_denc, scratch);
         count_launches(1);
     }

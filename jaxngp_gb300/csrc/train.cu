@@ -99,87 +99,182 @@ __global__ void __launch_bounds__(256) train_rays_kernel(
 // integrate_rays_backward (integrating.cu:106-240) with dL/dfinal_rgbd from the loss; dL/ddepth
 // is zero (the loss ignores depth).  Gradients are unnormalised; 1/n_valid is applied by the
 // field backward through `grad_scale`.
-__global__ void __launch_bounds__(256) integrate_loss_backward_kernel(
+//
+// A ray without samples is finished by its own lane.  A ray with samples is processed by its
+// whole warp: 32-sample chunks are loaded coalesced into shared memory, all lanes compute the
+// chunk's opacities in parallel, and one lane runs the compositing recurrence from shared memory
+// in the reference's order (so every rounding is the reference's); in the backward pass the same
+// lane writes per-sample gradients to shared memory and the warp stores them coalesced.  The
+// one-thread-per-ray form walks each long ray through dependent global loads while the rest of
+// its warp idles.
+constexpr int kIlbWarps = 4;
+
+struct IlbChunk {
+    float4 c[32];
+    float dt[32], z[32], a[32], om[32];
+    float4 g[32];
+};
+
+__device__ __forceinline__ float huber_grad(float e, float delta, float *loss) {
+    const float ae = fabsf(e);
+    *loss += ae <= delta ? 0.5f * e * e : delta * (ae - 0.5f * delta);
+    return ae <= delta ? e : copysignf(delta, e);
+}
+
+__global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_backward_kernel(
     std::uint32_t n_rays, std::uint32_t total_samples, float near_distance, float delta, const bool *__restrict__ valid,
     const std::uint32_t *__restrict__ startidx, const std::uint32_t *__restrict__ n_samples,
     const float *__restrict__ bgs, const float *__restrict__ gt, const float *__restrict__ dss,
     const float *__restrict__ z_vals, const float *__restrict__ drgbs,
     float *__restrict__ dL_ddrgbs, float *__restrict__ acc /* [loss, n_valid, measured] */) {
+    __shared__ IlbChunk chunks[kIlbWarps];
+    IlbChunk &ch = chunks[threadIdx.x >> 5];
+    const unsigned lane = lane_id();
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float loss = 0.f, nv = 0.f, used_f = 0.f;
+
+    std::uint32_t my_s = 0, my_n = 0;
+    float my_bg[3] = {0.f, 0.f, 0.f}, my_gt[3] = {0.f, 0.f, 0.f};
+    bool my_valid = false;
     if (i < n_rays) {
-        const std::uint32_t s = startidx[i];
-        const std::uint32_t n = s >= total_samples ? 0u : min(n_samples[i], total_samples - s);
-        const float *rd = dss + s, *rz = z_vals + s;
-        const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + s;
-        float4 *gc = reinterpret_cast<float4 *>(dL_ddrgbs) + s;
-        const float bg0 = bgs[i * 3 + 0], bg1 = bgs[i * 3 + 1], bg2 = bgs[i * 3 + 2];
-        // forward
-        float T = 1.f, r = 0.f, g = 0.f, b = 0.f, dep = 0.f;
-        std::uint32_t k = 0;
-        for (; T > kTThreshold && k < n; ++k) {
-            const float4 c = rc[k];
-            const float alpha = 1.f - expf(-c.x * rd[k]);
-            const float w = T * alpha;
-            r += w * c.y;
-            g += w * c.z;
-            b += w * c.w;
-            dep += w * rz[k];
-            T *= 1.f - alpha;
+        my_s = startidx[i];
+        my_n = my_s >= total_samples ? 0u : min(n_samples[i], total_samples - my_s);
+        my_valid = valid[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            my_bg[c] = bgs[i * 3 + c];
+            my_gt[c] = gt[i * 3 + c];
         }
-        const std::uint32_t used = k;
+        if (my_n == 0) {  // T = 1: the prediction is the background
+            if (my_valid) {
+                nv = 1.f;
+                float l = 0.f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) huber_grad(my_bg[c] - my_gt[c], delta, &l);
+                loss += l * (1.f / 3.f);
+            }
+        }
+    }
+
+    unsigned heavy = __ballot_sync(0xffffffffu, i < n_rays && my_n > 0);
+    while (heavy != 0u) {
+        const int j = __ffs(heavy) - 1;
+        heavy &= heavy - 1u;
+        const std::uint32_t s = __shfl_sync(0xffffffffu, my_s, j);
+        const std::uint32_t n = __shfl_sync(0xffffffffu, my_n, j);
+        const bool rv = __shfl_sync(0xffffffffu, my_valid ? 1 : 0, j) != 0;
+        float bg[3], tg[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            bg[c] = __shfl_sync(0xffffffffu, my_bg[c], j);
+            tg[c] = __shfl_sync(0xffffffffu, my_gt[c], j);
+        }
+        const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + s;
+        // ---- forward (integrating.cu:61-78)
+        float T = 1.f, r = 0.f, g = 0.f, b = 0.f, dep = 0.f;
+        std::uint32_t used = 0;
+        for (std::uint32_t base = 0; base < n; base += 32) {
+            const std::uint32_t cnt = min(32u, n - base);
+            if (lane < cnt) {
+                const float4 c = rc[base + lane];
+                const float dt = dss[s + base + lane];
+                ch.c[lane] = c;
+                ch.dt[lane] = dt;
+                ch.z[lane] = z_vals[s + base + lane];
+                const float a = 1.f - expf(-c.x * dt);
+                ch.a[lane] = a;
+                ch.om[lane] = 1.f - a;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                for (std::uint32_t q = 0; q < cnt && T > kTThreshold; ++q) {
+                    const float w = T * ch.a[q];
+                    const float4 c = ch.c[q];
+                    r += w * c.y;
+                    g += w * c.z;
+                    b += w * c.w;
+                    dep += w * ch.z[q];
+                    T *= ch.om[q];
+                    ++used;
+                }
+            }
+            T = __shfl_sync(0xffffffffu, T, 0);
+            __syncwarp();
+            if (!(T > kTThreshold)) break;
+        }
+        r = __shfl_sync(0xffffffffu, r, 0);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        dep = __shfl_sync(0xffffffffu, dep, 0);
+        used = __shfl_sync(0xffffffffu, used, 0);
         const float fo = 1.f - T;
-        float4 fr;
+        float fr[4];
         if (T <= kTThreshold) {
             const float id = 1.f / fo;
-            fr = make_float4(r * id, g * id, b * id, dep * id);
+            fr[0] = r * id; fr[1] = g * id; fr[2] = b * id; fr[3] = dep * id;
         } else {
-            fr = make_float4(r + T * bg0, g + T * bg1, b + T * bg2, dep);
+            fr[0] = r + T * bg[0]; fr[1] = g + T * bg[1]; fr[2] = b + T * bg[2]; fr[3] = dep;
         }
-        // loss and its gradient (mean over channels, sum over valid rays)
-        float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid[i]) {
-            nv = 1.f;
-            const float e[3] = {fr.x - gt[i * 3 + 0], fr.y - gt[i * 3 + 1], fr.z - gt[i * 3 + 2]};
-            float gg[3];
+        // ---- loss and dL/dfinal_rgbd (mean over channels)
+        float go[3] = {0.f, 0.f, 0.f}, l = 0.f;
+        if (rv) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float ae = fabsf(e[c]);
-                loss += ae <= delta ? 0.5f * e[c] * e[c] : delta * (ae - 0.5f * delta);
-                gg[c] = (ae <= delta ? e[c] : copysignf(delta, e[c])) * (1.f / 3.f);
-            }
-            loss *= 1.f / 3.f;
-            go = make_float4(gg[0], gg[1], gg[2], 0.f);
+            for (int c = 0; c < 3; ++c) go[c] = huber_grad(fr[c] - tg[c], delta, &l) * (1.f / 3.f);
         }
-        // backward (recomputes the forward, as integrating.cu:177-233 does)
+        if ((int)lane == j) {
+            if (rv) {
+                nv = 1.f;
+                loss += l * (1.f / 3.f);
+            }
+            used_f = (float)used;
+        }
+        // ---- backward (integrating.cu:173-233), recomputing the forward
         const bool terminated = fo >= 1.f - kTThreshold;
         const float bgterm = terminated ? 0.f : 1.f - fo;
-        T = 1.f;
-        float cr = 0.f, cg = 0.f, cb = 0.f, cd = 0.f;
-        for (k = 0; T > kTThreshold && k < n; ++k) {
-            const float4 c = rc[k];
-            const float z = rz[k], dt = rd[k];
-            const float alpha = 1.f - expf(-c.x * dt);
-            const float w = T * alpha;
-            cr += w * c.y;
-            cg += w * c.z;
-            cb += w * c.w;
-            cd += w * z;
-            T *= 1.f - alpha;
-            const float dsig = dt * (go.x * (T * c.y - (fr.x - cr) - bg0 * bgterm)
-                                   + go.y * (T * c.z - (fr.y - cg) - bg1 * bgterm)
-                                   + go.z * (T * c.w - (fr.z - cb) - bg2 * bgterm)
-                                   + go.w * (T * z - (fr.w - cd)));
-            const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
-            gc[k] = make_float4(fminf(z * z, 1.f) * dsig + reg, w * go.x, w * go.y, w * go.z);
+        float4 *gc = reinterpret_cast<float4 *>(dL_ddrgbs) + s;
+        float Tb = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, cd = 0.f;
+        for (std::uint32_t base = 0; base < used; base += 32) {
+            const std::uint32_t cnt = min(32u, used - base);
+            if (lane < cnt) {
+                const float4 c = rc[base + lane];
+                const float dt = dss[s + base + lane];
+                ch.c[lane] = c;
+                ch.dt[lane] = dt;
+                ch.z[lane] = z_vals[s + base + lane];
+                const float a = 1.f - expf(-c.x * dt);
+                ch.a[lane] = a;
+                ch.om[lane] = 1.f - a;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                for (std::uint32_t q = 0; q < cnt; ++q) {
+                    const float4 c = ch.c[q];
+                    const float z = ch.z[q], dt = ch.dt[q];
+                    const float w = Tb * ch.a[q];
+                    cr += w * c.y;
+                    cg += w * c.z;
+                    cb += w * c.w;
+                    cd += w * z;
+                    Tb *= ch.om[q];
+                    const float dsig = dt * (go[0] * (Tb * c.y - (fr[0] - cr) - bg[0] * bgterm)
+                                           + go[1] * (Tb * c.z - (fr[1] - cg) - bg[1] * bgterm)
+                                           + go[2] * (Tb * c.w - (fr[2] - cb) - bg[2] * bgterm)
+                                           + 0.f * (Tb * z - (fr[3] - cd)));
+                    const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
+                    ch.g[q] = make_float4(fminf(z * z, 1.f) * dsig + reg, w * go[0], w * go[1], w * go[2]);
+                }
+            }
+            __syncwarp();
+            if (lane < cnt) gc[base + lane] = ch.g[lane];
+            __syncwarp();
         }
-        for (; k < n; ++k) gc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        used_f = (float)used;
+        for (std::uint32_t k = used + lane; k < n; k += 32) gc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
+
     loss = warp_sum(loss);
     nv = warp_sum(nv);
     used_f = warp_sum(used_f);
-    if (lane_id() == 0) {
+    if (lane == 0) {
         if (loss != 0.f) atomicAdd(acc + 0, loss);
         if (nv != 0.f) atomicAdd(acc + 1, nv);
         if (used_f != 0.f) atomicAdd(acc + 2, used_f);
@@ -458,7 +553,7 @@ int launch_integrate_loss_backward(cudaStream_t stream, const NgpIntegrateLossDe
                   "integrate_loss_backward: drgbs and dL_ddrgbs must be 16-byte aligned");
     NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, 3 * sizeof(float), stream));
     if (d.n_rays > 0) {
-        integrate_loss_backward_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
+        integrate_loss_backward_kernel<<<(d.n_rays + 32 * kIlbWarps - 1) / (32 * kIlbWarps), 32 * kIlbWarps, 0, stream>>>(
             d.n_rays, d.total_samples, d.near_distance, d.huber_delta, valid, startidx, n_samples, bgs, gt, dss, z_vals, drgbs,
             dL_ddrgbs, acc);
         count_launches(1);

@@ -2,7 +2,7 @@
 
 One step (app/nerf/_utils.py:80-170 with models/renderers/cuda.py:100-162):
     ray batch (pixel indices -> rays, near/far, jitter, background, target colour)   ngp_train_rays
-    march_rays over the occupancy bitfield                                           march_rays
+    march_rays over the occupancy bitfield (training variant)                        ngp_march_rays_train
     hash-grid encoding of the samples                                                ngp_hashgrid_forward
     density/colour MLP                                                               ngp_field_forward
     integrate_rays + masked Huber loss + integrate_rays_backward                     ngp_integrate_loss_backward
@@ -112,6 +112,7 @@ class NGPTrainer:
         self.t0, self.t1, self.noise = torch.empty(R, **f32), torch.empty(R, **f32), torch.empty(R, **f32)
         self.bgs, self.gt = torch.empty(R, 3, **f32), torch.empty(R, 3, **f32)
         self.counters = torch.zeros(2, **i32)
+        self.queue = torch.zeros(1, **i32)
         self.count = torch.zeros(1, **i32)
         self.valid = torch.empty(R, dtype=torch.bool, device=self.dev)
         self.n_samples, self.startidx = torch.empty(R, **i32), torch.empty(R, **i32)
@@ -223,9 +224,10 @@ class NGPTrainer:
                                           self.bound, int(cfg.perturb), int(cfg.random_bg), (L.c_f32 * 3)(1, 1, 1), seed)
         L.call("ngp_train_rays", [self.data.transforms, self.data.rgbas, perm, self.rays_o, self.rays_d, self.t0,
                                   self.t1, self.noise, self.bgs, self.gt], d_rays)
-        L.call("march_rays", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
-                              self.counters[0:1], self.counters[1:2], self.valid, self.n_samples, self.startidx,
-                              self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals], self._d_march)
+        L.call("ngp_march_rays_train", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
+                                        self.counters[0:1], self.counters[1:2], self.valid, self.n_samples,
+                                        self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals,
+                                        self.queue], self._d_march)
         L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
         L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, self.count, self.enc], self._d_hg)
         L.call("ngp_field_forward", [self.enc, self.dirs, self.weights, self.count, self.drgbs], self._d_mlp)

@@ -68,6 +68,7 @@ def _lib(backend: str):
         "morton3d": [_U, _P, _P],
         "morton3d_invert": [_U, _P, _P],
         "march_rays": [_U, _U, _U, _U, _U, _F, _F] + [_P] * 6 + ([_P] * 2 if backend == "ref" else [_P]) + [_P] * 8,
+        "march_rays_ex": [_U, _U, _U, _U, _U, _F, _F] + [_P] * 6 + [_P] + [_P] * 8 + [ctypes.c_int],
         "march_rays_inference": [_U, _U, _U, _U, _U, _U, _F, _F] + [_P] * 14,
         "integrate_rays": [_U] + [_P] * 9,
         "integrate_rays_backward": [_U, _F] + [_P] * 12,
@@ -75,6 +76,8 @@ def _lib(backend: str):
     }
     fns = {}
     for name, argt in sigs.items():
+        if not hasattr(lib, prefix + name):
+            continue
         f = getattr(lib, prefix + name)
         f.argtypes = argt
         f.restype = None
@@ -131,8 +134,12 @@ def morton3d_invert(idcs, backend: str = "oracle") -> np.ndarray:
 
 def march_rays(total_samples, diagonal_n_steps, K, G, bound, stepsize_portion, rays_o, rays_d,
                t_starts, t_ends, noises, occupancy_bitfield, backend: str = "oracle",
-               return_counters: bool = False):
-    """marching/__init__.py:8-93 + marching.cu:101-268 (ray-order atomics)."""
+               return_counters: bool = False, early_exit: bool = True):
+    """marching/__init__.py:8-93 + marching.cu:101-268 (ray-order atomics).
+
+    early_exit=True is the reference run one thread at a time (a ray starting after the buffer
+    filled is dropped, marching.cu:135); early_exit=False counts every ray before any slot is taken
+    (the reference with its whole grid resident; oracle backend only)."""
     rays_o, rays_d = _f32(rays_o), _f32(rays_d)
     n = rays_o.shape[0]
     t_starts, t_ends = _f32(t_starts), _f32(t_ends)
@@ -151,11 +158,16 @@ def march_rays(total_samples, diagonal_n_steps, K, G, bound, stepsize_portion, r
     args = [n, total_samples, diagonal_n_steps, K, G, bound, stepsize_portion, _p(rays_o),
             _p(rays_d), _p(t_starts), _p(t_ends), _p(noises), _p(bits)]
     if backend == "ref":
+        if not early_exit:
+            raise ValueError("the reference build runs threads one at a time (early_exit=True)")
         args += [_p(counters[0:1]), ctypes.c_void_p(counters.ctypes.data + 4)]
     else:
         args += [_p(counters)]
     args += [_p(valid), _p(n_samples), _p(startidx), _p(idcs), _p(xyzs), _p(dirs), _p(dss), _p(zs)]
-    _lib(backend)["march_rays"](*args)
+    if backend == "oracle" and not early_exit:
+        _lib(backend)["march_rays_ex"](*args, 0)
+    else:
+        _lib(backend)["march_rays"](*args)
     measured = np.uint32(counters[0] - counters[1])
     out = (measured, valid.astype(bool), n_samples, startidx, idcs, xyzs, dirs, dss, zs)
     if return_counters:

@@ -215,14 +215,18 @@ static uint32_t march_one(const MarchDesc *dsc, v3f o, v3f d, float t0, float t1
 }
 
 /* Outputs must be zero-filled by the caller, as the reference launcher does (marching.cu:474-483).
- * counters[0] = next_sample_write_location, counters[1] = number_of_exceeded_samples. */
-void oracle_march_rays(uint32_t n_rays, uint32_t total_samples, uint32_t diagonal_n_steps,
+ * counters[0] = next_sample_write_location, counters[1] = number_of_exceeded_samples.
+ * With early_exit, rays are taken one after another in ray order, and a ray that starts after the
+ * buffer filled is dropped (marching.cu:135) -- the reference run one thread at a time.  Without
+ * it, every ray is counted before any is placed, and only then are slots taken in ray order --
+ * the reference when its whole grid is resident. */
+void oracle_march_rays_ex(uint32_t n_rays, uint32_t total_samples, uint32_t diagonal_n_steps,
                        uint32_t K, uint32_t G, float bound, float stepsize_portion,
                        const float *rays_o, const float *rays_d, const float *t_starts,
                        const float *t_ends, const float *noises, const uint8_t *bitfield,
                        uint32_t *counters, uint8_t *ray_is_valid, uint32_t *rays_n_samples,
                        uint32_t *rays_sample_startidx, uint32_t *idcs, float *xyzs, float *dirs,
-                       float *dss, float *z_vals) {
+                       float *dss, float *z_vals, int early_exit) {
     MarchDesc const dsc = {n_rays, total_samples, diagonal_n_steps, K, G, bound, stepsize_portion};
     uint32_t *cnt = (uint32_t *)calloc(n_rays ? n_rays : 1, sizeof(uint32_t));
     uint8_t *live = (uint8_t *)calloc(n_rays ? n_rays : 1, 1);
@@ -240,7 +244,7 @@ void oracle_march_rays(uint32_t n_rays, uint32_t total_samples, uint32_t diagona
     /* atomics of :135 and :205-209 taken in ray order */
     uint32_t loc = 0, exceeded = 0;
     for (uint32_t i = 0; i < n_rays; ++i) {
-        if (loc >= total_samples) { cnt[i] = 0; live[i] = 2; continue; }  /* :135 early exit */
+        if (early_exit && loc >= total_samples) { cnt[i] = 0; live[i] = 2; continue; }  /* :135 */
         if (!live[i]) continue;                                          /* :151 */
         if (cnt[i] == 0) { ray_is_valid[i] = 1; continue; }              /* :196-199 */
         uint32_t const start = loc;
@@ -269,6 +273,18 @@ void oracle_march_rays(uint32_t n_rays, uint32_t total_samples, uint32_t diagona
     }
     free(cnt);
     free(live);
+}
+
+void oracle_march_rays(uint32_t n_rays, uint32_t total_samples, uint32_t diagonal_n_steps,
+                       uint32_t K, uint32_t G, float bound, float stepsize_portion,
+                       const float *rays_o, const float *rays_d, const float *t_starts,
+                       const float *t_ends, const float *noises, const uint8_t *bitfield,
+                       uint32_t *counters, uint8_t *ray_is_valid, uint32_t *rays_n_samples,
+                       uint32_t *rays_sample_startidx, uint32_t *idcs, float *xyzs, float *dirs,
+                       float *dss, float *z_vals) {
+    oracle_march_rays_ex(n_rays, total_samples, diagonal_n_steps, K, G, bound, stepsize_portion, rays_o,
+                         rays_d, t_starts, t_ends, noises, bitfield, counters, ray_is_valid,
+                         rays_n_samples, rays_sample_startidx, idcs, xyzs, dirs, dss, z_vals, 1);
 }
 
 /* marching.cu:271-397.  Slots are processed in index order; terminated slots take the next ray
