@@ -44,6 +44,9 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--render-frames", type=int, default=12, help="1920x1080 frames rendered on a 120-pose orbit")
+    p.add_argument("--render-slots", type=int, default=1 << 18, help="rays in flight in the inference renderer")
+    p.add_argument("--render-cap", type=int, default=8, help="march_steps_cap of the inference renderer")
     return p.parse_args()
 
 
@@ -307,6 +310,8 @@ def run_ours(args) -> dict:
                 "algorithmic_flops_per_launch": units,
                 "note": "FP32 SIMT kernel measured against the BF16 tensor peak (no FP32 peak is measured)"}
 
+    render = render_fps(args, tr, stream) if args.render_frames > 0 else None
+
     out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -323,7 +328,63 @@ def run_ours(args) -> dict:
            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": 4 * R,
                    "d2h_bytes_per_step": 16},
            "gpu_launches": int(launches), "roofline": roof, "kernels": breakdown, "clocks": clk.summary()}
+    if render is not None:
+        out["render_1080p"] = render
     return out
+
+
+def render_fps(args, tr, stream) -> dict:
+    """1920x1080 frames of the trained field on a 120-pose orbit (render_image_inference,
+    models/renderers/cuda.py:244-373), each frame's u8 image copied to pinned host memory inside
+    the timed region."""
+    import torch
+    from jaxngp_gb300 import _lib as L
+    from jaxngp_gb300.renderer import Renderer
+    from jaxngp_gb300.scene import PinholeCamera, orbit_poses, poses_to_transforms
+
+    cam = PinholeCamera.from_fov(1920, 1080, 40.0)
+    poses = torch.from_numpy(poses_to_transforms(orbit_poses(120, 4.0))).cuda()
+    rnd = Renderer.from_trainer(tr, n_slots=args.render_slots, march_steps_cap=args.render_cap)
+    host_img = torch.empty(cam.height, cam.width, 3, dtype=torch.uint8).pin_memory()
+    for f in range(2):
+        rnd.render_image(cam, poses[f])
+    torch.cuda.synchronize()
+    n = args.render_frames
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters = 0
+    launches0 = L.lib().ngp_kernel_launches()
+    e0.record(stream)
+    for f in range(n):
+        rgb, _ = rnd.render_image(cam, poses[(f * 120) // n])
+        host_img.copy_(rgb, non_blocking=True)
+        iters += rnd.iterations
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = L.lib().ngp_kernel_launches() - launches0
+    # per-entry-point device time over one frame
+    times = {}
+    orig_call = L.call
+
+    def timed_call(name, buffers, desc=None, stream=None):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        orig_call(name, buffers, desc, stream)
+        s1.record()
+        times.setdefault(name, []).append((s0, s1))
+    L.call = timed_call
+    try:
+        rnd.render_image(cam, poses[7])
+        torch.cuda.synchronize()
+    finally:
+        L.call = orig_call
+    per = {k: sum(a.elapsed_time(b) for a, b in v) for k, v in times.items()}
+    return {"fps": round(n / (ms / 1e3), 2), "ms_per_frame": round(ms / n, 3), "frames": n,
+            "width": cam.width, "height": cam.height, "poses": "120-pose orbit, radius 4, elevation 25 deg, fov 40",
+            "slots": args.render_slots, "march_steps_cap": args.render_cap,
+            "iterations_per_frame": round(iters / n, 1), "gpu_launches": int(launches),
+            "d2h_bytes_per_frame": cam.width * cam.height * 3,
+            "ms_per_frame_by_entry": {k: round(v, 4) for k, v in sorted(per.items(), key=lambda kv: -kv[1])}}
 
 
 def main():

@@ -40,6 +40,8 @@ int ngp_last_status(void);
 const char *ngp_last_status_message(void);
 /* ABI version of this library (bumped on any signature or descriptor change). */
 int ngp_abi_version(void);
+/* Number of kernels this library has launched in this process (all devices, all threads). */
+unsigned long long ngp_kernel_launches(void);
 
 /* ------------------------------------------------------- volrendjax descriptors (byte-exact) */
 /* deps/volume-rendering-jax/lib/impl/volrend.h:23-29 */
