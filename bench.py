@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
+                   help="field MLP: fp32 SIMT (parity path) or bf16 tensor cores")
     p.add_argument("--render-frames", type=int, default=12, help="1920x1080 frames rendered on a 120-pose orbit")
     p.add_argument("--render-slots", type=int, default=1 << 18, help="rays in flight in the inference renderer")
     p.add_argument("--render-cap", type=int, default=8, help="march_steps_cap of the inference renderer")
@@ -201,7 +203,7 @@ def run_ours(args) -> dict:
 
     L.lib().ngp_kernel_launches.restype = __import__("ctypes").c_ulonglong
     data = make_scene_data(n_views=args.views, width=args.res, height=args.res, seed=0)
-    cfg = TrainConfig(total_samples=args.samples, seed=rank)
+    cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=args.precision)
     tr = NGPTrainer(data, cfg)
     tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
@@ -314,7 +316,7 @@ def run_ours(args) -> dict:
 
     out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f32 (field MLP bf16 operands, f32 accumulation)",
            "data": "synthetic (procedural 64-blob scene, GT by 4096-step quadrature; NeRF-synthetic not used)",
            "config": {"workload": WORKLOAD, "rays_per_step": R, "sample_budget": args.samples,
                       "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,

@@ -42,6 +42,10 @@ const char *ngp_last_status_message(void);
 int ngp_abi_version(void);
 /* Number of kernels this library has launched in this process (all devices, all threads). */
 unsigned long long ngp_kernel_launches(void);
+/* Synchronises the current device, then returns NGP_ERR_DEVICE (and clears the flag) if a kernel
+ * recorded a device-side error since the last call -- a tensor-core kernel whose bounded wait for
+ * its MMAs ran out -- else NGP_OK, or NGP_ERR_CUDA if the synchronisation failed. */
+int ngp_device_status(void);
 
 /* ------------------------------------------------------- volrendjax descriptors (byte-exact) */
 /* deps/volume-rendering-jax/lib/impl/volrend.h:23-29 */
@@ -267,6 +271,19 @@ size_t ngp_field_backward_scratch_floats(void);
 #define NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES 524288
 void ngp_field_backward_noalloc(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_field_backward_noalloc_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* The three field ops on the fifth-generation tensor cores: BF16 operands (weights, encodings and
+ * activations rounded to BF16 on their way into each MMA), FP32 accumulation in tensor memory,
+ * FP32 outputs and weight gradients.  Same buffers, descriptors and semantics as
+ * ngp_field_forward / ngp_field_density / ngp_field_backward; the reference's MLP has no BF16
+ * form (its flax Dense layers compute in the parameters' FP32).  The backward's scratch has the
+ * size ngp_field_backward_scratch_floats() gives. */
+void ngp_field_forward_bf16(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_forward_bf16_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+void ngp_field_density_bf16(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_density_bf16_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+void ngp_field_backward_bf16(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_backward_bf16_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
 /* --------------------------------------------------------------- training-step kernels */
 /* Camera of the training set: pinhole intrinsics plus one 3x4 camera-to-world matrix per view

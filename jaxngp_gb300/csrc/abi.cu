@@ -43,6 +43,14 @@ int launch_mlp_density(cudaStream_t, std::uint32_t, const float *, const float *
 int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                         const float *, const float *, const float *, float *, float *, float *, bool);
 std::size_t mlp_partials_floats();
+int launch_mlp_partials_reduce(cudaStream_t, unsigned, const float *, float *, bool, std::uint32_t, const std::uint32_t *,
+                               float *);
+int launch_mlp_bf16_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                            const float *, float *);
+int launch_mlp_bf16_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
+int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                             const float *, const float *, const float *, float *, float *, unsigned *);
+int device_status();
 int launch_mlp_backward_noalloc(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                                 const float *, const float *, const float *, float *, float *, bool);
 int launch_render_blobs(cudaStream_t, const NgpRenderBlobsDescriptor &, const float *, const float *, const float *,
@@ -130,6 +138,7 @@ int ngp_last_status(void) { return t_status; }
 const char *ngp_last_status_message(void) { return t_message; }
 int ngp_abi_version(void) { return 1; }
 unsigned long long ngp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+int ngp_device_status(void) { return device_status(); }
 
 NGP_ENTRY(pack_density_into_bits) {
     NGP_DESC(PackbitsDescriptor, d);
@@ -247,6 +256,25 @@ NGP_ENTRY(ngp_field_backward) {
 }
 
 size_t ngp_field_backward_scratch_floats(void) { return mlp_partials_floats(); }
+
+NGP_ENTRY(ngp_field_forward_bf16) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_mlp_bf16_forward(stream, d.n_samples, CU32(3), CF32(0), CF32(1), CF32(2), F32(4));
+}
+
+NGP_ENTRY(ngp_field_density_bf16) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_mlp_bf16_density(stream, d.n_samples, CF32(0), CF32(1), F32(2));
+}
+
+NGP_ENTRY(ngp_field_backward_bf16) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    unsigned parts = 0;
+    const int st = launch_mlp_bf16_backward(stream, d.n_samples, CU32(4), CF32(0), CF32(1), CF32(2), CF32(3), CF32(5),
+                                            F32(7), F32(6), &parts);
+    if (st != NGP_OK) return st;
+    return launch_mlp_partials_reduce(stream, parts, CF32(6), F32(8), d.accumulate != 0, d.n_samples, CU32(4), F32(7));
+}
 
 NGP_ENTRY(ngp_field_backward_noalloc) {
     NGP_DESC(NgpMlpDescriptor, d);

@@ -503,6 +503,19 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
     return launch_status();
 }
 
+// Sums `parts` dL/dW partials into dL_dweights (fixed order) and zeroes dL/denc rows past the
+// active count: the tail shared by the FP32 and BF16 field backwards.
+int launch_mlp_partials_reduce(cudaStream_t stream, unsigned parts, const float *partials, float *dL_dweights,
+                               bool accumulate, std::uint32_t n, const std::uint32_t *count, float *dL_denc) {
+    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(parts, partials, dL_dweights, accumulate ? 1 : 0);
+    count_launches(1);
+    if (count != nullptr && n > 0) {
+        zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
 // Device address of g_noalloc_partials on the current device, looked up once per device (the
 // array's host-side name is only a stand-in and must never be handed to a kernel).
 static int noalloc_scratch(float **out) {

@@ -1,0 +1,623 @@
+// Field MLP on the fifth-generation tensor cores (tcgen05), BF16 operands with FP32 accumulation:
+// forward, density-only forward and backward with recomputation.  Same network, weights and
+// buffers as the FP32 kernels in mlp.cu (models/nerfs.py:39-86, 89-128, 221-238, 422-454):
+//
+//   h1 = relu(enc @ W0)  [32->64]     x = h1 @ W1  [64->16]       sigma = exp(x[0])
+//   h2 = relu([x, SH4(dir)] @ W2)  [32->64]   h3 = relu(h2 @ W3)  [64->64]
+//   rgb = sigmoid(h3 @ W4)  [64->3]           drgb = [sigma, rgb]
+//
+// Layout.  A warpgroup (128 threads) owns a tile of 128 samples, one sample per thread, and runs
+// the tile's layers as M=128 MMAs: the thread writes its sample's layer input as one BF16 row of a
+// shared-memory operand (core-matrix layout, see tc.cuh), one elected thread issues the MMAs, the
+// FP32 result lands in tensor memory (lane = sample), and every thread reads its row back with
+// tcgen05.ld for the activation.  The weights are converted to BF16 once per CTA and stay in
+// shared memory for its lifetime.  Several warpgroups per CTA work on independent tiles so that
+// one warpgroup's MMA latency hides behind another's activation work.
+//
+// Backward.  The forward is recomputed for the tile and its layer inputs stay in shared memory;
+// the adjoint of each layer is then one M=128 MMA for the data gradient (dX = dH @ W^T) and one
+// M=64 MMA for the weight gradient (dW = X^T dH over the tile's 128 samples), the latter reading
+// the same shared-memory rows as MN-major operands and accumulating in tensor memory across all
+// of the warpgroup's tiles.  Relu adjoints overwrite the layer inputs in place once the MMAs that
+// read them have completed.  At the end the warpgroups of a CTA add their dW into one partial;
+// mlp.cu's reduction sums the partials in a fixed order.
+//
+// Every mbarrier wait gives up after kWaitLimit polls; the warpgroup then stops, records
+// NGP_ERR_DEVICE for ngp_device_status(), and releases its tensor memory.
+#include "common.cuh"
+#include "tc.cuh"
+
+namespace ngp {
+
+__device__ unsigned int g_device_error = 0;
+
+namespace {
+
+using tc::smem_addr;
+
+constexpr int kW0 = 0, kW1 = 2048, kW2 = 3072, kW3 = 5120, kW4 = 9216, kNW = 9408;  // FP32 packed, flax [in][out]
+constexpr int kRows = 128;                    // samples per tile (MMA M)
+constexpr std::uint32_t kWaitLimit = 1u << 22;
+
+// BF16 weight operands (element offsets).  Forward: B[n = out][k = in] (= W^T); backward data
+// gradients: B[n = in][k = out] (= W).  Layer 4 has 3 outputs, padded to 16 with zeros.
+constexpr int kF0 = 0, kF1 = 2048, kF2 = 3072, kF3 = 5120, kF4 = 9216, kFwdW = 10240;
+constexpr int kG4 = 10240, kG3 = 11264, kG2 = 15360, kG1 = 16384, kG0 = 17408, kAllW = 19456;
+
+// Per-warpgroup activation rows (element offsets): layer inputs of the tile, and the output-layer
+// gradient for the backward.
+constexpr int kX0 = 0, kH1 = 4096, kX2 = 12288, kH2 = 16384, kH3 = 24576, kDY = 32768;
+constexpr int kFwdAct = 32768, kBwdAct = 34816;
+
+// Tensor-memory columns of a warpgroup.
+constexpr std::uint32_t kDA = 0, kDB = 64;                                    // layer outputs
+constexpr std::uint32_t kA0 = 80, kA1 = 112, kA2 = 128, kA3 = 160, kA4 = 224;  // dW accumulators
+
+__device__ __forceinline__ std::uint32_t active_count(std::uint32_t n, const std::uint32_t *count) {
+    return count != nullptr ? min(n, *count) : n;
+}
+
+bool aligned16(const void *p) { return ((std::uintptr_t)p & 15u) == 0; }
+
+// Element offset of X[r][c] in a row-block buffer with `cols` BF16 columns.
+__device__ __forceinline__ int rb(int r, int c, int cols) {
+    return (r >> 3) * (cols * 8) + (c >> 3) * 64 + (r & 7) * 8 + (c & 7);
+}
+
+// Stores v[0..n) as row r of a buffer with n columns (n % 8 == 0), 16 bytes at a time.
+template <int N>
+__device__ __forceinline__ void store_row(__nv_bfloat16 *buf, int r, const float *v) {
+#pragma unroll
+    for (int c = 0; c < N; c += 8) {
+        uint4 q;
+        q.x = tc::pack_bf16(v[c + 0], v[c + 1]);
+        q.y = tc::pack_bf16(v[c + 2], v[c + 3]);
+        q.z = tc::pack_bf16(v[c + 4], v[c + 5]);
+        q.w = tc::pack_bf16(v[c + 6], v[c + 7]);
+        *reinterpret_cast<uint4 *>(buf + rb(r, c, N)) = q;
+    }
+}
+
+// Loads row r of a buffer with N columns.
+template <int N>
+__device__ __forceinline__ void load_row(const __nv_bfloat16 *buf, int r, float *v) {
+#pragma unroll
+    for (int c = 0; c < N; c += 8) {
+        const uint4 q = *reinterpret_cast<const uint4 *>(buf + rb(r, c, N));
+        const std::uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
+            const float2 f = __bfloat1622float2(h);
+            v[c + 2 * j] = f.x;
+            v[c + 2 * j + 1] = f.y;
+        }
+    }
+}
+
+__device__ __forceinline__ void sh4(float x, float y, float z, float *o) {
+    const float xy = x * y, xz = x * z, yz = y * z, x2 = x * x, y2 = y * y, z2 = z * z;
+    o[0] = 0.28209479177387814f;
+    o[1] = -0.48860251190291987f * y;
+    o[2] = 0.48860251190291987f * z;
+    o[3] = -0.48860251190291987f * x;
+    o[4] = 1.0925484305920792f * xy;
+    o[5] = -1.0925484305920792f * yz;
+    o[6] = 0.94617469575755997f * z2 - 0.31539156525251999f;
+    o[7] = -1.0925484305920792f * xz;
+    o[8] = 0.54627421529603959f * x2 - 0.54627421529603959f * y2;
+    o[9] = 0.59004358992664352f * y * (-3.0f * x2 + y2);
+    o[10] = 2.8906114426405538f * xy * z;
+    o[11] = 0.45704579946446572f * y * (1.0f - 5.0f * z2);
+    o[12] = 0.3731763325901154f * z * (5.0f * z2 - 3.0f);
+    o[13] = 0.45704579946446572f * x * (1.0f - 5.0f * z2);
+    o[14] = 1.4453057213202769f * z * (x2 - y2);
+    o[15] = 0.59004358992664352f * x * (-x2 + 3.0f * y2);
+}
+
+// Converts the FP32 weights into the BF16 operand layouts (backward copies only when `bwd`).
+__device__ void load_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *sw, bool bwd) {
+    const int total = bwd ? kAllW : kFwdW;
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    for (int i = threadIdx.x; i < total; i += blockDim.x) sw[i] = zero;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kNW; i += blockDim.x) {
+        const __nv_bfloat16 v = __float2bfloat16(w[i]);
+        if (i < kW1) {  // W0 [32][64]
+            const int in = i / 64, out = i % 64;
+            sw[kF0 + rb(out, in, 32)] = v;
+            if (bwd) sw[kG0 + rb(in, out, 64)] = v;
+        } else if (i < kW2) {  // W1 [64][16]
+            const int j = i - kW1, in = j / 16, out = j % 16;
+            sw[kF1 + rb(out, in, 64)] = v;
+            if (bwd) sw[kG1 + rb(in, out, 16)] = v;
+        } else if (i < kW3) {  // W2 [32][64]; the data gradient needs rows 0..15 (x) only
+            const int j = i - kW2, in = j / 64, out = j % 64;
+            sw[kF2 + rb(out, in, 32)] = v;
+            if (bwd && in < 16) sw[kG2 + rb(in, out, 64)] = v;
+        } else if (i < kW4) {  // W3 [64][64]
+            const int j = i - kW3, in = j / 64, out = j % 64;
+            sw[kF3 + rb(out, in, 64)] = v;
+            if (bwd) sw[kG3 + rb(in, out, 64)] = v;
+        } else {  // W4 [64][3]
+            const int j = i - kW4, in = j / 3, out = j % 3;
+            sw[kF4 + rb(out, in, 64)] = v;
+            if (bwd) sw[kG4 + rb(in, out, 16)] = v;
+        }
+    }
+}
+
+// D (tmem) = A @ B^T with both operands K-major: A = rows of a buffer with K columns (M = 128
+// samples), B = weight operand [N][K].
+__device__ __forceinline__ void mma_kk(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int K, int N,
+                                       bool acc) {
+    const std::uint32_t id = tc::idesc_bf16(128, N, false, false);
+    const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), sbo = (std::uint32_t)K * 16;
+    for (int j = 0; j < K / 16; ++j)
+        tc::mma_bf16(d, tc::sdesc(sa + j * 256, 128, sbo), tc::sdesc(sb + j * 256, 128, sbo), id, acc || j > 0);
+}
+
+// D (tmem, M = 64) += A^T @ B over the tile's 128 samples: A = buffer with 64 columns, B = buffer
+// with N columns, both read MN-major (the sample index is the contraction).
+__device__ __forceinline__ void mma_mn(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int N, bool acc) {
+    const std::uint32_t id = tc::idesc_bf16(64, N, true, true);
+    const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), la = 64 * 16, lb = (std::uint32_t)N * 16;
+    for (int j = 0; j < kRows / 16; ++j)
+        tc::mma_bf16(d, tc::sdesc(sa + j * 2 * la, la, 128), tc::sdesc(sb + j * 2 * lb, lb, 128), id, acc || j > 0);
+}
+
+// TMEM lane that holds row m of an M = 64 result: rows 16j..16j+15 sit in lanes 32j..32j+15
+// (measured with known operands).
+__device__ __forceinline__ int m64_lane(int m) { return (m >> 4) * 32 + (m & 15); }
+
+struct WarpGroup {
+    int g;             // warpgroup index in the CTA
+    int r;             // this thread's row (sample) in the tile, = its TMEM lane
+    std::uint32_t tm;  // tensor-memory address of the warpgroup's columns, lane base of this warp
+    std::uint64_t *bar;
+    std::uint32_t phase;
+    int *fail;
+
+    // Waits for the warpgroup's MMAs to complete; records a time-out.
+    __device__ __forceinline__ void wait() {
+        if (!tc::mbar_wait(bar, phase, kWaitLimit)) *fail = 1;
+        phase ^= 1u;
+        tc::fence_after();
+    }
+    // Makes this thread's shared-memory rows and tensor-memory reads ordered before the MMAs that
+    // the elected thread issues next.
+    __device__ __forceinline__ void sync() {
+        tc::fence_async_smem();
+        tc::fence_before();
+        tc::bar_sync(1 + g, 128);
+        tc::fence_after();
+    }
+};
+
+// Forward through one tile; on return H1, X2, H2, H3 hold the layer inputs (BF16), and x0 / rgb
+// this thread's pre-activation density and colour.
+__device__ __forceinline__ void tile_forward(WarpGroup &wg, const __nv_bfloat16 *sw, __nv_bfloat16 *act,
+                                             const float dir[3], float &x0, float rgb[3]) {
+    float v[64];
+    const bool leader = wg.r == 0;
+    // layer 0
+    wg.sync();
+    if (leader) { mma_kk(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
+    wg.wait();
+    tc::ld64(wg.tm + kDA, v);
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+    store_row<64>(act + kH1, wg.r, v);
+    // layer 1
+    wg.sync();
+    if (leader) { mma_kk(wg.tm + kDB, act + kH1, sw + kF1, 64, 16, false); tc::commit(wg.bar); }
+    wg.wait();
+    tc::ld16(wg.tm + kDB, v);
+    x0 = v[0];
+    sh4(dir[0], dir[1], dir[2], v + 16);
+    store_row<32>(act + kX2, wg.r, v);
+    // layer 2
+    wg.sync();
+    if (leader) { mma_kk(wg.tm + kDA, act + kX2, sw + kF2, 32, 64, false); tc::commit(wg.bar); }
+    wg.wait();
+    tc::ld64(wg.tm + kDA, v);
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+    store_row<64>(act + kH2, wg.r, v);
+    // layer 3
+    wg.sync();
+    if (leader) { mma_kk(wg.tm + kDA, act + kH2, sw + kF3, 64, 64, false); tc::commit(wg.bar); }
+    wg.wait();
+    tc::ld64(wg.tm + kDA, v);
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+    store_row<64>(act + kH3, wg.r, v);
+    // layer 4
+    wg.sync();
+    if (leader) { mma_kk(wg.tm + kDB, act + kH3, sw + kF4, 64, 16, false); tc::commit(wg.bar); }
+    wg.wait();
+    tc::ld16(wg.tm + kDB, v);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rgb[c] = 1.f / (1.f + expf(-v[c]));
+}
+
+__device__ __forceinline__ void load_enc_row(const float *__restrict__ enc, std::size_t s, bool valid, float *v) {
+#pragma unroll
+    for (int c = 0; c < 32; c += 4) {
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) q = *reinterpret_cast<const float4 *>(enc + s * 32 + c);
+        v[c] = q.x;
+        v[c + 1] = q.y;
+        v[c + 2] = q.z;
+        v[c + 3] = q.w;
+    }
+}
+
+template <int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_forward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ std::uint64_t bars[NWG];
+    __shared__ std::uint32_t tbase;
+    __shared__ int fails[NWG];
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
+    __nv_bfloat16 *act = sw + kFwdW + g * kFwdAct;
+    load_weights_bf16(weights, sw, false);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NWG; ++k) {
+            tc::mbar_init(&bars[k], 1);
+            fails[k] = 0;
+        }
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(&tbase, 512);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    WarpGroup wg{g, r, tbase + (std::uint32_t)g * 128u + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
+
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += gridDim.x * NWG) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n_act;
+        float v[32], dir[3] = {0.f, 0.f, 1.f};
+        load_enc_row(enc, s, valid, v);
+        if (valid) {
+            dir[0] = dirs[s * 3 + 0];
+            dir[1] = dirs[s * 3 + 1];
+            dir[2] = dirs[s * 3 + 2];
+        }
+        store_row<32>(act + kX0, r, v);
+        float x0, rgb[3];
+        tile_forward(wg, sw, act, dir, x0, rgb);
+        if (valid) reinterpret_cast<float4 *>(drgb)[s] = make_float4(expf(x0), rgb[0], rgb[1], rgb[2]);
+        tc::bar_sync(1 + g, 128);
+        if (*wg.fail) break;
+    }
+    if (*wg.fail && r == 0) atomicOr(&g_device_error, 1u);
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
+}
+
+// sigma only (NeRF.__call__ with dir=None, nerfs.py:71-72): layers 0 and 1.
+template <int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_density_kernel(
+    std::uint32_t n, const float *__restrict__ enc, const float *__restrict__ weights, float *__restrict__ sigma) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ std::uint64_t bars[NWG];
+    __shared__ std::uint32_t tbase;
+    __shared__ int fails[NWG];
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
+    __nv_bfloat16 *act = sw + kFwdW + g * kFwdAct;
+    load_weights_bf16(weights, sw, false);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NWG; ++k) {
+            tc::mbar_init(&bars[k], 1);
+            fails[k] = 0;
+        }
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(&tbase, 512);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    WarpGroup wg{g, r, tbase + (std::uint32_t)g * 128u + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
+    const bool leader = r == 0;
+    const std::uint32_t n_tiles = (n + kRows - 1) / kRows;
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += gridDim.x * NWG) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n;
+        float v[64];
+        load_enc_row(enc, s, valid, v);
+        store_row<32>(act + kX0, r, v);
+        wg.sync();
+        if (leader) { mma_kk(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld64(wg.tm + kDA, v);
+#pragma unroll
+        for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+        store_row<64>(act + kH1, r, v);
+        wg.sync();
+        if (leader) { mma_kk(wg.tm + kDB, act + kH1, sw + kF1, 64, 16, false); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld16(wg.tm + kDB, v);
+        if (valid) sigma[s] = expf(v[0]);
+        tc::bar_sync(1 + g, 128);
+        if (*wg.fail) break;
+    }
+    if (*wg.fail && r == 0) atomicOr(&g_device_error, 1u);
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
+}
+
+// Backward.  `grad_scale` multiplies dL/ddrgb; `partials` receives one [9408] dL/dW partial per CTA.
+template <int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_backward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ dirs, const float *__restrict__ weights, const float *__restrict__ dL_ddrgb,
+    const float *__restrict__ grad_scale, float *__restrict__ dL_denc, float *__restrict__ partials) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ std::uint64_t bars[NWG];
+    __shared__ std::uint32_t tbase;
+    __shared__ int fails[NWG];
+    __shared__ int tiles_done[NWG];
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
+    __nv_bfloat16 *act = sw + kAllW + g * kBwdAct;
+    load_weights_bf16(weights, sw, true);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NWG; ++k) {
+            tc::mbar_init(&bars[k], 1);
+            fails[k] = 0;
+            tiles_done[k] = 0;
+        }
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(&tbase, 512);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const std::uint32_t tm0 = tbase + (std::uint32_t)g * 256u;
+    WarpGroup wg{g, r, tm0 + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
+    const bool leader = r == 0;
+    const float gs = grad_scale != nullptr ? *grad_scale : 1.f;
+
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
+    bool first = true;
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += gridDim.x * NWG) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n_act;
+        float v[64], dir[3] = {0.f, 0.f, 1.f};
+        load_enc_row(enc, s, valid, v);
+        if (valid) {
+            dir[0] = dirs[s * 3 + 0];
+            dir[1] = dirs[s * 3 + 1];
+            dir[2] = dirs[s * 3 + 2];
+        }
+        store_row<32>(act + kX0, r, v);
+        float x0, rgb[3];
+        tile_forward(wg, sw, act, dir, x0, rgb);
+
+        // output layer: dL/da4 (3, padded to 16) and dL/dx0 through the truncated exponential
+        float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) go = reinterpret_cast<const float4 *>(dL_ddrgb)[s];
+        const float dx0 = gs * go.x * expf(fminf(fmaxf(x0, -15.f), 15.f));
+        {
+            float d[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) d[i] = 0.f;
+            d[0] = gs * go.y * rgb[0] * (1.f - rgb[0]);
+            d[1] = gs * go.z * rgb[1] * (1.f - rgb[1]);
+            d[2] = gs * go.w * rgb[2] * (1.f - rgb[2]);
+            store_row<16>(act + kDY, r, d);
+        }
+        // layer 4: dW4 += h3^T dA4;  dh3 = dA4 @ W4^T
+        wg.sync();
+        if (leader) {
+            mma_mn(tm0 + kA4, act + kH3, act + kDY, 16, !first);
+            mma_kk(tm0 + kDA, act + kDY, sw + kG4, 16, 64, false);
+            tc::commit(wg.bar);
+        }
+        wg.wait();
+        tc::ld64(wg.tm + kDA, v);
+        {
+            float h[64];
+            load_row<64>(act + kH3, r, h);
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
+        }
+        store_row<64>(act + kH3, r, v);  // dA3 over h3
+        // layer 3: dW3^T += dA3^T h2;  dh2 = dA3 @ W3^T
+        wg.sync();
+        if (leader) {
+            mma_mn(tm0 + kA3, act + kH3, act + kH2, 64, !first);
+            mma_kk(tm0 + kDA, act + kH3, sw + kG3, 64, 64, false);
+            tc::commit(wg.bar);
+        }
+        wg.wait();
+        tc::ld64(wg.tm + kDA, v);
+        {
+            float h[64];
+            load_row<64>(act + kH2, r, h);
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
+        }
+        store_row<64>(act + kH2, r, v);  // dA2 over h2
+        // layer 2: dW2^T += dA2^T [x, sh];  dx = dA2 @ W2[:16]^T
+        wg.sync();
+        if (leader) {
+            mma_mn(tm0 + kA2, act + kH2, act + kX2, 32, !first);
+            mma_kk(tm0 + kDB, act + kH2, sw + kG2, 64, 16, false);
+            tc::commit(wg.bar);
+        }
+        wg.wait();
+        tc::ld16(wg.tm + kDB, v);
+        v[0] += dx0;
+        store_row<16>(act + kX2, r, v);  // dx (16 columns) over [x, sh]
+        // layer 1: dW1 += h1^T dx;  dh1 = dx @ W1^T
+        wg.sync();
+        if (leader) {
+            mma_mn(tm0 + kA1, act + kH1, act + kX2, 16, !first);
+            mma_kk(tm0 + kDA, act + kX2, sw + kG1, 16, 64, false);
+            tc::commit(wg.bar);
+        }
+        wg.wait();
+        tc::ld64(wg.tm + kDA, v);
+        {
+            float h[64];
+            load_row<64>(act + kH1, r, h);
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
+        }
+        store_row<64>(act + kH1, r, v);  // dA1 over h1
+        // layer 0: dW0^T += dA1^T enc;  denc = dA1 @ W0^T
+        wg.sync();
+        if (leader) {
+            mma_mn(tm0 + kA0, act + kH1, act + kX0, 32, !first);
+            mma_kk(tm0 + kDA, act + kH1, sw + kG0, 64, 32, false);
+            tc::commit(wg.bar);
+        }
+        wg.wait();
+        tc::ld32(wg.tm + kDA, v);
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < 32; c += 4)
+                *reinterpret_cast<float4 *>(dL_denc + s * 32 + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+        }
+        first = false;
+        tc::bar_sync(1 + g, 128);
+        if (*wg.fail) break;
+    }
+    if (r == 0) {
+        tiles_done[g] = first ? 0 : 1;
+        if (*wg.fail) atomicOr(&g_device_error, 1u);
+    }
+
+    // dW: every warpgroup writes its sums, in the packed [in][out] layout, over its own activation
+    // rows (free now); the CTA then adds the warpgroups' copies in a fixed order into its partial.
+    // Row m of an M = 64 accumulator sits in TMEM lane m64_lane(m); each element has one writer.
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    float *mine = reinterpret_cast<float *>(act);
+    if (tiles_done[g]) {
+        const int lane = q * 32 + (threadIdx.x & 31);
+        const std::uint32_t base = tm0 + ((std::uint32_t)(q * 32) << 16);
+        int m = -1;
+        for (int k = 0; k < 64; ++k)
+            if (m64_lane(k) == lane) m = k;
+        float a[64];
+        tc::ld32(base + kA0, a);  // dW0^T: row = out, 32 columns = in
+        if (m >= 0)
+            for (int i = 0; i < 32; ++i) mine[kW0 + i * 64 + m] = a[i];
+        tc::ld16(base + kA1, a);  // dW1: row = in, 16 columns = out
+        if (m >= 0)
+            for (int o = 0; o < 16; ++o) mine[kW1 + m * 16 + o] = a[o];
+        tc::ld32(base + kA2, a);  // dW2^T: row = out, 32 columns = in
+        if (m >= 0)
+            for (int i = 0; i < 32; ++i) mine[kW2 + i * 64 + m] = a[i];
+        tc::ld64(base + kA3, a);  // dW3^T: row = out, 64 columns = in
+        if (m >= 0)
+            for (int i = 0; i < 64; ++i) mine[kW3 + i * 64 + m] = a[i];
+        tc::ld16(base + kA4, a);  // dW4: row = in, columns 0..2 = out
+        if (m >= 0)
+            for (int o = 0; o < 3; ++o) mine[kW4 + m * 3 + o] = a[o];
+    } else {
+        for (int i = r; i < kNW; i += 128) mine[i] = 0.f;
+    }
+    __syncthreads();
+    float *p = partials + (std::size_t)blockIdx.x * kNW;
+    for (int i = threadIdx.x; i < kNW; i += NWG * 128) {
+        float a = 0.f;
+#pragma unroll
+        for (int k = 0; k < NWG; ++k) a += reinterpret_cast<const float *>(sw + kAllW + k * kBwdAct)[i];
+        p[i] = a;
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
+}
+
+constexpr int kFwdWgs = 3, kBwdWgs = 2;
+constexpr std::size_t kFwdSmem = (std::size_t)(kFwdW + kFwdWgs * kFwdAct) * 2;
+constexpr std::size_t kBwdSmem = (std::size_t)(kAllW + kBwdWgs * kBwdAct) * 2;
+static_assert(kBwdAct * 2 >= kNW * 4, "dW sums fit over a warpgroup's rows");
+
+}  // namespace
+
+// ------------------------------------------------------------------------------- launchers
+
+int launch_mlp_bf16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                            const float *dirs, const float *weights, float *drgb) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp (bf16): enc, weights and drgb must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_bf16_forward_kernel<kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        attr = true;
+    }
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kRows - 1) / kRows;
+    const unsigned want = (tiles + kFwdWgs - 1) / kFwdWgs;
+    const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
+    mlp_bf16_forward_kernel<kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
+    count_launches(1);
+    return launch_status();
+}
+
+int launch_mlp_bf16_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp (bf16): enc and weights must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_bf16_density_kernel<kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        attr = true;
+    }
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kRows - 1) / kRows;
+    const unsigned want = (tiles + kFwdWgs - 1) / kFwdWgs;
+    const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
+    mlp_bf16_density_kernel<kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(n, enc, weights, sigma);
+    count_launches(1);
+    return launch_status();
+}
+
+// `partials` holds at least sm_count() x 9408 floats; one partial per CTA, grid = sm_count().
+int launch_mlp_bf16_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                             const float *dirs, const float *weights, const float *dL_ddrgb, const float *grad_scale,
+                             float *dL_denc, float *partials, unsigned *grid_out) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
+                  "mlp (bf16): buffers must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_bf16_backward_kernel<kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        attr = true;
+    }
+    const unsigned grid = (unsigned)sm_count();
+    mlp_bf16_backward_kernel<kBwdWgs><<<grid, kBwdWgs * 128, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
+                                                                                grad_scale, dL_denc, partials);
+    count_launches(1);
+    *grid_out = grid;
+    return launch_status();
+}
+
+// Reads and clears the device error word (synchronises the device).
+int device_status() {
+    unsigned v = 0;
+    NGP_CUDA_TRY(cudaDeviceSynchronize());
+    NGP_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_device_error, sizeof(v)));
+    if (v != 0) {
+        const unsigned zero = 0;
+        NGP_CUDA_TRY(cudaMemcpyToSymbol(g_device_error, &zero, sizeof(zero)));
+        set_last_status(NGP_ERR_DEVICE, "a tensor-core kernel gave up waiting for its MMAs");
+        return NGP_ERR_DEVICE;
+    }
+    return launch_status();
+}
+
+}  // namespace ngp

@@ -38,20 +38,34 @@ def unpack_weights(flat: torch.Tensor) -> Dict[str, torch.Tensor]:
 
 # ------------------------------------------------------------------------------ raw entry points
 
+PRECISIONS = ("fp32", "bf16")
+
+
+def entry(name: str, precision: str) -> str:
+    """Entry point of a field op for a precision: "fp32" (SIMT, the parity path) or "bf16"
+    (tensor cores, BF16 operands with FP32 accumulation)."""
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
+    return name if precision == "fp32" else f"{name}_{precision}"
+
+
 def field_forward(enc: torch.Tensor, dirs: torch.Tensor, weights: torch.Tensor,
-                  count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+                  count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None,
+                  precision: str = "fp32") -> torch.Tensor:
     n = enc.shape[0]
     if out is None:
         out = torch.empty(n, 4, dtype=torch.float32, device=enc.device)
-    L.call("ngp_field_forward", [enc.contiguous(), dirs.contiguous(), weights, count, out], L.NgpMlpDescriptor(n, 0))
+    L.call(entry("ngp_field_forward", precision), [enc.contiguous(), dirs.contiguous(), weights, count, out],
+           L.NgpMlpDescriptor(n, 0))
     return out
 
 
-def field_density(enc: torch.Tensor, weights: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+def field_density(enc: torch.Tensor, weights: torch.Tensor, out: Optional[torch.Tensor] = None,
+                  precision: str = "fp32") -> torch.Tensor:
     n = enc.shape[0]
     if out is None:
         out = torch.empty(n, dtype=torch.float32, device=enc.device)
-    L.call("ngp_field_density", [enc.contiguous(), weights, out], L.NgpMlpDescriptor(n, 0))
+    L.call(entry("ngp_field_density", precision), [enc.contiguous(), weights, out], L.NgpMlpDescriptor(n, 0))
     return out
 
 
@@ -69,7 +83,7 @@ def backward_scratch(device) -> torch.Tensor:
 def field_backward(enc: torch.Tensor, dirs: torch.Tensor, weights: torch.Tensor, dL_ddrgb: torch.Tensor,
                    count: Optional[torch.Tensor] = None, grad_scale: Optional[torch.Tensor] = None,
                    dL_denc: Optional[torch.Tensor] = None, dL_dw: Optional[torch.Tensor] = None,
-                   accumulate: bool = False, scratch: Optional[torch.Tensor] = None):
+                   accumulate: bool = False, scratch: Optional[torch.Tensor] = None, precision: str = "fp32"):
     n = enc.shape[0]
     dev = enc.device
     if dL_denc is None:
@@ -78,8 +92,9 @@ def field_backward(enc: torch.Tensor, dirs: torch.Tensor, weights: torch.Tensor,
         dL_dw = torch.zeros(L.MLP_WEIGHTS, dtype=torch.float32, device=dev)
     if scratch is None:
         scratch = backward_scratch(dev)
-    L.call("ngp_field_backward", [enc.contiguous(), dirs.contiguous(), weights, dL_ddrgb.contiguous(), count,
-                                  grad_scale, scratch, dL_denc, dL_dw], L.NgpMlpDescriptor(n, 1 if accumulate else 0))
+    L.call(entry("ngp_field_backward", precision),
+           [enc.contiguous(), dirs.contiguous(), weights, dL_ddrgb.contiguous(), count, grad_scale, scratch, dL_denc,
+            dL_dw], L.NgpMlpDescriptor(n, 1 if accumulate else 0))
     return dL_denc, dL_dw
 
 

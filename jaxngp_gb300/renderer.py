@@ -17,15 +17,17 @@ import torch
 
 from . import _lib as L
 from .encoders import LevelTable
+from .field import entry as field_entry
 
 
 class Renderer:
     def __init__(self, latents: torch.Tensor, weights: torch.Tensor, table: LevelTable, bitfield: torch.Tensor,
                  K: int, G: int, bound: float, stepsize_portion: float, diagonal_n_steps: int = 1024,
-                 n_slots: int = 1 << 18, march_steps_cap: int = 8, poll_every: int = 4):
+                 n_slots: int = 1 << 18, march_steps_cap: int = 8, poll_every: int = 4, precision: str = "fp32"):
         self.latents, self.weights, self.table, self.bitfield = latents, weights, table, bitfield
         self.K, self.G, self.bound, self.sp, self.dns = K, G, float(bound), float(stepsize_portion), diagonal_n_steps
         self.n_slots, self.cap, self.poll_every = n_slots, march_steps_cap, poll_every
+        self.field_fwd = field_entry("ngp_field_forward", precision)
         dev = latents.device
         n, c = n_slots, march_steps_cap
         f32 = dict(dtype=torch.float32, device=dev)
@@ -45,6 +47,7 @@ class Renderer:
 
     @classmethod
     def from_trainer(cls, tr, **kw) -> "Renderer":
+        kw.setdefault("precision", tr.cfg.mlp_precision)
         return cls(tr.latents, tr.weights, tr.table, tr.bitfield, tr.K, tr.cfg.G, tr.bound, tr.sp,
                    tr.cfg.diagonal_n_steps, **kw)
 
@@ -71,7 +74,7 @@ class Renderer:
                        [rays_o, rays_d, t_starts, t_ends, self.bitfield, self.terminated, self.indices, self.next_ray,
                         self.n_samples, self.xyzs, self.dirs, self.dss, self.zs], dm)
                 L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, None, self.enc], dh)
-                L.call("ngp_field_forward", [self.enc, self.dirs, self.weights, None, self.drgbs], df)
+                L.call(self.field_fwd, [self.enc, self.dirs, self.weights, None, self.drgbs], df)
                 L.call("ngp_integrate_rays_inference_inplace",
                        [rays_bg, rgbd, T, self.n_samples, self.indices, self.dss, self.zs, self.drgbs, self.total,
                         self.terminated], di)

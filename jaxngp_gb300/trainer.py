@@ -26,7 +26,7 @@ import torch
 
 from . import _lib as L
 from .encoders import LevelTable
-from .field import SHAPES, glorot_uniform, pack_weights
+from .field import SHAPES, entry as field_entry, glorot_uniform, pack_weights
 from .scene import SceneData
 
 
@@ -47,6 +47,7 @@ class TrainConfig:
     near: float = 0.3
     huber_delta: float = 0.1
     seed: int = 0
+    mlp_precision: str = "fp32"        # "fp32" (SIMT parity path) or "bf16" (tensor cores)
 
 
 def cascades_for(bound: float) -> int:
@@ -141,6 +142,9 @@ class NGPTrainer:
         self.mark_untrained_grid()
 
     # ---------------------------------------------------------------------------- helpers
+    def _mlp(self, name: str) -> str:
+        return field_entry(name, self.cfg.mlp_precision)
+
     def _next_seed(self) -> int:
         return int(self._seed.spawn(1)[0].generate_state(1, np.uint64)[0])
 
@@ -207,7 +211,7 @@ class NGPTrainer:
                 n = min(chunk, M - s)
                 enc = self.enc[:n] if n <= self.S else torch.empty(n, 32, dtype=torch.float32, device=self.dev)
                 L.call("ngp_hashgrid_forward", [xyz[s:s + n], self.latents, None, enc], self.table.descriptor(n, self.bound))
-                L.call("ngp_field_density", [enc, self.weights, sigma[s:s + n]], L.NgpMlpDescriptor(n, 0))
+                L.call(self._mlp("ngp_field_density"), [enc, self.weights, sigma[s:s + n]], L.NgpMlpDescriptor(n, 0))
             L.call("ngp_ogrid_max", [cells, sigma, self.density], d)
         L.call("ngp_ogrid_threshold", [self.density, self.thr_scratch, self.threshold], self._ogrid_desc())
         L.call("ngp_packbits_scalar", [self.threshold, self.density, self.occ_mask, self.bitfield],
@@ -230,11 +234,11 @@ class NGPTrainer:
                                         self.queue], self._d_march)
         L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
         L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, self.count, self.enc], self._d_hg)
-        L.call("ngp_field_forward", [self.enc, self.dirs, self.weights, self.count, self.drgbs], self._d_mlp)
+        L.call(self._mlp("ngp_field_forward"), [self.enc, self.dirs, self.weights, self.count, self.drgbs], self._d_mlp)
         L.call("ngp_integrate_loss_backward", [self.valid, self.startidx, self.n_samples, self.bgs, self.gt, self.dss,
                                                self.z_vals, self.drgbs, self.count, self.loss_scratch, self.g_drgbs,
                                                self.stats, self.grad_scale], self._d_loss)
-        L.call("ngp_field_backward", [self.enc, self.dirs, self.weights, self.g_drgbs, self.count, self.grad_scale,
+        L.call(self._mlp("ngp_field_backward"), [self.enc, self.dirs, self.weights, self.g_drgbs, self.count, self.grad_scale,
                                       self.mlp_scratch, self.g_enc, self.g_w], self._d_mlp)
         L.call("ngp_hashgrid_backward", [self.xyzs, self.g_enc, self.count, self.g_lat], self._d_hg_acc)
         count = self.step_count
@@ -274,7 +278,7 @@ class NGPTrainer:
             enc = torch.empty(max_samples, 32, device=self.dev)
             L.call("ngp_hashgrid_forward", [xyz, self.latents, count, enc], self.table.descriptor(max_samples, self.bound))
             drgb = torch.zeros(max_samples, 4, device=self.dev)
-            L.call("ngp_field_forward", [enc, dirs, self.weights, count, drgb], L.NgpMlpDescriptor(max_samples, 0))
+            L.call(self._mlp("ngp_field_forward"), [enc, dirs, self.weights, count, drgb], L.NgpMlpDescriptor(max_samples, 0))
             m = torch.empty(1, **i32)
             rgbd = torch.empty(n, 4, device=self.dev)
             opac = torch.empty(n, device=self.dev)

@@ -113,6 +113,66 @@ def backward(dL_ddrgb: np.ndarray, cache, w: Dict[str, np.ndarray], dtype=np.flo
     return denc, grads
 
 
+def round_bf16(x) -> np.ndarray:
+    """float32 values rounded to bfloat16 (nearest, ties to even), returned as float32."""
+    a = np.ascontiguousarray(x, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).reshape(a.shape)
+
+
+def _bf(x):
+    return round_bf16(np.asarray(x, np.float32)).astype(np.float64)
+
+
+def forward_bf16(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray]):
+    """The BF16 tensor-core forward restated: every MMA operand (weights, encodings, layer inputs)
+    rounded to bfloat16, products accumulated exactly (FP64 here, FP32 on the GPU).  Returns
+    (drgb [S,4] float64, cache)."""
+    wb = {k: _bf(v) for k, v in w.items()}
+    enc_b = _bf(enc)
+    a1 = enc_b @ wb["W0"]
+    h1 = _bf(np.maximum(a1, 0))
+    x = h1 @ wb["W1"]
+    sigma = np.exp(x[:, :1])
+    sh = sh4(np.asarray(dirs, np.float32)).astype(np.float64)
+    c = _bf(np.concatenate([x, sh], axis=-1))
+    a2 = c @ wb["W2"]
+    h2 = _bf(np.maximum(a2, 0))
+    a3 = h2 @ wb["W3"]
+    h3 = _bf(np.maximum(a3, 0))
+    a4 = h3 @ wb["W4"]
+    rgb = 1 / (1 + np.exp(-a4))
+    drgb = np.concatenate([sigma, rgb], axis=-1)
+    return drgb, dict(enc=enc_b, h1=h1, x=x, c=c, h2=h2, h3=h3, rgb=rgb, wb=wb)
+
+
+def backward_bf16(dL_ddrgb: np.ndarray, cache, grad_scale: float = 1.0):
+    """The BF16 tensor-core backward restated: each layer's output gradient is rounded to bfloat16
+    before it enters the data- and weight-gradient MMAs; relu masks come from the BF16 layer
+    inputs.  Returns (dL_denc [S,32], dict of dL_dW) in float64."""
+    c, wb = cache, cache["wb"]
+    g = np.asarray(dL_ddrgb, np.float64) * grad_scale
+    dx0 = g[:, 0] * np.exp(np.clip(c["x"][:, 0], -15, 15))
+    rgb = c["rgb"]
+    d4 = np.zeros((g.shape[0], 3))
+    d4[:] = g[:, 1:] * rgb * (1 - rgb)
+    d4 = _bf(d4)
+    grads = {"W4": c["h3"].T @ d4}
+    d3 = _bf((d4 @ wb["W4"].T) * (c["h3"] > 0))
+    grads["W3"] = c["h2"].T @ d3
+    d2 = _bf((d3 @ wb["W3"].T) * (c["h2"] > 0))
+    grads["W2"] = c["c"].T @ d2
+    dx = d2 @ wb["W2"][:16].T
+    dx[:, 0] += dx0
+    dx = _bf(dx)
+    grads["W1"] = c["h1"].T @ dx
+    d1 = _bf((dx @ wb["W1"].T) * (c["h1"] > 0))
+    grads["W0"] = c["enc"].T @ d1
+    denc = d1 @ wb["W0"].T
+    return denc, grads
+
+
 def density_only(enc: np.ndarray, w: Dict[str, np.ndarray], dtype=np.float32) -> np.ndarray:
     """NeRF.__call__ with dir=None (nerfs.py:71-72): sigma [S]."""
     w = {k: np.asarray(v, dtype) for k, v in w.items()}

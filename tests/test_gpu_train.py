@@ -20,10 +20,11 @@ def test_scene_ground_truth(small_scene):
     assert torch.isfinite(rgba).all()
 
 
-def test_train_loss_decreases(small_scene):
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_train_loss_decreases(small_scene, precision):
     from jaxngp_gb300 import _lib as L
     from jaxngp_gb300.trainer import NGPTrainer, TrainConfig
-    tr = NGPTrainer(small_scene, TrainConfig(total_samples=1 << 14, T=1 << 16, seed=1))
+    tr = NGPTrainer(small_scene, TrainConfig(total_samples=1 << 14, T=1 << 16, seed=1, mlp_precision=precision))
     before = L.lib().ngp_kernel_launches
     before.restype = __import__("ctypes").c_ulonglong
     n0 = before()
