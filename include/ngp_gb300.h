@@ -146,6 +146,27 @@ int ngp_march_rays_inference_inplace_status(cudaStream_t stream, void **buffers,
 void ngp_integrate_rays_inference_inplace(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_integrate_rays_inference_inplace_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* ngp_march_rays_inference_inplace with the samples' positions and directions packed densely, so
+ * that the encoder and the MLP run on the samples that exist instead of n * cap entries (no
+ * reference counterpart).  A warp reserves one range of sample_count for its slots' samples;
+ * sample_start[i] is where slot i's samples begin.  dss and z_vals stay [n, cap].  The caller
+ * zeroes sample_count before each call.  march_steps_cap <= 16.
+ * buffers: rays_o f32[N,3], rays_d f32[N,3], t_starts f32[N] (in/out), t_ends f32[N],
+ * occupancy_bitfield u8[K*G^3/8], terminated bool[n], indices u32[n] (in/out),
+ * next_ray_index u32[1] (in/out) -> n_samples u32[n], sample_start u32[n], sample_count u32[1]
+ * (in/out), xyzs f32[n*cap,3], dirs f32[n*cap,3], dss f32[n,cap], z_vals f32[n,cap].
+ * opaque: MarchingInferenceDescriptor. */
+void ngp_march_rays_inference_compact(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_march_rays_inference_compact_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* ngp_integrate_rays_inference_inplace reading slot i's colours from drgbs[sample_start[i] + k]
+ * (the packed layout of ngp_march_rays_inference_compact).
+ * buffers: rays_bg f32[N,3], rays_rgbd f32[N,4] (in/out), rays_T f32[N] (in/out), n_samples u32[n],
+ * indices u32[n], dss f32[n,cap], z_vals f32[n,cap], drgbs f32[n*cap,4], sample_start u32[n],
+ * terminate_total u32[1] (in/out) -> terminated bool[n].  opaque: IntegratingInferenceDescriptor. */
+void ngp_integrate_rays_inference_compact(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_integrate_rays_inference_compact_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* Replaces volrendjax::morton3d (volrend.h:143-148; marching.cu:687-694).
  * buffers: xyzs u32[N,3] -> idcs u32[N]; opaque: Morton3DDescriptor. */
 void morton3d(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);

@@ -18,10 +18,12 @@ int launch_march_rays_inference(cudaStream_t, const MarchingInferenceDescriptor 
                                 std::uint32_t *, float *, float *, float *, float *);
 int launch_march_rays_inference_inplace(cudaStream_t, const MarchingInferenceDescriptor &, const float *, const float *,
                                         float *, const float *, const std::uint8_t *, const bool *, std::uint32_t *,
-                                        std::uint32_t *, std::uint32_t *, float *, float *, float *, float *);
+                                        std::uint32_t *, std::uint32_t *, std::uint32_t *, std::uint32_t *, float *,
+                                        float *, float *, float *);
 int launch_integrate_rays_inference_inplace(cudaStream_t, const IntegratingInferenceDescriptor &, const float *, float *,
                                             float *, const std::uint32_t *, const std::uint32_t *, const float *,
-                                            const float *, const float *, std::uint32_t *, bool *);
+                                            const float *, const float *, const std::uint32_t *, std::uint32_t *,
+                                            bool *);
 int launch_morton3d(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t *);
 int launch_morton3d_invert(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t *);
 int launch_integrate_rays(cudaStream_t, const IntegratingDescriptor &, const std::uint32_t *, const std::uint32_t *,
@@ -172,13 +174,27 @@ NGP_ENTRY(march_rays_inference) {
 NGP_ENTRY(ngp_march_rays_inference_inplace) {
     NGP_DESC(MarchingInferenceDescriptor, d);
     return launch_march_rays_inference_inplace(stream, d, CF32(0), CF32(1), F32(2), CF32(3), CU8(4), CB8(5), U32(6),
-                                               U32(7), U32(8), F32(9), F32(10), F32(11), F32(12));
+                                               U32(7), U32(8), nullptr, nullptr, F32(9), F32(10), F32(11), F32(12));
+}
+
+NGP_ENTRY(ngp_march_rays_inference_compact) {
+    NGP_DESC(MarchingInferenceDescriptor, d);
+    NGP_CHECK_ARG(buffers[9] != nullptr && buffers[10] != nullptr, "march_rays_inference_compact: sample_start and sample_count are required");
+    return launch_march_rays_inference_inplace(stream, d, CF32(0), CF32(1), F32(2), CF32(3), CU8(4), CB8(5), U32(6),
+                                               U32(7), U32(8), U32(9), U32(10), F32(11), F32(12), F32(13), F32(14));
 }
 
 NGP_ENTRY(ngp_integrate_rays_inference_inplace) {
     NGP_DESC(IntegratingInferenceDescriptor, d);
     return launch_integrate_rays_inference_inplace(stream, d, CF32(0), F32(1), F32(2), CU32(3), CU32(4), CF32(5),
-                                                   CF32(6), CF32(7), U32(8), B8(9));
+                                                   CF32(6), CF32(7), nullptr, U32(8), B8(9));
+}
+
+NGP_ENTRY(ngp_integrate_rays_inference_compact) {
+    NGP_DESC(IntegratingInferenceDescriptor, d);
+    NGP_CHECK_ARG(buffers[8] != nullptr, "integrate_rays_inference_compact: sample_start is required");
+    return launch_integrate_rays_inference_inplace(stream, d, CF32(0), F32(1), F32(2), CU32(3), CU32(4), CF32(5),
+                                                   CF32(6), CF32(7), CU32(8), U32(9), B8(10));
 }
 
 NGP_ENTRY(morton3d) {

@@ -173,14 +173,17 @@ __global__ void __launch_bounds__(256) integrate_rays_inference_inplace_kernel(
     const float *__restrict__ rays_bg, float *__restrict__ rays_rgbd, float *__restrict__ rays_T,
     const std::uint32_t *__restrict__ n_samples, const std::uint32_t *__restrict__ indices,
     const float *__restrict__ dss, const float *__restrict__ z_vals, const float *__restrict__ drgbs,
-    std::uint32_t *__restrict__ terminate_total, bool *__restrict__ terminated) {
+    const std::uint32_t *__restrict__ sample_start, std::uint32_t *__restrict__ terminate_total,
+    bool *__restrict__ terminated) {
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool term = false;
     if (i < n_rays) {
         const std::uint32_t n = min(n_samples[i], cap), r = indices[i];
         if (r < n_total_rays) {
             const float *rd = dss + (std::size_t)i * cap, *rz = z_vals + (std::size_t)i * cap;
-            const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + (std::size_t)i * cap;
+            // the slot's colours: strided like dss, or packed from sample_start[i] (compact march)
+            const float4 *rc = reinterpret_cast<const float4 *>(drgbs) +
+                               (sample_start != nullptr ? (std::size_t)sample_start[i] : (std::size_t)i * cap);
             float T = rays_T[r];
             const float4 acc = reinterpret_cast<const float4 *>(rays_rgbd)[r];
             float cr = acc.x, cg = acc.y, cb = acc.z, cd = acc.w;
@@ -277,13 +280,14 @@ int launch_integrate_rays_inference_inplace(cudaStream_t stream, const Integrati
                                             const float *rays_bg, float *rays_rgbd, float *rays_T,
                                             const std::uint32_t *n_samples, const std::uint32_t *indices,
                                             const float *dss, const float *z_vals, const float *drgbs,
-                                            std::uint32_t *terminate_total, bool *terminated) {
+                                            const std::uint32_t *sample_start, std::uint32_t *terminate_total,
+                                            bool *terminated) {
     NGP_CHECK_ARG(((std::uintptr_t)rays_rgbd & 15u) == 0 && ((std::uintptr_t)drgbs & 15u) == 0,
                   "integrate_rays_inference: rays_rgbd and drgbs must be 16-byte aligned");
     if (d.n_rays > 0) {
         integrate_rays_inference_inplace_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_total_rays, d.n_rays, d.march_steps_cap, rays_bg, rays_rgbd, rays_T, n_samples, indices, dss, z_vals,
-            drgbs, terminate_total, terminated);
+            drgbs, sample_start, terminate_total, terminated);
         count_launches(1);
     }
     return launch_status();

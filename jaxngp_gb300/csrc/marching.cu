@@ -411,16 +411,79 @@ __global__ void __launch_bounds__(256) march_rays_inference_kernel(
     t_starts_out[i] = wrote_t ? t : 0.f;
 }
 
-// In-place form for the device-resident renderer: the slot indices and the next-ray counter are
+// Marches one ray of the inference renderer from t0 for at most `cap` samples (marching.cu:315-396):
+// sample k goes to sx[3k..3k+2], sd[k], sz[k].  Returns the number of samples; t_out receives the
+// advanced t to scatter into t_starts (0 for a ray with t_end < t_start).
+__device__ __forceinline__ std::uint32_t march_inference_ray(const MarchParams &m, std::uint32_t cap, const V3 &o,
+                                                             const V3 &d, float t0, float t1,
+                                                             const std::uint8_t *__restrict__ bits, float *sx,
+                                                             float *sd, float *sz, float &t_out) {
+    std::uint32_t steps = 0;
+    float t = 0.f;
+    if (!(t1 < t0)) {
+        const V3 inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+        t = t0;
+        for (std::uint32_t it = 0; steps < cap && t < t1 && it < kMaxMarchIters; ++it) {
+            V3 pos = at(o, d, t);
+            float ds = calc_ds(t, m);
+            V3 g;
+            float mb;
+            if (occupied_at(m, pos, ds, bits, g, mb)) {
+                sx[steps * 3 + 0] = pos.x;
+                sx[steps * 3 + 1] = pos.y;
+                sx[steps * 3 + 2] = pos.z;
+                sd[steps] = ds;
+                sz[steps] = t;
+                ++steps;
+                t = t + ds;
+            } else {
+                t = skip_empty(m, t, g, mb, pos, d, inv_d);
+            }
+        }
+        if (t >= t1) {
+            V3 pos = at(o, d, t1);
+            float ds = calc_ds(t1, m);
+            V3 g;
+            float mb;
+            if (occupied_at(m, pos, ds, bits, g, mb)) {
+                if (steps > 0 && sd[steps - 1] + sz[steps - 1] >= t1) sd[steps - 1] = t1 - sz[steps - 1];
+                if (steps < cap) {
+                    sx[steps * 3 + 0] = pos.x;
+                    sx[steps * 3 + 1] = pos.y;
+                    sx[steps * 3 + 2] = pos.z;
+                    sd[steps] = ds;
+                    sz[steps] = t1;
+                    ++steps;
+                } else {
+                    t = t1;
+                }
+            }
+        }
+    }
+    t_out = t;
+    return steps;
+}
+
+// In-place forms for the device-resident renderer: the slot indices and the next-ray counter are
 // read and updated in place, the advanced t is scattered straight into t_starts (what
 // marching/__init__.py:156 does with .at[].set on the host side), and each sample also gets its
 // ray's direction (the field needs it; renderers/cuda.py:225 broadcasts rays_d[indices]).
+//
+// kCompact = false: samples stay in the slot's `cap` strided entries (unused ones zeroed).
+// kCompact = true:  dss / z_vals stay strided, but positions and directions are packed densely:
+// a warp reserves one range of *sample_count for its lanes' samples (one atomic per warp) and
+// sample_start[i] records where slot i's samples begin, so the encoder and the MLP run on
+// *sample_count samples instead of n * cap.
+constexpr std::uint32_t kCompactMaxCap = 16;
+
+template <bool kCompact>
 __global__ void __launch_bounds__(256) march_rays_inference_inplace_kernel(
     std::uint32_t n_total_rays, std::uint32_t n_rays, std::uint32_t cap, MarchParams m,
     const float *__restrict__ rays_o, const float *__restrict__ rays_d, float *__restrict__ t_starts,
     const float *__restrict__ t_ends, const std::uint8_t *__restrict__ bits, const bool *__restrict__ terminated,
     std::uint32_t *__restrict__ indices, std::uint32_t *__restrict__ next_ray_index,
-    std::uint32_t *__restrict__ n_samples, float *__restrict__ xyzs, float *__restrict__ dirs,
+    std::uint32_t *__restrict__ n_samples, std::uint32_t *__restrict__ sample_start,
+    std::uint32_t *__restrict__ sample_count, float *__restrict__ xyzs, float *__restrict__ dirs,
     float *__restrict__ dss, float *__restrict__ z_vals) {
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in_range = i < n_rays;
@@ -430,75 +493,62 @@ __global__ void __launch_bounds__(256) march_rays_inference_inplace_kernel(
     std::uint32_t base = 0;
     if (ballot != 0 && (int)lane_id() == leader) base = atomicAdd(next_ray_index, (unsigned)__popc(ballot));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (!in_range) return;
-    const std::uint32_t r = refill ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : indices[i];
-    indices[i] = r;
-    float *rx = xyzs + (std::size_t)i * cap * 3, *rdir = dirs + (std::size_t)i * cap * 3;
+    if (!kCompact && !in_range) return;
+    std::uint32_t r = n_total_rays;
+    if (in_range) {
+        r = refill ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : indices[i];
+        indices[i] = r;
+    }
+    float lx[kCompact ? kCompactMaxCap * 3 : 1];
+    float *rx = kCompact ? lx : xyzs + (std::size_t)i * cap * 3;
     float *rs = dss + (std::size_t)i * cap, *rz = z_vals + (std::size_t)i * cap;
     std::uint32_t steps = 0;
-    if (r < n_total_rays) {
+    V3 d = {0.f, 0.f, 1.f};
+    if (in_range && r < n_total_rays) {
         const V3 o = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
-        const V3 d = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
-        const float t0 = t_starts[r], t1 = t_ends[r];
-        float t = 0.f;
-        if (!(t1 < t0)) {
-            const V3 inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-            t = t0;
-            for (std::uint32_t it = 0; steps < cap && t < t1 && it < kMaxMarchIters; ++it) {
-                V3 pos = at(o, d, t);
-                float ds = calc_ds(t, m);
-                V3 g;
-                float mb;
-                if (occupied_at(m, pos, ds, bits, g, mb)) {
-                    rx[steps * 3 + 0] = pos.x;
-                    rx[steps * 3 + 1] = pos.y;
-                    rx[steps * 3 + 2] = pos.z;
-                    rs[steps] = ds;
-                    rz[steps] = t;
-                    ++steps;
-                    t = t + ds;
-                } else {
-                    t = skip_empty(m, t, g, mb, pos, d, inv_d);
-                }
-            }
-            if (t >= t1) {
-                V3 pos = at(o, d, t1);
-                float ds = calc_ds(t1, m);
-                V3 g;
-                float mb;
-                if (occupied_at(m, pos, ds, bits, g, mb)) {
-                    if (steps > 0 && rs[steps - 1] + rz[steps - 1] >= t1) rs[steps - 1] = t1 - rz[steps - 1];
-                    if (steps < cap) {
-                        rx[steps * 3 + 0] = pos.x;
-                        rx[steps * 3 + 1] = pos.y;
-                        rx[steps * 3 + 2] = pos.z;
-                        rs[steps] = ds;
-                        rz[steps] = t1;
-                        ++steps;
-                    } else {
-                        t = t1;
-                    }
-                }
-            }
+        d = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
+        float t;
+        steps = march_inference_ray(m, cap, o, d, t_starts[r], t_ends[r], bits, rx, rs, rz, t);
+        t_starts[r] = t;  // marching.cu:396 + marching/__init__.py:156
+    }
+    if (in_range) {
+        for (std::uint32_t k = steps; k < cap; ++k) {
+            rs[k] = 0.f;
+            rz[k] = 0.f;
         }
-        t_starts[r] = t;  // marching.cu:396 + marching/__init__.py:156 (0 for a ray with t_end < t_start)
+        n_samples[i] = steps;
+    }
+    if (!kCompact) {
+        float *rdir = dirs + (std::size_t)i * cap * 3;
+        for (std::uint32_t k = 0; k < cap; ++k) {
+            const bool s = k < steps;
+            if (!s) {
+                rx[k * 3 + 0] = 0.f;
+                rx[k * 3 + 1] = 0.f;
+                rx[k * 3 + 2] = 0.f;
+            }
+            rdir[k * 3 + 0] = s ? d.x : 0.f;
+            rdir[k * 3 + 1] = s ? d.y : 0.f;
+            rdir[k * 3 + 2] = s ? d.z : 1.f;
+        }
+    } else {
+        const std::uint32_t incl = warp_inclusive_scan(steps);
+        const std::uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        std::uint32_t wbase = 0;
+        if (lane_id() == 31 && total > 0) wbase = atomicAdd(sample_count, total);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        const std::uint32_t start = wbase + incl - steps;
+        if (in_range) sample_start[i] = start;
         for (std::uint32_t k = 0; k < steps; ++k) {
-            rdir[k * 3 + 0] = d.x;
-            rdir[k * 3 + 1] = d.y;
-            rdir[k * 3 + 2] = d.z;
+            float *px = xyzs + (std::size_t)(start + k) * 3, *pd = dirs + (std::size_t)(start + k) * 3;
+            px[0] = rx[k * 3 + 0];
+            px[1] = rx[k * 3 + 1];
+            px[2] = rx[k * 3 + 2];
+            pd[0] = d.x;
+            pd[1] = d.y;
+            pd[2] = d.z;
         }
     }
-    for (std::uint32_t k = steps; k < cap; ++k) {
-        rx[k * 3 + 0] = 0.f;
-        rx[k * 3 + 1] = 0.f;
-        rx[k * 3 + 2] = 0.f;
-        rdir[k * 3 + 0] = 0.f;
-        rdir[k * 3 + 1] = 0.f;
-        rdir[k * 3 + 2] = 1.f;
-        rs[k] = 0.f;
-        rz[k] = 0.f;
-    }
-    n_samples[i] = steps;
 }
 
 __global__ void copy_counter_kernel(const std::uint32_t *__restrict__ src, std::uint32_t *__restrict__ dst) {
@@ -603,15 +653,25 @@ int launch_march_rays_inference(cudaStream_t stream, const MarchingInferenceDesc
 int launch_march_rays_inference_inplace(cudaStream_t stream, const MarchingInferenceDescriptor &d, const float *rays_o,
                                         const float *rays_d, float *t_starts, const float *t_ends,
                                         const std::uint8_t *bits, const bool *terminated, std::uint32_t *indices,
-                                        std::uint32_t *next_ray_index, std::uint32_t *n_samples, float *xyzs,
+                                        std::uint32_t *next_ray_index, std::uint32_t *n_samples,
+                                        std::uint32_t *sample_start, std::uint32_t *sample_count, float *xyzs,
                                         float *dirs, float *dss, float *z_vals) {
     NGP_CHECK_ARG(d.K > 0 && d.K <= 16 && d.G > 0 && d.G <= 1024 && (d.G & (d.G - 1)) == 0 && d.diagonal_n_steps > 0,
                   "march_rays_inference: bad K, G or diagonal_n_steps");
+    const bool compact = sample_start != nullptr;
+    NGP_CHECK_ARG(!compact || (sample_count != nullptr && d.march_steps_cap <= kCompactMaxCap),
+                  "march_rays_inference (compact): needs sample_count and march_steps_cap <= 16");
     const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
     if (d.n_rays > 0) {
-        march_rays_inference_inplace_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
-            d.n_total_rays, d.n_rays, d.march_steps_cap, m, rays_o, rays_d, t_starts, t_ends, bits, terminated, indices,
-            next_ray_index, n_samples, xyzs, dirs, dss, z_vals);
+        const unsigned grid = (d.n_rays + 255) / 256;
+        if (compact)
+            march_rays_inference_inplace_kernel<true><<<grid, 256, 0, stream>>>(
+                d.n_total_rays, d.n_rays, d.march_steps_cap, m, rays_o, rays_d, t_starts, t_ends, bits, terminated,
+                indices, next_ray_index, n_samples, sample_start, sample_count, xyzs, dirs, dss, z_vals);
+        else
+            march_rays_inference_inplace_kernel<false><<<grid, 256, 0, stream>>>(
+                d.n_total_rays, d.n_rays, d.march_steps_cap, m, rays_o, rays_d, t_starts, t_ends, bits, terminated,
+                indices, next_ray_index, n_samples, nullptr, nullptr, xyzs, dirs, dss, z_vals);
         count_launches(1);
     }
     return launch_status();

@@ -23,11 +23,15 @@ from .field import entry as field_entry
 class Renderer:
     def __init__(self, latents: torch.Tensor, weights: torch.Tensor, table: LevelTable, bitfield: torch.Tensor,
                  K: int, G: int, bound: float, stepsize_portion: float, diagonal_n_steps: int = 1024,
-                 n_slots: int = 1 << 18, march_steps_cap: int = 8, poll_every: int = 4, precision: str = "fp32"):
+                 n_slots: int = 1 << 18, march_steps_cap: int = 8, poll_every: int = 4, precision: str = "fp32",
+                 compact: bool = True):
         self.latents, self.weights, self.table, self.bitfield = latents, weights, table, bitfield
         self.K, self.G, self.bound, self.sp, self.dns = K, G, float(bound), float(stepsize_portion), diagonal_n_steps
         self.n_slots, self.cap, self.poll_every = n_slots, march_steps_cap, poll_every
         self.field_fwd = field_entry("ngp_field_forward", precision)
+        self.compact = compact
+        if compact and march_steps_cap > 16:
+            raise ValueError("the compact renderer supports march_steps_cap <= 16")
         dev = latents.device
         n, c = n_slots, march_steps_cap
         f32 = dict(dtype=torch.float32, device=dev)
@@ -41,6 +45,8 @@ class Renderer:
         self.indices = torch.empty(n, dtype=torch.int32, device=dev)
         self.terminated = torch.empty(n, dtype=torch.bool, device=dev)
         self.next_ray = torch.empty(1, dtype=torch.int32, device=dev)
+        self.sample_start = torch.empty(n, dtype=torch.int32, device=dev)
+        self.sample_count = torch.empty(1, dtype=torch.int32, device=dev)
         self.total = torch.empty(1, dtype=torch.int32, device=dev)
         self.total_host = torch.empty(1, dtype=torch.int32).pin_memory()
         self.iterations = 0
@@ -70,14 +76,26 @@ class Renderer:
         it = 0
         while it < max_iterations:
             for _ in range(self.poll_every):
-                L.call("ngp_march_rays_inference_inplace",
-                       [rays_o, rays_d, t_starts, t_ends, self.bitfield, self.terminated, self.indices, self.next_ray,
-                        self.n_samples, self.xyzs, self.dirs, self.dss, self.zs], dm)
-                L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, None, self.enc], dh)
-                L.call(self.field_fwd, [self.enc, self.dirs, self.weights, None, self.drgbs], df)
-                L.call("ngp_integrate_rays_inference_inplace",
-                       [rays_bg, rgbd, T, self.n_samples, self.indices, self.dss, self.zs, self.drgbs, self.total,
-                        self.terminated], di)
+                if self.compact:
+                    self.sample_count.zero_()
+                    L.call("ngp_march_rays_inference_compact",
+                           [rays_o, rays_d, t_starts, t_ends, self.bitfield, self.terminated, self.indices,
+                            self.next_ray, self.n_samples, self.sample_start, self.sample_count, self.xyzs, self.dirs,
+                            self.dss, self.zs], dm)
+                    L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, self.sample_count, self.enc], dh)
+                    L.call(self.field_fwd, [self.enc, self.dirs, self.weights, self.sample_count, self.drgbs], df)
+                    L.call("ngp_integrate_rays_inference_compact",
+                           [rays_bg, rgbd, T, self.n_samples, self.indices, self.dss, self.zs, self.drgbs,
+                            self.sample_start, self.total, self.terminated], di)
+                else:
+                    L.call("ngp_march_rays_inference_inplace",
+                           [rays_o, rays_d, t_starts, t_ends, self.bitfield, self.terminated, self.indices,
+                            self.next_ray, self.n_samples, self.xyzs, self.dirs, self.dss, self.zs], dm)
+                    L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, None, self.enc], dh)
+                    L.call(self.field_fwd, [self.enc, self.dirs, self.weights, None, self.drgbs], df)
+                    L.call("ngp_integrate_rays_inference_inplace",
+                           [rays_bg, rgbd, T, self.n_samples, self.indices, self.dss, self.zs, self.drgbs, self.total,
+                            self.terminated], di)
                 it += 1
             self.total_host.copy_(self.total, non_blocking=True)
             torch.cuda.current_stream().synchronize()

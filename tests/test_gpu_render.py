@@ -51,8 +51,9 @@ def host_loop(tr, o, d, t0, t1, bg, n_slots, cap):
     return rgbd, it
 
 
+@pytest.mark.parametrize("compact", [False, True])
 @pytest.mark.parametrize("n_slots,cap", [(512, 8), (4096, 8), (1000, 3)])
-def test_renderer_matches_host_loop(trained, n_slots, cap):
+def test_renderer_matches_host_loop(trained, n_slots, cap, compact):
     from jaxngp_gb300.renderer import Renderer
     from jaxngp_gb300.trainer import camera_rays, near_far
     tr = trained
@@ -60,11 +61,12 @@ def test_renderer_matches_host_loop(trained, n_slots, cap):
     t0, t1 = near_far(tr.bound, o, d)
     bg = torch.rand(o.shape[0], 3, device=o.device, generator=torch.Generator(o.device).manual_seed(7))
     want, _ = host_loop(tr, o, d, t0, t1, bg, n_slots, cap)
-    r = Renderer.from_trainer(tr, n_slots=n_slots, march_steps_cap=cap, poll_every=3)
+    r = Renderer.from_trainer(tr, n_slots=n_slots, march_steps_cap=cap, poll_every=3, compact=compact)
     got, iters = r.render_rays(o, d, t0.clone(), t1, bg)
     torch.cuda.synchronize()
     assert iters > 0
-    # every ray's march and compositing is independent of which slot and iteration carry it
+    # every ray's march and compositing is independent of which slot, iteration and (compact)
+    # sample position carry it
     assert torch.equal(got, want), (got - want).abs().max()
     assert torch.isfinite(got).all()
     # some rays terminate on opacity, some reach the far plane and show the background
@@ -103,3 +105,55 @@ def test_renderer_empty_grid(trained):
     got, iters = r.render_rays(o, d, t0.clone(), t1, bg)
     assert iters == 1
     assert torch.equal(got[:, :3], bg) and torch.equal(got[:, 3], torch.zeros_like(got[:, 3]))
+
+
+def test_compact_march_packs_samples(trained):
+    """The compact march writes each slot's samples contiguously from sample_start, the ranges
+    tile [0, sample_count) without gaps, and positions equal the strided march's."""
+    from jaxngp_gb300 import _lib as L
+    from jaxngp_gb300.trainer import camera_rays, near_far
+    tr = trained
+    o, d = camera_rays(tr.data.camera, tr.data.transforms[2])
+    t0, t1 = near_far(tr.bound, o, d)
+    N, n, cap = o.shape[0], 3000, 8
+    i32 = dict(dtype=torch.int32, device="cuda")
+    dm = L.MarchingInferenceDescriptor(N, n, tr.cfg.diagonal_n_steps, tr.K, tr.cfg.G, cap, tr.bound, tr.sp)
+
+    def run(compact):
+        ts = t0.clone()
+        term = torch.ones(n, dtype=torch.bool, device="cuda")
+        idx, nri, ns = torch.zeros(n, **i32), torch.zeros(1, **i32), torch.zeros(n, **i32)
+        xyz, dirs = torch.zeros(n * cap, 3, device="cuda"), torch.zeros(n * cap, 3, device="cuda")
+        dss, zs = torch.zeros(n, cap, device="cuda"), torch.zeros(n, cap, device="cuda")
+        if compact:
+            start, cnt = torch.zeros(n, **i32), torch.zeros(1, **i32)
+            L.call("ngp_march_rays_inference_compact",
+                   [o, d, ts, t1, tr.bitfield, term, idx, nri, ns, start, cnt, xyz, dirs, dss, zs], dm)
+            return ts, idx, ns, xyz, dirs, dss, zs, start, cnt
+        L.call("ngp_march_rays_inference_inplace", [o, d, ts, t1, tr.bitfield, term, idx, nri, ns, xyz, dirs, dss, zs],
+               dm)
+        return ts, idx, ns, xyz, dirs, dss, zs
+
+    a, b = run(False), run(True)
+    # which slot takes which ray follows the order of the warps' atomics: compare per ray
+    assert torch.equal(a[0], b[0])  # advanced t of every ray
+    ia, ib = a[1].long().cpu(), b[1].long().cpu()
+    assert torch.equal(torch.sort(ia).values, torch.sort(ib).values)
+    pa, pb = torch.empty(N, dtype=torch.long), torch.empty(N, dtype=torch.long)
+    pa[ia], pb[ib] = torch.arange(n), torch.arange(n)   # ray -> slot
+    rays = ia
+    for k in (2, 5, 6):  # n_samples, dss, z_vals
+        assert torch.equal(a[k].cpu()[pa[rays]], b[k].cpu()[pb[rays]])
+    ns, start, cnt = b[2].long().cpu(), b[7].long().cpu(), int(b[8])
+    assert cnt == int(ns.sum()) and cnt > 0
+    cover = torch.zeros(cnt, dtype=torch.int32)
+    for i in torch.nonzero(ns).flatten().tolist():
+        cover[start[i]:start[i] + ns[i]] += 1
+    assert (cover == 1).all()
+    xa, da = a[3].view(n, cap, 3).cpu(), a[4].view(n, cap, 3).cpu()
+    xb, db = b[3].cpu(), b[4].cpu()
+    for r in rays[::97].tolist():
+        i, j = int(pa[r]), int(pb[r])
+        k = int(ns[j])
+        assert torch.equal(xb[start[j]:start[j] + k], xa[i, :k])
+        assert torch.equal(db[start[j]:start[j] + k], da[i, :k])
