@@ -342,7 +342,8 @@ typedef struct NgpIntegrateLossDescriptor {
  * mean_c huber(pred - gt) / n_valid; dL_ddrgbs are written unnormalised and `grad_scale`
  * receives 1/n_valid for the field backward.
  * buffers: ray_is_valid bool[R], rays_sample_startidx, rays_n_samples, bgs f32[R,3],
- * gt_rgbs f32[R,3], dss, z_vals, drgbs, active_count u32[1], scratch f32[3] -> dL_ddrgbs f32[S,4],
+ * gt_rgbs f32[R,3], dss, z_vals, drgbs, active_count u32[1], scratch f32[4 + R] (loss sums and the
+ * list of rays with samples) -> dL_ddrgbs f32[S,4],
  * stats f32[4] (loss, n_valid_rays, measured_batch_size, samples before compaction),
  * grad_scale f32[1].  opaque: NgpIntegrateLossDescriptor. */
 void ngp_integrate_loss_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
@@ -429,6 +430,69 @@ int ngp_ogrid_mark_untrained_status(cudaStream_t stream, void **buffers, const c
  * opaque: PackbitsDescriptor. */
 void ngp_packbits_scalar(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_packbits_scalar_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* --------------------------------------------------------------------- learned proposal sampler
+ * No reference counterpart (the reference samples by marching the occupancy grid only).  A ray's
+ * samples come from a small density network instead of the march: a 3D DDA over coarse blocks of
+ * 8^3 occupancy cells gives the ray's occupied interval (no interval: a valid ray with no
+ * samples), the interval is cut into NGP_PROPOSAL_BINS bins, the proposal network's log density
+ * at the bin centres defines a piecewise-constant pdf (mixed with 10% of a uniform one), whose
+ * inverse CDF at stratified levels cuts the interval into NGP_PROPOSAL_SAMPLES pieces, dense where
+ * the pdf is high; a sample sits at the middle of each piece and stands for it (dss = its length),
+ * written in march_rays' layout so that the field, the integrator and the loss run unchanged.  Slot j of a
+ * fitting ray starts at sample j * NGP_PROPOSAL_SAMPLES.  The network (4-level hash grid, MLP
+ * 8 -> 64 -> 64 -> 1) regresses the field's log density at the field's samples. */
+#define NGP_PROPOSAL_BINS 64
+#define NGP_PROPOSAL_SAMPLES 48
+#define NGP_PROPOSAL_WEIGHTS 4672 /* P0[8,64] P1[64,64] P2[64,1], packed */
+
+typedef struct NgpProposalDescriptor {
+    uint32_t n;             /* rays (proposal_rays) or points (proposal_loss) */
+    uint32_t total_samples; /* sample budget S; slots = S / NGP_PROPOSAL_SAMPLES */
+    uint32_t G;             /* occupancy grid resolution (cascade 0; a multiple of 8) */
+    float bound;
+    uint32_t perturb;       /* proposal_sample: jitter the stratified draws */
+    uint32_t seed_lo, seed_hi;
+    uint32_t count_index;   /* proposal_loss: points bounded by counts[count_index] (0 slots, 1 bins,
+                               2 samples); 3 = all n points */
+    uint32_t sigma_stride;  /* proposal_loss: stride of the target densities (4 for drgbs rows) */
+} NgpProposalDescriptor;
+
+/* buffers: occupancy_bitfield u8[G^3/8] -> coarse u8[(G/8)^3]. */
+void ngp_proposal_coarse(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_coarse_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* buffers: rays_o f32[R,3], rays_d f32[R,3], t_starts f32[R], t_ends f32[R], coarse u8[(G/8)^3]
+ * -> next_sample_write_location u32[1], number_of_exceeded_samples u32[1], ray_is_valid bool[R],
+ * rays_n_samples u32[R], rays_sample_startidx u32[R], ray_of_slot u32[S/48], slot_t_start f32[S/48],
+ * slot_t_end f32[S/48], counts u32[3] (slots, bin points, samples). */
+void ngp_proposal_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_t_start, slot_t_end -> points f32[S/48*64,3]. */
+void ngp_proposal_bin_points(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_bin_points_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_t_start, slot_t_end, x_bins f32[S/48*64]
+ * -> idcs u32[S], xyzs f32[S,3], dirs f32[S,3], dss f32[S], z_vals f32[S]. */
+void ngp_proposal_sample(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_sample_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* Log-density regression: dL/dx = 2 w (x - log(sigma + 1e-3)) / n, w = 2 below the target, else 1.
+ * buffers: counts u32[3] or NULL, x f32[n], sigma f32[n*stride] -> dL_dx f32[n], loss f32[1]
+ * (the loss sum is added; the caller zeroes it). */
+void ngp_proposal_loss(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_loss_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* The proposal network's MLP.  forward buffers: encodings f32[n,8], weights f32[4672],
+ * active_count u32[1] or NULL -> x f32[n].  backward buffers: encodings, weights, dL_dx f32[n],
+ * active_count or NULL, scratch f32[ngp_proposal_backward_scratch_floats()] -> dL_dencodings
+ * f32[n,8], dL_dweights f32[4672].  opaque: NgpMlpDescriptor. */
+void ngp_proposal_mlp_forward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_mlp_forward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+void ngp_proposal_mlp_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_mlp_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+size_t ngp_proposal_backward_scratch_floats(void);
 
 #ifdef __cplusplus
 }

@@ -92,6 +92,11 @@ class NgpAdamDescriptor(_Desc):
                 ("eps_root", c_f32), ("weight_decay", c_f32), ("zero_grad", c_u32)]
 
 
+class NgpProposalDescriptor(_Desc):
+    _fields_ = [("n", c_u32), ("total_samples", c_u32), ("G", c_u32), ("bound", c_f32), ("perturb", c_u32),
+                ("seed_lo", c_u32), ("seed_hi", c_u32), ("count_index", c_u32), ("sigma_stride", c_u32)]
+
+
 class NgpOgridDescriptor(_Desc):
     _fields_ = [("K", c_u32), ("G", c_u32), ("cascade", c_u32), ("n_points", c_u32), ("update_all", c_u32),
                 ("bound", c_f32), ("decay", c_f32), ("threshold_step", c_f32), ("seed", c_u64),
@@ -151,6 +156,11 @@ def call(name: str, buffers: Sequence, desc: _Desc | None = None, stream=None) -
     st = fn(ctypes.c_void_p(stream), arr, ctypes.c_char_p(opaque), ctypes.c_size_t(len(opaque)))
     if st != 0:
         raise NgpError(name, st, L.ngp_last_status_message().decode())
+
+
+def proposal_backward_scratch_floats() -> int:
+    lib().ngp_proposal_backward_scratch_floats.restype = ctypes.c_size_t
+    return int(lib().ngp_proposal_backward_scratch_floats())
 
 
 def field_backward_scratch_floats() -> int:

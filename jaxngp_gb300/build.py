@@ -22,8 +22,9 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", 
 # Per-file flags.  The marcher and the integrators are compiled without multiply-add contraction
 # so that their float arithmetic is the reference's source arithmetic, one rounding per operation
 # (sample counts and early-termination steps then agree exactly with the reference built that way).
-EXTRA = {"marching.cu": ["--fmad=false"], "integrating.cu": ["--fmad=false"], "train.cu": ["--fmad=false"]}
-SOURCES = ["abi.cu", "marching.cu", "integrating.cu", "packbits.cu", "hashgrid.cu", "mlp.cu", "mlp_tc.cu", "train.cu",
+EXTRA = {"marching.cu": ["--fmad=false"], "integrating.cu": ["--fmad=false"], "train.cu": ["--fmad=false"],
+         "proposal.cu": ["--fmad=false"]}
+SOURCES = ["abi.cu", "marching.cu", "integrating.cu", "packbits.cu", "hashgrid.cu", "mlp.cu", "mlp_tc.cu", "proposal.cu", "train.cu",
            "scene.cu"]
 
 

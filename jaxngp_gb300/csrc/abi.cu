@@ -53,6 +53,21 @@ int launch_mlp_bf16_density(cudaStream_t, std::uint32_t, const float *, const fl
 int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                              const float *, const float *, const float *, float *, float *, unsigned *);
 int device_status();
+int launch_proposal_coarse(cudaStream_t, std::uint32_t, const std::uint8_t *, std::uint8_t *);
+int launch_proposal_rays(cudaStream_t, std::uint32_t, std::uint32_t, std::uint32_t, float, const float *, const float *,
+                         const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *, bool *,
+                         std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, std::uint32_t *);
+int launch_proposal_bin_points(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                               const std::uint32_t *, const float *, const float *, float *);
+int launch_proposal_sample(cudaStream_t, std::uint32_t, const std::uint32_t *, bool, std::uint64_t, const float *,
+                           const float *, const std::uint32_t *, const float *, const float *, const float *,
+                           std::uint32_t *, float *, float *, float *, float *);
+int launch_proposal_loss(cudaStream_t, std::uint32_t, const std::uint32_t *, int, const float *, const float *, int,
+                         float *, float *);
+int launch_prop_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *, float *);
+int launch_prop_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *, const float *,
+                         float *, float *, float *, bool);
+std::size_t prop_partials_floats();
 int launch_mlp_backward_noalloc(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                                 const float *, const float *, const float *, float *, float *, bool);
 int launch_render_blobs(cudaStream_t, const NgpRenderBlobsDescriptor &, const float *, const float *, const float *,
@@ -345,5 +360,49 @@ NGP_ENTRY(ngp_ogrid_mark_untrained) {
     return launch_ogrid_mark_untrained(stream, d.K, d.G, d.bound, d.n_views, CF32(0), d.fx, d.fy, d.cx, d.cy, d.width,
                                        d.height, F32(1));
 }
+
+NGP_ENTRY(ngp_proposal_coarse) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    return launch_proposal_coarse(stream, d.G, CU8(0), U8(1));
+}
+
+NGP_ENTRY(ngp_proposal_rays) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    return launch_proposal_rays(stream, d.n, d.total_samples, d.G, d.bound, CF32(0), CF32(1), CF32(2), CF32(3), CU8(4),
+                                U32(5), U32(6), B8(7), U32(8), U32(9), U32(10), F32(11), F32(12), U32(13));
+}
+
+NGP_ENTRY(ngp_proposal_bin_points) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    return launch_proposal_bin_points(stream, d.total_samples / NGP_PROPOSAL_SAMPLES, CU32(0), CF32(1), CF32(2), CU32(3),
+                                      CF32(4), CF32(5), F32(6));
+}
+
+NGP_ENTRY(ngp_proposal_sample) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    const std::uint64_t seed = ((std::uint64_t)d.seed_hi << 32) | d.seed_lo;
+    return launch_proposal_sample(stream, d.total_samples / NGP_PROPOSAL_SAMPLES, CU32(0), d.perturb != 0, seed, CF32(1),
+                                  CF32(2), CU32(3), CF32(4), CF32(5), CF32(6), U32(7), F32(8), F32(9), F32(10), F32(11));
+}
+
+NGP_ENTRY(ngp_proposal_loss) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    const bool all = d.count_index == 3 || buffers[0] == nullptr;
+    return launch_proposal_loss(stream, d.n, all ? nullptr : CU32(0), all ? 0 : (int)d.count_index, CF32(1), CF32(2),
+                                (int)d.sigma_stride, F32(3), F32(4));
+}
+
+NGP_ENTRY(ngp_proposal_mlp_forward) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_prop_forward(stream, d.n_samples, CU32(2), CF32(0), CF32(1), F32(3));
+}
+
+NGP_ENTRY(ngp_proposal_mlp_backward) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_prop_backward(stream, d.n_samples, CU32(3), CF32(0), CF32(1), CF32(2), F32(5), F32(6), F32(4),
+                                d.accumulate != 0);
+}
+
+size_t ngp_proposal_backward_scratch_floats(void) { return prop_partials_floats(); }
 
 }  // extern "C"

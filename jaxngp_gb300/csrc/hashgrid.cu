@@ -1,9 +1,10 @@
 // Multiresolution hash-grid encoder for sm_103a: forward gather and gradient scatter.
 //
 // Replaces HashGridEncoder.__call__ (models/encoders.py:83-256) and the scatter-add that JAX's
-// autodiff makes of its gather (encoders.py:226).  One thread handles one (point, level) pair, a
-// warp covers two points x sixteen levels, so the level-major output row of a point
-// (column l*F + f, encoders.py:233) is written by consecutive lanes in one 256-byte burst.
+// autodiff makes of its gather (encoders.py:226).  In both directions a warp handles 32
+// consecutive points at one level (lane = point): the level's scale, resolution and offset are
+// uniform across the warp, and where neighbouring points share grid cells (samples along one
+// ray, or rays of neighbouring pixels) the warp's gathers hit the same sectors.
 //
 // The index and weight arithmetic uses explicitly rounded intrinsics, one rounding per
 // operation in the reference's order, so corner indices are bit-identical to the reference and
@@ -26,7 +27,8 @@ struct Corner8 {
     float w[8];
 };
 
-__device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, std::uint32_t l,
+// `tmask` = T - 1 when T is a power of two (then h mod T = h & tmask), else 0.
+__device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, std::uint32_t l, std::uint32_t tmask,
                                               float px, float py, float pz, Corner8 &c) {
     const float b = d.bound;
     const float two_b = d.two_bound;
@@ -52,34 +54,58 @@ __device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, st
         const std::uint32_t ox = (k >> 2) & 1, oy = (k >> 1) & 1, oz = k & 1;
         const std::uint32_t x = bx + ox, y = by + oy, z = bz + oz;
         const std::uint32_t h = dense ? (x + y * res + z * res2) : (x ^ (y * 2654435761u) ^ (z * 805459861u));
-        std::uint32_t idx = h % T + off;
+        std::uint32_t idx = (tmask != 0u ? (h & tmask) : h % T) + off;
         c.idx[k] = idx < last ? idx : last;
         c.w[k] = __fmul_rn(__fmul_rn(wx[ox], wy[oy]), wz[oz]);
     }
 }
 
-// enc[n, l*2 + f] for n < n_points (n_points read from `count` when given).
+// enc[n, l*2 + f] for n < n_points (n_points read from `count` when given).  A CTA takes tiles of
+// 32 points; warp w computes levels w, w + 8, ... for them and the tile's rows [32][L] leave
+// through shared memory as one contiguous block.
+constexpr int kHgTile = 32, kHgRow = NGP_MAX_LEVELS + 1;   // padded row: lanes hit different banks
+
 __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
     NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
     const float *__restrict__ pos, const float2 *__restrict__ latents, float2 *__restrict__ enc) {
+    __shared__ float2 rows[kHgTile * kHgRow];
     std::uint32_t n_active = n_points;
     if (count != nullptr) n_active = min(n_active, *count);
-    const std::size_t total = (std::size_t)n_active * d.L;
-    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
-    for (std::size_t t = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        const std::uint32_t n = (std::uint32_t)(t / d.L), l = (std::uint32_t)(t % d.L);
-        Corner8 c;
-        level_corners(d, l, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
-        float2 v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = __ldg(latents + c.idx[k]);
-        float a0 = __fmul_rn(v[0].x, c.w[0]), a1 = __fmul_rn(v[0].y, c.w[0]);
-#pragma unroll
-        for (int k = 1; k < 8; ++k) {
-            a0 = __fadd_rn(a0, __fmul_rn(v[k].x, c.w[k]));
-            a1 = __fadd_rn(a1, __fmul_rn(v[k].y, c.w[k]));
+    const std::uint32_t L = d.L, tmask = (d.T & (d.T - 1u)) == 0u ? d.T - 1u : 0u;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+    const std::uint32_t n_tiles = (n_active + kHgTile - 1) / kHgTile;
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::uint32_t n = tile * kHgTile + lane;
+        const bool in = n < n_active;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (in) {
+            px = pos[(std::size_t)n * 3 + 0];
+            py = pos[(std::size_t)n * 3 + 1];
+            pz = pos[(std::size_t)n * 3 + 2];
         }
-        enc[t] = make_float2(a0, a1);
+        for (std::uint32_t l = warp; l < L; l += n_warps) {
+            float2 r = make_float2(0.f, 0.f);
+            if (in) {
+                Corner8 c;
+                level_corners(d, l, tmask, px, py, pz, c);
+                float2 v[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v[k] = __ldg(latents + c.idx[k]);
+                float a0 = __fmul_rn(v[0].x, c.w[0]), a1 = __fmul_rn(v[0].y, c.w[0]);
+#pragma unroll
+                for (int k = 1; k < 8; ++k) {
+                    a0 = __fadd_rn(a0, __fmul_rn(v[k].x, c.w[k]));
+                    a1 = __fadd_rn(a1, __fmul_rn(v[k].y, c.w[k]));
+                }
+                r = make_float2(a0, a1);
+            }
+            rows[lane * kHgRow + l] = r;
+        }
+        __syncthreads();
+        const std::uint32_t n_rows = min((std::uint32_t)kHgTile, n_active - tile * kHgTile);
+        float2 *dst = enc + (std::size_t)tile * kHgTile * L;
+        for (std::uint32_t i = threadIdx.x; i < n_rows * L; i += blockDim.x) dst[i] = rows[(i / L) * kHgRow + i % L];
+        __syncthreads();
     }
 }
 
@@ -95,6 +121,7 @@ __global__ void __launch_bounds__(256) hashgrid_backward_kernel(
     const float *__restrict__ pos, const float2 *__restrict__ dL_denc, float2 *__restrict__ dL_dlat) {
     std::uint32_t n_active = n_points;
     if (count != nullptr) n_active = min(n_active, *count);
+    const std::uint32_t tmask = (d.T & (d.T - 1u)) == 0u ? d.T - 1u : 0u;
     const unsigned lane = lane_id();
     const std::size_t n_groups = (std::size_t)((n_active + 31) / 32) * d.L;   // (32 points, level) per warp
     const std::size_t warp0 = ((std::size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -107,7 +134,7 @@ __global__ void __launch_bounds__(256) hashgrid_backward_kernel(
         Corner8 c;
         if (in) {
             g = dL_denc[(std::size_t)n * d.L + l];
-            level_corners(d, l, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
+            level_corners(d, l, tmask, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
         } else {
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -163,9 +190,9 @@ int launch_hashgrid_forward(cudaStream_t stream, const NgpHashGridDescriptor &d,
     if (st != NGP_OK) return st;
     NGP_CHECK_ARG(((std::uintptr_t)latents & 7u) == 0 && ((std::uintptr_t)enc & 7u) == 0,
                   "hashgrid: latents and encodings must be 8-byte aligned");
-    const std::size_t items = (std::size_t)d.n_coords * d.L;
-    if (items > 0) {
-        hashgrid_forward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
+    const std::size_t tiles = ((std::size_t)d.n_coords + kHgTile - 1) / kHgTile;
+    if (tiles > 0) {
+        hashgrid_forward_kernel<<<grid_for(tiles, 1, 8), 256, 0, stream>>>(
             d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(latents), reinterpret_cast<float2 *>(enc));
         count_launches(1);
     }

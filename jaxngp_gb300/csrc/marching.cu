@@ -13,6 +13,8 @@
 // grid-stride kernel that reads the final counters, instead of ten full-buffer memsets up front;
 // the refill of finished slots in the inference marcher is warp-aggregated too, and the inference
 // launcher never blocks the host (the reference synchronises the stream at marching.cu:562).
+#include <cstring>
+
 #include "common.cuh"
 
 namespace ngp {
@@ -69,9 +71,19 @@ struct MarchParams {
     std::uint32_t dns, K, G;
     float bound, sp, inv_G;
     float ds_lo, ds_hi;   // calc_ds clamp bounds: 2 sqrt3 min(bound,1) / dns and 2 sqrt3 bound / G
+    // stepsize_portion == 0 (bound <= 1): clamp(t * 0, lo, hi) is min(lo, hi) for every t (a NaN
+    // product is dropped by fmaxf), so the step is one constant
+    bool const_ds;
+    float ds_const;
+    // K == 1: every sample is in cascade 0, whose half-width min(2^0, bound) and its reciprocal
+    // are fixed per launch
+    float mb0, inv_mb0;
+    bool pow2_0;
 };
 
-__device__ __forceinline__ float calc_ds(float t, const MarchParams &m) { return calc_ds_bounds(t, m.sp, m.ds_lo, m.ds_hi); }
+__device__ __forceinline__ float calc_ds(float t, const MarchParams &m) {
+    return m.const_ds ? m.ds_const : calc_ds_bounds(t, m.sp, m.ds_lo, m.ds_hi);
+}
 
 // x / mb where mb = min(2^cascade, bound).  When mb is a power of two the quotient is the product
 // with its exact reciprocal, bit for bit (both are the exact value rounded once); otherwise divide.
@@ -85,13 +97,24 @@ constexpr std::uint32_t kMaxSkipIters = 1u << 20;
 
 // marching.cu:79-98, :41-50, :174-176: is the cell under `pos` occupied?  Also returns the
 // continuous grid position and the cascade's half-width for the empty-space skip.
+// `expand` (optional) holds expand_bits(v) for v < G.
 __device__ __forceinline__ bool occupied_at(const MarchParams &m, V3 pos, float ds,
-                                            const std::uint8_t *__restrict__ bits, V3 &g, float &mb) {
-    std::uint32_t c0 = mip_from_xyz(pos, m.K), c1 = mip_from_ds(ds, m.G, m.K);
-    std::uint32_t cascade = c0 > c1 ? c0 : c1;
-    mb = fminf(scalbnf(1.0f, (int)cascade), m.bound);
-    const bool pow2 = (__float_as_uint(mb) & 0x007FFFFFu) == 0u && mb >= 1.17549435e-38f;
-    const float inv_mb = pow2 ? __uint_as_float(0x7F000000u - __float_as_uint(mb)) : 0.f;  // 2^-e for mb = 2^e
+                                            const std::uint8_t *__restrict__ bits, V3 &g, float &mb,
+                                            const std::uint32_t *expand = nullptr) {
+    std::uint32_t cascade = 0;
+    bool pow2;
+    float inv_mb;
+    if (m.K == 1) {
+        mb = m.mb0;
+        pow2 = m.pow2_0;
+        inv_mb = m.inv_mb0;
+    } else {
+        std::uint32_t c0 = mip_from_xyz(pos, m.K), c1 = mip_from_ds(ds, m.G, m.K);
+        cascade = c0 > c1 ? c0 : c1;
+        mb = fminf(scalbnf(1.0f, (int)cascade), m.bound);
+        pow2 = (__float_as_uint(mb) & 0x007FFFFFu) == 0u && mb >= 1.17549435e-38f;
+        inv_mb = pow2 ? __uint_as_float(0x7F000000u - __float_as_uint(mb)) : 0.f;  // 2^-e for mb = 2^e
+    }
     float Gf = (float)m.G;
     g.x = ((div_mb(pos.x, mb, inv_mb, pow2) + 1.0f) * 0.5f) * Gf;
     g.y = ((div_mb(pos.y, mb, inv_mb, pow2) + 1.0f) * 0.5f) * Gf;
@@ -100,7 +123,8 @@ __device__ __forceinline__ bool occupied_at(const MarchParams &m, V3 pos, float 
     std::uint32_t gx = (std::uint32_t)clampi((int)floorf(g.x), 0, Gi);
     std::uint32_t gy = (std::uint32_t)clampi((int)floorf(g.y), 0, Gi);
     std::uint32_t gz = (std::uint32_t)clampi((int)floorf(g.z), 0, Gi);
-    std::uint32_t idx = cascade * (m.G * m.G * m.G) + morton3(gx, gy, gz);
+    const std::uint32_t code = expand != nullptr ? (expand[gx] | (expand[gy] << 1) | (expand[gz] << 2)) : morton3(gx, gy, gz);
+    std::uint32_t idx = cascade * (m.G * m.G * m.G) + code;
     return (__ldg(bits + (idx >> 3)) >> (idx & 7u)) & 1u;
 }
 
@@ -115,7 +139,12 @@ __device__ __forceinline__ float skip_empty(const MarchParams &m, float t, V3 g,
     float dy = (((ny * m.inv_G - 0.5f) * 2.0f) * mb - pos.y) * inv_d.y;
     float dz = (((nz * m.inv_G - 0.5f) * 2.0f) * mb - pos.z) * inv_d.z;
     float next_t = t + fmaxf(0.0f, fminf(dx, fminf(dy, dz)));
-    for (std::uint32_t it = 0; nt < next_t && it < kMaxSkipIters; ++it) nt += calc_ds(nt, m);
+    if (m.const_ds) {
+        const float c = m.ds_const;
+        for (std::uint32_t it = 0; nt < next_t && it < kMaxSkipIters; ++it) nt += c;
+    } else {
+        for (std::uint32_t it = 0; nt < next_t && it < kMaxSkipIters; ++it) nt += calc_ds(nt, m);
+    }
     return nt;
 }
 
@@ -124,7 +153,7 @@ __device__ __forceinline__ V3 at(V3 o, V3 d, float t) { return {o.x + t * d.x, o
 // ------------------------------------------------------------------------------- march_rays
 
 constexpr int kMarchBlock = 128;
-constexpr int kMarchBlocksPerSm = 6;
+constexpr int kMarchBlocksPerSm = 10;   // 40 warps per SM at <= 48 registers
 
 enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
 
@@ -137,7 +166,9 @@ enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
 // warp w takes 32-ray chunks w, w + n_warps, w + 2 n_warps, ...
 //
 // Per ray the arithmetic and the two passes (count, then write) are the reference's
-// (marching.cu:162-192, :224-267).  Slots are allocated once per trip for all lanes that finished
+// (marching.cu:162-192, :224-267), except that the write pass resumes at the t of the first
+// occupied sample the count pass met instead of re-marching the empty space before it: the march
+// state is t alone, so the samples from there on are the same.  Slots are allocated once per trip for all lanes that finished
 // counting in it (one atomic).  A ray with no sample is valid (marching.cu:196-199); a ray that
 // does not fit the budget is not (:206-209).  The reference also drops a ray whose thread starts
 // after the buffer filled (:135), which only happens when its grid does not fit on the GPU at
@@ -149,7 +180,7 @@ enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
 // next_sample_write_location - number_of_exceeded_samples (the samples written) is exact while
 // the two counters themselves leave out such rays.
 template <bool kProbe>
-__global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
+__global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_kernel(
     std::uint32_t n_rays, std::uint32_t total_samples, MarchParams m,
     const float *__restrict__ rays_o, const float *__restrict__ rays_d,
     const float *__restrict__ t_starts, const float *__restrict__ t_ends,
@@ -159,6 +190,9 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
     std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
     std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
     float *__restrict__ dss, float *__restrict__ z_vals) {
+    __shared__ std::uint32_t expand[1024];  // expand_bits(v), v < G (G <= 1024)
+    for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
+    __syncthreads();
     const unsigned lane = lane_id();
     const unsigned lt_mask = (1u << lane) - 1u;
     const std::uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -168,7 +202,7 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
     int phase = kIdle;
     std::uint32_t ray = 0, n = 0, k = 0, start = 0, it = 0;
     V3 o{0.f, 0.f, 0.f}, d{1.f, 1.f, 1.f}, inv_d{1.f, 1.f, 1.f};
-    float t = 0.f, t1 = 0.f, t_first = 0.f;
+    float t = 0.f, t1 = 0.f, t_hit = 0.f;
     std::uint32_t cursor = 0;   // static interleaving: rays handed out so far by this warp
     bool exhausted = false;     // warp-uniform
 
@@ -197,8 +231,7 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
                     t1 = t_ends[r];
                     if (t1 > t0) {  // marching.cu:151
                         inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-                        t_first = t0 + calc_ds(t0, m) * noises[r];
-                        t = t_first;
+                        t = t0 + calc_ds(t0, m) * noises[r];
                         n = 0;
                         it = 0;
                         phase = kCount;
@@ -226,7 +259,7 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
             const float ds = calc_ds(t, m);
             V3 g;
             float mb;
-            if (occupied_at(m, pos, ds, bits, g, mb)) {
+            if (occupied_at(m, pos, ds, bits, g, mb, expand)) {
                 if (phase == kWrite) {
                     const std::uint32_t s = start + k;
                     idcs[s] = ray;
@@ -240,6 +273,7 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
                     z_vals[s] = t;
                     ++k;
                 } else {
+                    if (n == 0) t_hit = t;
                     ++n;
                     first_hit = (n & 15u) == 1u;  // at the first occupied sample and every 16 after
                 }
@@ -284,7 +318,7 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_kernel(
                 rays_startidx[ray] = fits ? start : 0u;
                 if (fits) {  // second pass writes the samples (marching.cu:224-267)
                     phase = kWrite;
-                    t = t_first;
+                    t = t_hit;
                     k = 0;
                     it = 0;
                 } else {
@@ -581,6 +615,15 @@ MarchParams make_params(std::uint32_t dns, std::uint32_t K, std::uint32_t G, flo
     m.inv_G = 1.0f / (float)G;
     m.ds_lo = 2.0f * kSqrt3 * fminf(bound, 1.0f) / (float)dns;
     m.ds_hi = 2.0f * kSqrt3 * bound * m.inv_G;
+    m.const_ds = sp == 0.0f;
+    m.ds_const = fminf(m.ds_lo, m.ds_hi);
+    m.mb0 = fminf(1.0f, bound);
+    std::uint32_t u;
+    std::memcpy(&u, &m.mb0, 4);
+    m.pow2_0 = (u & 0x007FFFFFu) == 0u && m.mb0 >= 1.17549435e-38f;
+    const std::uint32_t iu = 0x7F000000u - u;
+    m.inv_mb0 = 0.f;
+    if (m.pow2_0) std::memcpy(&m.inv_mb0, &iu, 4);
     return m;
 }
 

@@ -420,6 +420,132 @@ __global__ void zero_rows_kernel(std::uint32_t n, const std::uint32_t *__restric
         x[i] = 0.f;
 }
 
+// ------------------------------------------------------------------- proposal-field MLP
+//
+// The learned proposal's density network: x = relu(relu(enc @ P0) @ P1) @ P2 with enc the
+// 4-level hash encoding (8 features), P0 [8][64], P1 [64][64], P2 [64][1] packed in that order
+// (4672 floats), x the log density.  Same tiling as the field MLP above (64 samples per tile,
+// weights in shared memory); the backward recomputes the tile and keeps per-thread dL/dP shares
+// across tiles, one partial per CTA.
+constexpr int kP0 = 0, kP1 = 512, kP2 = 4608, kNP = 4672;
+
+template <int NT>
+__device__ __forceinline__ void load_prop_weights(const float *__restrict__ w, float *sP, float *sT) {
+    // sP: P0 [8][64], P1 [64][64], P2 padded to [64][4] (columns 1..3 zero)
+    for (int i = threadIdx.x; i < kP2; i += NT) sP[i] = w[i];
+    for (int i = threadIdx.x; i < 256; i += NT) sP[kP2 + i] = (i % 4 == 0) ? w[kP2 + i / 4] : 0.f;
+    if (sT != nullptr) {  // P1^T [64][64] @0, P0^T [64][8] @4096
+        for (int i = threadIdx.x; i < 4096; i += NT) sT[(i % 64) * 64 + i / 64] = w[kP1 + i];
+        for (int i = threadIdx.x; i < 512; i += NT) sT[4096 + (i % 64) * 8 + i / 64] = w[kP0 + i];
+    }
+    __syncthreads();
+}
+
+template <int NT>
+__device__ __forceinline__ void load_enc8(const float *__restrict__ enc, std::size_t s0, int rows, float *X) {
+    for (int i = threadIdx.x; i < kTile * 2; i += NT) {
+        const int r = i / 2, c = (i % 2) * 4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r < rows) v = *reinterpret_cast<const float4 *>(enc + (s0 + r) * 8 + c);
+        *reinterpret_cast<float4 *>(X + r * kLd + c) = v;
+    }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) prop_forward_kernel(std::uint32_t n, const std::uint32_t *__restrict__ count,
+                                                          const float *__restrict__ enc, const float *__restrict__ w,
+                                                          float *__restrict__ x) {
+    extern __shared__ __align__(16) float smem[];
+    float *sP = smem, *X0 = sP + kP2 + 256, *H1 = X0 + kTile * kLd, *H2 = H1 + kTile * kLd, *O = H2 + kTile * kLd;
+    load_prop_weights<NT>(w, sP, nullptr);
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::size_t s0 = (std::size_t)tile * kTile;
+        const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
+        load_enc8<NT>(enc, s0, rows, X0);
+        __syncthreads();
+        mm<NT, 8, 64, true>(X0, kLd, sP + kP0, H1, kLd);
+        __syncthreads();
+        mm<NT, 64, 64, true>(H1, kLd, sP + kP1, H2, kLd);
+        __syncthreads();
+        mm<NT, 64, 4, false>(H2, kLd, sP + kP2, O, 4);
+        __syncthreads();
+        for (int r = threadIdx.x; r < rows; r += NT) x[s0 + r] = O[r * 4];
+        __syncthreads();
+    }
+}
+
+// dL/dx rows past the active count are ignored; dL/denc rows past it are left unwritten.
+template <int NT>
+__global__ void __launch_bounds__(NT) prop_backward_kernel(std::uint32_t n, const std::uint32_t *__restrict__ count,
+                                                           const float *__restrict__ enc, const float *__restrict__ w,
+                                                           const float *__restrict__ dL_dx, float *__restrict__ dL_denc,
+                                                           float *__restrict__ partials) {
+    extern __shared__ __align__(16) float smem[];
+    float *sP = smem, *sT = sP + kP2 + 256, *X0 = sT + 4608, *H1 = X0 + kTile * kLd, *H2 = H1 + kTile * kLd;
+    float *G = H2 + kTile * kLd;   // dL/dx of the tile
+    load_prop_weights<NT>(w, sP, sT);
+    WGrad<NT, 8, 64> g0;
+    WGrad<NT, 64, 64> g1;
+    float g2 = 0.f;   // thread t < 64 owns dL/dP2[t]
+    g0.zero();
+    g1.zero();
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::size_t s0 = (std::size_t)tile * kTile;
+        const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
+        load_enc8<NT>(enc, s0, rows, X0);
+        for (int r = threadIdx.x; r < kTile; r += NT) G[r] = r < rows ? dL_dx[s0 + r] : 0.f;
+        __syncthreads();
+        mm<NT, 8, 64, true>(X0, kLd, sP + kP0, H1, kLd);
+        __syncthreads();
+        mm<NT, 64, 64, true>(H1, kLd, sP + kP1, H2, kLd);
+        __syncthreads();
+        if (threadIdx.x < 64) {  // dP2 += h2^T dx
+            float a = 0.f;
+            for (int s = 0; s < kTile; ++s) a += H2[s * kLd + threadIdx.x] * G[s];
+            g2 += a;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < kTile * 64; i += NT) {  // dA2 = dx P2^T * (h2 > 0), over H2
+            const int r = i / 64, c = i % 64;
+            H2[r * kLd + c] = H2[r * kLd + c] > 0.f ? G[r] * sP[kP2 + c * 4] : 0.f;
+        }
+        __syncthreads();
+        g1.add(H1, kLd, H2, kLd, kTile);
+        __syncthreads();
+        mm_mask_inplace<NT, 64, 64>(H2, kLd, sT, H1, kLd);  // dA1 over H1
+        __syncthreads();
+        g0.add(X0, kLd, H1, kLd, kTile);
+        __syncthreads();
+        mm<NT, 64, 8, false>(H1, kLd, sT + 4096, X0, kLd);  // dL/denc over X0
+        __syncthreads();
+        for (int i = threadIdx.x; i < rows * 2; i += NT) {
+            const int r = i / 2, c = (i % 2) * 4;
+            *reinterpret_cast<float4 *>(dL_denc + (s0 + r) * 8 + c) = *reinterpret_cast<const float4 *>(X0 + r * kLd + c);
+        }
+        __syncthreads();
+    }
+    float *p = partials + (std::size_t)blockIdx.x * kNP;
+    g0.store(p + kP0);
+    g1.store(p + kP1);
+    if (threadIdx.x < 64) p[kP2 + threadIdx.x] = g2;
+}
+
+__global__ void reduce_partials_n_kernel(std::uint32_t n_parts, std::uint32_t n, const float *__restrict__ partials,
+                                         float *__restrict__ dW, int accumulate) {
+    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float a = 0.f;
+    for (std::uint32_t c = 0; c < n_parts; ++c) a += partials[(std::size_t)c * n + j];
+    dW[j] = accumulate ? dW[j] + a : a;
+}
+
+constexpr std::size_t kPropFwdSmem = (std::size_t)(kP2 + 256 + 3 * kTile * kLd + kTile * 4) * sizeof(float);
+constexpr std::size_t kPropBwdSmem = (std::size_t)(kP2 + 256 + 4608 + 3 * kTile * kLd + kTile) * sizeof(float);
+
 constexpr std::size_t kFwdSmem = (std::size_t)(kNW + kFwdActFloats) * sizeof(float);
 constexpr std::size_t kBwdSmem = (std::size_t)(kNW + kNT + kActFloats) * sizeof(float);
 constexpr std::size_t kDensSmem = (std::size_t)(kNW + 3 * kTile * kLd) * sizeof(float);
@@ -500,6 +626,43 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
         zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
         count_launches(1);
     }
+    return launch_status();
+}
+
+int launch_prop_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                        const float *weights, float *x) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "proposal mlp: enc and weights must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(prop_forward_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropFwdSmem));
+        attr = true;
+    }
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kTile - 1) / kTile;
+    const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
+    prop_forward_kernel<256><<<grid, 256, kPropFwdSmem, stream>>>(n, count, enc, weights, x);
+    count_launches(1);
+    return launch_status();
+}
+
+std::size_t prop_partials_floats() { return (std::size_t)sm_count() * kNP; }
+
+// `partials` holds prop_partials_floats() floats.
+int launch_prop_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                         const float *weights, const float *dL_dx, float *dL_denc, float *dL_dweights, float *partials,
+                         bool accumulate) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_denc) && aligned16(partials),
+                  "proposal mlp: buffers must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(prop_backward_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropBwdSmem));
+        attr = true;
+    }
+    const unsigned grid = (unsigned)sm_count();
+    prop_backward_kernel<256><<<grid, 256, kPropBwdSmem, stream>>>(n, count, enc, weights, dL_dx, dL_denc, partials);
+    count_launches(1);
+    reduce_partials_n_kernel<<<(kNP + 255) / 256, 256, 0, stream>>>(grid, kNP, partials, dL_dweights, accumulate ? 1 : 0);
+    count_launches(1);
     return launch_status();
 }
 

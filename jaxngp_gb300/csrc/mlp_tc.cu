@@ -253,6 +253,19 @@ __device__ __forceinline__ void load_enc_row(const float *__restrict__ enc, std:
     }
 }
 
+// Row r of tile `tile`: encoding, direction (+z past the end) and, when `g` is given, dL/ddrgb.
+__device__ __forceinline__ void fetch_row(const float *__restrict__ enc, const float *__restrict__ dirs,
+                                          const float *__restrict__ dL_ddrgb, std::uint32_t tile, int r,
+                                          std::uint32_t n_act, float *v, float *dir, float4 *g) {
+    const std::size_t s = (std::size_t)tile * kRows + r;
+    const bool valid = s < n_act;
+    load_enc_row(enc, s, valid, v);
+    dir[0] = valid ? dirs[s * 3 + 0] : 0.f;
+    dir[1] = valid ? dirs[s * 3 + 1] : 0.f;
+    dir[2] = valid ? dirs[s * 3 + 2] : 1.f;
+    if (g != nullptr) *g = valid ? reinterpret_cast<const float4 *>(dL_ddrgb)[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 template <int NWG>
 __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_forward_kernel(
     std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
@@ -280,16 +293,19 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_forward_kernel(
 
     const std::uint32_t n_act = active_count(n, count);
     const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
-    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += gridDim.x * NWG) {
+    const std::uint32_t step = gridDim.x * NWG;
+    float nv[32], nd[3];  // the next tile's row, loaded while the current tile computes
+    fetch_row(enc, dirs, nullptr, blockIdx.x * NWG + g, r, n_act, nv, nd, nullptr);
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
-        float v[32], dir[3] = {0.f, 0.f, 1.f};
-        load_enc_row(enc, s, valid, v);
-        if (valid) {
-            dir[0] = dirs[s * 3 + 0];
-            dir[1] = dirs[s * 3 + 1];
-            dir[2] = dirs[s * 3 + 2];
-        }
+        float v[32], dir[3];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = nv[i];
+        dir[0] = nd[0];
+        dir[1] = nd[1];
+        dir[2] = nd[2];
+        fetch_row(enc, dirs, nullptr, tile + step, r, n_act, nv, nd, nullptr);
         store_row<32>(act + kX0, r, v);
         float x0, rgb[3];
         tile_forward(wg, sw, act, dir, x0, rgb);
@@ -391,23 +407,26 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_backward_kernel(
     const std::uint32_t n_act = active_count(n, count);
     const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
     bool first = true;
-    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += gridDim.x * NWG) {
+    const std::uint32_t step = gridDim.x * NWG;
+    float nv[32], nd[3];  // the next tile's row, loaded while the current tile computes
+    float4 ng;
+    fetch_row(enc, dirs, dL_ddrgb, blockIdx.x * NWG + g, r, n_act, nv, nd, &ng);
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
-        float v[64], dir[3] = {0.f, 0.f, 1.f};
-        load_enc_row(enc, s, valid, v);
-        if (valid) {
-            dir[0] = dirs[s * 3 + 0];
-            dir[1] = dirs[s * 3 + 1];
-            dir[2] = dirs[s * 3 + 2];
-        }
+        float v[64], dir[3];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = nv[i];
+        dir[0] = nd[0];
+        dir[1] = nd[1];
+        dir[2] = nd[2];
+        const float4 go = ng;
+        fetch_row(enc, dirs, dL_ddrgb, tile + step, r, n_act, nv, nd, &ng);
         store_row<32>(act + kX0, r, v);
         float x0, rgb[3];
         tile_forward(wg, sw, act, dir, x0, rgb);
 
         // output layer: dL/da4 (3, padded to 16) and dL/dx0 through the truncated exponential
-        float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid) go = reinterpret_cast<const float4 *>(dL_ddrgb)[s];
         const float dx0 = gs * go.x * expf(fminf(fmaxf(x0, -15.f), 15.f));
         {
             float d[16];

@@ -1,0 +1,342 @@
+// Learned proposal sampler for sm_103a: coarse occupancy blocks, per-ray occupied interval and
+// sample-slot allocation, proposal bin points, inverse-CDF sampling and the proposal's
+// log-density regression loss.  The reference has no proposal sampler; this is the project's own
+// algorithm, restated for the tests in the CPU oracle (one rounding per float operation in the
+// oracle's order: this file is built without FMA contraction).
+//
+// Training step with the proposal (per ray, R rays, a budget of S samples):
+//   1. coarse DDA over blocks of 8^3 occupancy cells (grown by one cell): no occupied block ->
+//      the ray is valid with no samples (it shows its background); else its interval [t_a, t_b]
+//   2. a ray with an interval takes N_SAMPLES slots (one atomic per warp); rays past the budget
+//      are invalid, as in march_rays (marching.cu:206-209 of the reference)
+//   3. N_BINS points over the interval -> proposal field (hash grid + MLP, other files) -> log
+//      densities -> N_SAMPLES stratified inverse-CDF samples written in march_rays' layout
+//      (xyzs, dirs, dss, z_vals at rays_sample_startidx), so the field, the integrator and the
+//      loss run unchanged
+//   4. the proposal regresses the field's log density at the field's samples (loss kernel here)
+#include "common.cuh"
+
+namespace ngp {
+namespace {
+
+constexpr int kBins = 64, kSamples = 48;
+constexpr float kMix = 0.1f, kEps = 1e-3f, kUnder = 2.0f;
+
+__device__ __forceinline__ std::uint32_t expand_bits(std::uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// coarse[cx + cy Gc + cz Gc^2] = any occupied fine cell in the block grown by one cell.
+__global__ void coarse_grid_kernel(std::uint32_t G, const std::uint8_t *__restrict__ bits, std::uint8_t *__restrict__ coarse) {
+    const std::uint32_t Gc = G / 8, n = Gc * Gc * Gc;
+    const std::uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int cx = (int)(c % Gc), cy = (int)((c / Gc) % Gc), cz = (int)(c / (Gc * Gc));
+    const int lo[3] = {max(cx * 8 - 1, 0), max(cy * 8 - 1, 0), max(cz * 8 - 1, 0)};
+    const int hi[3] = {min(cx * 8 + 8, (int)G - 1), min(cy * 8 + 8, (int)G - 1), min(cz * 8 + 8, (int)G - 1)};
+    std::uint8_t any = 0;
+    for (int z = lo[2]; z <= hi[2] && !any; ++z)
+        for (int y = lo[1]; y <= hi[1] && !any; ++y)
+            for (int x = lo[0]; x <= hi[0]; ++x) {
+                const std::uint32_t m = expand_bits((std::uint32_t)x) | (expand_bits((std::uint32_t)y) << 1) |
+                                        (expand_bits((std::uint32_t)z) << 2);
+                if ((bits[m >> 3] >> (m & 7u)) & 1u) {
+                    any = 1;
+                    break;
+                }
+            }
+    coarse[c] = any;
+}
+
+// The ray's occupied interval over the coarse grid (a 3D DDA, x/y/z order on ties).
+__device__ __forceinline__ bool ray_interval(float ox, float oy, float oz, float dx, float dy, float dz, float t0,
+                                             float t1, const std::uint8_t *__restrict__ coarse, int Gc, float mb,
+                                             float &ta, float &tb) {
+    ta = 0.f;
+    tb = 0.f;
+    if (!(t0 < t1)) return false;
+    const float o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
+    const float scale = (float)Gc / (2.0f * mb);
+    int cell[3], step[3];
+    float tmax[3], tdel[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float g = ((o[a] + t0 * d[a]) + mb) * scale;
+        cell[a] = min(max((int)floorf(g), 0), Gc - 1);
+        if (d[a] > 0.f) {
+            step[a] = 1;
+            tmax[a] = (((float)(cell[a] + 1) / scale - mb) - o[a]) / d[a];
+            tdel[a] = (1.0f / scale) / d[a];
+        } else if (d[a] < 0.f) {
+            step[a] = -1;
+            tmax[a] = (((float)cell[a] / scale - mb) - o[a]) / d[a];
+            tdel[a] = (-1.0f / scale) / d[a];
+        } else {
+            step[a] = 0;
+            tmax[a] = __int_as_float(0x7f800000);
+            tdel[a] = __int_as_float(0x7f800000);
+        }
+    }
+    float t = t0;
+    bool hit = false;
+    for (int it = 0; it < 3 * Gc + 3; ++it) {
+        if (!(t < t1)) break;
+        const float m = fminf(tmax[0], fminf(tmax[1], tmax[2]));
+        const int a = tmax[0] == m ? 0 : (tmax[1] == m ? 1 : 2);
+        const float tn = fminf(m, t1);
+        if (coarse[cell[0] + cell[1] * Gc + cell[2] * Gc * Gc]) {
+            if (!hit) ta = t;
+            hit = true;
+            tb = tn;
+        }
+        cell[a] += step[a];
+        if (cell[a] < 0 || cell[a] >= Gc) break;
+        t = m;
+        tmax[a] = tmax[a] + tdel[a];
+    }
+    return hit;
+}
+
+// Step 1-2: interval, slot allocation.  Slot j = startidx / kSamples of a fitting ray records the
+// ray (ray_of_slot) and its interval (slot_ta, slot_tb).
+__global__ void __launch_bounds__(256) proposal_rays_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, int Gc, float mb, const float *__restrict__ rays_o,
+    const float *__restrict__ rays_d, const float *__restrict__ t_starts, const float *__restrict__ t_ends,
+    const std::uint8_t *__restrict__ coarse, std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded,
+    bool *__restrict__ ray_is_valid, std::uint32_t *__restrict__ rays_n_samples,
+    std::uint32_t *__restrict__ rays_startidx, std::uint32_t *__restrict__ ray_of_slot, float *__restrict__ slot_ta,
+    float *__restrict__ slot_tb) {
+    const std::uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = r < n_rays;
+    float ta = 0.f, tb = 0.f;
+    bool hit = false;
+    if (in)
+        hit = ray_interval(rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2],
+                           rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2],
+                           t_starts[r], t_ends[r], coarse, Gc, mb, ta, tb);
+    hit = hit && tb > ta;
+    const std::uint32_t need = hit ? (std::uint32_t)kSamples : 0u;
+    const std::uint32_t incl = warp_inclusive_scan(need);
+    const std::uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    std::uint32_t base = 0;
+    if (lane_id() == 31 && total > 0) base = atomicAdd(next_loc, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    const std::uint32_t start = base + incl - need;
+    const bool fits = hit && (std::uint64_t)start + kSamples <= total_samples;
+    const unsigned over = __ballot_sync(0xffffffffu, hit && !fits);
+    if (lane_id() == 0 && over != 0u) atomicAdd(n_exceeded, (std::uint32_t)__popc(over) * kSamples);
+    if (!in) return;
+    if (!hit) {
+        ray_is_valid[r] = true;
+        rays_n_samples[r] = 0;
+        rays_startidx[r] = 0;
+        return;
+    }
+    ray_is_valid[r] = fits;
+    rays_n_samples[r] = fits ? (std::uint32_t)kSamples : 0u;
+    rays_startidx[r] = fits ? start : 0u;
+    if (fits) {
+        const std::uint32_t j = start / kSamples;
+        ray_of_slot[j] = r;
+        slot_ta[j] = ta;
+        slot_tb[j] = tb;
+    }
+}
+
+// counts[0] = slots (fitting rays), counts[1] = bin points, counts[2] = samples.
+__global__ void proposal_counts_kernel(std::uint32_t total_samples, const std::uint32_t *__restrict__ next_loc,
+                                       std::uint32_t *__restrict__ counts) {
+    const std::uint32_t slots = min(*next_loc / kSamples, total_samples / kSamples);
+    counts[0] = slots;
+    counts[1] = slots * kBins;
+    counts[2] = slots * kSamples;
+}
+
+// Step 3a: bin centres of every slot's interval.
+__global__ void __launch_bounds__(256) proposal_bin_points_kernel(
+    const std::uint32_t *__restrict__ counts, const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+    const std::uint32_t *__restrict__ ray_of_slot, const float *__restrict__ slot_ta, const float *__restrict__ slot_tb,
+    float *__restrict__ points) {
+    const std::uint32_t n = counts[1];
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    for (std::size_t p = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+        const std::uint32_t j = (std::uint32_t)(p / kBins), i = (std::uint32_t)(p % kBins);
+        const std::uint32_t r = ray_of_slot[j];
+        const float ta = slot_ta[j], delta = (slot_tb[j] - ta) / (float)kBins;
+        const float c = ta + ((float)i + 0.5f) * delta;
+        points[p * 3 + 0] = rays_o[(std::size_t)r * 3 + 0] + c * rays_d[(std::size_t)r * 3 + 0];
+        points[p * 3 + 1] = rays_o[(std::size_t)r * 3 + 1] + c * rays_d[(std::size_t)r * 3 + 1];
+        points[p * 3 + 2] = rays_o[(std::size_t)r * 3 + 2] + c * rays_d[(std::size_t)r * 3 + 2];
+    }
+}
+
+__device__ __forceinline__ std::uint64_t splitmix(std::uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Step 3c: one thread per slot turns the bins' log densities into kSamples samples.
+__global__ void __launch_bounds__(128) proposal_sample_kernel(
+    const std::uint32_t *__restrict__ counts, int perturb, std::uint64_t seed, const float *__restrict__ rays_o,
+    const float *__restrict__ rays_d, const std::uint32_t *__restrict__ ray_of_slot, const float *__restrict__ slot_ta,
+    const float *__restrict__ slot_tb, const float *__restrict__ x_bins, std::uint32_t *__restrict__ idcs,
+    float *__restrict__ xyzs, float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals) {
+    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= counts[0]) return;
+    const std::uint32_t r = ray_of_slot[j];
+    const float ta = slot_ta[j], tb = slot_tb[j];
+    const float delta = (tb - ta) / (float)kBins;
+    const float *xb = x_bins + (std::size_t)j * kBins;
+    float w[kBins];
+    float acc = 0.f, W = 0.f;
+#pragma unroll 8
+    for (int i = 0; i < kBins; ++i) {
+        const float s = expf(fminf(fmaxf(xb[i], -15.f), 15.f));
+        const float T = expf(-(delta * acc));
+        const float a = -expm1f(-(s * delta));
+        w[i] = T * a;
+        W = W + w[i];
+        acc = acc + s;
+    }
+    // pdf mixed with a uniform one, in place
+#pragma unroll 8
+    for (int i = 0; i < kBins; ++i) {
+        const float wi = W > 0.f ? w[i] / W : 1.0f / (float)kBins;
+        w[i] = (1.0f - kMix) * wi + kMix / (float)kBins;
+    }
+    const float o[3] = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
+    const float d[3] = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
+    const std::size_t s0 = (std::size_t)j * kSamples;
+    // inverse-CDF edges e_0 = t_a, e_k (0 < k < kSamples), e_kSamples = t_b; sample k at the
+    // midpoint of [e_k, e_k+1], standing for that interval
+    int b = 0;
+    float c_lo = 0.f, c_hi = w[0], e_prev = ta;
+    for (int k = 1; k <= kSamples; ++k) {
+        float e = tb;
+        if (k < kSamples) {
+            float xi = 0.5f;
+            if (perturb)
+                xi = (float)(splitmix(seed ^ ((std::uint64_t)r * kSamples + (std::uint64_t)k) * 0x2545F4914F6CDD1Dull) >> 40) *
+                     (1.0f / 16777216.0f);
+            const float u = (((float)k - 0.5f) + xi) / (float)kSamples;
+            while (u >= c_hi && b < kBins - 1) {
+                ++b;
+                c_lo = c_hi;
+                c_hi = c_hi + w[b];
+            }
+            const float frac = fminf(fmaxf((u - c_lo) / w[b], 0.f), 1.f);
+            e = ta + ((float)b + frac) * delta;
+        }
+        const float t = (e_prev + e) * 0.5f;
+        const std::size_t s = s0 + (k - 1);
+        idcs[s] = r;
+        xyzs[s * 3 + 0] = o[0] + t * d[0];
+        xyzs[s * 3 + 1] = o[1] + t * d[1];
+        xyzs[s * 3 + 2] = o[2] + t * d[2];
+        dirs[s * 3 + 0] = d[0];
+        dirs[s * 3 + 1] = d[1];
+        dirs[s * 3 + 2] = d[2];
+        z_vals[s] = t;
+        dss[s] = e - e_prev;
+        e_prev = e;
+    }
+}
+
+// Step 4: dL/dx of the log-density regression over the first counts[count_index] points (or n
+// when counts is NULL): L = sum w (x - log(sigma + eps))^2 / n with w = kUnder below the target.
+// sigma is read with a stride (4 for drgbs rows).  loss[0] accumulates the sum.
+__global__ void __launch_bounds__(256) proposal_loss_kernel(
+    std::uint32_t n_max, const std::uint32_t *__restrict__ counts, int count_index, const float *__restrict__ x,
+    const float *__restrict__ sigma, int sigma_stride, float *__restrict__ dL_dx, float *__restrict__ loss) {
+    const std::uint32_t n = counts != nullptr ? min(n_max, counts[count_index]) : n_max;
+    const float inv_n = n > 0 ? 1.0f / (float)n : 0.f;
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (i < n) {
+        const float y = logf(sigma[(std::size_t)i * sigma_stride] + kEps);
+        const float res = x[i] - y;
+        const float w = res < 0.f ? kUnder : 1.0f;
+        dL_dx[i] = 2.0f * w * res * inv_n;
+        l = w * res * res;
+    } else if (i < n_max) {
+        dL_dx[i] = 0.f;
+    }
+    l = warp_sum(l);
+    if (lane_id() == 0 && l != 0.f) atomicAdd(loss, l);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------- launchers
+
+int launch_proposal_coarse(cudaStream_t stream, std::uint32_t G, const std::uint8_t *bits, std::uint8_t *coarse) {
+    NGP_CHECK_ARG(G >= 8 && G % 8 == 0 && G <= 1024, "proposal: G must be a multiple of 8 in [8, 1024]");
+    const std::uint32_t n = (G / 8) * (G / 8) * (G / 8);
+    coarse_grid_kernel<<<(n + 127) / 128, 128, 0, stream>>>(G, bits, coarse);
+    count_launches(1);
+    return launch_status();
+}
+
+int launch_proposal_rays(cudaStream_t stream, std::uint32_t n_rays, std::uint32_t total_samples, std::uint32_t G,
+                         float bound, const float *rays_o, const float *rays_d, const float *t_starts,
+                         const float *t_ends, const std::uint8_t *coarse, std::uint32_t *next_loc,
+                         std::uint32_t *n_exceeded, bool *valid, std::uint32_t *n_samples, std::uint32_t *startidx,
+                         std::uint32_t *ray_of_slot, float *slot_ta, float *slot_tb, std::uint32_t *counts) {
+    NGP_CHECK_ARG(G >= 8 && G % 8 == 0 && G <= 1024, "proposal: G must be a multiple of 8 in [8, 1024]");
+    NGP_CHECK_ARG(bound > 0.f, "proposal: bound must be positive");
+    NGP_CUDA_TRY(cudaMemsetAsync(next_loc, 0, sizeof(std::uint32_t), stream));
+    NGP_CUDA_TRY(cudaMemsetAsync(n_exceeded, 0, sizeof(std::uint32_t), stream));
+    if (n_rays > 0) {
+        proposal_rays_kernel<<<(n_rays + 255) / 256, 256, 0, stream>>>(
+            n_rays, total_samples, (int)(G / 8), fminf(1.0f, bound), rays_o, rays_d, t_starts, t_ends, coarse, next_loc,
+            n_exceeded, valid, n_samples, startidx, ray_of_slot, slot_ta, slot_tb);
+        count_launches(1);
+    }
+    proposal_counts_kernel<<<1, 1, 0, stream>>>(total_samples, next_loc, counts);
+    count_launches(1);
+    return launch_status();
+}
+
+int launch_proposal_bin_points(cudaStream_t stream, std::uint32_t max_slots, const std::uint32_t *counts,
+                               const float *rays_o, const float *rays_d, const std::uint32_t *ray_of_slot,
+                               const float *slot_ta, const float *slot_tb, float *points) {
+    if (max_slots > 0) {
+        proposal_bin_points_kernel<<<grid_for((std::size_t)max_slots * kBins, 256, 8), 256, 0, stream>>>(
+            counts, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, points);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+int launch_proposal_sample(cudaStream_t stream, std::uint32_t max_slots, const std::uint32_t *counts, bool perturb,
+                           std::uint64_t seed, const float *rays_o, const float *rays_d,
+                           const std::uint32_t *ray_of_slot, const float *slot_ta, const float *slot_tb,
+                           const float *x_bins, std::uint32_t *idcs, float *xyzs, float *dirs, float *dss,
+                           float *z_vals) {
+    if (max_slots > 0) {
+        proposal_sample_kernel<<<(max_slots + 127) / 128, 128, 0, stream>>>(
+            counts, perturb ? 1 : 0, seed, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, idcs, xyzs, dirs, dss,
+            z_vals);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+int launch_proposal_loss(cudaStream_t stream, std::uint32_t n_max, const std::uint32_t *counts, int count_index,
+                         const float *x, const float *sigma, int sigma_stride, float *dL_dx, float *loss) {
+    NGP_CHECK_ARG(count_index >= 0 && count_index < 3 && sigma_stride >= 1, "proposal loss: bad count index or stride");
+    if (n_max > 0) {
+        proposal_loss_kernel<<<(n_max + 255) / 256, 256, 0, stream>>>(n_max, counts, count_index, x, sigma,
+                                                                       sigma_stride, dL_dx, loss);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+}  // namespace ngp

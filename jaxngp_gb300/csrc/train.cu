@@ -100,13 +100,16 @@ __global__ void __launch_bounds__(256) train_rays_kernel(
 // is zero (the loss ignores depth).  Gradients are unnormalised; 1/n_valid is applied by the
 // field backward through `grad_scale`.
 //
-// A ray without samples is finished by its own lane.  A ray with samples is processed by its
-// whole warp: 32-sample chunks are loaded coalesced into shared memory, all lanes compute the
-// chunk's opacities in parallel, and one lane runs the compositing recurrence from shared memory
-// in the reference's order (so every rounding is the reference's); in the backward pass the same
-// lane writes per-sample gradients to shared memory and the warp stores them coalesced.  The
-// one-thread-per-ray form walks each long ray through dependent global loads while the rest of
-// its warp idles.
+// Two passes.  The light pass (a thread per ray) finishes every ray without samples -- its
+// prediction is the background -- and appends the rays with samples to a list (one atomic per
+// warp).  The heavy pass gives each listed ray a whole warp, warps taking rays from the list in
+// turn: 32-sample chunks are loaded coalesced into shared memory, all lanes compute the chunk's
+// opacities in parallel, and one lane runs the compositing recurrence from shared memory in the
+// reference's order (so every rounding is the reference's); in the backward pass the same lane
+// writes per-sample gradients to shared memory and the warp stores them coalesced.  Taking rays
+// from a list keeps the warps evenly loaded however the rays with samples cluster in the batch
+// (which rays fit the sample budget follows the order of the allocation atomics).  The loss sums
+// are reduced per block before their one atomic each.
 constexpr int kIlbWarps = 4;
 
 struct IlbChunk {
@@ -121,53 +124,86 @@ __device__ __forceinline__ float huber_grad(float e, float delta, float *loss) {
     return ae <= delta ? e : copysignf(delta, e);
 }
 
-__global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_backward_kernel(
-    std::uint32_t n_rays, std::uint32_t total_samples, float near_distance, float delta, const bool *__restrict__ valid,
-    const std::uint32_t *__restrict__ startidx, const std::uint32_t *__restrict__ n_samples,
-    const float *__restrict__ bgs, const float *__restrict__ gt, const float *__restrict__ dss,
-    const float *__restrict__ z_vals, const float *__restrict__ drgbs,
-    float *__restrict__ dL_ddrgbs, float *__restrict__ acc /* [loss, n_valid, measured] */) {
-    __shared__ IlbChunk chunks[kIlbWarps];
-    IlbChunk &ch = chunks[threadIdx.x >> 5];
-    const unsigned lane = lane_id();
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    float loss = 0.f, nv = 0.f, used_f = 0.f;
+// Adds v[0..2] of every thread of the block into acc[0..2] (one atomic per quantity per block).
+template <int NT>
+__device__ __forceinline__ void block_accumulate(float l, float nv, float used, float *__restrict__ acc) {
+    __shared__ float part[NT / 32][3];
+    l = warp_sum(l);
+    nv = warp_sum(nv);
+    used = warp_sum(used);
+    const unsigned w = threadIdx.x >> 5;
+    if (lane_id() == 0) {
+        part[w][0] = l;
+        part[w][1] = nv;
+        part[w][2] = used;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        float a = 0.f;
+        for (int k = 0; k < NT / 32; ++k) a += part[k][threadIdx.x];
+        if (a != 0.f) atomicAdd(acc + threadIdx.x, a);
+    }
+}
 
-    std::uint32_t my_s = 0, my_n = 0;
-    float my_bg[3] = {0.f, 0.f, 0.f}, my_gt[3] = {0.f, 0.f, 0.f};
-    bool my_valid = false;
+constexpr int kIlbLight = 256;
+
+__global__ void __launch_bounds__(kIlbLight) integrate_loss_light_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, float delta, const bool *__restrict__ valid,
+    const std::uint32_t *__restrict__ startidx, const std::uint32_t *__restrict__ n_samples,
+    const float *__restrict__ bgs, const float *__restrict__ gt, float *__restrict__ acc,
+    std::uint32_t *__restrict__ heavy_count, std::uint32_t *__restrict__ heavy) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float loss = 0.f, nv = 0.f;
+    bool is_heavy = false;
     if (i < n_rays) {
-        my_s = startidx[i];
-        my_n = my_s >= total_samples ? 0u : min(n_samples[i], total_samples - my_s);
-        my_valid = valid[i];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            my_bg[c] = bgs[i * 3 + c];
-            my_gt[c] = gt[i * 3 + c];
-        }
-        if (my_n == 0) {  // T = 1: the prediction is the background
-            if (my_valid) {
+        const std::uint32_t s = startidx[i];
+        const std::uint32_t n = s >= total_samples ? 0u : min(n_samples[i], total_samples - s);
+        if (n == 0) {  // T = 1: the prediction is the background
+            if (valid[i]) {
                 nv = 1.f;
                 float l = 0.f;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) huber_grad(my_bg[c] - my_gt[c], delta, &l);
-                loss += l * (1.f / 3.f);
+                for (int c = 0; c < 3; ++c) huber_grad(bgs[i * 3 + c] - gt[i * 3 + c], delta, &l);
+                loss = l * (1.f / 3.f);
             }
+        } else {
+            is_heavy = true;
         }
     }
+    const unsigned hb = __ballot_sync(0xffffffffu, is_heavy);
+    if (hb != 0u) {
+        std::uint32_t base = 0;
+        if (lane_id() == 0) base = atomicAdd(heavy_count, (unsigned)__popc(hb));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (is_heavy) heavy[base + __popc(hb & ((1u << lane_id()) - 1u))] = i;
+    }
+    block_accumulate<kIlbLight>(loss, nv, 0.f, acc);
+}
 
-    unsigned heavy = __ballot_sync(0xffffffffu, i < n_rays && my_n > 0);
-    while (heavy != 0u) {
-        const int j = __ffs(heavy) - 1;
-        heavy &= heavy - 1u;
-        const std::uint32_t s = __shfl_sync(0xffffffffu, my_s, j);
-        const std::uint32_t n = __shfl_sync(0xffffffffu, my_n, j);
-        const bool rv = __shfl_sync(0xffffffffu, my_valid ? 1 : 0, j) != 0;
+__global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_heavy_kernel(
+    std::uint32_t total_samples, float near_distance, float delta, const bool *__restrict__ valid,
+    const std::uint32_t *__restrict__ startidx, const std::uint32_t *__restrict__ n_samples,
+    const float *__restrict__ bgs, const float *__restrict__ gt, const float *__restrict__ dss,
+    const float *__restrict__ z_vals, const float *__restrict__ drgbs, const std::uint32_t *__restrict__ heavy_count,
+    const std::uint32_t *__restrict__ heavy, float *__restrict__ dL_ddrgbs, float *__restrict__ acc) {
+    __shared__ IlbChunk chunks[kIlbWarps];
+    IlbChunk &ch = chunks[threadIdx.x >> 5];
+    const unsigned lane = lane_id();
+    const std::uint32_t n_heavy = *heavy_count;
+    const std::uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const std::uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    float loss = 0.f, nv = 0.f, used_f = 0.f;   // lane 0's sums for its warp's rays
+
+    for (std::uint32_t h = warp0; h < n_heavy; h += n_warps) {
+        const std::uint32_t ray = heavy[h];
+        const std::uint32_t s = startidx[ray];
+        const std::uint32_t n = min(n_samples[ray], total_samples - s);
+        const bool rv = valid[ray];
         float bg[3], tg[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            bg[c] = __shfl_sync(0xffffffffu, my_bg[c], j);
-            tg[c] = __shfl_sync(0xffffffffu, my_gt[c], j);
+            bg[c] = bgs[ray * 3 + c];
+            tg[c] = gt[ray * 3 + c];
         }
         const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + s;
         // ---- forward (integrating.cu:61-78)
@@ -221,12 +257,12 @@ __global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_backward_kernel
 #pragma unroll
             for (int c = 0; c < 3; ++c) go[c] = huber_grad(fr[c] - tg[c], delta, &l) * (1.f / 3.f);
         }
-        if ((int)lane == j) {
+        if (lane == 0) {
             if (rv) {
-                nv = 1.f;
+                nv += 1.f;
                 loss += l * (1.f / 3.f);
             }
-            used_f = (float)used;
+            used_f += (float)used;
         }
         // ---- backward (integrating.cu:173-233), recomputing the forward
         const bool terminated = fo >= 1.f - kTThreshold;
@@ -270,15 +306,7 @@ __global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_backward_kernel
         }
         for (std::uint32_t k = used + lane; k < n; k += 32) gc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-
-    loss = warp_sum(loss);
-    nv = warp_sum(nv);
-    used_f = warp_sum(used_f);
-    if (lane == 0) {
-        if (loss != 0.f) atomicAdd(acc + 0, loss);
-        if (nv != 0.f) atomicAdd(acc + 1, nv);
-        if (used_f != 0.f) atomicAdd(acc + 2, used_f);
-    }
+    block_accumulate<32 * kIlbWarps>(loss, nv, used_f, acc);
 }
 
 // stats = [loss / n_valid, n_valid, measured_batch_size, samples before compaction];
@@ -543,20 +571,29 @@ int launch_train_rays(cudaStream_t stream, const NgpTrainRaysDescriptor &d, cons
     return launch_status();
 }
 
-// `acc` is a 3-float scratch accumulator.
+// `scratch` holds 4 + n_rays words: the 3 loss sums (f32), the count of rays with samples (u32)
+// and their list (u32).
 int launch_integrate_loss_backward(cudaStream_t stream, const NgpIntegrateLossDescriptor &d, const bool *valid,
                                    const std::uint32_t *startidx, const std::uint32_t *n_samples,
                                    const float *bgs, const float *gt, const float *dss, const float *z_vals,
                                    const float *drgbs, const std::uint32_t *count, float *dL_ddrgbs,
-                                   float *stats, float *grad_scale, float *acc) {
+                                   float *stats, float *grad_scale, float *scratch) {
     NGP_CHECK_ARG(((std::uintptr_t)drgbs & 15u) == 0 && ((std::uintptr_t)dL_ddrgbs & 15u) == 0,
                   "integrate_loss_backward: drgbs and dL_ddrgbs must be 16-byte aligned");
-    NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, 3 * sizeof(float), stream));
+    float *acc = scratch;
+    std::uint32_t *heavy_count = reinterpret_cast<std::uint32_t *>(scratch + 3);
+    std::uint32_t *heavy = heavy_count + 1;
+    NGP_CUDA_TRY(cudaMemsetAsync(scratch, 0, 4 * sizeof(float), stream));
     if (d.n_rays > 0) {
-        integrate_loss_backward_kernel<<<(d.n_rays + 32 * kIlbWarps - 1) / (32 * kIlbWarps), 32 * kIlbWarps, 0, stream>>>(
-            d.n_rays, d.total_samples, d.near_distance, d.huber_delta, valid, startidx, n_samples, bgs, gt, dss, z_vals, drgbs,
-            dL_ddrgbs, acc);
-        count_launches(1);
+        integrate_loss_light_kernel<<<(d.n_rays + kIlbLight - 1) / kIlbLight, kIlbLight, 0, stream>>>(
+            d.n_rays, d.total_samples, d.huber_delta, valid, startidx, n_samples, bgs, gt, acc, heavy_count, heavy);
+        const unsigned warps = (d.n_rays + 31) / 32;
+        const unsigned blocks_max = (warps + kIlbWarps - 1) / kIlbWarps;
+        const unsigned cap = (unsigned)sm_count() * 16;
+        integrate_loss_heavy_kernel<<<blocks_max < cap ? blocks_max : cap, 32 * kIlbWarps, 0, stream>>>(
+            d.total_samples, d.near_distance, d.huber_delta, valid, startidx, n_samples, bgs, gt, dss, z_vals, drgbs,
+            heavy_count, heavy, dL_ddrgbs, acc);
+        count_launches(2);
     }
     if (d.total_samples > 0) {
         zero_tail4_kernel<<<grid_for(d.total_samples, 256, 4), 256, 0, stream>>>(

@@ -48,6 +48,9 @@ class TrainConfig:
     huber_delta: float = 0.1
     seed: int = 0
     mlp_precision: str = "fp32"        # "fp32" (SIMT parity path) or "bf16" (tensor cores)
+    sampler: str = "march"             # "march" (occupancy grid, the reference's) or "proposal"
+    proposal_every: int = 4            # proposal updates every k steps
+    proposal_distill: bool = True      # also regress the proposal at points drawn in occupied cells
 
 
 def cascades_for(bound: float) -> int:
@@ -126,7 +129,7 @@ class NGPTrainer:
         self.g_enc = torch.empty(S, 32, **f32)
         self.stats = torch.zeros(4, **f32)
         self.grad_scale = torch.zeros(1, **f32)
-        self.loss_scratch = torch.zeros(3, **f32)
+        self.loss_scratch = torch.zeros(4 + R, **f32)
         self.mlp_scratch = torch.empty(L.field_backward_scratch_floats(), **f32)
         self.step_count = 0
         self._seed = np.random.SeedSequence(cfg.seed)
@@ -139,6 +142,15 @@ class NGPTrainer:
                                                     cfg.huber_delta)
         self._n_alive = None
         self.cadence_offset = 0   # added to step_count for the occupancy-grid cadence only
+        self.prop = None
+        if cfg.sampler == "proposal":
+            from .proposal import ProposalSampler
+            if self.K != 1:
+                raise ValueError("the proposal sampler supports scenes with one occupancy cascade (bound <= 1)")
+            self.prop = ProposalSampler(R, S, cfg.G, bound, self.dev, seed=cfg.seed)
+            self.enc_d = torch.empty(self.prop.M, 32, **f32)
+        elif cfg.sampler != "march":
+            raise ValueError(f"sampler must be 'march' or 'proposal', got {cfg.sampler!r}")
         self.mark_untrained_grid()
 
     # ---------------------------------------------------------------------------- helpers
@@ -159,6 +171,8 @@ class NGPTrainer:
         thr = torch.full((1,), -0.5, dtype=torch.float32, device=self.dev)
         L.call("ngp_packbits_scalar", [thr, self.density, self.occ_mask, self.bitfield],
                L.PackbitsDescriptor(self.K * self.G3 // 8))
+        if self.prop is not None:
+            self.prop.refresh(self.bitfield)
         self._n_alive = [int((self.density[c * self.G3:(c + 1) * self.G3] >= 0).sum().item()) for c in range(self.K)]
 
     @torch.no_grad()
@@ -180,12 +194,20 @@ class NGPTrainer:
                 x = centres[s0:s0 + (1 << 18)]
                 r2 = ((x[:, None, :] - blobs[None, :, :3]) ** 2).sum(-1)
                 dens[s0:s0 + (1 << 18)] = (blobs[None, :, 4] * torch.exp(-r2 / (2 * blobs[None, :, 3] ** 2))).sum(-1)
+                if len(scene.shells):   # thin shells: every cell the shell passes through
+                    sh = torch.from_numpy(scene.shells).to(self.dev).double()
+                    half_diag = 3 ** 0.5 * mb / G
+                    dist = ((x[:, None, :] - sh[None, :, :3]) ** 2).sum(-1).sqrt() - sh[None, :, 3]
+                    near = dist.abs() <= sh[None, :, 4] + half_diag
+                    dens[s0:s0 + (1 << 18)] += (near.double() * sh[None, :, 5]).sum(-1)
             cur = self.density[c * G3:(c + 1) * G3]
             cur.copy_(torch.where(cur < 0, cur, dens.float()))
         live0 = self.density[:G3][self.density[:G3] >= 0]
         self.threshold.fill_(min(self.thr_step, float(live0.mean().item())))
         L.call("ngp_packbits_scalar", [self.threshold, self.density, self.occ_mask, self.bitfield],
                L.PackbitsDescriptor(self.K * self.G3 // 8))
+        if self.prop is not None:
+            self.prop.refresh(self.bitfield)
         if steady_state:
             self.cadence_offset = 256
 
@@ -216,6 +238,17 @@ class NGPTrainer:
         L.call("ngp_ogrid_threshold", [self.density, self.thr_scratch, self.threshold], self._ogrid_desc())
         L.call("ngp_packbits_scalar", [self.threshold, self.density, self.occ_mask, self.bitfield],
                L.PackbitsDescriptor(self.K * self.G3 // 8))
+        if self.prop is not None:
+            self.prop.refresh(self.bitfield)
+
+    def _distill(self, xyz: torch.Tensor, sigma: torch.Tensor):
+        """The field's density at points drawn in the occupancy grid (half anywhere, half in
+        occupied cells), for the proposal's regression."""
+        M = xyz.shape[0]
+        d = self._ogrid_desc(0, M, False, self._next_seed())
+        L.call("ngp_ogrid_sample", [self.density, self.bitfield, self.prop.cells, xyz], d)
+        L.call("ngp_hashgrid_forward", [xyz, self.latents, None, self.enc_d], self.table.descriptor(M, self.bound))
+        L.call(self._mlp("ngp_field_density"), [self.enc_d, self.weights, sigma], L.NgpMlpDescriptor(M, 0))
 
     # ------------------------------------------------------------------------------- step
     def step(self, perm: Optional[torch.Tensor] = None) -> torch.Tensor:
@@ -228,19 +261,27 @@ class NGPTrainer:
                                           self.bound, int(cfg.perturb), int(cfg.random_bg), (L.c_f32 * 3)(1, 1, 1), seed)
         L.call("ngp_train_rays", [self.data.transforms, self.data.rgbas, perm, self.rays_o, self.rays_d, self.t0,
                                   self.t1, self.noise, self.bgs, self.gt], d_rays)
-        L.call("ngp_march_rays_train", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
-                                        self.counters[0:1], self.counters[1:2], self.valid, self.n_samples,
-                                        self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals,
-                                        self.queue], self._d_march)
-        L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
-        L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, self.count, self.enc], self._d_hg)
-        L.call(self._mlp("ngp_field_forward"), [self.enc, self.dirs, self.weights, self.count, self.drgbs], self._d_mlp)
+        if self.prop is None:
+            L.call("ngp_march_rays_train", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
+                                            self.counters[0:1], self.counters[1:2], self.valid, self.n_samples,
+                                            self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals,
+                                            self.queue], self._d_march)
+            L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
+            cnt = self.count
+        else:
+            cnt = self.prop.sample(self.rays_o, self.rays_d, self.t0, self.t1, self.valid, self.n_samples,
+                                   self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals, cfg.perturb,
+                                   seed ^ 0x5BD1E9955BD1E995)
+        L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, cnt, self.enc], self._d_hg)
+        L.call(self._mlp("ngp_field_forward"), [self.enc, self.dirs, self.weights, cnt, self.drgbs], self._d_mlp)
+        if self.prop is not None and self.step_count % cfg.proposal_every == 0:
+            self.prop.train(self.xyzs, self.drgbs, self._distill if cfg.proposal_distill else None)
         L.call("ngp_integrate_loss_backward", [self.valid, self.startidx, self.n_samples, self.bgs, self.gt, self.dss,
-                                               self.z_vals, self.drgbs, self.count, self.loss_scratch, self.g_drgbs,
+                                               self.z_vals, self.drgbs, cnt, self.loss_scratch, self.g_drgbs,
                                                self.stats, self.grad_scale], self._d_loss)
-        L.call(self._mlp("ngp_field_backward"), [self.enc, self.dirs, self.weights, self.g_drgbs, self.count, self.grad_scale,
+        L.call(self._mlp("ngp_field_backward"), [self.enc, self.dirs, self.weights, self.g_drgbs, cnt, self.grad_scale,
                                       self.mlp_scratch, self.g_enc, self.g_w], self._d_mlp)
-        L.call("ngp_hashgrid_backward", [self.xyzs, self.g_enc, self.count, self.g_lat], self._d_hg_acc)
+        L.call("ngp_hashgrid_backward", [self.xyzs, self.g_enc, cnt, self.g_lat], self._d_hg_acc)
         count = self.step_count
         lr = lr_at(cfg.lr, count)
         L.call("ngp_adam", [self.latents, self.g_lat, self.m_lat, self.v_lat],
@@ -319,3 +360,25 @@ def near_far(bound: float, o: torch.Tensor, d: torch.Tensor):
     ts = torch.maximum(torch.minimum(t0, t1).amax(-1), torch.zeros((), device=o.device))
     te = torch.maximum(t0, t1).amin(-1)
     return ts.contiguous(), te.contiguous()
+
+
+@torch.no_grad()
+def evaluate_psnr(tr: "NGPTrainer", n_views: int = 2, seed: int = 12345, n_steps: int = 4096,
+                  radius: float = 4.0) -> float:
+    """Mean PSNR (utils/data.py:407-410) over held-out views -- poses on the training hemisphere
+    drawn with another seed -- rendered by the occupancy-grid inference renderer over a white
+    background, against the scene's quadrature ground truth blended over white."""
+    from .renderer import Renderer
+    from .scene import hemisphere_poses, poses_to_transforms, psnr_u8, render_views
+    cam = tr.data.camera
+    poses = hemisphere_poses(n_views, radius, np.random.default_rng(seed))
+    transforms = torch.from_numpy(poses_to_transforms(poses)).to(tr.dev)
+    gt = render_views(tr.data.scene, cam, transforms, n_steps).view(n_views, cam.height, cam.width, 4).float() / 255
+    gt_rgb = (gt[..., :3] * gt[..., 3:] + (1 - gt[..., 3:])).mul(255).round().to(torch.uint8)
+    r = Renderer.from_trainer(tr, n_slots=1 << 18)
+    vals = []
+    for v in range(n_views):
+        rgb, _ = r.render_image(cam, transforms[v], bg=(1.0, 1.0, 1.0))
+        vals.append(psnr_u8(rgb, gt_rgb[v]))
+    return float(np.mean(vals))
+
