@@ -1,16 +1,20 @@
 #!/usr/bin/env python
-"""Training throughput of the plain NGP step (hash grid + occupancy-grid march + fused field MLP +
-volume integrator, FP32) on the synthetic 64-blob scene: 100 views at 800x800, 2^18 rays and a
-2^18-sample budget per step.
+"""Training throughput of the NGP step (hash grid + sampler + fused field MLP + volume integrator)
+on the synthetic 64-blob scene: 100 views at 800x800, 2^18 rays and a 2^18-sample budget per step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--forms ...]
 
-Prints one JSON line.  `value` is train rays/s (sum of n_valid_rays over the timed steps / time,
-the reference's own throughput count, app/nerf/train.py:59) with every input resident on the GPU;
-`e2e` is the same step driven through the public API with the pixel indices copied from pinned
-host memory and the step's metrics copied back every step.  `--impl reference` times the CPU
-restatement of the same step (the reference has no CPU path for its volume-rendering ops) on
-the host's cores, on a bounded sample of the batch, extrapolated to the full batch.
+Prints one JSON line.  The headline (`value`) is the first form, by default the plain step --
+the reference's algorithm (occupancy-grid march, FP32 field MLP) -- in train rays/s (sum of
+n_valid_rays over the timed steps / time, the reference's own throughput count,
+app/nerf/train.py:59) with every input resident on the GPU; `e2e` is the same step driven through
+the public API with the pixel indices copied from pinned host memory and the step's metrics copied
+back every step.  `forms` repeats the measurement for the BF16 tensor-core field MLP and for the
+learned proposal sampler with it, each with the held-out PSNR of the trained field and 1080p
+inference FPS, and `learned_proposal_vs_plain` gives their ratio and PSNR difference.
+`--impl reference` times the CPU restatement of the plain step (the reference has no CPU path for
+its volume-rendering ops) on the host's cores, on a bounded sample of the batch, extrapolated to
+the full batch.
 """
 from __future__ import annotations
 
@@ -26,6 +30,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "train rays/s (plain FP32 hash-grid NeRF step, 64-blob scene)"
+FORMS = {"fp32-march": ("fp32", "march"), "bf16-march": ("bf16", "march"), "bf16-proposal": ("bf16", "proposal")}
 UNIT = "rays/s"
 WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
            "L16 F2 T2^19 Nmin16 Nmax2048, MLP 32-64-16 / 32-64-64-3, R=S=2^18, Adam lr1e-2, fp32"
@@ -44,10 +49,10 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
-                   help="field MLP: fp32 SIMT (parity path) or bf16 tensor cores")
-    p.add_argument("--sampler", default="march", choices=["march", "proposal"],
-                   help="occupancy-grid march (the reference's) or the learned proposal sampler")
+    p.add_argument("--forms", default="fp32-march,bf16-march,bf16-proposal",
+                   help="training forms to run, the first is the headline: fp32-march (the reference's "
+                        "algorithm, FP32 SIMT field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
+                        "(learned proposal sampler + BF16 MLP)")
     p.add_argument("--render-frames", type=int, default=12, help="1920x1080 frames rendered on a 120-pose orbit")
     p.add_argument("--render-slots", type=int, default=1 << 18, help="rays in flight in the inference renderer")
     p.add_argument("--render-cap", type=int, default=8, help="march_steps_cap of the inference renderer")
@@ -184,11 +189,10 @@ def algorithmic(name: str, R: int, S: int, P: int, G: int) -> tuple:
     return ("hbm", 0)
 
 
-def run_ours(args) -> dict:
-    import numpy as np
+def setup_device(args):
+    """Process group (N > 1), device, built library; returns (world, rank, local)."""
     import torch
     import torch.distributed as dist
-
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -199,13 +203,22 @@ def run_ours(args) -> dict:
     __graft_entry__.build() if rank == 0 and not os.path.exists(os.path.join(ROOT, "jaxngp_gb300", "libngp_gb300.so")) else None
     if world > 1:
         dist.barrier()
+    return world, rank, local
+
+
+def run_ours(args, data, precision: str, sampler: str, with_render: bool) -> dict:
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
     from jaxngp_gb300 import _lib as L
-    from jaxngp_gb300.scene import make_scene_data
     from jaxngp_gb300.trainer import NGPTrainer, TrainConfig
 
     L.lib().ngp_kernel_launches.restype = __import__("ctypes").c_ulonglong
-    data = make_scene_data(n_views=args.views, width=args.res, height=args.res, seed=0)
-    cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=args.precision, sampler=args.sampler)
+    cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=precision, sampler=sampler)
     tr = NGPTrainer(data, cfg)
     tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
@@ -314,14 +327,14 @@ def run_ours(args) -> dict:
                 "algorithmic_flops_per_launch": units,
                 "note": "FP32 SIMT kernel measured against the BF16 tensor peak (no FP32 peak is measured)"}
 
-    render = render_fps(args, tr, stream) if args.render_frames > 0 else None
+    render = render_fps(args, tr, stream) if (with_render and args.render_frames > 0) else None
     from jaxngp_gb300.trainer import evaluate_psnr
     quality = {"psnr_heldout": round(evaluate_psnr(tr, n_views=2), 3), "views": 2, "steps_trained": tr.step_count,
                "judge": "occupancy-grid inference renderer, white background, 4096-step quadrature ground truth"}
 
     out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f32 (field MLP bf16 operands, f32 accumulation)",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == "fp32" else "f32 (field MLP bf16 operands, f32 accumulation)",
            "data": "synthetic (procedural 64-blob scene, GT by 4096-step quadrature; NeRF-synthetic not used)",
            "config": {"workload": WORKLOAD, "rays_per_step": R, "sample_budget": args.samples,
                       "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,
@@ -420,7 +433,31 @@ def main():
                "wall_s": round(time.perf_counter() - t, 2)}
         print(json.dumps(out))
         return 0
-    out = run_ours(args)
+    world, rank, _ = setup_device(args)
+    from jaxngp_gb300.scene import make_scene_data
+    data = make_scene_data(n_views=args.views, width=args.res, height=args.res, seed=0)
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    results = {}
+    for f in forms:
+        precision, sampler = FORMS[f]
+        results[f] = run_ours(args, data, precision, sampler, with_render=True)
+    head = results[forms[0]]
+    out = dict(head)
+    out["config"] = dict(head["config"], form=forms[0])
+    if len(forms) > 1:
+        out["forms"] = {f: {k: r[k] for k in ("value", "ms_per_step", "dtype", "e2e", "gpu_launches", "quality",
+                                               "roofline", "clocks")} | {
+                            "valid_rays_per_step": r["config"]["valid_rays_per_step"],
+                            "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
+                            "top_kernels": dict(list(r["kernels"].items())[:6])}
+                        for f, r in results.items()}
+        if "fp32-march" in results and "bf16-proposal" in results:
+            a, b = results["fp32-march"], results["bf16-proposal"]
+            out["learned_proposal_vs_plain"] = {
+                "train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
+                "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
+                "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3),
+                "plain": "fp32-march", "proposal": "bf16-proposal"}
     if rank == 0:
         if not args.no_cpu_baseline:
             from jaxngp_gb300.scene import BlobScene, PinholeCamera, hemisphere_poses, poses_to_transforms

@@ -436,11 +436,12 @@ int ngp_packbits_scalar_status(cudaStream_t stream, void **buffers, const char *
  * samples come from a small density network instead of the march: a 3D DDA over coarse blocks of
  * 8^3 occupancy cells gives the ray's occupied interval (no interval: a valid ray with no
  * samples), the interval is cut into NGP_PROPOSAL_BINS bins, the proposal network's log density
- * at the bin centres defines a piecewise-constant pdf (mixed with 10% of a uniform one), whose
- * inverse CDF at stratified levels cuts the interval into NGP_PROPOSAL_SAMPLES pieces, dense where
+ * at the bin centres defines a piecewise-constant pdf (mixed with a share `mix` of a uniform one), whose
+ * inverse CDF at stratified levels cuts the interval into spr pieces (samples per ray), dense where
  * the pdf is high; a sample sits at the middle of each piece and stands for it (dss = its length),
  * written in march_rays' layout so that the field, the integrator and the loss run unchanged.  Slot j of a
- * fitting ray starts at sample j * NGP_PROPOSAL_SAMPLES.  The network (4-level hash grid, MLP
+ * fitting ray starts at sample j * spr, spr = the descriptor's samples_per_ray (default
+ * NGP_PROPOSAL_SAMPLES); below, S/spr is the number of slots.  The network (4-level hash grid, MLP
  * 8 -> 64 -> 64 -> 1) regresses the field's log density at the field's samples. */
 #define NGP_PROPOSAL_BINS 64
 #define NGP_PROPOSAL_SAMPLES 48
@@ -448,7 +449,7 @@ int ngp_packbits_scalar_status(cudaStream_t stream, void **buffers, const char *
 
 typedef struct NgpProposalDescriptor {
     uint32_t n;             /* rays (proposal_rays) or points (proposal_loss) */
-    uint32_t total_samples; /* sample budget S; slots = S / NGP_PROPOSAL_SAMPLES */
+    uint32_t total_samples; /* sample budget S; slots = S / samples_per_ray */
     uint32_t G;             /* occupancy grid resolution (cascade 0; a multiple of 8) */
     float bound;
     uint32_t perturb;       /* proposal_sample: jitter the stratified draws */
@@ -456,6 +457,8 @@ typedef struct NgpProposalDescriptor {
     uint32_t count_index;   /* proposal_loss: points bounded by counts[count_index] (0 slots, 1 bins,
                                2 samples); 3 = all n points */
     uint32_t sigma_stride;  /* proposal_loss: stride of the target densities (4 for drgbs rows) */
+    uint32_t samples_per_ray; /* samples of a ray with an interval, 1..1024; 0 = NGP_PROPOSAL_SAMPLES */
+    float mix;              /* proposal_sample: share of a uniform pdf mixed into the proposal's */
 } NgpProposalDescriptor;
 
 /* buffers: occupancy_bitfield u8[G^3/8] -> coarse u8[(G/8)^3]. */
@@ -464,16 +467,16 @@ int ngp_proposal_coarse_status(cudaStream_t stream, void **buffers, const char *
 
 /* buffers: rays_o f32[R,3], rays_d f32[R,3], t_starts f32[R], t_ends f32[R], coarse u8[(G/8)^3]
  * -> next_sample_write_location u32[1], number_of_exceeded_samples u32[1], ray_is_valid bool[R],
- * rays_n_samples u32[R], rays_sample_startidx u32[R], ray_of_slot u32[S/48], slot_t_start f32[S/48],
- * slot_t_end f32[S/48], counts u32[3] (slots, bin points, samples). */
+ * rays_n_samples u32[R], rays_sample_startidx u32[R], ray_of_slot u32[S/spr], slot_t_start f32[S/spr],
+ * slot_t_end f32[S/spr], counts u32[3] (slots, bin points, samples). */
 void ngp_proposal_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
-/* buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_t_start, slot_t_end -> points f32[S/48*64,3]. */
+/* buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_t_start, slot_t_end -> points f32[S/spr*64,3]. */
 void ngp_proposal_bin_points(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_bin_points_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
-/* buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_t_start, slot_t_end, x_bins f32[S/48*64]
+/* buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_t_start, slot_t_end, x_bins f32[S/spr*64]
  * -> idcs u32[S], xyzs f32[S,3], dirs f32[S,3], dss f32[S], z_vals f32[S]. */
 void ngp_proposal_sample(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_sample_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);

@@ -94,7 +94,8 @@ class NgpAdamDescriptor(_Desc):
 
 class NgpProposalDescriptor(_Desc):
     _fields_ = [("n", c_u32), ("total_samples", c_u32), ("G", c_u32), ("bound", c_f32), ("perturb", c_u32),
-                ("seed_lo", c_u32), ("seed_hi", c_u32), ("count_index", c_u32), ("sigma_stride", c_u32)]
+                ("seed_lo", c_u32), ("seed_hi", c_u32), ("count_index", c_u32), ("sigma_stride", c_u32),
+                ("samples_per_ray", c_u32), ("mix", c_f32)]
 
 
 class NgpOgridDescriptor(_Desc):

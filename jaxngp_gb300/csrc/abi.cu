@@ -54,12 +54,14 @@ int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *,
                              const float *, const float *, const float *, float *, float *, unsigned *);
 int device_status();
 int launch_proposal_coarse(cudaStream_t, std::uint32_t, const std::uint8_t *, std::uint8_t *);
-int launch_proposal_rays(cudaStream_t, std::uint32_t, std::uint32_t, std::uint32_t, float, const float *, const float *,
+int launch_proposal_rays(cudaStream_t, std::uint32_t, std::uint32_t, std::uint32_t, std::uint32_t, float, const float *,
+                         const float *,
                          const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *, bool *,
                          std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, std::uint32_t *);
 int launch_proposal_bin_points(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                                const std::uint32_t *, const float *, const float *, float *);
-int launch_proposal_sample(cudaStream_t, std::uint32_t, const std::uint32_t *, bool, std::uint64_t, const float *,
+int launch_proposal_sample(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t, float, bool, std::uint64_t,
+                           const float *,
                            const float *, const std::uint32_t *, const float *, const float *, const float *,
                            std::uint32_t *, float *, float *, float *, float *);
 int launch_proposal_loss(cudaStream_t, std::uint32_t, const std::uint32_t *, int, const float *, const float *, int,
@@ -366,22 +368,28 @@ NGP_ENTRY(ngp_proposal_coarse) {
     return launch_proposal_coarse(stream, d.G, CU8(0), U8(1));
 }
 
+static std::uint32_t proposal_spr(const NgpProposalDescriptor &d) {
+    return d.samples_per_ray != 0 ? d.samples_per_ray : (std::uint32_t)NGP_PROPOSAL_SAMPLES;
+}
+
 NGP_ENTRY(ngp_proposal_rays) {
     NGP_DESC(NgpProposalDescriptor, d);
-    return launch_proposal_rays(stream, d.n, d.total_samples, d.G, d.bound, CF32(0), CF32(1), CF32(2), CF32(3), CU8(4),
+    return launch_proposal_rays(stream, d.n, d.total_samples, proposal_spr(d), d.G, d.bound, CF32(0), CF32(1), CF32(2), CF32(3), CU8(4),
                                 U32(5), U32(6), B8(7), U32(8), U32(9), U32(10), F32(11), F32(12), U32(13));
 }
 
 NGP_ENTRY(ngp_proposal_bin_points) {
     NGP_DESC(NgpProposalDescriptor, d);
-    return launch_proposal_bin_points(stream, d.total_samples / NGP_PROPOSAL_SAMPLES, CU32(0), CF32(1), CF32(2), CU32(3),
+    return launch_proposal_bin_points(stream, d.total_samples / proposal_spr(d), CU32(0), CF32(1), CF32(2), CU32(3),
                                       CF32(4), CF32(5), F32(6));
 }
 
 NGP_ENTRY(ngp_proposal_sample) {
     NGP_DESC(NgpProposalDescriptor, d);
     const std::uint64_t seed = ((std::uint64_t)d.seed_hi << 32) | d.seed_lo;
-    return launch_proposal_sample(stream, d.total_samples / NGP_PROPOSAL_SAMPLES, CU32(0), d.perturb != 0, seed, CF32(1),
+    return launch_proposal_sample(stream, d.total_samples / proposal_spr(d), CU32(0), proposal_spr(d), d.mix, d.perturb != 0,
+                                  seed,
+                                  CF32(1),
                                   CF32(2), CU32(3), CF32(4), CF32(5), CF32(6), U32(7), F32(8), F32(9), F32(10), F32(11));
 }
 

@@ -19,8 +19,8 @@
 namespace ngp {
 namespace {
 
-constexpr int kBins = 64, kSamples = 48;
-constexpr float kMix = 0.1f, kEps = 1e-3f, kUnder = 2.0f;
+constexpr int kBins = 64;
+constexpr float kEps = 1e-3f, kUnder = 2.0f;
 
 __device__ __forceinline__ std::uint32_t expand_bits(std::uint32_t v) {
     v = (v * 0x00010001u) & 0xFF0000FFu;
@@ -101,10 +101,10 @@ __device__ __forceinline__ bool ray_interval(float ox, float oy, float oz, float
     return hit;
 }
 
-// Step 1-2: interval, slot allocation.  Slot j = startidx / kSamples of a fitting ray records the
+// Step 1-2: interval, slot allocation.  Slot j = startidx / spr of a fitting ray records the
 // ray (ray_of_slot) and its interval (slot_ta, slot_tb).
 __global__ void __launch_bounds__(256) proposal_rays_kernel(
-    std::uint32_t n_rays, std::uint32_t total_samples, int Gc, float mb, const float *__restrict__ rays_o,
+    std::uint32_t n_rays, std::uint32_t total_samples, std::uint32_t spr, int Gc, float mb, const float *__restrict__ rays_o,
     const float *__restrict__ rays_d, const float *__restrict__ t_starts, const float *__restrict__ t_ends,
     const std::uint8_t *__restrict__ coarse, std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded,
     bool *__restrict__ ray_is_valid, std::uint32_t *__restrict__ rays_n_samples,
@@ -119,16 +119,16 @@ __global__ void __launch_bounds__(256) proposal_rays_kernel(
                            rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2],
                            t_starts[r], t_ends[r], coarse, Gc, mb, ta, tb);
     hit = hit && tb > ta;
-    const std::uint32_t need = hit ? (std::uint32_t)kSamples : 0u;
+    const std::uint32_t need = hit ? spr : 0u;
     const std::uint32_t incl = warp_inclusive_scan(need);
     const std::uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     std::uint32_t base = 0;
     if (lane_id() == 31 && total > 0) base = atomicAdd(next_loc, total);
     base = __shfl_sync(0xffffffffu, base, 31);
     const std::uint32_t start = base + incl - need;
-    const bool fits = hit && (std::uint64_t)start + kSamples <= total_samples;
+    const bool fits = hit && (std::uint64_t)start + spr <= total_samples;
     const unsigned over = __ballot_sync(0xffffffffu, hit && !fits);
-    if (lane_id() == 0 && over != 0u) atomicAdd(n_exceeded, (std::uint32_t)__popc(over) * kSamples);
+    if (lane_id() == 0 && over != 0u) atomicAdd(n_exceeded, (std::uint32_t)__popc(over) * spr);
     if (!in) return;
     if (!hit) {
         ray_is_valid[r] = true;
@@ -137,10 +137,10 @@ __global__ void __launch_bounds__(256) proposal_rays_kernel(
         return;
     }
     ray_is_valid[r] = fits;
-    rays_n_samples[r] = fits ? (std::uint32_t)kSamples : 0u;
+    rays_n_samples[r] = fits ? spr : 0u;
     rays_startidx[r] = fits ? start : 0u;
     if (fits) {
-        const std::uint32_t j = start / kSamples;
+        const std::uint32_t j = start / spr;
         ray_of_slot[j] = r;
         slot_ta[j] = ta;
         slot_tb[j] = tb;
@@ -148,12 +148,12 @@ __global__ void __launch_bounds__(256) proposal_rays_kernel(
 }
 
 // counts[0] = slots (fitting rays), counts[1] = bin points, counts[2] = samples.
-__global__ void proposal_counts_kernel(std::uint32_t total_samples, const std::uint32_t *__restrict__ next_loc,
-                                       std::uint32_t *__restrict__ counts) {
-    const std::uint32_t slots = min(*next_loc / kSamples, total_samples / kSamples);
+__global__ void proposal_counts_kernel(std::uint32_t total_samples, std::uint32_t spr,
+                                       const std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ counts) {
+    const std::uint32_t slots = min(*next_loc / spr, total_samples / spr);
     counts[0] = slots;
     counts[1] = slots * kBins;
-    counts[2] = slots * kSamples;
+    counts[2] = slots * spr;
 }
 
 // Step 3a: bin centres of every slot's interval.
@@ -181,9 +181,10 @@ __device__ __forceinline__ std::uint64_t splitmix(std::uint64_t x) {
     return x ^ (x >> 31);
 }
 
-// Step 3c: one thread per slot turns the bins' log densities into kSamples samples.
+// Step 3c: one thread per slot turns the bins' log densities into spr samples.
 __global__ void __launch_bounds__(128) proposal_sample_kernel(
-    const std::uint32_t *__restrict__ counts, int perturb, std::uint64_t seed, const float *__restrict__ rays_o,
+    const std::uint32_t *__restrict__ counts, std::uint32_t spr, float mix, int perturb, std::uint64_t seed,
+    const float *__restrict__ rays_o,
     const float *__restrict__ rays_d, const std::uint32_t *__restrict__ ray_of_slot, const float *__restrict__ slot_ta,
     const float *__restrict__ slot_tb, const float *__restrict__ x_bins, std::uint32_t *__restrict__ idcs,
     float *__restrict__ xyzs, float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals) {
@@ -208,23 +209,23 @@ __global__ void __launch_bounds__(128) proposal_sample_kernel(
 #pragma unroll 8
     for (int i = 0; i < kBins; ++i) {
         const float wi = W > 0.f ? w[i] / W : 1.0f / (float)kBins;
-        w[i] = (1.0f - kMix) * wi + kMix / (float)kBins;
+        w[i] = (1.0f - mix) * wi + mix / (float)kBins;
     }
     const float o[3] = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
     const float d[3] = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
-    const std::size_t s0 = (std::size_t)j * kSamples;
-    // inverse-CDF edges e_0 = t_a, e_k (0 < k < kSamples), e_kSamples = t_b; sample k at the
+    const std::size_t s0 = (std::size_t)j * spr;
+    // inverse-CDF edges e_0 = t_a, e_k (0 < k < spr), e_spr = t_b; sample k at the
     // midpoint of [e_k, e_k+1], standing for that interval
     int b = 0;
     float c_lo = 0.f, c_hi = w[0], e_prev = ta;
-    for (int k = 1; k <= kSamples; ++k) {
+    for (int k = 1; k <= (int)spr; ++k) {
         float e = tb;
-        if (k < kSamples) {
+        if (k < (int)spr) {
             float xi = 0.5f;
             if (perturb)
-                xi = (float)(splitmix(seed ^ ((std::uint64_t)r * kSamples + (std::uint64_t)k) * 0x2545F4914F6CDD1Dull) >> 40) *
+                xi = (float)(splitmix(seed ^ ((std::uint64_t)r * spr + (std::uint64_t)k) * 0x2545F4914F6CDD1Dull) >> 40) *
                      (1.0f / 16777216.0f);
-            const float u = (((float)k - 0.5f) + xi) / (float)kSamples;
+            const float u = (((float)k - 0.5f) + xi) / (float)spr;
             while (u >= c_hi && b < kBins - 1) {
                 ++b;
                 c_lo = c_hi;
@@ -283,22 +284,24 @@ int launch_proposal_coarse(cudaStream_t stream, std::uint32_t G, const std::uint
     return launch_status();
 }
 
-int launch_proposal_rays(cudaStream_t stream, std::uint32_t n_rays, std::uint32_t total_samples, std::uint32_t G,
+int launch_proposal_rays(cudaStream_t stream, std::uint32_t n_rays, std::uint32_t total_samples, std::uint32_t spr,
+                         std::uint32_t G,
                          float bound, const float *rays_o, const float *rays_d, const float *t_starts,
                          const float *t_ends, const std::uint8_t *coarse, std::uint32_t *next_loc,
                          std::uint32_t *n_exceeded, bool *valid, std::uint32_t *n_samples, std::uint32_t *startidx,
                          std::uint32_t *ray_of_slot, float *slot_ta, float *slot_tb, std::uint32_t *counts) {
     NGP_CHECK_ARG(G >= 8 && G % 8 == 0 && G <= 1024, "proposal: G must be a multiple of 8 in [8, 1024]");
     NGP_CHECK_ARG(bound > 0.f, "proposal: bound must be positive");
+    NGP_CHECK_ARG(spr >= 1 && spr <= 1024, "proposal: samples_per_ray must be in [1, 1024]");
     NGP_CUDA_TRY(cudaMemsetAsync(next_loc, 0, sizeof(std::uint32_t), stream));
     NGP_CUDA_TRY(cudaMemsetAsync(n_exceeded, 0, sizeof(std::uint32_t), stream));
     if (n_rays > 0) {
         proposal_rays_kernel<<<(n_rays + 255) / 256, 256, 0, stream>>>(
-            n_rays, total_samples, (int)(G / 8), fminf(1.0f, bound), rays_o, rays_d, t_starts, t_ends, coarse, next_loc,
+            n_rays, total_samples, spr, (int)(G / 8), fminf(1.0f, bound), rays_o, rays_d, t_starts, t_ends, coarse, next_loc,
             n_exceeded, valid, n_samples, startidx, ray_of_slot, slot_ta, slot_tb);
         count_launches(1);
     }
-    proposal_counts_kernel<<<1, 1, 0, stream>>>(total_samples, next_loc, counts);
+    proposal_counts_kernel<<<1, 1, 0, stream>>>(total_samples, spr, next_loc, counts);
     count_launches(1);
     return launch_status();
 }
@@ -314,14 +317,16 @@ int launch_proposal_bin_points(cudaStream_t stream, std::uint32_t max_slots, con
     return launch_status();
 }
 
-int launch_proposal_sample(cudaStream_t stream, std::uint32_t max_slots, const std::uint32_t *counts, bool perturb,
+int launch_proposal_sample(cudaStream_t stream, std::uint32_t max_slots, const std::uint32_t *counts, std::uint32_t spr,
+                           float mix, bool perturb,
                            std::uint64_t seed, const float *rays_o, const float *rays_d,
                            const std::uint32_t *ray_of_slot, const float *slot_ta, const float *slot_tb,
                            const float *x_bins, std::uint32_t *idcs, float *xyzs, float *dirs, float *dss,
                            float *z_vals) {
+    NGP_CHECK_ARG(mix >= 0.f && mix <= 1.f, "proposal: mix must be in [0, 1]");
     if (max_slots > 0) {
         proposal_sample_kernel<<<(max_slots + 127) / 128, 128, 0, stream>>>(
-            counts, perturb ? 1 : 0, seed, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, idcs, xyzs, dirs, dss,
+            counts, spr, mix, perturb ? 1 : 0, seed, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, idcs, xyzs, dirs, dss,
             z_vals);
         count_launches(1);
     }

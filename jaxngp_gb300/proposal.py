@@ -4,12 +4,17 @@ models/renderers/cuda.py:100-162); the kernels are ngp_proposal_* in include/ngp
 
 Per training step:
   rays      -> ngp_proposal_rays: coarse-block DDA (occupied interval, or an empty valid ray) and
-               NGP_PROPOSAL_SAMPLES sample slots per fitting ray
+               samples_per_ray (48 by default) sample slots per fitting ray
   bins      -> ngp_proposal_bin_points, the proposal field (4-level hash grid + MLP) at the bin
                centres, ngp_proposal_sample: inverse-CDF samples in march_rays' layout
   field     -> unchanged (encoder, MLP, fused integrator/loss, backwards, Adam)
   proposal  -> regresses the field's log density at the field's samples and at points drawn in
                occupied cells (ngp_proposal_loss), its own backward and Adam
+
+Every k-th training step (TrainConfig.march_every, 8 by default) marches the occupancy grid instead
+-- the sampler's fallback: its evenly spread samples train the field's empty space, which the
+proposal's concentrated samples rarely visit, and teach the proposal where its density is wrong.
+Without it the field keeps density the occupancy-grid renderer (the judge) then shows.
 
 Everything stays on the device; the sample count of a step is read by the kernels from `counts`.
 """
@@ -37,11 +42,15 @@ def proposal_table() -> LevelTable:
 
 class ProposalSampler:
     def __init__(self, n_rays: int, total_samples: int, G: int, bound: float, device="cuda", seed: int = 0,
-                 lr: float = 1e-2, distill_points: int = 1 << 14):
+                 lr: float = 1e-2, distill_points: int = 1 << 14, samples_per_ray: int = SAMPLES, mix: float = 0.1):
         if G % 8 != 0:
             raise ValueError("the proposal sampler needs an occupancy grid resolution divisible by 8")
         self.R, self.S, self.G, self.bound = n_rays, total_samples, G, float(bound)
-        self.slots = total_samples // SAMPLES
+        self.spr = int(samples_per_ray)
+        if not 1 <= self.spr <= 1024:
+            raise ValueError("samples_per_ray must be in [1, 1024]")
+        self.slots = total_samples // self.spr
+        self.mix = float(mix)
         self.dev = torch.device(device)
         self.table = proposal_table()
         self.lr = lr
@@ -84,7 +93,7 @@ class ProposalSampler:
 
     def _desc(self, n=0, perturb=False, seed=0, count_index=3, sigma_stride=1) -> L.NgpProposalDescriptor:
         return L.NgpProposalDescriptor(n, self.S, self.G, self.bound, int(perturb), seed & 0xFFFFFFFF,
-                                       (seed >> 32) & 0xFFFFFFFF, count_index, sigma_stride)
+                                       (seed >> 32) & 0xFFFFFFFF, count_index, sigma_stride, self.spr, self.mix)
 
     # ----------------------------------------------------------------------------- sampling
     def refresh(self, bitfield: torch.Tensor):
@@ -111,15 +120,18 @@ class ProposalSampler:
         return self.counts[2:3]
 
     # ----------------------------------------------------------------------------- training
-    def train(self, xyzs: torch.Tensor, drgbs: torch.Tensor, distill: Optional[Callable] = None, lr: Optional[float] = None):
-        """One proposal update from the field's densities at its samples (drgbs[:, 0]), plus, when
+    def train(self, xyzs: torch.Tensor, drgbs: torch.Tensor, distill: Optional[Callable] = None, lr: Optional[float] = None,
+              count: Optional[torch.Tensor] = None, max_points: Optional[int] = None):
+        """One proposal update from the field's densities at a step's samples (drgbs[:, 0]; the
+        first `count` of them, by default this sampler's own, at most `max_points` -- samples sit
+        in allocation order, so the first ones are a spread of rays), plus, when
         `distill(xyz, sigma)` is given, at points drawn in occupied cells."""
-        S = xyzs.shape[0]
-        cnt = self.counts[2:3]
+        S = xyzs.shape[0] if max_points is None else min(xyzs.shape[0], max_points)
+        cnt = self.counts[2:3] if count is None else count
         self.loss.zero_()
         self.network(xyzs, self.enc_t[:S], self.x_t[:S], cnt)
-        L.call("ngp_proposal_loss", [self.counts, self.x_t[:S], drgbs, self.g_x[:S], self.loss[0:1]],
-               self._desc(S, count_index=2, sigma_stride=4))
+        L.call("ngp_proposal_loss", [cnt, self.x_t[:S], drgbs, self.g_x[:S], self.loss[0:1]],
+               self._desc(S, count_index=0, sigma_stride=4))
         L.call("ngp_proposal_mlp_backward", [self.enc_t[:S], self.weights, self.g_x[:S], cnt, self.scratch,
                                              self.g_enc[:S], self.g_w], L.NgpMlpDescriptor(S, 0))
         L.call("ngp_hashgrid_backward", [xyzs, self.g_enc[:S], cnt, self.g_lat], self.table.descriptor(S, self.bound))

@@ -51,6 +51,10 @@ class TrainConfig:
     sampler: str = "march"             # "march" (occupancy grid, the reference's) or "proposal"
     proposal_every: int = 4            # proposal updates every k steps
     proposal_distill: bool = True      # also regress the proposal at points drawn in occupied cells
+    proposal_samples: int = 48         # samples on each ray the proposal samples
+    proposal_mix: float = 0.1          # share of a uniform pdf mixed into the proposal's
+    march_every: int = 8               # proposal sampler: every k-th step marches the occupancy grid (0: never)
+    proposal_train_points: int = 1 << 16   # field samples a proposal update regresses on (at most)
 
 
 def cascades_for(bound: float) -> int:
@@ -147,7 +151,8 @@ class NGPTrainer:
             from .proposal import ProposalSampler
             if self.K != 1:
                 raise ValueError("the proposal sampler supports scenes with one occupancy cascade (bound <= 1)")
-            self.prop = ProposalSampler(R, S, cfg.G, bound, self.dev, seed=cfg.seed)
+            self.prop = ProposalSampler(R, S, cfg.G, bound, self.dev, seed=cfg.seed, samples_per_ray=cfg.proposal_samples,
+                                        mix=cfg.proposal_mix)
             self.enc_d = torch.empty(self.prop.M, 32, **f32)
         elif cfg.sampler != "march":
             raise ValueError(f"sampler must be 'march' or 'proposal', got {cfg.sampler!r}")
@@ -261,7 +266,8 @@ class NGPTrainer:
                                           self.bound, int(cfg.perturb), int(cfg.random_bg), (L.c_f32 * 3)(1, 1, 1), seed)
         L.call("ngp_train_rays", [self.data.transforms, self.data.rgbas, perm, self.rays_o, self.rays_d, self.t0,
                                   self.t1, self.noise, self.bgs, self.gt], d_rays)
-        if self.prop is None:
+        use_march = self.prop is None or (cfg.march_every > 0 and self.step_count % cfg.march_every == cfg.march_every - 1)
+        if use_march:
             L.call("ngp_march_rays_train", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
                                             self.counters[0:1], self.counters[1:2], self.valid, self.n_samples,
                                             self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals,
@@ -274,8 +280,10 @@ class NGPTrainer:
                                    seed ^ 0x5BD1E9955BD1E995)
         L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, cnt, self.enc], self._d_hg)
         L.call(self._mlp("ngp_field_forward"), [self.enc, self.dirs, self.weights, cnt, self.drgbs], self._d_mlp)
-        if self.prop is not None and self.step_count % cfg.proposal_every == 0:
-            self.prop.train(self.xyzs, self.drgbs, self._distill if cfg.proposal_distill else None)
+        if self.prop is not None and (use_march or self.step_count % cfg.proposal_every == 0):
+            # march steps teach the proposal at the march's evenly spread samples
+            self.prop.train(self.xyzs, self.drgbs, self._distill if cfg.proposal_distill else None, count=cnt,
+                            max_points=cfg.proposal_train_points)
         L.call("ngp_integrate_loss_backward", [self.valid, self.startidx, self.n_samples, self.bgs, self.gt, self.dss,
                                                self.z_vals, self.drgbs, cnt, self.loss_scratch, self.g_drgbs,
                                                self.stats, self.grad_scale], self._d_loss)

@@ -193,8 +193,8 @@ def bin_points(o, d, ta, tb):
     return (o[None, :] + c[:, None] * d[None, :]).astype(f), delta
 
 
-def sample_ray(x_bins: np.ndarray, ta: float, tb: float, xi: np.ndarray):
-    """Returns (t [N_SAMPLES], ds [N_SAMPLES]) for one ray."""
+def sample_ray(x_bins: np.ndarray, ta: float, tb: float, xi: np.ndarray, n_samples: int = N_SAMPLES, mix=MIX):
+    """Returns (t [n_samples], ds [n_samples]) for one ray; xi[k] jitters edge k (0 < k < n_samples)."""
     f = np.float32
     ta, tb = f(ta), f(tb)
     delta = (tb - ta) / f(N_BINS)
@@ -211,12 +211,12 @@ def sample_ray(x_bins: np.ndarray, ta: float, tb: float, xi: np.ndarray):
     p = np.empty(N_BINS, f)
     for i in range(N_BINS):
         wi = (w[i] / W) if W > 0 else f(1) / f(N_BINS)
-        p[i] = (f(1) - MIX) * wi + MIX / f(N_BINS)
-    e = np.empty(N_SAMPLES + 1, f)
-    e[0], e[N_SAMPLES] = ta, tb
+        p[i] = (f(1) - f(mix)) * wi + f(mix) / f(N_BINS)
+    e = np.empty(n_samples + 1, f)
+    e[0], e[n_samples] = ta, tb
     b, c_lo, c_hi = 0, f(0), p[0]
-    for k in range(1, N_SAMPLES):
-        u = (f(k) - f(0.5) + f(xi[k])) / f(N_SAMPLES)
+    for k in range(1, n_samples):
+        u = (f(k) - f(0.5) + f(xi[k])) / f(n_samples)
         while u >= c_hi and b < N_BINS - 1:
             b += 1
             c_lo = c_hi

@@ -22,9 +22,9 @@ def cu(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def desc(n=0, S=48 * 64, G=128, bound=1.0, perturb=0, seed=0, count_index=3, stride=1):
+def desc(n=0, S=48 * 64, G=128, bound=1.0, perturb=0, seed=0, count_index=3, stride=1, spr=0, mix=0.1):
     from jaxngp_gb300 import _lib as L
-    return L.NgpProposalDescriptor(n, S, G, bound, perturb, seed & 0xFFFFFFFF, seed >> 32, count_index, stride)
+    return L.NgpProposalDescriptor(n, S, G, bound, perturb, seed & 0xFFFFFFFF, seed >> 32, count_index, stride, spr, mix)
 
 
 @pytest.fixture(scope="module")
@@ -77,15 +77,16 @@ def test_intervals_and_allocation(grid):
         assert ta[j] == ref[r][1] and tb[j] == ref[r][2]
 
 
-def test_bins_network_and_samples(grid):
+@pytest.mark.parametrize("spr", [48, 20])
+def test_bins_network_and_samples(grid, spr):
     """Bin points bit-exact; proposal MLP against FP64; samples against the oracle."""
     from jaxngp_gb300 import _lib as L
     from jaxngp_gb300.proposal import ProposalSampler
     G, bits, coarse = grid
     rng = np.random.default_rng(4)
     o, d, t0, t1 = make_rays(rng, 3000, 1.0)
-    S = 48 * 512
-    ps = ProposalSampler(3000, S, G, 1.0, seed=5)
+    S = spr * 512
+    ps = ProposalSampler(3000, S, G, 1.0, seed=5, samples_per_ray=spr)
     with torch.no_grad():
         ps.latents.uniform_(-1, 1)
     ps.refresh(cu(bits))
@@ -98,7 +99,7 @@ def test_bins_network_and_samples(grid):
     dss, zs = torch.zeros(S, device="cuda"), torch.zeros(S, device="cuda")
     cnt = ps.sample(cu(o), cu(d), cu(t0), cu(t1), valid, ns, st, idcs, xyzs, dirs, dss, zs, False, 0)
     n_slots = int(ps.counts[0])
-    assert int(cnt) == 48 * n_slots and n_slots == 512
+    assert int(cnt) == spr * n_slots and n_slots == 512
     ros, ta, tb = ps.ray_of_slot.cpu().numpy(), ps.slot_ta.cpu().numpy(), ps.slot_tb.cpu().numpy()
     pts = ps.points.cpu().numpy()
     for j in range(0, n_slots, 37):
@@ -118,13 +119,13 @@ def test_bins_network_and_samples(grid):
     X, Ds, Zs, Dr = xyzs.cpu().numpy(), dss.cpu().numpy(), zs.cpu().numpy(), dirs.cpu().numpy()
     for j in range(0, n_slots, 29):
         r = ros[j]
-        t, ds = P.sample_ray(xg[j * 64:(j + 1) * 64], ta[j], tb[j], np.full(48, 0.5, np.float32))
-        s = slice(j * 48, (j + 1) * 48)
+        t, ds = P.sample_ray(xg[j * 64:(j + 1) * 64], ta[j], tb[j], np.full(spr, 0.5, np.float32), spr)
+        s = slice(j * spr, (j + 1) * spr)
         scale = max(1.0, abs(float(tb[j])))
         assert np.abs(Zs[s] - t).max() <= 1e-5 * scale
         assert np.abs(Ds[s] - ds).max() <= 2e-5 * scale
         assert np.allclose(X[s], o[r][None] + Zs[s][:, None] * d[r][None], rtol=0, atol=1e-6)
-        assert np.array_equal(Dr[s], np.repeat(d[r][None], 48, 0))
+        assert np.array_equal(Dr[s], np.repeat(d[r][None], spr, 0))
         assert (np.diff(Zs[s]) >= 0).all() and Zs[s][0] >= ta[j] and Zs[s][-1] <= tb[j]
         assert (idcs.cpu().numpy()[s] == r).all()
 
@@ -218,9 +219,10 @@ def trained_pair():
 
 
 def test_proposal_training_matches_march_quality(trained_pair):
-    """Both samplers train; at equal steps the proposal's held-out PSNR (judged by the same
-    occupancy-grid renderer) is within 0.5 dB of the march's or better, with its fixed 48 samples
-    on each ray that carries samples."""
+    """Both samplers train; at equal steps the proposal sampler's held-out PSNR (judged by the
+    same occupancy-grid renderer) is within 0.1 dB of the march's or better.  The proposal runs
+    with its default fallback, a march step every 8th step whose evenly spread samples also teach
+    the proposal; proposal steps put 48 samples on each ray that carries samples."""
     from jaxngp_gb300.trainer import evaluate_psnr
     data, out = trained_pair
     psnr = {}
@@ -228,9 +230,10 @@ def test_proposal_training_matches_march_quality(trained_pair):
         assert np.isfinite(losses).all()
         assert np.mean(losses[-5:]) < 0.5 * losses[0], (sampler, losses)
         psnr[sampler] = evaluate_psnr(tr, n_views=2)
-    assert psnr["proposal"] >= psnr["march"] - 0.5, psnr
-    assert np.mean(out["proposal"][2][-5:]) == 48.0
-    assert np.mean(out["march"][2][-5:]) > 0
+    assert psnr["proposal"] >= psnr["march"] - 0.1, psnr
+    tr = out["proposal"][0]
+    assert tr.cfg.march_every == 8
+    assert out["proposal"][2][-1] == 48.0   # step 499 is a proposal step
 
 
 def test_proposal_samples_place_like_dense(trained_pair):
