@@ -171,22 +171,32 @@ ALGO = {}
 
 def algorithmic(name: str, R: int, S: int, P: int, G: int) -> tuple:
     """Algorithmic bytes (or FLOPs) of one launch of each entry point (minimum DRAM traffic: every
-    input read once, every output written once)."""
-    if name == "march_rays":
+    input read once, every output written once).  P = hash-table rows (2 floats each)."""
+    slots = S // 48
+    if name in ("march_rays", "ngp_march_rays_train"):
         return ("hbm", 45 * R + 36 * S + G ** 3 // 8)
     if name == "ngp_hashgrid_forward":
         return ("hbm", S * (12 + 128) + 8 * P)
     if name == "ngp_hashgrid_backward":
         return ("hbm", S * (12 + 128) + 2 * 8 * P)
-    if name == "ngp_field_forward":
+    if name in ("ngp_field_forward", "ngp_field_forward_bf16"):
         return ("flop", 18816 * S)
-    if name == "ngp_field_backward":
+    if name in ("ngp_field_backward", "ngp_field_backward_bf16"):
         return ("flop", 3 * 18816 * S)
     if name == "ngp_integrate_loss_backward":
         return ("hbm", R * 33 + S * 40)
-    if name == "ngp_adam":
-        return ("hbm", 7 * 4 * (2 * P + 9408))
+    if name == "ngp_adam":   # the table's and the MLP's launches alternate: their mean
+        return ("hbm", 7 * 4 * (2 * P + 9408) // 2)
+    if name == "ngp_proposal_mlp_forward":   # the bins of a step: 8 -> 64 -> 64 -> 1
+        return ("flop", 2 * 4672 * slots * 64)
+    if name == "ngp_proposal_sample":        # 64 bin values + ray + interval in, 48 samples out
+        return ("hbm", slots * (64 * 4 + 24 + 8 + 48 * 36))
+    if name == "ngp_proposal_rays":
+        return ("hbm", R * (32 + 9) + slots * 12 + (G // 8) ** 3)
     return ("hbm", 0)
+
+
+FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # SMs x FP32 lanes x FMA x max clock
 
 
 def setup_device(args):
@@ -325,7 +335,11 @@ def run_ours(args, data, precision: str, sampler: str, with_render: bool) -> dic
         roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic, "kernel": top,
                 "algorithmic_flops_per_launch": units,
-                "note": "FP32 SIMT kernel measured against the BF16 tensor peak (no FP32 peak is measured)"}
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if "bf16_tflops_sustained" in peaks
+                               else "fallback 1700 TFLOP/s"}
+        if precision == "fp32" and top in ("ngp_field_backward", "ngp_field_forward"):
+            roof["note"] = "FP32 SIMT kernel: no FP32 peak is measured; frac_of_fp32_simt_nominal uses 152 SMs x 128 lanes x 2 x 2.07 GHz"
+            roof["frac_of_fp32_simt_nominal"] = round(achieved / FP32_SIMT_NOMINAL_TFLOPS, 4)
 
     render = render_fps(args, tr, stream) if (with_render and args.render_frames > 0) else None
     from jaxngp_gb300.trainer import evaluate_psnr
