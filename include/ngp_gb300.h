@@ -191,6 +191,17 @@ int integrate_rays_status(cudaStream_t stream, void **buffers, const char *opaqu
 void integrate_rays_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int integrate_rays_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* The exact adjoint of integrate_rays as computed (no reference counterpart; the reference's
+ * integrate_rays_backward scales density gradients by min(z^2, 1), adds a near-plane penalty,
+ * counts the background twice in the density gradient of a ray that reaches it, and does not
+ * differentiate the opacity normalisation of a terminated ray).  With out the ray's colour or
+ * depth, cur_k the sum of its first k+1 weighted samples and norm = 1 (ray reaches the
+ * background) or its opacity (terminated ray): d out/d sigma_k = dt_k (T_{k+1} c_k - (out -
+ * cur_k)) / norm, d out/d c_k = w_k / norm, d out/d z_k = w_k / norm (depth), d out/d bg = T_N.
+ * Same buffers and descriptor as integrate_rays_backward (near_distance unused). */
+void ngp_integrate_rays_backward_exact(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_integrate_rays_backward_exact_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* Replaces volrendjax::integrate_rays_inference (volrend.h:170-175; integrating.cu:530-537).
  * buffers: rays_bg f32[N,3], rays_rgbd f32[N,4], rays_T f32[N], n_samples u32[n],
  * indices u32[n], dss f32[n,cap], z_vals f32[n,cap], drgbs f32[n,cap,4] -> terminate_cnt u32[1],

@@ -30,7 +30,7 @@ int launch_integrate_rays(cudaStream_t, const IntegratingDescriptor &, const std
                           const float *, const float *, const float *, const float *, std::uint32_t *, float *, float *);
 int launch_integrate_rays_backward(cudaStream_t, const IntegratingBackwardDescriptor &, const std::uint32_t *,
                                    const std::uint32_t *, const float *, const float *, const float *, const float *,
-                                   const float *, const float *, const float *, float *, float *, float *);
+                                   const float *, const float *, const float *, float *, float *, float *, bool);
 int launch_integrate_rays_inference(cudaStream_t, const IntegratingInferenceDescriptor &, const float *, const float *,
                                     const float *, const std::uint32_t *, const std::uint32_t *, const float *,
                                     const float *, const float *, std::uint32_t *, bool *, float *, float *);
@@ -237,7 +237,15 @@ NGP_ENTRY(integrate_rays_backward) {
     NGP_CHECK_ARG(!misaligned16(buffers[5]) && !misaligned16(buffers[6]) && !misaligned16(buffers[8]) && !misaligned16(buffers[11]),
                   "integrate_rays_backward: drgbs, final_rgbds, dL_dfinal_rgbds and dL_ddrgbs must be 16-byte aligned");
     return launch_integrate_rays_backward(stream, d, CU32(0), CU32(1), CF32(2), CF32(3), CF32(4), CF32(5), CF32(6),
-                                          CF32(7), CF32(8), F32(9), F32(10), F32(11));
+                                          CF32(7), CF32(8), F32(9), F32(10), F32(11), false);
+}
+
+NGP_ENTRY(ngp_integrate_rays_backward_exact) {
+    NGP_DESC(IntegratingBackwardDescriptor, d);
+    NGP_CHECK_ARG(!misaligned16(buffers[5]) && !misaligned16(buffers[6]) && !misaligned16(buffers[8]) && !misaligned16(buffers[11]),
+                  "integrate_rays_backward_exact: drgbs, final_rgbds, dL_dfinal_rgbds and dL_ddrgbs must be 16-byte aligned");
+    return launch_integrate_rays_backward(stream, d, CU32(0), CU32(1), CF32(2), CF32(3), CF32(4), CF32(5), CF32(6),
+                                          CF32(7), CF32(8), F32(9), F32(10), F32(11), true);
 }
 
 NGP_ENTRY(integrate_rays_inference) {

@@ -15,7 +15,8 @@
 //   index  = x + y*res + z*res^2           (dense levels)   encoders.py:134-155
 //          = x ^ y*2654435761 ^ z*805459861 (hashed levels) encoders.py:157-177
 //            then mod T, + offsets[l]; clamped to the table  encoders.py:179-189
-//   weight = prod_d (o_d ? frac_d : 1 - frac_d)             encoders.py:191-213
+//   weight = prod_d clip(o_d ? frac_d : 1 - frac_d, 0, 1)   encoders.py:191-213
+//            (frac = modf's fractional part, signed like the coordinate)
 //   enc    = sum over corners in corner order               encoders.py:231
 #include "common.cuh"
 
@@ -42,10 +43,12 @@ __device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, st
     const float sz = __fadd_rn(__fmul_rn(uz, s), 0.5f);
     const float fx = floorf(sx), fy = floorf(sy), fz = floorf(sz);
     const std::uint32_t bx = (std::uint32_t)(int)fx, by = (std::uint32_t)(int)fy, bz = (std::uint32_t)(int)fz;
-    const float rx = __fsub_rn(sx, fx), ry = __fsub_rn(sy, fy), rz = __fsub_rn(sz, fz);
-    const float wx[2] = {__fsub_rn(1.f, rx), rx};
-    const float wy[2] = {__fsub_rn(1.f, ry), ry};
-    const float wz[2] = {__fsub_rn(1.f, rz), rz};
+    // modf's fractional part (the sign of the coordinate) and the clip to [0, 1] of
+    // encoders.py:204-212: a point below the grid gives all its weight to the lower corner
+    const float rx = __fsub_rn(sx, truncf(sx)), ry = __fsub_rn(sy, truncf(sy)), rz = __fsub_rn(sz, truncf(sz));
+    const float wx[2] = {fminf(fmaxf(__fsub_rn(1.f, rx), 0.f), 1.f), fminf(fmaxf(rx, 0.f), 1.f)};
+    const float wy[2] = {fminf(fmaxf(__fsub_rn(1.f, ry), 0.f), 1.f), fminf(fmaxf(ry, 0.f), 1.f)};
+    const float wz[2] = {fminf(fmaxf(__fsub_rn(1.f, rz), 0.f), 1.f), fminf(fmaxf(rz, 0.f), 1.f)};
     const bool dense = l < d.first_hash_level;
     const std::uint32_t res = d.resolutions[l], res2 = res * res;
     const std::uint32_t off = d.offsets[l], last = d.n_params - 1u, T = d.T;

@@ -64,6 +64,15 @@ __global__ void __launch_bounds__(256) integrate_rays_kernel(
     if (lane_id() == 0 && used > 0) atomicAdd(measured, used);
 }
 
+// kExact = false: the reference's gradient (integrating.cu:173-233): density gradients scaled by
+// min(z^2, 1), the near-plane penalty added, the background counted in (final - cur) and again in
+// bg * (1 - opacity), the opacity normalisation of terminated rays not differentiated.
+// kExact = true: the adjoint of the forward as computed.  With out = colour (or depth) of the ray
+// and cur_k the sum of the first k+1 weighted samples,
+//   d out / d sigma_k = dt_k (T_{k+1} c_k - (out - cur_k)) / norm,   d out / d c_k = w_k / norm,
+// where norm = 1 for a ray that reaches the background (out - cur_k already holds T_N bg) and
+// norm = 1 - T_N = opacity for a terminated ray (out = cur_N / opacity).
+template <bool kExact>
 __global__ void __launch_bounds__(256) integrate_rays_backward_kernel(
     std::uint32_t n_rays, std::uint32_t total_samples, float near_distance, const std::uint32_t *__restrict__ startidx,
     const std::uint32_t *__restrict__ n_samples, const float *__restrict__ bgs,
@@ -79,9 +88,13 @@ __global__ void __launch_bounds__(256) integrate_rays_backward_kernel(
     const float4 fr = reinterpret_cast<const float4 *>(final_rgbds)[i];
     const float fo = final_opacities[i];
     const bool terminated = fo >= 1.f - kTThreshold;
-    const float4 go = reinterpret_cast<const float4 *>(dL_dfinal_rgbds)[i];
+    float4 go = reinterpret_cast<const float4 *>(dL_dfinal_rgbds)[i];
     const float bg0 = bgs[i * 3 + 0], bg1 = bgs[i * 3 + 1], bg2 = bgs[i * 3 + 2];
-    const float bgterm = terminated ? 0.f : 1.f - fo;
+    const float bgterm = (kExact || terminated) ? 0.f : 1.f - fo;
+    if (kExact && terminated) {
+        const float inv = 1.f / fo;
+        go = make_float4(go.x * inv, go.y * inv, go.z * inv, go.w * inv);
+    }
     float *gz = dL_dz_vals + s;
     float4 *gc = reinterpret_cast<float4 *>(dL_ddrgbs) + s;
     float T = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, cd = 0.f;
@@ -100,9 +113,13 @@ __global__ void __launch_bounds__(256) integrate_rays_backward_kernel(
                                + go.y * (T * c.z - (fr.y - cg) - bg1 * bgterm)
                                + go.z * (T * c.w - (fr.z - cb) - bg2 * bgterm)
                                + go.w * (T * z - (fr.w - cd)));
-        const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
-        const float scale = fminf(z * z, 1.f);
-        gc[k] = make_float4(scale * dsig + reg, w * go.x, w * go.y, w * go.z);
+        if (kExact) {
+            gc[k] = make_float4(dsig, w * go.x, w * go.y, w * go.z);
+        } else {
+            const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
+            const float scale = fminf(z * z, 1.f);
+            gc[k] = make_float4(scale * dsig + reg, w * go.x, w * go.y, w * go.z);
+        }
     }
     if (T > kTThreshold) {
         dL_dbgs[i * 3 + 0] = T * go.x;
@@ -241,16 +258,21 @@ int launch_integrate_rays_backward(cudaStream_t stream, const IntegratingBackwar
                                    const float *bgs, const float *dss, const float *z_vals,
                                    const float *drgbs, const float *final_rgbds,
                                    const float *final_opacities, const float *dL_dfinal_rgbds,
-                                   float *dL_dbgs, float *dL_dz_vals, float *dL_ddrgbs) {
+                                   float *dL_dbgs, float *dL_dz_vals, float *dL_ddrgbs, bool exact) {
     NGP_CHECK_ARG(d.near_distance >= 0.f, "integrate_rays_backward: near_distance must be non-negative");
     // samples past a ray's termination and slots that belong to no ray get zero gradients
     NGP_CUDA_TRY(cudaMemsetAsync(dL_dbgs, 0, (std::size_t)d.n_rays * 3 * sizeof(float), stream));
     NGP_CUDA_TRY(cudaMemsetAsync(dL_dz_vals, 0, (std::size_t)d.total_samples * sizeof(float), stream));
     NGP_CUDA_TRY(cudaMemsetAsync(dL_ddrgbs, 0, (std::size_t)d.total_samples * 4 * sizeof(float), stream));
     if (d.n_rays > 0) {
-        integrate_rays_backward_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
-            d.n_rays, d.total_samples, d.near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs, final_rgbds,
-            final_opacities, dL_dfinal_rgbds, dL_dbgs, dL_dz_vals, dL_ddrgbs);
+        if (exact)
+            integrate_rays_backward_kernel<true><<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
+                d.n_rays, d.total_samples, d.near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs, final_rgbds,
+                final_opacities, dL_dfinal_rgbds, dL_dbgs, dL_dz_vals, dL_ddrgbs);
+        else
+            integrate_rays_backward_kernel<false><<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
+                d.n_rays, d.total_samples, d.near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs, final_rgbds,
+                final_opacities, dL_dfinal_rgbds, dL_dbgs, dL_dz_vals, dL_ddrgbs);
         count_launches(1);
     }
     return launch_status();

@@ -187,8 +187,9 @@ def _integrate_forward(startidx, n_samples, bgs, dss, z_vals, drgbs):
 
 
 def integrate_rays_backward(near_distance: float, rays_sample_startidx, rays_n_samples, bgs, dss, z_vals, drgbs,
-                            final_rgbds, final_opacities, dL_dfinal_rgbds):
-    """The reference's backward kernel (integrating/impl.py:109-141).  Returns
+                            final_rgbds, final_opacities, dL_dfinal_rgbds, exact: bool = False):
+    """The reference's backward kernel (integrating/impl.py:109-141), or with `exact` the exact
+    adjoint of the forward (ngp_integrate_rays_backward_exact).  Returns
     (dL_dbgs [R,3], dL_dz_vals [S], dL_ddrgbs [S,4])."""
     startidx, n_samples = _as_u32(rays_sample_startidx).contiguous(), _as_u32(rays_n_samples).contiguous()
     n = startidx.shape[0]
@@ -200,7 +201,8 @@ def integrate_rays_backward(near_distance: float, rays_sample_startidx, rays_n_s
     g_c = torch.empty(s, 4, dtype=torch.float32, device=dev)
     if near_distance < 0:
         raise ValueError("near_distance must be non-negative")
-    L.call("integrate_rays_backward", [startidx, n_samples, bgs, dss.contiguous(), z_vals.contiguous(),
+    L.call("ngp_integrate_rays_backward_exact" if exact else "integrate_rays_backward",
+           [startidx, n_samples, bgs, dss.contiguous(), z_vals.contiguous(),
                                        drgbs.contiguous(), final_rgbds.contiguous(), final_opacities.contiguous(),
                                        dL_dfinal_rgbds.contiguous(), g_bgs, g_z, g_c],
            L.IntegratingBackwardDescriptor(n, s, near_distance))
@@ -212,9 +214,10 @@ class _IntegrateRays(torch.autograd.Function):
     near_distance, the index arrays or dss (impl.py:126-141)."""
 
     @staticmethod
-    def forward(ctx, near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs):
+    def forward(ctx, near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs, exact=False):
         measured, rgbds, opac = _integrate_forward(startidx, n_samples, bgs, dss, z_vals, drgbs)
         ctx.near_distance = float(near_distance)
+        ctx.exact = bool(exact)
         ctx.save_for_backward(startidx, n_samples, bgs, dss, z_vals, drgbs, rgbds, opac)
         ctx.mark_non_differentiable(measured)
         return measured, rgbds, opac
@@ -225,16 +228,18 @@ class _IntegrateRays(torch.autograd.Function):
         if g_rgbds is None:
             g_rgbds = torch.zeros_like(rgbds)
         g_bgs, g_z, g_c = integrate_rays_backward(ctx.near_distance, startidx, n_samples, bgs, dss, z_vals, drgbs,
-                                                  rgbds, opac, g_rgbds.contiguous())
-        return None, None, None, g_bgs, None, g_z, g_c
+                                                  rgbds, opac, g_rgbds.contiguous(), exact=ctx.exact)
+        return None, None, None, g_bgs, None, g_z, g_c, None
 
 
 def integrate_rays(near_distance: float, rays_sample_startidx: torch.Tensor, rays_n_samples: torch.Tensor,
-                   bgs: torch.Tensor, dss: torch.Tensor, z_vals: torch.Tensor, drgbs: torch.Tensor):
+                   bgs: torch.Tensor, dss: torch.Tensor, z_vals: torch.Tensor, drgbs: torch.Tensor,
+                   exact_adjoint: bool = False):
     """Front-to-back compositing with early termination at T <= 1e-4.
 
     Returns (measured_batch_size, final_rgbds [R,4], final_opacities [R]); differentiable w.r.t.
-    bgs, z_vals and drgbs."""
+    bgs, z_vals and drgbs, through the reference's backward, or with `exact_adjoint` through the
+    exact adjoint of the forward."""
     startidx, n_samples = _as_u32(rays_sample_startidx).contiguous(), _as_u32(rays_n_samples).contiguous()
     n = startidx.shape[0]
     s = dss.shape[0]
@@ -244,7 +249,7 @@ def integrate_rays(near_distance: float, rays_sample_startidx: torch.Tensor, ray
     _f32(drgbs, "integrate_rays")
     bgs = torch.broadcast_to(torch.as_tensor(bgs, dtype=torch.float32, device=drgbs.device), (n, 3)).contiguous()
     measured, rgbds, opac = _IntegrateRays.apply(near_distance, startidx, n_samples, bgs, dss.contiguous(),
-                                                 z_vals.contiguous(), drgbs.contiguous())
+                                                 z_vals.contiguous(), drgbs.contiguous(), exact_adjoint)
     return measured[0], rgbds, opac
 
 

@@ -124,6 +124,20 @@ def encode(pos: np.ndarray, latents: np.ndarray, bound: float, tab: LevelTable, 
     return np.ascontiguousarray(acc.transpose(1, 0, 2).reshape(n, tab.L * tab.F))
 
 
+def encode_as_f32(pos: np.ndarray, latents: np.ndarray, bound: float, tab: LevelTable) -> np.ndarray:
+    """The float32 encoder's corners and weights (the ones the GPU and the reference compute) applied
+    to float64 latents: the encoder as a function of the table, for central differences."""
+    p01 = normalize(pos, bound, np.float32)
+    idx, w, _ = corner_indices(p01, tab, np.float32)
+    lat = np.asarray(latents, np.float64)
+    w = w.astype(np.float64)
+    acc = lat[idx[:, :, 0]] * w[:, :, 0, None]
+    for c in range(1, 8):
+        acc = acc + lat[idx[:, :, c]] * w[:, :, c, None]
+    n = p01.shape[0]
+    return np.ascontiguousarray(acc.transpose(1, 0, 2).reshape(n, tab.L * tab.F))
+
+
 def encode_backward(pos: np.ndarray, dL_denc: np.ndarray, bound: float, tab: LevelTable,
                     dtype=np.float64) -> np.ndarray:
     """dL/dlatents [P, F]: scatter-add of w * dL/denc (the transpose of the gather)."""

@@ -170,3 +170,17 @@ def test_field_module_autograd():
     gwt = unpack_weights(f.weights.grad)
     for k in gw:
         assert rel_err(gwt[k].cpu().numpy(), gw[k], axis=None) <= 1e-4, k
+
+
+def test_hashgrid_points_outside_the_box():
+    """Points outside [-bound, bound] (negative scaled coordinates at the coarse levels): the
+    weights follow modf's signed fractional part and the clip of encoders.py:204-212."""
+    from jaxngp_gb300.encoders import LevelTable, hashgrid_forward
+    rng = np.random.default_rng(21)
+    tab = H.LevelTable(16, 1 << 14, 2, 16, 2048)
+    t = LevelTable(16, 1 << 14, 2, 16, 2048)
+    lat = rng.uniform(-1, 1, size=(tab.n_params, 2)).astype(np.float32)
+    pos = rng.uniform(-1.6, 1.6, size=(20000, 3)).astype(np.float32)
+    want = H.encode(pos, lat, 1.0, tab)
+    got = hashgrid_forward(t, cu(pos), cu(lat), 1.0).cpu().numpy()
+    assert np.array_equal(got, want)
