@@ -214,9 +214,13 @@ int integrate_rays_inference_status(cudaStream_t stream, void **buffers, const c
  * fits the sample budget, with every sample-less ray valid and every ray that does not fit
  * invalid; but a ray that meets its first occupied sample after the budget is full stops there
  * (it could only overflow) and is left out of both counters, whose difference -- the samples
- * written -- stays exact.  Rays are taken from a work queue in index order.
- * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call).
- * opaque: MarchingDescriptor. */
+ * written -- stays exact.  Rays are taken from a work queue in index order.  With coarse
+ * occupancy blocks (ngp_proposal_coarse of the same bitfield; K = 1, G a multiple of 8), a ray
+ * whose segment crosses no occupied block is finished at once -- valid, no samples -- instead of
+ * being marched through empty cells: the same result, since every cell the march could look up
+ * lies in such a block.
+ * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call), then
+ * coarse u8[(G/8)^3] or NULL.  opaque: MarchingDescriptor. */
 void ngp_march_rays_train(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_march_rays_train_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
@@ -504,6 +508,10 @@ int ngp_proposal_loss_status(cudaStream_t stream, void **buffers, const char *op
  * f32[n,8], dL_dweights f32[4672].  opaque: NgpMlpDescriptor. */
 void ngp_proposal_mlp_forward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_mlp_forward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+/* ngp_proposal_mlp_forward on the tensor cores (tcgen05, FP16 operands, FP32 accumulation); same
+ * buffers.  The sampler evaluates its bins with it. */
+void ngp_proposal_mlp_forward_f16(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_mlp_forward_f16_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 void ngp_proposal_mlp_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_mlp_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 size_t ngp_proposal_backward_scratch_floats(void);

@@ -11,7 +11,7 @@ namespace ngp {
 int launch_march_rays(cudaStream_t, const MarchingDescriptor &, const float *, const float *, const float *,
                       const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *,
                       bool *, std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, float *, float *,
-                      std::uint32_t *, bool);
+                      std::uint32_t *, bool, const std::uint8_t *);
 int launch_march_rays_inference(cudaStream_t, const MarchingInferenceDescriptor &, const float *, const float *,
                                 const float *, const float *, const std::uint8_t *, const std::uint32_t *,
                                 const bool *, const std::uint32_t *, std::uint32_t *, std::uint32_t *,
@@ -70,6 +70,7 @@ int launch_prop_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, cons
 int launch_prop_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *, const float *,
                          float *, float *, float *, bool);
 std::size_t prop_partials_floats();
+int launch_prop_f16_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *, float *);
 int launch_mlp_backward_noalloc(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                                 const float *, const float *, const float *, float *, float *, bool);
 int launch_render_blobs(cudaStream_t, const NgpRenderBlobsDescriptor &, const float *, const float *, const float *,
@@ -172,14 +173,14 @@ NGP_ENTRY(ngp_packbits_scalar) {
 NGP_ENTRY(march_rays) {
     NGP_DESC(MarchingDescriptor, d);
     return launch_march_rays(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
-                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), nullptr, false);
+                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), nullptr, false, nullptr);
 }
 
 NGP_ENTRY(ngp_march_rays_train) {
     NGP_DESC(MarchingDescriptor, d);
     NGP_CHECK_ARG(buffers[16] != nullptr, "ngp_march_rays_train: the queue counter (buffer 16) is required");
     return launch_march_rays(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
-                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), U32(16), true);
+                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), U32(16), true, CU8(17));
 }
 
 NGP_ENTRY(march_rays_inference) {
@@ -411,6 +412,11 @@ NGP_ENTRY(ngp_proposal_loss) {
 NGP_ENTRY(ngp_proposal_mlp_forward) {
     NGP_DESC(NgpMlpDescriptor, d);
     return launch_prop_forward(stream, d.n_samples, CU32(2), CF32(0), CF32(1), F32(3));
+}
+
+NGP_ENTRY(ngp_proposal_mlp_forward_f16) {
+    NGP_DESC(NgpMlpDescriptor, d);
+    return launch_prop_f16_forward(stream, d.n_samples, CU32(2), CF32(0), CF32(1), F32(3));
 }
 
 NGP_ENTRY(ngp_proposal_mlp_backward) {

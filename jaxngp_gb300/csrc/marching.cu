@@ -16,6 +16,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "coarse.cuh"
 
 namespace ngp {
 namespace {
@@ -152,6 +153,24 @@ __device__ __forceinline__ V3 at(V3 o, V3 d, float t) { return {o.x + t * d.x, o
 
 // ------------------------------------------------------------------------------- march_rays
 
+// True when the ray cannot take a sample: every cell the march could look up on [t0, t1) lies in
+// a coarse block (8^3 cells grown by one cell) that holds no occupied cell.  The march looks up
+// the cell under o + t d for t on [t0, t1) (rounded positions, clamped into the grid); the coarse
+// DDA walks the blocks the same segment crosses, and the one-cell growth of every block covers
+// both roundings.  Positions clamped from outside the grid are covered only within half a cell of
+// its faces, so rays whose ends lie farther out are marched in full.  K = 1 only.
+__device__ __forceinline__ bool no_sample_possible(const MarchParams &m, const V3 &o, const V3 &d, float t0, float t1,
+                                                   const std::uint8_t *__restrict__ coarse) {
+    if (m.K != 1 || (m.G & 7u) != 0u) return false;
+    const float lim = m.mb0 + 0.5f * (2.0f * m.mb0 / (float)m.G);
+    const V3 a = at(o, d, t0), b = at(o, d, t1);
+    if (fabsf(a.x) > lim || fabsf(a.y) > lim || fabsf(a.z) > lim || fabsf(b.x) > lim || fabsf(b.y) > lim ||
+        fabsf(b.z) > lim)
+        return false;
+    float ta, tb;
+    return !coarse_ray_interval(o.x, o.y, o.z, d.x, d.y, d.z, t0, t1, coarse, (int)(m.G / 8u), m.mb0, ta, tb);
+}
+
 constexpr int kMarchBlock = 128;
 constexpr int kMarchBlocksPerSm = 10;   // 40 warps per SM at <= 48 registers
 
@@ -189,7 +208,7 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
     std::uint32_t *__restrict__ queue, bool *__restrict__ ray_is_valid,
     std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
     std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
-    float *__restrict__ dss, float *__restrict__ z_vals) {
+    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse) {
     __shared__ std::uint32_t expand[1024];  // expand_bits(v), v < G (G <= 1024)
     for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
     __syncthreads();
@@ -229,12 +248,16 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
                     d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
                     const float t0 = t_starts[r];
                     t1 = t_ends[r];
-                    if (t1 > t0) {  // marching.cu:151
+                    if (t1 > t0 && !(coarse != nullptr && no_sample_possible(m, o, d, t0, t1, coarse))) {  // marching.cu:151
                         inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
                         t = t0 + calc_ds(t0, m) * noises[r];
                         n = 0;
                         it = 0;
                         phase = kCount;
+                    } else if (t1 > t0) {  // marching.cu:196-199: no occupied block on the way
+                        ray_is_valid[r] = true;
+                        rays_n_samples[r] = 0;
+                        rays_startidx[r] = 0;
                     } else {
                         ray_is_valid[r] = false;
                         rays_n_samples[r] = 0;
@@ -636,7 +659,7 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
                       const float *noises, const std::uint8_t *bits, std::uint32_t *next_loc,
                       std::uint32_t *n_exceeded, bool *ray_is_valid, std::uint32_t *rays_n_samples,
                       std::uint32_t *rays_startidx, std::uint32_t *idcs, float *xyzs, float *dirs,
-                      float *dss, float *z_vals, std::uint32_t *queue, bool probe) {
+                      float *dss, float *z_vals, std::uint32_t *queue, bool probe, const std::uint8_t *coarse) {
     NGP_CHECK_ARG(d.K > 0 && d.G > 0 && d.diagonal_n_steps > 0, "march_rays: K, G and diagonal_n_steps must be positive");
     NGP_CHECK_ARG(d.G <= 1024 && (d.G & (d.G - 1)) == 0, "march_rays: G must be a power of two <= 1024 (Morton codes of other sizes exceed G^3)");
     NGP_CHECK_ARG(d.K <= 16, "march_rays: at most 16 cascades");
@@ -653,11 +676,11 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
         if (probe) {
             march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals);
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
         } else {
             march_rays_kernel<false><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals);
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
         }
         count_launches(1);
     }

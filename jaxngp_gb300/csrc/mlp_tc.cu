@@ -564,6 +564,117 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_backward_kernel(
     if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
 }
 
+// ------------------------------------------------------------------ proposal network (FP16)
+//
+// The learned proposal's MLP x = relu(relu(enc @ P0) @ P1) @ P2 (enc 8 features; P0 [8][64],
+// P1 [64][64], P2 [64][1] packed, 4672 floats) with FP16 operands and FP32 accumulation: layer 0
+// has its K padded to 16 with zeros, layer 2 its N padded to 16.  Same structure as the field
+// forward above (a warpgroup per tile of 128 points, one point per thread).
+constexpr int kQ0 = 0, kQ1 = 1024, kQ2 = 5120, kQW = 6144;        // FP16 operands: P0^T [64][16], P1^T [64][64], P2^T [16][64]
+constexpr int kQX = 0, kQH1 = 2048, kQH2 = 10240, kQAct = 18432;  // per warpgroup: X [128][16], H1, H2 [128][64]
+constexpr int kPropWgs = 4;
+constexpr std::size_t kPropSmem = (std::size_t)(kQW + kPropWgs * kQAct) * 2;
+
+template <int N>
+__device__ __forceinline__ void store_row_f16(__half *buf, int r, const float *v) {
+#pragma unroll
+    for (int c = 0; c < N; c += 8) {
+        uint4 q;
+        q.x = tc::pack_f16(v[c + 0], v[c + 1]);
+        q.y = tc::pack_f16(v[c + 2], v[c + 3]);
+        q.z = tc::pack_f16(v[c + 4], v[c + 5]);
+        q.w = tc::pack_f16(v[c + 6], v[c + 7]);
+        *reinterpret_cast<uint4 *>(buf + rb(r, c, N)) = q;
+    }
+}
+
+__device__ __forceinline__ void mma_kk_f16(std::uint32_t d, const __half *a, const __half *b, int K, int N) {
+    const std::uint32_t id = tc::idesc_f16(128, N);
+    const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), sbo = (std::uint32_t)K * 16;
+    for (int j = 0; j < K / 16; ++j)
+        tc::mma_bf16(d, tc::sdesc(sa + j * 256, 128, sbo), tc::sdesc(sb + j * 256, 128, sbo), id, j > 0);
+}
+
+template <int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) prop_f16_forward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ weights, float *__restrict__ x_out) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ std::uint64_t bars[NWG];
+    __shared__ std::uint32_t tbase;
+    __shared__ int fails[NWG];
+    __half *sw = reinterpret_cast<__half *>(smem_raw);
+    const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
+    __half *act = sw + kQW + g * kQAct;
+    for (int i = threadIdx.x; i < kQW; i += blockDim.x) sw[i] = __float2half_rn(0.f);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4672; i += blockDim.x) {
+        const __half v = __float2half_rn(weights[i]);
+        if (i < 512) {           // P0 [8][64] -> P0^T [64][16]
+            const int in = i / 64, out = i % 64;
+            sw[kQ0 + rb(out, in, 16)] = v;
+        } else if (i < 4608) {   // P1 [64][64] -> P1^T
+            const int j = i - 512, in = j / 64, out = j % 64;
+            sw[kQ1 + rb(out, in, 64)] = v;
+        } else {                 // P2 [64][1] -> P2^T row 0 of [16][64]
+            sw[kQ2 + rb(0, i - 4608, 64)] = v;
+        }
+    }
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NWG; ++k) {
+            tc::mbar_init(&bars[k], 1);
+            fails[k] = 0;
+        }
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(&tbase, 512);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    WarpGroup wg{g, r, tbase + (std::uint32_t)g * 128u + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
+    const bool leader = r == 0;
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += gridDim.x * NWG) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n_act;
+        float v[64];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) v[c] = 0.f;
+        if (valid) {
+            const float4 a = reinterpret_cast<const float4 *>(enc + s * 8)[0];
+            const float4 b = reinterpret_cast<const float4 *>(enc + s * 8)[1];
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        }
+        store_row_f16<16>(act + kQX, r, v);
+        wg.sync();
+        if (leader) { mma_kk_f16(wg.tm + kDA, act + kQX, sw + kQ0, 16, 64); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld64(wg.tm + kDA, v);
+#pragma unroll
+        for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+        store_row_f16<64>(act + kQH1, r, v);
+        wg.sync();
+        if (leader) { mma_kk_f16(wg.tm + kDA, act + kQH1, sw + kQ1, 64, 64); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld64(wg.tm + kDA, v);
+#pragma unroll
+        for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+        store_row_f16<64>(act + kQH2, r, v);
+        wg.sync();
+        if (leader) { mma_kk_f16(wg.tm + kDB, act + kQH2, sw + kQ2, 64, 16); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld16(wg.tm + kDB, v);
+        if (valid) x_out[s] = v[0];
+        tc::bar_sync(1 + g, 128);
+        if (*wg.fail) break;
+    }
+    if (*wg.fail && r == 0) atomicOr(&g_device_error, 1u);
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
+}
+
 constexpr int kFwdWgs = 3, kBwdWgs = 2;
 constexpr std::size_t kFwdSmem = (std::size_t)(kFwdW + kFwdWgs * kFwdAct) * 2;
 constexpr std::size_t kBwdSmem = (std::size_t)(kAllW + kBwdWgs * kBwdAct) * 2;
@@ -622,6 +733,23 @@ int launch_mlp_bf16_backward(cudaStream_t stream, std::uint32_t n, const std::ui
                                                                                 grad_scale, dL_denc, partials);
     count_launches(1);
     *grid_out = grid;
+    return launch_status();
+}
+
+int launch_prop_f16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                            const float *weights, float *x) {
+    NGP_CHECK_ARG(aligned16(enc), "proposal mlp (fp16): encodings must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(prop_f16_forward_kernel<kPropWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropSmem));
+        attr = true;
+    }
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kRows - 1) / kRows;
+    const unsigned want = (tiles + kPropWgs - 1) / kPropWgs;
+    const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
+    prop_f16_forward_kernel<kPropWgs><<<grid, kPropWgs * 128, kPropSmem, stream>>>(n, count, enc, weights, x);
+    count_launches(1);
     return launch_status();
 }
 

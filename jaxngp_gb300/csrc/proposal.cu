@@ -15,6 +15,7 @@
 //      loss run unchanged
 //   4. the proposal regresses the field's log density at the field's samples (loss kernel here)
 #include "common.cuh"
+#include "coarse.cuh"
 
 namespace ngp {
 namespace {
@@ -52,55 +53,6 @@ __global__ void coarse_grid_kernel(std::uint32_t G, const std::uint8_t *__restri
     coarse[c] = any;
 }
 
-// The ray's occupied interval over the coarse grid (a 3D DDA, x/y/z order on ties).
-__device__ __forceinline__ bool ray_interval(float ox, float oy, float oz, float dx, float dy, float dz, float t0,
-                                             float t1, const std::uint8_t *__restrict__ coarse, int Gc, float mb,
-                                             float &ta, float &tb) {
-    ta = 0.f;
-    tb = 0.f;
-    if (!(t0 < t1)) return false;
-    const float o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
-    const float scale = (float)Gc / (2.0f * mb);
-    int cell[3], step[3];
-    float tmax[3], tdel[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float g = ((o[a] + t0 * d[a]) + mb) * scale;
-        cell[a] = min(max((int)floorf(g), 0), Gc - 1);
-        if (d[a] > 0.f) {
-            step[a] = 1;
-            tmax[a] = (((float)(cell[a] + 1) / scale - mb) - o[a]) / d[a];
-            tdel[a] = (1.0f / scale) / d[a];
-        } else if (d[a] < 0.f) {
-            step[a] = -1;
-            tmax[a] = (((float)cell[a] / scale - mb) - o[a]) / d[a];
-            tdel[a] = (-1.0f / scale) / d[a];
-        } else {
-            step[a] = 0;
-            tmax[a] = __int_as_float(0x7f800000);
-            tdel[a] = __int_as_float(0x7f800000);
-        }
-    }
-    float t = t0;
-    bool hit = false;
-    for (int it = 0; it < 3 * Gc + 3; ++it) {
-        if (!(t < t1)) break;
-        const float m = fminf(tmax[0], fminf(tmax[1], tmax[2]));
-        const int a = tmax[0] == m ? 0 : (tmax[1] == m ? 1 : 2);
-        const float tn = fminf(m, t1);
-        if (coarse[cell[0] + cell[1] * Gc + cell[2] * Gc * Gc]) {
-            if (!hit) ta = t;
-            hit = true;
-            tb = tn;
-        }
-        cell[a] += step[a];
-        if (cell[a] < 0 || cell[a] >= Gc) break;
-        t = m;
-        tmax[a] = tmax[a] + tdel[a];
-    }
-    return hit;
-}
-
 // Step 1-2: interval, slot allocation.  Slot j = startidx / spr of a fitting ray records the
 // ray (ray_of_slot) and its interval (slot_ta, slot_tb).
 __global__ void __launch_bounds__(256) proposal_rays_kernel(
@@ -115,7 +67,7 @@ __global__ void __launch_bounds__(256) proposal_rays_kernel(
     float ta = 0.f, tb = 0.f;
     bool hit = false;
     if (in)
-        hit = ray_interval(rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2],
+        hit = coarse_ray_interval(rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2],
                            rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2],
                            t_starts[r], t_ends[r], coarse, Gc, mb, ta, tb);
     hit = hit && tb > ta;
@@ -181,71 +133,99 @@ __device__ __forceinline__ std::uint64_t splitmix(std::uint64_t x) {
     return x ^ (x >> 31);
 }
 
-// Step 3c: one thread per slot turns the bins' log densities into spr samples.
-__global__ void __launch_bounds__(128) proposal_sample_kernel(
+// Step 3c: a warp per slot turns the bins' log densities into spr samples.  Lane l holds bins
+// 2l and 2l+1; the exclusive prefix of the densities (transmittance) and the CDF are warp scans;
+// every lane then inverts the CDF (binary search in shared memory) for the edges of its samples
+// k = l, l + 32, ...: e_0 = t_a, e_k = F^-1(((k - 1/2) + xi_k) / spr) (0 < k < spr), e_spr = t_b,
+// sample k at the middle of [e_k, e_k+1], standing for that interval.
+constexpr int kSampleWarps = 4;
+
+__device__ __forceinline__ float warp_inclusive_scan_f(float v) {
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float proposal_edge(int k, std::uint32_t spr, float ta, float tb, float delta, bool perturb,
+                                               std::uint64_t seed, std::uint32_t r, const float *cdf, const float *pdf) {
+    if (k <= 0) return ta;
+    if (k >= (int)spr) return tb;
+    float xi = 0.5f;
+    if (perturb)
+        xi = (float)(splitmix(seed ^ ((std::uint64_t)r * spr + (std::uint64_t)k) * 0x2545F4914F6CDD1Dull) >> 40) *
+             (1.0f / 16777216.0f);
+    const float u = (((float)k - 0.5f) + xi) / (float)spr;
+    int lo = 0, hi = kBins - 1;   // first bin whose inclusive CDF exceeds u (the last bin if none)
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (u < cdf[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    const float c_lo = lo > 0 ? cdf[lo - 1] : 0.f;
+    const float frac = fminf(fmaxf((u - c_lo) / pdf[lo], 0.f), 1.f);
+    return ta + ((float)lo + frac) * delta;
+}
+
+__global__ void __launch_bounds__(32 * kSampleWarps) proposal_sample_kernel(
     const std::uint32_t *__restrict__ counts, std::uint32_t spr, float mix, int perturb, std::uint64_t seed,
     const float *__restrict__ rays_o,
     const float *__restrict__ rays_d, const std::uint32_t *__restrict__ ray_of_slot, const float *__restrict__ slot_ta,
     const float *__restrict__ slot_tb, const float *__restrict__ x_bins, std::uint32_t *__restrict__ idcs,
     float *__restrict__ xyzs, float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals) {
-    const std::uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= counts[0]) return;
-    const std::uint32_t r = ray_of_slot[j];
-    const float ta = slot_ta[j], tb = slot_tb[j];
-    const float delta = (tb - ta) / (float)kBins;
-    const float *xb = x_bins + (std::size_t)j * kBins;
-    float w[kBins];
-    float acc = 0.f, W = 0.f;
-#pragma unroll 8
-    for (int i = 0; i < kBins; ++i) {
-        const float s = expf(fminf(fmaxf(xb[i], -15.f), 15.f));
-        const float T = expf(-(delta * acc));
-        const float a = -expm1f(-(s * delta));
-        w[i] = T * a;
-        W = W + w[i];
-        acc = acc + s;
-    }
-    // pdf mixed with a uniform one, in place
-#pragma unroll 8
-    for (int i = 0; i < kBins; ++i) {
-        const float wi = W > 0.f ? w[i] / W : 1.0f / (float)kBins;
-        w[i] = (1.0f - mix) * wi + mix / (float)kBins;
-    }
-    const float o[3] = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
-    const float d[3] = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
-    const std::size_t s0 = (std::size_t)j * spr;
-    // inverse-CDF edges e_0 = t_a, e_k (0 < k < spr), e_spr = t_b; sample k at the
-    // midpoint of [e_k, e_k+1], standing for that interval
-    int b = 0;
-    float c_lo = 0.f, c_hi = w[0], e_prev = ta;
-    for (int k = 1; k <= (int)spr; ++k) {
-        float e = tb;
-        if (k < (int)spr) {
-            float xi = 0.5f;
-            if (perturb)
-                xi = (float)(splitmix(seed ^ ((std::uint64_t)r * spr + (std::uint64_t)k) * 0x2545F4914F6CDD1Dull) >> 40) *
-                     (1.0f / 16777216.0f);
-            const float u = (((float)k - 0.5f) + xi) / (float)spr;
-            while (u >= c_hi && b < kBins - 1) {
-                ++b;
-                c_lo = c_hi;
-                c_hi = c_hi + w[b];
-            }
-            const float frac = fminf(fmaxf((u - c_lo) / w[b], 0.f), 1.f);
-            e = ta + ((float)b + frac) * delta;
+    __shared__ float cdf_s[kSampleWarps][kBins], pdf_s[kSampleWarps][kBins];
+    float *cdf = cdf_s[threadIdx.x >> 5], *pdf = pdf_s[threadIdx.x >> 5];
+    const unsigned lane = lane_id();
+    const std::uint32_t n_slots = counts[0];
+    const std::uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (std::uint32_t j = warp0; j < n_slots; j += n_warps) {
+        const std::uint32_t r = ray_of_slot[j];
+        const float ta = slot_ta[j], tb = slot_tb[j];
+        const float delta = (tb - ta) / (float)kBins;
+        const float2 xv = reinterpret_cast<const float2 *>(x_bins + (std::size_t)j * kBins)[lane];
+        const float s0 = expf(fminf(fmaxf(xv.x, -15.f), 15.f)), s1 = expf(fminf(fmaxf(xv.y, -15.f), 15.f));
+        const float pair = s0 + s1;
+        const float acc0 = warp_inclusive_scan_f(pair) - pair, acc1 = acc0 + s0;
+        const float w0 = expf(-(delta * acc0)) * -expm1f(-(s0 * delta));
+        const float w1 = expf(-(delta * acc1)) * -expm1f(-(s1 * delta));
+        const float W = warp_sum_f(w0 + w1);
+        const float p0 = (1.0f - mix) * (W > 0.f ? w0 / W : 1.0f / (float)kBins) + mix / (float)kBins;
+        const float p1 = (1.0f - mix) * (W > 0.f ? w1 / W : 1.0f / (float)kBins) + mix / (float)kBins;
+        const float pp = p0 + p1;
+        const float ci = warp_inclusive_scan_f(pp);
+        cdf[2 * lane] = ci - pp + p0;
+        cdf[2 * lane + 1] = ci;
+        pdf[2 * lane] = p0;
+        pdf[2 * lane + 1] = p1;
+        __syncwarp();
+        const float o[3] = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
+        const float d[3] = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
+        const std::size_t s_base = (std::size_t)j * spr;
+        for (int k = (int)lane; k < (int)spr; k += 32) {
+            const float e_lo = proposal_edge(k, spr, ta, tb, delta, perturb != 0, seed, r, cdf, pdf);
+            const float e_hi = proposal_edge(k + 1, spr, ta, tb, delta, perturb != 0, seed, r, cdf, pdf);
+            const float t = (e_lo + e_hi) * 0.5f;
+            const std::size_t s = s_base + k;
+            idcs[s] = r;
+            xyzs[s * 3 + 0] = o[0] + t * d[0];
+            xyzs[s * 3 + 1] = o[1] + t * d[1];
+            xyzs[s * 3 + 2] = o[2] + t * d[2];
+            dirs[s * 3 + 0] = d[0];
+            dirs[s * 3 + 1] = d[1];
+            dirs[s * 3 + 2] = d[2];
+            z_vals[s] = t;
+            dss[s] = e_hi - e_lo;
         }
-        const float t = (e_prev + e) * 0.5f;
-        const std::size_t s = s0 + (k - 1);
-        idcs[s] = r;
-        xyzs[s * 3 + 0] = o[0] + t * d[0];
-        xyzs[s * 3 + 1] = o[1] + t * d[1];
-        xyzs[s * 3 + 2] = o[2] + t * d[2];
-        dirs[s * 3 + 0] = d[0];
-        dirs[s * 3 + 1] = d[1];
-        dirs[s * 3 + 2] = d[2];
-        z_vals[s] = t;
-        dss[s] = e - e_prev;
-        e_prev = e;
+        __syncwarp();
     }
 }
 
@@ -325,7 +305,8 @@ int launch_proposal_sample(cudaStream_t stream, std::uint32_t max_slots, const s
                            float *z_vals) {
     NGP_CHECK_ARG(mix >= 0.f && mix <= 1.f, "proposal: mix must be in [0, 1]");
     if (max_slots > 0) {
-        proposal_sample_kernel<<<(max_slots + 127) / 128, 128, 0, stream>>>(
+        const unsigned want = (max_slots + kSampleWarps - 1) / kSampleWarps;
+        proposal_sample_kernel<<<grid_for(want, 1, 16), 32 * kSampleWarps, 0, stream>>>(
             counts, spr, mix, perturb ? 1 : 0, seed, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, idcs, xyzs, dirs, dss,
             z_vals);
         count_launches(1);

@@ -16,6 +16,7 @@
 #include <cstdint>
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace ngp {
 namespace tc {
@@ -36,6 +37,12 @@ __host__ __device__ constexpr std::uint32_t idesc_bf16(int M, int N, bool a_mn, 
            ((std::uint32_t)(N >> 3) << 17) | ((std::uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor of kind::f16 with FP16 operands and an FP32 accumulator.
+__host__ __device__ constexpr std::uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((std::uint32_t)(N >> 3) << 17) | ((std::uint32_t)(M >> 4) << 24);
+}
+
+// kind::f16 MMA (BF16 or FP16 operands, as the instruction descriptor says).
 __device__ __forceinline__ void mma_bf16(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b, std::uint32_t idesc,
                                          bool accumulate) {
     asm volatile(
@@ -123,6 +130,11 @@ __device__ __forceinline__ void ld64(std::uint32_t taddr, float *v) {
         : "r"(taddr) : "memory");
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ std::uint32_t pack_f16(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const std::uint32_t *>(&h);
 }
 
 __device__ __forceinline__ std::uint32_t pack_bf16(float a, float b) {

@@ -51,6 +51,7 @@ class ProposalSampler:
             raise ValueError("samples_per_ray must be in [1, 1024]")
         self.slots = total_samples // self.spr
         self.mix = float(mix)
+        self.f16 = True   # bins through the FP16 tensor-core MLP
         self.dev = torch.device(device)
         self.table = proposal_table()
         self.lr = lr
@@ -100,10 +101,14 @@ class ProposalSampler:
         """Coarse occupancy blocks from the (cascade-0) occupancy bitfield."""
         L.call("ngp_proposal_coarse", [bitfield, self.coarse], self._desc())
 
-    def network(self, points: torch.Tensor, enc: torch.Tensor, x: torch.Tensor, count: Optional[torch.Tensor]):
+    def network(self, points: torch.Tensor, enc: torch.Tensor, x: torch.Tensor, count: Optional[torch.Tensor],
+                f16: bool = False):
+        """Log density at `points`: FP32 (training, consistent with its backward) or, for the
+        sampler's bins, FP16 tensor cores."""
         n = points.shape[0]
         L.call("ngp_hashgrid_forward", [points, self.latents, count, enc], self.table.descriptor(n, self.bound))
-        L.call("ngp_proposal_mlp_forward", [enc, self.weights, count, x], L.NgpMlpDescriptor(n, 0))
+        L.call("ngp_proposal_mlp_forward_f16" if f16 else "ngp_proposal_mlp_forward", [enc, self.weights, count, x],
+               L.NgpMlpDescriptor(n, 0))
 
     def sample(self, rays_o, rays_d, t0, t1, valid, n_samples, startidx, idcs, xyzs, dirs, dss, z_vals,
                perturb: bool, seed: int) -> torch.Tensor:
@@ -114,7 +119,7 @@ class ProposalSampler:
                self._desc(n))
         L.call("ngp_proposal_bin_points", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb,
                                            self.points], self._desc())
-        self.network(self.points, self.enc_b, self.x_b, self.counts[1:2])
+        self.network(self.points, self.enc_b, self.x_b, self.counts[1:2], f16=self.f16)
         L.call("ngp_proposal_sample", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb,
                                        self.x_b, idcs, xyzs, dirs, dss, z_vals], self._desc(perturb=perturb, seed=seed))
         return self.counts[2:3]

@@ -87,6 +87,7 @@ def test_bins_network_and_samples(grid, spr):
     o, d, t0, t1 = make_rays(rng, 3000, 1.0)
     S = spr * 512
     ps = ProposalSampler(3000, S, G, 1.0, seed=5, samples_per_ray=spr)
+    ps.f16 = False   # FP32 bins: checked against FP64 below (the FP16 path has its own test)
     with torch.no_grad():
         ps.latents.uniform_(-1, 1)
     ps.refresh(cu(bits))
@@ -287,3 +288,21 @@ def test_proposal_samples_place_like_dense(trained_pair):
     e_prop = float((prop - dense).abs().mean())
     e_unif = float((unif - dense).abs().mean())
     assert e_prop < 1.5 * e_unif, (e_prop, e_unif)
+
+
+def test_proposal_mlp_f16_forward():
+    """The FP16 tensor-core forward against FP64: within 2e-2 of the output scale (FP16 operands),
+    and its active count respected."""
+    from jaxngp_gb300 import _lib as L
+    rng = np.random.default_rng(12)
+    n = 70000
+    enc = rng.normal(scale=0.5, size=(n, 8)).astype(np.float32)
+    w = P.init_weights(13)
+    x64, _ = P.mlp_forward(enc, w, dtype=np.float64)
+    out = torch.full((n,), -9.0, device="cuda")
+    count = torch.tensor([n - 123], dtype=torch.int32, device="cuda")
+    L.call("ngp_proposal_mlp_forward_f16", [cu(enc), cu(P.pack(w)), count, out], L.NgpMlpDescriptor(n, 0))
+    got = out.cpu().numpy()
+    assert np.abs(got[:n - 123] - x64[:n - 123]).max() <= 2e-2 * np.abs(x64).max()
+    assert (got[n - 123:] == -9.0).all()
+    assert L.lib().ngp_device_status() == 0

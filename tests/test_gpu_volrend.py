@@ -287,7 +287,7 @@ def test_march_rays_inference_multiwarp_vs_oracle(vr):
         idx_h, nri_h, t_h = ref[1], ref[0], ref[3]
 
 
-def _march_train(z, total):
+def _march_train(z, total, coarse=None):
     from jaxngp_gb300 import _lib as L
     n = z["rays_o"].shape[0]
     i32 = dict(dtype=torch.int32, device="cuda")
@@ -299,7 +299,7 @@ def _march_train(z, total):
     d = L.MarchingDescriptor(n, total, int(z["diagonal_n_steps"]), int(z["K"]), int(z["G"]), float(z["bound"]),
                              float(z["stepsize_portion"]))
     L.call("ngp_march_rays_train", [dev(z["rays_o"]), dev(z["rays_d"]), dev(z["t_starts"]), dev(z["t_ends"]),
-                                    dev(z["noises"]), dev(z["bitfield"])] + out + [queue], d)
+                                    dev(z["noises"]), dev(z["bitfield"])] + out + [queue, coarse], d)
     return [host(x) for x in out]
 
 
@@ -333,3 +333,39 @@ def test_march_rays_train_variant(vr, budget_frac):
         assert not idcs[m:].any() and not zs[m:].any()
     if budget_frac is None:
         assert np.array_equal(valid, ref[1]) and np.array_equal(ns, full_n)
+
+
+@pytest.mark.parametrize("budget_frac", [None, 0.3])
+def test_march_rays_train_coarse_shortcut(vr, budget_frac):
+    """With coarse occupancy blocks the training marcher finishes rays that cross no occupied
+    block at once; on a grid of a few blobs (most rays miss them) every ray's result is still the
+    oracle's, bit for bit, and the same as without the shortcut."""
+    from jaxngp_gb300 import _lib as L
+    from tests.test_oracle_proposal import blob_bitfield
+    rng = np.random.default_rng(22)
+    n, G = 8000, 128
+    o, d, t0, t1 = make_rays(rng, n, 1.0)
+    noise = rng.uniform(size=n).astype(np.float32)
+    bits = blob_bitfield(G, [(0.3, -0.2, 0.1), (-0.4, 0.35, -0.3), (0.05, 0.5, -0.5)], 0.12)
+    ref = V.march_rays(1 << 24, 1024, 1, G, 1.0, 0.0, o, d, t0, t1, noise, bits, early_exit=False)
+    full_n = ref[2]
+    assert (full_n == 0).mean() > 0.3 and (full_n > 0).sum() > 100
+    coarse = torch.zeros((G // 8) ** 3, dtype=torch.uint8, device="cuda")
+    L.call("ngp_proposal_coarse", [dev(bits), coarse],
+           L.NgpProposalDescriptor(0, 48, G, 1.0, 0, 0, 0, 3, 1, 0, 0.1))
+    total = (1 << 24) if budget_frac is None else max(1, int(full_n.sum() * budget_frac))
+    z = dict(diagonal_n_steps=1024, K=1, G=G, bound=1.0, stepsize_portion=0.0, rays_o=o, rays_d=d, t_starts=t0,
+             t_ends=t1, noises=noise, bitfield=bits)
+    with_c = _march_train(z, total, coarse)
+    c0, c1, valid, ns, st, idcs, xyzs, dirs, dss, zs = with_c
+    fit = ns > 0
+    assert np.array_equal(ns[fit], full_n[fit])
+    live = t1 > t0
+    assert np.array_equal(valid, (live & (full_n == 0)) | fit)
+    for r in np.nonzero(fit)[0][::5]:
+        a, b, k = st[r], ref[3][r], ns[r]
+        assert np.array_equal(xyzs[a:a + k], ref[5][b:b + k]) and np.array_equal(zs[a:a + k], ref[8][b:b + k])
+    if budget_frac is None:
+        assert np.array_equal(ns, full_n) and np.array_equal(valid, ref[1])
+        without = _march_train(z, total)
+        assert np.array_equal(without[3], ns) and np.array_equal(without[2], valid)
