@@ -70,32 +70,58 @@ struct Strip {
     static_assert(NT % G == 0 && (kIdle || ROWS % R == 0), "tile shape");
 };
 
-// C[s][n] = act(sum_k A[s][k] * B[k][n]) for s < kTile, n < N (N % 4 == 0).
+// acc[q][j] += sum over k in [k0, k0 + 4) of A[row_q][k] * B[k][c0 + j], A read as one float4
+// per row (rows 16-byte aligned), in k order.
+template <int RPT>
+__device__ __forceinline__ void fma4(float (&acc)[RPT][4], const float *A, int lda, const int *rows, const float *B,
+                                     int ldb, int k0, int c0) {
+    const float4 b0 = *reinterpret_cast<const float4 *>(B + (k0 + 0) * ldb + c0);
+    const float4 b1 = *reinterpret_cast<const float4 *>(B + (k0 + 1) * ldb + c0);
+    const float4 b2 = *reinterpret_cast<const float4 *>(B + (k0 + 2) * ldb + c0);
+    const float4 b3 = *reinterpret_cast<const float4 *>(B + (k0 + 3) * ldb + c0);
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+        const float4 a = *reinterpret_cast<const float4 *>(A + rows[q] * lda + k0);
+        acc[q][0] += a.x * b0.x;
+        acc[q][1] += a.x * b0.y;
+        acc[q][2] += a.x * b0.z;
+        acc[q][3] += a.x * b0.w;
+        acc[q][0] += a.y * b1.x;
+        acc[q][1] += a.y * b1.y;
+        acc[q][2] += a.y * b1.z;
+        acc[q][3] += a.y * b1.w;
+        acc[q][0] += a.z * b2.x;
+        acc[q][1] += a.z * b2.y;
+        acc[q][2] += a.z * b2.z;
+        acc[q][3] += a.z * b2.w;
+        acc[q][0] += a.w * b3.x;
+        acc[q][1] += a.w * b3.y;
+        acc[q][2] += a.w * b3.z;
+        acc[q][3] += a.w * b3.w;
+    }
+}
+
+// C[s][n] = act(sum_k A[s][k] * B[k][n]) for s < kTile, n < N (N % 4 == 0, K % 4 == 0).
 template <int NT, int K, int N, bool kRelu>
 __device__ __forceinline__ void mm(const float *A, int lda, const float *B, float *C, int ldc) {
     using S = Strip<NT, kTile, N>;
+    static_assert(K % 4 == 0, "K must be a multiple of 4");
     const int t = threadIdx.x, c0 = (t % S::G) * 4, r0 = t / S::G;
     if (S::kIdle && r0 >= kTile) return;
+    int rows[S::RPT];
     float acc[S::RPT][4];
 #pragma unroll
-    for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-#pragma unroll 8
-    for (int k = 0; k < K; ++k) {
-        const float4 b = *reinterpret_cast<const float4 *>(B + k * N + c0);
-#pragma unroll
-        for (int q = 0; q < S::RPT; ++q) {
-            const float a = A[(r0 + q * S::R) * lda + k];
-            acc[q][0] += a * b.x;
-            acc[q][1] += a * b.y;
-            acc[q][2] += a * b.z;
-            acc[q][3] += a * b.w;
-        }
+    for (int q = 0; q < S::RPT; ++q) {
+        rows[q] = r0 + q * S::R;
+        acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
     }
+#pragma unroll 2
+    for (int k = 0; k < K; k += 4) fma4<S::RPT>(acc, A, lda, rows, B, N, k, c0);
 #pragma unroll
     for (int q = 0; q < S::RPT; ++q) {
         float4 v = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
         if (kRelu) v = make_float4(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f), fmaxf(v.z, 0.f), fmaxf(v.w, 0.f));
-        *reinterpret_cast<float4 *>(C + (r0 + q * S::R) * ldc + c0) = v;
+        *reinterpret_cast<float4 *>(C + rows[q] * ldc + c0) = v;
     }
 }
 
@@ -104,38 +130,36 @@ __device__ __forceinline__ void mm(const float *A, int lda, const float *B, floa
 template <int NT, int K, int N>
 __device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const float *B, float *M, int ldm) {
     using S = Strip<NT, kTile, N>;
+    static_assert(K % 4 == 0, "K must be a multiple of 4");
     const int t = threadIdx.x, c0 = (t % S::G) * 4, r0 = t / S::G;
     if (S::kIdle && r0 >= kTile) return;
+    int rows[S::RPT];
     float acc[S::RPT][4];
 #pragma unroll
-    for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-#pragma unroll 8
-    for (int k = 0; k < K; ++k) {
-        const float4 b = *reinterpret_cast<const float4 *>(B + k * N + c0);
-#pragma unroll
-        for (int q = 0; q < S::RPT; ++q) {
-            const float a = A[(r0 + q * S::R) * lda + k];
-            acc[q][0] += a * b.x;
-            acc[q][1] += a * b.y;
-            acc[q][2] += a * b.z;
-            acc[q][3] += a * b.w;
-        }
+    for (int q = 0; q < S::RPT; ++q) {
+        rows[q] = r0 + q * S::R;
+        acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
     }
+#pragma unroll 2
+    for (int k = 0; k < K; k += 4) fma4<S::RPT>(acc, A, lda, rows, B, N, k, c0);
 #pragma unroll
     for (int q = 0; q < S::RPT; ++q) {
-        float4 *p = reinterpret_cast<float4 *>(M + (r0 + q * S::R) * ldm + c0);
+        float4 *p = reinterpret_cast<float4 *>(M + rows[q] * ldm + c0);
         const float4 m = *p;
         *p = make_float4(m.x > 0.f ? acc[q][0] : 0.f, m.y > 0.f ? acc[q][1] : 0.f,
                          m.z > 0.f ? acc[q][2] : 0.f, m.w > 0.f ? acc[q][3] : 0.f);
     }
 }
 
-// acc[m][n] += sum_s A[s][m] * D[s][n] over the tile's rows (the weight-gradient GEMM).
+// acc[m][n] += sum_s A[s][m] * D[s][n] over the tile's rows (the weight-gradient GEMM).  With four
+// rows per thread the rows are consecutive, so A's four values of a sample are one float4.
 template <int NT, int M, int N>
 struct WGrad {
     using S = Strip<NT, M, N>;
+    static constexpr bool kVec = S::RPT == 4;
     float acc[S::RPT][4];
     __device__ __forceinline__ bool owner() const { return !S::kIdle || (int)threadIdx.x / S::G < M; }
+    __device__ __forceinline__ int row(int m0, int q) const { return kVec ? m0 * 4 + q : m0 + q * S::R; }
     __device__ __forceinline__ void zero() {
 #pragma unroll
         for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
@@ -146,13 +170,25 @@ struct WGrad {
 #pragma unroll 4
         for (int s = 0; s < rows; ++s) {
             const float4 d = *reinterpret_cast<const float4 *>(D + s * ldd + c0);
+            if constexpr (kVec) {
+                const float4 a4 = *reinterpret_cast<const float4 *>(A + s * lda + m0 * 4);
+                const float a[4] = {a4.x, a4.y, a4.z, a4.w};
 #pragma unroll
-            for (int q = 0; q < S::RPT; ++q) {
-                const float a = A[s * lda + m0 + q * S::R];
-                acc[q][0] += a * d.x;
-                acc[q][1] += a * d.y;
-                acc[q][2] += a * d.z;
-                acc[q][3] += a * d.w;
+                for (int q = 0; q < 4; ++q) {
+                    acc[q][0] += a[q] * d.x;
+                    acc[q][1] += a[q] * d.y;
+                    acc[q][2] += a[q] * d.z;
+                    acc[q][3] += a[q] * d.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < S::RPT; ++q) {
+                    const float a = A[s * lda + m0 + q * S::R];
+                    acc[q][0] += a * d.x;
+                    acc[q][1] += a * d.y;
+                    acc[q][2] += a * d.z;
+                    acc[q][3] += a * d.w;
+                }
             }
         }
     }
@@ -161,7 +197,7 @@ struct WGrad {
         if (!owner()) return;
 #pragma unroll
         for (int q = 0; q < S::RPT; ++q)
-            *reinterpret_cast<float4 *>(out + (m0 + q * S::R) * N + c0) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
+            *reinterpret_cast<float4 *>(out + row(m0, q) * N + c0) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
     }
 };
 
