@@ -10,8 +10,10 @@ n_valid_rays over the timed steps / time, the reference's own throughput count,
 app/nerf/train.py:59) with every input resident on the GPU; `e2e` is the same step driven through
 the public API with the pixel indices copied from pinned host memory and the step's metrics copied
 back every step.  `forms` repeats the measurement for the BF16 tensor-core field MLP and for the
-learned proposal sampler with it, each with the held-out PSNR of the trained field and 1080p
-inference FPS, and `learned_proposal_vs_plain` gives their ratio and PSNR difference.
+learned proposal sampler with it (also with a 16-bit table copy and 16-bit encodings, BF16 or
+FP16 under a dynamic loss scale), each with the held-out PSNR of the trained field and 1080p
+inference FPS, and `learned_proposal_vs_plain` gives each proposal form's throughput ratio and
+PSNR difference against the plain step.
 `--impl reference` times the CPU restatement of the plain step (the reference has no CPU path for
 its volume-rendering ops) on the host's cores, on a bounded sample of the batch, extrapolated to
 the full batch.
@@ -30,7 +32,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "train rays/s (plain FP32 hash-grid NeRF step, 64-blob scene)"
-FORMS = {"fp32-march": ("fp32", "march"), "bf16-march": ("bf16", "march"), "bf16-proposal": ("bf16", "proposal")}
+# form: (field MLP operands, sampler, latent-table copy the encoder gathers from, 16-bit encodings)
+FORMS = {"fp32-march": ("fp32", "march", "fp32", False), "bf16-march": ("bf16", "march", "fp32", False),
+         "bf16-proposal": ("bf16", "proposal", "fp32", False),
+         "bf16x-march": ("bf16", "march", "bf16", True), "fp16x-march": ("fp16", "march", "fp16", True),
+         "bf16x-proposal": ("bf16", "proposal", "bf16", True), "fp16x-proposal": ("fp16", "proposal", "fp16", True)}
 UNIT = "rays/s"
 WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
            "L16 F2 T2^19 Nmin16 Nmax2048, MLP 32-64-16 / 32-64-64-3, R=S=2^18, Adam lr1e-2, fp32"
@@ -49,10 +55,11 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--forms", default="fp32-march,bf16-march,bf16-proposal",
+    p.add_argument("--forms", default="fp32-march,bf16-march,bf16-proposal,bf16x-proposal,fp16x-proposal",
                    help="training forms to run, the first is the headline: fp32-march (the reference's "
                         "algorithm, FP32 SIMT field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
-                        "(learned proposal sampler + BF16 MLP)")
+                        "(learned proposal sampler + BF16 MLP); the x forms (bf16x-*, fp16x-*) also gather from a "
+                        "16-bit copy of the table and keep the encodings in 16 bits (fp16 under a dynamic loss scale)")
     p.add_argument("--render-frames", type=int, default=12, help="1920x1080 frames rendered on a 120-pose orbit")
     p.add_argument("--render-slots", type=int, default=1 << 18, help="rays in flight in the inference renderer")
     p.add_argument("--render-cap", type=int, default=8, help="march_steps_cap of the inference renderer")
@@ -169,24 +176,25 @@ def cpu_baseline(args, scene_np, rank_cores: int) -> dict:
 ALGO = {}
 
 
-def algorithmic(name: str, R: int, S: int, P: int, G: int) -> tuple:
+def algorithmic(name: str, R: int, S: int, P: int, G: int, tb: int = 4, eb: int = 4) -> tuple:
     """Algorithmic bytes (or FLOPs) of one launch of each entry point (minimum DRAM traffic: every
-    input read once, every output written once).  P = hash-table rows (2 floats each)."""
+    input read once, every output written once).  P = hash-table rows (2 values each); tb / eb =
+    bytes of one table value / one encoding value (4, or 2 in the 16-bit forms)."""
     slots = S // 48
     if name in ("march_rays", "ngp_march_rays_train"):
         return ("hbm", 45 * R + 36 * S + G ** 3 // 8)
-    if name == "ngp_hashgrid_forward":
-        return ("hbm", S * (12 + 128) + 8 * P)
-    if name == "ngp_hashgrid_backward":
-        return ("hbm", S * (12 + 128) + 2 * 8 * P)
-    if name in ("ngp_field_forward", "ngp_field_forward_bf16"):
+    if name in ("ngp_hashgrid_forward", "ngp_hashgrid_forward_mixed"):
+        return ("hbm", S * (12 + 32 * eb) + 2 * tb * P)
+    if name in ("ngp_hashgrid_backward", "ngp_hashgrid_backward_mixed"):
+        return ("hbm", S * (12 + 32 * eb) + 2 * 8 * P)
+    if name in ("ngp_field_forward", "ngp_field_forward_bf16", "ngp_field_forward_mixed"):
         return ("flop", 18816 * S)
-    if name in ("ngp_field_backward", "ngp_field_backward_bf16"):
+    if name in ("ngp_field_backward", "ngp_field_backward_bf16", "ngp_field_backward_mixed"):
         return ("flop", 3 * 18816 * S)
     if name == "ngp_integrate_loss_backward":
         return ("hbm", R * 33 + S * 40)
-    if name == "ngp_adam":   # the table's and the MLP's launches alternate: their mean
-        return ("hbm", 7 * 4 * (2 * P + 9408) // 2)
+    if name in ("ngp_adam", "ngp_adam_mixed"):   # the table's and the MLP's launches alternate: their mean
+        return ("hbm", (7 * 4 * (2 * P + 9408) + (2 * tb * P if tb == 2 else 0)) // 2)
     if name == "ngp_proposal_mlp_forward":   # the bins of a step: 8 -> 64 -> 64 -> 1
         return ("flop", 2 * 4672 * slots * 64)
     if name == "ngp_proposal_sample":        # 64 bin values + ray + interval in, 48 samples out
@@ -194,6 +202,20 @@ def algorithmic(name: str, R: int, S: int, P: int, G: int) -> tuple:
     if name == "ngp_proposal_rays":
         return ("hbm", R * (32 + 9) + slots * 12 + (G // 8) ** 3)
     return ("hbm", 0)
+
+
+def dtype_of(form: str) -> str:
+    precision, _, table, half_act = FORMS[form]
+    if precision == "fp32":
+        return "f32"
+    parts = [f"field MLP {precision} operands, f32 accumulation"]
+    if table != "fp32":
+        parts.append(f"{table} copy of the f32 table for the gather")
+    if half_act:
+        parts.append(f"{precision} encodings and encoding gradients")
+    if precision == "fp16":
+        parts.append("dynamic loss scale")
+    return "f32 (" + "; ".join(parts) + ")"
 
 
 FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # SMs x FP32 lanes x FMA x max clock
@@ -216,7 +238,7 @@ def setup_device(args):
     return world, rank, local
 
 
-def run_ours(args, data, precision: str, sampler: str, with_render: bool) -> dict:
+def run_ours(args, data, form: str, with_render: bool) -> dict:
     import numpy as np
     import torch
     import torch.distributed as dist
@@ -228,7 +250,9 @@ def run_ours(args, data, precision: str, sampler: str, with_render: bool) -> dic
     from jaxngp_gb300.trainer import NGPTrainer, TrainConfig
 
     L.lib().ngp_kernel_launches.restype = __import__("ctypes").c_ulonglong
-    cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=precision, sampler=sampler)
+    precision, sampler, table, half_act = FORMS[form]
+    cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=precision, sampler=sampler,
+                      table_precision=table, half_activations=half_act)
     tr = NGPTrainer(data, cfg)
     tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
@@ -314,7 +338,8 @@ def run_ours(args, data, precision: str, sampler: str, with_render: bool) -> dic
     breakdown = {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 5), "share": round(sum(v) / total, 4)}
                  for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1]))}
     top = next(iter(breakdown))
-    bound_kind, units = algorithmic(top, R, int(samples_used), tr.table.n_params, cfg.G)
+    bound_kind, units = algorithmic(top, R, int(samples_used), tr.table.n_params, cfg.G,
+                                    2 if table != "fp32" else 4, 2 if half_act else 4)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     avg_s = breakdown[top]["avg_ms"] / 1e3
@@ -348,7 +373,7 @@ def run_ours(args, data, precision: str, sampler: str, with_render: bool) -> dic
 
     out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == "fp32" else "f32 (field MLP bf16 operands, f32 accumulation)",
+           "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(form),
            "data": "synthetic (procedural 64-blob scene, GT by 4096-step quadrature; NeRF-synthetic not used)",
            "config": {"workload": WORKLOAD, "rays_per_step": R, "sample_budget": args.samples,
                       "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,
@@ -453,8 +478,7 @@ def main():
     forms = [f.strip() for f in args.forms.split(",") if f.strip()]
     results = {}
     for f in forms:
-        precision, sampler = FORMS[f]
-        results[f] = run_ours(args, data, precision, sampler, with_render=True)
+        results[f] = run_ours(args, data, f, with_render=True)
     head = results[forms[0]]
     out = dict(head)
     out["config"] = dict(head["config"], form=forms[0])
@@ -465,13 +489,17 @@ def main():
                             "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
                             "top_kernels": dict(list(r["kernels"].items())[:6])}
                         for f, r in results.items()}
-        if "fp32-march" in results and "bf16-proposal" in results:
-            a, b = results["fp32-march"], results["bf16-proposal"]
-            out["learned_proposal_vs_plain"] = {
-                "train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
-                "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
-                "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3),
-                "plain": "fp32-march", "proposal": "bf16-proposal"}
+        if "fp32-march" in results:
+            a = results["fp32-march"]
+            cmp = {}
+            for f, b in results.items():
+                if FORMS[f][1] != "proposal":
+                    continue
+                cmp[f] = {"train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
+                          "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
+                          "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3)}
+            if cmp:
+                out["learned_proposal_vs_plain"] = {"plain": "fp32-march", **cmp}
     if rank == 0:
         if not args.no_cpu_baseline:
             from jaxngp_gb300.scene import BlobScene, PinholeCamera, hemisphere_poses, poses_to_transforms

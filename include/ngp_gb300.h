@@ -378,6 +378,103 @@ typedef struct NgpAdamDescriptor {
 void ngp_adam(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_adam_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* ------------------------------------------------------------------ mixed precision */
+/* No counterpart in the reference (its encoder table, activations and gradients are FP32).
+ * 16-bit storage types: NGP_DTYPE_BF16 (8-bit exponent) and NGP_DTYPE_F16 (5-bit exponent, so
+ * gradients need loss scaling); arithmetic accumulates in FP32 throughout and gradients reach the
+ * FP32 parameters through FP32 atomics and sums. */
+#define NGP_DTYPE_F32 0u
+#define NGP_DTYPE_BF16 1u
+#define NGP_DTYPE_F16 2u
+
+/* Dynamic loss scale, kept on the device (16 bytes).  The field backward multiplies its incoming
+ * gradient by `scale` and sets `overflow` when a value it stores does not fit its type; the Adam
+ * update skips a step with `overflow` set (and divides the gradients by `scale` otherwise);
+ * ngp_loss_scale_update then adjusts `scale` and clears `overflow`.  `skipped_steps` counts the
+ * skipped updates (the Adam bias correction uses step - skipped_steps). */
+typedef struct NgpLossScale {
+    float scale;
+    uint32_t overflow;
+    uint32_t good_steps;     /* updates since the last change of scale */
+    uint32_t skipped_steps;
+} NgpLossScale;
+
+typedef struct NgpLossScaleDescriptor {
+    float growth_factor;     /* 2 */
+    float backoff_factor;    /* 0.5 */
+    uint32_t growth_interval;/* 2000 updates without overflow double the scale */
+    float max_scale;         /* 2^24 */
+    float min_scale;         /* 1 */
+} NgpLossScaleDescriptor;
+
+/* After both Adam updates of a step: on overflow, scale *= backoff (not below min_scale),
+ * good_steps = 0, skipped_steps += 1; else good_steps += 1 and every growth_interval such steps
+ * scale *= growth (not above max_scale).  Clears overflow.
+ * buffers: loss_scale NgpLossScale[1] (updated in place, passed as the result). */
+void ngp_loss_scale_update(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_loss_scale_update_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+typedef struct NgpFieldMixedDescriptor {
+    uint32_t n_samples;
+    uint32_t accumulate;     /* backward only: add into dL_dweights instead of overwriting */
+    uint32_t operand;        /* MMA operand type: NGP_DTYPE_BF16 or NGP_DTYPE_F16 */
+    uint32_t activations;    /* storage of encodings and dL_dencodings: NGP_DTYPE_F32 or `operand` */
+} NgpFieldMixedDescriptor;
+
+/* The field ops on the tensor cores with a chosen 16-bit operand type, FP32 accumulation and
+ * FP32 outputs (drgbs, sigma, dL_dweights).  Encodings (and their gradient) are FP32 or stored in
+ * the operand type; 16-bit encodings give the same result as their FP32 values, since those are
+ * rounded to the operand type on the way into the first MMA.
+ * forward:  encodings, dirs f32[S,3], weights f32[9408], active_count u32[1] or NULL -> drgbs f32[S,4]
+ * density:  encodings, weights -> sigma f32[S]
+ * backward: encodings, dirs, weights, dL_ddrgbs f32[S,4], active_count or NULL, grad_scale f32[1]
+ *           or NULL, loss_scale NgpLossScale[1] or NULL, scratch f32[ngp_field_backward_scratch_floats()]
+ *           -> dL_dencodings, dL_dweights f32[9408]
+ * opaque: NgpFieldMixedDescriptor.  With a loss scale the gradients come out multiplied by its
+ * scale, and a value that overflows its 16-bit type sets its overflow flag. */
+void ngp_field_forward_mixed(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_forward_mixed_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+void ngp_field_density_mixed(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_density_mixed_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+void ngp_field_backward_mixed(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_field_backward_mixed_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+typedef struct NgpHashGridMixedDescriptor {
+    NgpHashGridDescriptor grid;
+    uint32_t table;          /* forward: latents' type (NGP_DTYPE_F32, _BF16 or _F16) */
+    uint32_t encodings;      /* encodings / dL_dencodings type (NGP_DTYPE_F32, _BF16 or _F16) */
+} NgpHashGridMixedDescriptor;
+
+/* ngp_hashgrid_forward reading a 16-bit copy of the latent table and/or writing 16-bit encodings:
+ * the corner values are widened to FP32 and interpolated in the FP32 order of the FP32 op, the
+ * result rounded once to the encodings' type.
+ * buffers: pos f32[N,3], latents [P,2] of `table`, active_count u32[1] or NULL -> encodings [N,L*2]
+ * of `encodings`.  opaque: NgpHashGridMixedDescriptor. */
+void ngp_hashgrid_forward_mixed(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_hashgrid_forward_mixed_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* ngp_hashgrid_backward with dL_dencodings of type `encodings` (`table` is ignored: the gradient
+ * table is FP32, accumulated with FP32 atomics).
+ * buffers: pos f32[N,3], dL_dencodings [N,L*2], active_count u32[1] or NULL -> dL_dlatents f32[P,2].
+ * opaque: NgpHashGridMixedDescriptor. */
+void ngp_hashgrid_backward_mixed(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_hashgrid_backward_mixed_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+typedef struct NgpAdamMixedDescriptor {
+    NgpAdamDescriptor adam;
+    uint32_t half_copy;      /* NGP_DTYPE_BF16 / _F16: also write the updated params in that type;
+                              * NGP_DTYPE_F32: no copy */
+} NgpAdamMixedDescriptor;
+
+/* ngp_adam on FP32 master parameters with a dynamic loss scale and a 16-bit working copy.  With a
+ * loss scale: a step whose overflow flag is set leaves params and moments unchanged (the gradient
+ * is still zeroed when zero_grad is set); otherwise the gradient is divided by the scale first and
+ * the bias correction uses step - skipped_steps.  Without one this is ngp_adam.
+ * buffers: params f32[n], grads f32[n], m f32[n], v f32[n], loss_scale NgpLossScale[1] or NULL
+ * -> params_half [n] of half_copy (or NULL).  opaque: NgpAdamMixedDescriptor. */
+void ngp_adam_mixed(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_adam_mixed_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* ------------------------------------------------------------------ synthetic scene data */
 typedef struct NgpRenderBlobsDescriptor {
     uint32_t n_rays;       /* pixels to render: view0 * H * W onwards, n_rays of them */

@@ -111,6 +111,26 @@ class NgpRenderBlobsDescriptor(_Desc):
                 ("cx", c_f32), ("cy", c_f32), ("bound", c_f32)]
 
 
+DTYPE_F32, DTYPE_BF16, DTYPE_F16 = 0, 1, 2
+
+
+class NgpLossScaleDescriptor(_Desc):
+    _fields_ = [("growth_factor", c_f32), ("backoff_factor", c_f32), ("growth_interval", c_u32), ("max_scale", c_f32),
+                ("min_scale", c_f32)]
+
+
+class NgpFieldMixedDescriptor(_Desc):
+    _fields_ = [("n_samples", c_u32), ("accumulate", c_u32), ("operand", c_u32), ("activations", c_u32)]
+
+
+class NgpHashGridMixedDescriptor(_Desc):
+    _fields_ = [("grid", NgpHashGridDescriptor), ("table", c_u32), ("encodings", c_u32)]
+
+
+class NgpAdamMixedDescriptor(_Desc):
+    _fields_ = [("adam", NgpAdamDescriptor), ("half_copy", c_u32)]
+
+
 # ------------------------------------------------------------------------------------ loading
 
 _lib = None

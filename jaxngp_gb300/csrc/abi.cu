@@ -46,13 +46,26 @@ int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, cons
                         const float *, const float *, const float *, float *, float *, float *, bool);
 std::size_t mlp_partials_floats();
 int launch_mlp_partials_reduce(cudaStream_t, unsigned, const float *, float *, bool, std::uint32_t, const std::uint32_t *,
-                               float *);
+                               float *, unsigned);
 int launch_mlp_bf16_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                             const float *, float *);
 int launch_mlp_bf16_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
 int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                              const float *, const float *, const float *, float *, float *, unsigned *);
 int device_status();
+int launch_mlp_tc_forward(cudaStream_t, std::uint32_t, bool, std::uint32_t, const std::uint32_t *, const void *,
+                          const float *, const float *, float *);
+int launch_mlp_tc_density(cudaStream_t, std::uint32_t, bool, std::uint32_t, const void *, const float *, float *);
+int launch_mlp_tc_backward(cudaStream_t, std::uint32_t, bool, std::uint32_t, const std::uint32_t *, const void *,
+                           const float *, const float *, const float *, const float *, NgpLossScale *, void *, float *,
+                           unsigned *);
+int launch_hashgrid_forward_mixed(cudaStream_t, const NgpHashGridDescriptor &, std::uint32_t, std::uint32_t,
+                                  const std::uint32_t *, const float *, const void *, void *);
+int launch_hashgrid_backward_mixed(cudaStream_t, const NgpHashGridDescriptor &, std::uint32_t, const std::uint32_t *,
+                                   const float *, const void *, float *, bool);
+int launch_adam_mixed(cudaStream_t, const NgpAdamDescriptor &, std::uint32_t, float *, float *, float *, float *,
+                      const NgpLossScale *, void *);
+int launch_loss_scale_update(cudaStream_t, const NgpLossScaleDescriptor &, NgpLossScale *);
 int launch_proposal_coarse(cudaStream_t, std::uint32_t, const std::uint8_t *, std::uint8_t *);
 int launch_proposal_rays(cudaStream_t, std::uint32_t, std::uint32_t, std::uint32_t, std::uint32_t, float, const float *,
                          const float *,
@@ -315,7 +328,58 @@ NGP_ENTRY(ngp_field_backward_bf16) {
     const int st = launch_mlp_bf16_backward(stream, d.n_samples, CU32(4), CF32(0), CF32(1), CF32(2), CF32(3), CF32(5),
                                             F32(7), F32(6), &parts);
     if (st != NGP_OK) return st;
-    return launch_mlp_partials_reduce(stream, parts, CF32(6), F32(8), d.accumulate != 0, d.n_samples, CU32(4), F32(7));
+    return launch_mlp_partials_reduce(stream, parts, CF32(6), F32(8), d.accumulate != 0, d.n_samples, CU32(4), F32(7), 32u);
+}
+
+NGP_ENTRY(ngp_field_forward_mixed) {
+    NGP_DESC(NgpFieldMixedDescriptor, d);
+    NGP_CHECK_ARG(d.activations == NGP_DTYPE_F32 || d.activations == d.operand,
+                  "field (mixed): activations must be FP32 or the operand type");
+    return launch_mlp_tc_forward(stream, d.operand, d.activations != NGP_DTYPE_F32, d.n_samples, CU32(3), buffers[0],
+                                 CF32(1), CF32(2), F32(4));
+}
+
+NGP_ENTRY(ngp_field_density_mixed) {
+    NGP_DESC(NgpFieldMixedDescriptor, d);
+    NGP_CHECK_ARG(d.activations == NGP_DTYPE_F32 || d.activations == d.operand,
+                  "field (mixed): activations must be FP32 or the operand type");
+    return launch_mlp_tc_density(stream, d.operand, d.activations != NGP_DTYPE_F32, d.n_samples, buffers[0], CF32(1),
+                                 F32(2));
+}
+
+NGP_ENTRY(ngp_field_backward_mixed) {
+    NGP_DESC(NgpFieldMixedDescriptor, d);
+    NGP_CHECK_ARG(d.activations == NGP_DTYPE_F32 || d.activations == d.operand,
+                  "field (mixed): activations must be FP32 or the operand type");
+    unsigned parts = 0;
+    const int st = launch_mlp_tc_backward(stream, d.operand, d.activations != NGP_DTYPE_F32, d.n_samples, CU32(4),
+                                          buffers[0], CF32(1), CF32(2), CF32(3), CF32(5),
+                                          static_cast<NgpLossScale *>(buffers[6]), buffers[8], F32(7), &parts);
+    if (st != NGP_OK) return st;
+    return launch_mlp_partials_reduce(stream, parts, CF32(7), F32(9), d.accumulate != 0, d.n_samples, CU32(4), F32(8),
+                                      d.activations != NGP_DTYPE_F32 ? 16u : 32u);
+}
+
+NGP_ENTRY(ngp_hashgrid_forward_mixed) {
+    NGP_DESC(NgpHashGridMixedDescriptor, d);
+    return launch_hashgrid_forward_mixed(stream, d.grid, d.table, d.encodings, CU32(2), CF32(0), buffers[1], buffers[3]);
+}
+
+NGP_ENTRY(ngp_hashgrid_backward_mixed) {
+    NGP_DESC(NgpHashGridMixedDescriptor, d);
+    return launch_hashgrid_backward_mixed(stream, d.grid, d.encodings, CU32(2), CF32(0), buffers[1], F32(3),
+                                          d.grid.accumulate != 0);
+}
+
+NGP_ENTRY(ngp_adam_mixed) {
+    NGP_DESC(NgpAdamMixedDescriptor, d);
+    return launch_adam_mixed(stream, d.adam, d.half_copy, F32(0), F32(1), F32(2), F32(3),
+                             static_cast<const NgpLossScale *>(buffers[4]), buffers[5]);
+}
+
+NGP_ENTRY(ngp_loss_scale_update) {
+    NGP_DESC(NgpLossScaleDescriptor, d);
+    return launch_loss_scale_update(stream, d, static_cast<NgpLossScale *>(buffers[0]));
 }
 
 NGP_ENTRY(ngp_field_backward_noalloc) {

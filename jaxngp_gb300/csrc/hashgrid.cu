@@ -19,6 +19,7 @@
 //            (frac = modf's fractional part, signed like the coordinate)
 //   enc    = sum over corners in corner order               encoders.py:231
 #include "common.cuh"
+#include "half.cuh"
 
 namespace ngp {
 namespace {
@@ -26,6 +27,25 @@ namespace {
 struct Corner8 {
     std::uint32_t idx[8];
     float w[8];
+};
+
+// Storage of a [rows][2] array (latent table, encodings, their gradients): FP32 pairs, or pairs of
+// a 16-bit type packed in one 32-bit word.  get() widens to FP32; put() rounds to the type.
+struct PairF32 {
+    static __device__ __forceinline__ float2 get(const void *a, std::size_t i) {
+        return __ldg(reinterpret_cast<const float2 *>(a) + i);
+    }
+    static __device__ __forceinline__ void put(void *a, std::size_t i, float2 v) { reinterpret_cast<float2 *>(a)[i] = v; }
+};
+
+template <class E>
+struct PairHalf {
+    static __device__ __forceinline__ float2 get(const void *a, std::size_t i) {
+        return E::unpack(__ldg(reinterpret_cast<const std::uint32_t *>(a) + i));
+    }
+    static __device__ __forceinline__ void put(void *a, std::size_t i, float2 v) {
+        reinterpret_cast<std::uint32_t *>(a)[i] = E::pack(v.x, v.y);
+    }
 };
 
 // `tmask` = T - 1 when T is a power of two (then h mod T = h & tmask), else 0.
@@ -68,9 +88,10 @@ __device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, st
 // through shared memory as one contiguous block.
 constexpr int kHgTile = 32, kHgRow = NGP_MAX_LEVELS + 1;   // padded row: lanes hit different banks
 
+template <class Tab, class Enc>
 __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
     NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
-    const float *__restrict__ pos, const float2 *__restrict__ latents, float2 *__restrict__ enc) {
+    const float *__restrict__ pos, const void *__restrict__ latents, void *__restrict__ enc) {
     __shared__ float2 rows[kHgTile * kHgRow];
     std::uint32_t n_active = n_points;
     if (count != nullptr) n_active = min(n_active, *count);
@@ -93,7 +114,7 @@ __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
                 level_corners(d, l, tmask, px, py, pz, c);
                 float2 v[8];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) v[k] = __ldg(latents + c.idx[k]);
+                for (int k = 0; k < 8; ++k) v[k] = Tab::get(latents, c.idx[k]);
                 float a0 = __fmul_rn(v[0].x, c.w[0]), a1 = __fmul_rn(v[0].y, c.w[0]);
 #pragma unroll
                 for (int k = 1; k < 8; ++k) {
@@ -106,8 +127,8 @@ __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
         }
         __syncthreads();
         const std::uint32_t n_rows = min((std::uint32_t)kHgTile, n_active - tile * kHgTile);
-        float2 *dst = enc + (std::size_t)tile * kHgTile * L;
-        for (std::uint32_t i = threadIdx.x; i < n_rows * L; i += blockDim.x) dst[i] = rows[(i / L) * kHgRow + i % L];
+        const std::size_t dst = (std::size_t)tile * kHgTile * L;
+        for (std::uint32_t i = threadIdx.x; i < n_rows * L; i += blockDim.x) Enc::put(enc, dst + i, rows[(i / L) * kHgRow + i % L]);
         __syncthreads();
     }
 }
@@ -119,9 +140,10 @@ __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
 // segmented warp reduction and their last lane issues the one float2 atomic for the run.  Levels
 // where no two neighbouring lanes share a corner issue one atomic per lane.  Points whose incoming
 // gradient is zero at that level (samples past a ray's termination) contribute nothing.
+template <class Enc>
 __global__ void __launch_bounds__(256) hashgrid_backward_kernel(
     NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
-    const float *__restrict__ pos, const float2 *__restrict__ dL_denc, float2 *__restrict__ dL_dlat) {
+    const float *__restrict__ pos, const void *__restrict__ dL_denc, float2 *__restrict__ dL_dlat) {
     std::uint32_t n_active = n_points;
     if (count != nullptr) n_active = min(n_active, *count);
     const std::uint32_t tmask = (d.T & (d.T - 1u)) == 0u ? d.T - 1u : 0u;
@@ -136,7 +158,7 @@ __global__ void __launch_bounds__(256) hashgrid_backward_kernel(
         float2 g = make_float2(0.f, 0.f);
         Corner8 c;
         if (in) {
-            g = dL_denc[(std::size_t)n * d.L + l];
+            g = Enc::get(dL_denc, (std::size_t)n * d.L + l);
             level_corners(d, l, tmask, pos[(std::size_t)n * 3 + 0], pos[(std::size_t)n * 3 + 1], pos[(std::size_t)n * 3 + 2], c);
         } else {
 #pragma unroll
@@ -186,17 +208,72 @@ int check_hashgrid_descriptor(const NgpHashGridDescriptor &d) {
     return NGP_OK;
 }
 
+namespace {
+
+bool valid_dtype(std::uint32_t t) { return t == NGP_DTYPE_F32 || t == NGP_DTYPE_BF16 || t == NGP_DTYPE_F16; }
+
+template <class Tab>
+void forward_for_table(cudaStream_t stream, std::uint32_t enc_type, unsigned grid, const NgpHashGridDescriptor &d,
+                       const std::uint32_t *count, const float *pos, const void *latents, void *enc) {
+    if (enc_type == NGP_DTYPE_BF16)
+        hashgrid_forward_kernel<Tab, PairHalf<Bf16Op>><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
+    else if (enc_type == NGP_DTYPE_F16)
+        hashgrid_forward_kernel<Tab, PairHalf<F16Op>><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
+    else
+        hashgrid_forward_kernel<Tab, PairF32><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
+}
+
+}  // namespace
+
+int launch_hashgrid_forward_mixed(cudaStream_t stream, const NgpHashGridDescriptor &d, std::uint32_t table_type,
+                                  std::uint32_t enc_type, const std::uint32_t *count, const float *pos,
+                                  const void *latents, void *enc) {
+    int st = check_hashgrid_descriptor(d);
+    if (st != NGP_OK) return st;
+    NGP_CHECK_ARG(valid_dtype(table_type) && valid_dtype(enc_type), "hashgrid: unknown table or encoding type");
+    const std::uintptr_t a = table_type == NGP_DTYPE_F32 ? 7u : 3u, b = enc_type == NGP_DTYPE_F32 ? 7u : 3u;
+    NGP_CHECK_ARG(((std::uintptr_t)latents & a) == 0 && ((std::uintptr_t)enc & b) == 0,
+                  "hashgrid: latents and encodings must be aligned to one row of two features");
+    const std::size_t tiles = ((std::size_t)d.n_coords + kHgTile - 1) / kHgTile;
+    if (tiles > 0) {
+        const unsigned grid = grid_for(tiles, 1, 8);
+        if (table_type == NGP_DTYPE_BF16)
+            forward_for_table<PairHalf<Bf16Op>>(stream, enc_type, grid, d, count, pos, latents, enc);
+        else if (table_type == NGP_DTYPE_F16)
+            forward_for_table<PairHalf<F16Op>>(stream, enc_type, grid, d, count, pos, latents, enc);
+        else
+            forward_for_table<PairF32>(stream, enc_type, grid, d, count, pos, latents, enc);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
 int launch_hashgrid_forward(cudaStream_t stream, const NgpHashGridDescriptor &d,
                             const std::uint32_t *count, const float *pos, const float *latents,
                             float *enc) {
+    return launch_hashgrid_forward_mixed(stream, d, NGP_DTYPE_F32, NGP_DTYPE_F32, count, pos, latents, enc);
+}
+
+int launch_hashgrid_backward_mixed(cudaStream_t stream, const NgpHashGridDescriptor &d, std::uint32_t enc_type,
+                                   const std::uint32_t *count, const float *pos, const void *dL_denc,
+                                   float *dL_dlatents, bool accumulate) {
     int st = check_hashgrid_descriptor(d);
     if (st != NGP_OK) return st;
-    NGP_CHECK_ARG(((std::uintptr_t)latents & 7u) == 0 && ((std::uintptr_t)enc & 7u) == 0,
-                  "hashgrid: latents and encodings must be 8-byte aligned");
-    const std::size_t tiles = ((std::size_t)d.n_coords + kHgTile - 1) / kHgTile;
-    if (tiles > 0) {
-        hashgrid_forward_kernel<<<grid_for(tiles, 1, 8), 256, 0, stream>>>(
-            d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(latents), reinterpret_cast<float2 *>(enc));
+    NGP_CHECK_ARG(valid_dtype(enc_type), "hashgrid: unknown encoding type");
+    const std::uintptr_t b = enc_type == NGP_DTYPE_F32 ? 7u : 3u;
+    NGP_CHECK_ARG(((std::uintptr_t)dL_denc & b) == 0 && ((std::uintptr_t)dL_dlatents & 7u) == 0,
+                  "hashgrid: gradients must be aligned to one row of two features");
+    if (!accumulate) NGP_CUDA_TRY(cudaMemsetAsync(dL_dlatents, 0, (std::size_t)d.n_params * 2 * sizeof(float), stream));
+    const std::size_t items = (std::size_t)((d.n_coords + 31) / 32) * 32 * d.L;
+    if (items > 0) {
+        const unsigned grid = grid_for(items, 256, 8);
+        float2 *out = reinterpret_cast<float2 *>(dL_dlatents);
+        if (enc_type == NGP_DTYPE_BF16)
+            hashgrid_backward_kernel<PairHalf<Bf16Op>><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, dL_denc, out);
+        else if (enc_type == NGP_DTYPE_F16)
+            hashgrid_backward_kernel<PairHalf<F16Op>><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, dL_denc, out);
+        else
+            hashgrid_backward_kernel<PairF32><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, dL_denc, out);
         count_launches(1);
     }
     return launch_status();
@@ -205,18 +282,7 @@ int launch_hashgrid_forward(cudaStream_t stream, const NgpHashGridDescriptor &d,
 int launch_hashgrid_backward(cudaStream_t stream, const NgpHashGridDescriptor &d,
                              const std::uint32_t *count, const float *pos, const float *dL_denc,
                              float *dL_dlatents, bool accumulate) {
-    int st = check_hashgrid_descriptor(d);
-    if (st != NGP_OK) return st;
-    NGP_CHECK_ARG(((std::uintptr_t)dL_denc & 7u) == 0 && ((std::uintptr_t)dL_dlatents & 7u) == 0,
-                  "hashgrid: gradients must be 8-byte aligned");
-    if (!accumulate) NGP_CUDA_TRY(cudaMemsetAsync(dL_dlatents, 0, (std::size_t)d.n_params * 2 * sizeof(float), stream));
-    const std::size_t items = (std::size_t)((d.n_coords + 31) / 32) * 32 * d.L;
-    if (items > 0) {
-        hashgrid_backward_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(
-            d, d.n_coords, count, pos, reinterpret_cast<const float2 *>(dL_denc), reinterpret_cast<float2 *>(dL_dlatents));
-        count_launches(1);
-    }
-    return launch_status();
+    return launch_hashgrid_backward_mixed(stream, d, NGP_DTYPE_F32, count, pos, dL_denc, dL_dlatents, accumulate);
 }
 
 }  // namespace ngp

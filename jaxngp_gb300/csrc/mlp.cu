@@ -704,12 +704,15 @@ int launch_prop_backward(cudaStream_t stream, std::uint32_t n, const std::uint32
 
 // Sums `parts` dL/dW partials into dL_dweights (fixed order) and zeroes dL/denc rows past the
 // active count: the tail shared by the FP32 and BF16 field backwards.
+// Sums the per-CTA dL/dW partials in CTA order and zeroes the dL/denc rows past the active count
+// (`row_floats` 32-bit words per row: 32 for FP32 encodings, 16 for 16-bit ones).
 int launch_mlp_partials_reduce(cudaStream_t stream, unsigned parts, const float *partials, float *dL_dweights,
-                               bool accumulate, std::uint32_t n, const std::uint32_t *count, float *dL_denc) {
+                               bool accumulate, std::uint32_t n, const std::uint32_t *count, float *dL_denc,
+                               unsigned row_floats) {
     reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(parts, partials, dL_dweights, accumulate ? 1 : 0);
     count_launches(1);
     if (count != nullptr && n > 0) {
-        zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
+        zero_rows_kernel<<<grid_for((std::size_t)n * row_floats, 256, 4), 256, 0, stream>>>(n, count, dL_denc, row_floats);
         count_launches(1);
     }
     return launch_status();

@@ -25,6 +25,7 @@
 // Every mbarrier wait gives up after kWaitLimit polls; the warpgroup then stops, records
 // NGP_ERR_DEVICE for ngp_device_status(), and releases its tensor memory.
 #include "common.cuh"
+#include "half.cuh"
 #include "tc.cuh"
 
 namespace ngp {
@@ -59,40 +60,48 @@ __device__ __forceinline__ std::uint32_t active_count(std::uint32_t n, const std
 
 bool aligned16(const void *p) { return ((std::uintptr_t)p & 15u) == 0; }
 
-// Element offset of X[r][c] in a row-block buffer with `cols` BF16 columns.
+// Element offset of X[r][c] in a row-block buffer with `cols` 16-bit columns.
 __device__ __forceinline__ int rb(int r, int c, int cols) {
     return (r >> 3) * (cols * 8) + (c >> 3) * 64 + (r & 7) * 8 + (c & 7);
 }
 
 // Stores v[0..n) as row r of a buffer with n columns (n % 8 == 0), 16 bytes at a time.
-template <int N>
-__device__ __forceinline__ void store_row(__nv_bfloat16 *buf, int r, const float *v) {
+template <class E, int N>
+__device__ __forceinline__ void store_row(typename E::T *buf, int r, const float *v) {
 #pragma unroll
     for (int c = 0; c < N; c += 8) {
         uint4 q;
-        q.x = tc::pack_bf16(v[c + 0], v[c + 1]);
-        q.y = tc::pack_bf16(v[c + 2], v[c + 3]);
-        q.z = tc::pack_bf16(v[c + 4], v[c + 5]);
-        q.w = tc::pack_bf16(v[c + 6], v[c + 7]);
+        q.x = E::pack(v[c + 0], v[c + 1]);
+        q.y = E::pack(v[c + 2], v[c + 3]);
+        q.z = E::pack(v[c + 4], v[c + 5]);
+        q.w = E::pack(v[c + 6], v[c + 7]);
         *reinterpret_cast<uint4 *>(buf + rb(r, c, N)) = q;
     }
 }
 
 // Loads row r of a buffer with N columns.
-template <int N>
-__device__ __forceinline__ void load_row(const __nv_bfloat16 *buf, int r, float *v) {
+template <class E, int N>
+__device__ __forceinline__ void load_row(const typename E::T *buf, int r, float *v) {
 #pragma unroll
     for (int c = 0; c < N; c += 8) {
         const uint4 q = *reinterpret_cast<const uint4 *>(buf + rb(r, c, N));
         const std::uint32_t w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&w[j]);
-            const float2 f = __bfloat1622float2(h);
+            const float2 f = E::unpack(w[j]);
             v[c + 2 * j] = f.x;
             v[c + 2 * j + 1] = f.y;
         }
     }
+}
+
+// False when a value is NaN or would not fit the 16-bit type (the overflow test of loss scaling).
+template <class E, int N>
+__device__ __forceinline__ bool row_fits(const float *v) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < N; ++i) ok &= fabsf(v[i]) <= E::kMax;
+    return ok;
 }
 
 __device__ __forceinline__ void sh4(float x, float y, float z, float *o) {
@@ -115,14 +124,16 @@ __device__ __forceinline__ void sh4(float x, float y, float z, float *o) {
     o[15] = 0.59004358992664352f * x * (-x2 + 3.0f * y2);
 }
 
-// Converts the FP32 weights into the BF16 operand layouts (backward copies only when `bwd`).
-__device__ void load_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *sw, bool bwd) {
+// Converts the FP32 weights into the 16-bit operand layouts (backward copies only when `bwd`).
+template <class E>
+__device__ void load_weights_tc(const float *__restrict__ w, typename E::T *sw, bool bwd) {
+    using T = typename E::T;
     const int total = bwd ? kAllW : kFwdW;
-    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    const T zero = E::cvt(0.f);
     for (int i = threadIdx.x; i < total; i += blockDim.x) sw[i] = zero;
     __syncthreads();
     for (int i = threadIdx.x; i < kNW; i += blockDim.x) {
-        const __nv_bfloat16 v = __float2bfloat16(w[i]);
+        const T v = E::cvt(w[i]);
         if (i < kW1) {  // W0 [32][64]
             const int in = i / 64, out = i % 64;
             sw[kF0 + rb(out, in, 32)] = v;
@@ -149,9 +160,10 @@ __device__ void load_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *sw
 
 // D (tmem) = A @ B^T with both operands K-major: A = rows of a buffer with K columns (M = 128
 // samples), B = weight operand [N][K].
-__device__ __forceinline__ void mma_kk(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int K, int N,
+template <class E>
+__device__ __forceinline__ void mma_kk(std::uint32_t d, const typename E::T *a, const typename E::T *b, int K, int N,
                                        bool acc) {
-    const std::uint32_t id = tc::idesc_bf16(128, N, false, false);
+    const std::uint32_t id = tc::idesc_kf16(128, N, E::kFmt, false, false);
     const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), sbo = (std::uint32_t)K * 16;
     for (int j = 0; j < K / 16; ++j)
         tc::mma_bf16(d, tc::sdesc(sa + j * 256, 128, sbo), tc::sdesc(sb + j * 256, 128, sbo), id, acc || j > 0);
@@ -159,8 +171,9 @@ __device__ __forceinline__ void mma_kk(std::uint32_t d, const __nv_bfloat16 *a, 
 
 // D (tmem, M = 64) += A^T @ B over the tile's 128 samples: A = buffer with 64 columns, B = buffer
 // with N columns, both read MN-major (the sample index is the contraction).
-__device__ __forceinline__ void mma_mn(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int N, bool acc) {
-    const std::uint32_t id = tc::idesc_bf16(64, N, true, true);
+template <class E>
+__device__ __forceinline__ void mma_mn(std::uint32_t d, const typename E::T *a, const typename E::T *b, int N, bool acc) {
+    const std::uint32_t id = tc::idesc_kf16(64, N, E::kFmt, true, true);
     const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), la = 64 * 16, lb = (std::uint32_t)N * 16;
     for (int j = 0; j < kRows / 16; ++j)
         tc::mma_bf16(d, tc::sdesc(sa + j * 2 * la, la, 128), tc::sdesc(sb + j * 2 * lb, lb, 128), id, acc || j > 0);
@@ -194,90 +207,145 @@ struct WarpGroup {
     }
 };
 
-// Forward through one tile; on return H1, X2, H2, H3 hold the layer inputs (BF16), and x0 / rgb
-// this thread's pre-activation density and colour.
-__device__ __forceinline__ void tile_forward(WarpGroup &wg, const __nv_bfloat16 *sw, __nv_bfloat16 *act,
-                                             const float dir[3], float &x0, float rgb[3]) {
+// Forward through one tile; on return H1, X2, H2, H3 hold the layer inputs (16-bit), and x0 / rgb
+// this thread's pre-activation density and colour.  With `fits` given, every layer input is also
+// checked against the 16-bit range (loss scaling's overflow test).
+template <class E>
+__device__ __forceinline__ void tile_forward(WarpGroup &wg, const typename E::T *sw, typename E::T *act,
+                                             const float dir[3], float &x0, float rgb[3], bool *fits) {
     float v[64];
     const bool leader = wg.r == 0;
     // layer 0
     wg.sync();
-    if (leader) { mma_kk(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
+    if (leader) { mma_kk<E>(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
     wg.wait();
     tc::ld64(wg.tm + kDA, v);
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
-    store_row<64>(act + kH1, wg.r, v);
+    if (fits) *fits &= row_fits<E, 64>(v);
+    store_row<E, 64>(act + kH1, wg.r, v);
     // layer 1
     wg.sync();
-    if (leader) { mma_kk(wg.tm + kDB, act + kH1, sw + kF1, 64, 16, false); tc::commit(wg.bar); }
+    if (leader) { mma_kk<E>(wg.tm + kDB, act + kH1, sw + kF1, 64, 16, false); tc::commit(wg.bar); }
     wg.wait();
     tc::ld16(wg.tm + kDB, v);
     x0 = v[0];
     sh4(dir[0], dir[1], dir[2], v + 16);
-    store_row<32>(act + kX2, wg.r, v);
+    if (fits) *fits &= row_fits<E, 16>(v);
+    store_row<E, 32>(act + kX2, wg.r, v);
     // layer 2
     wg.sync();
-    if (leader) { mma_kk(wg.tm + kDA, act + kX2, sw + kF2, 32, 64, false); tc::commit(wg.bar); }
+    if (leader) { mma_kk<E>(wg.tm + kDA, act + kX2, sw + kF2, 32, 64, false); tc::commit(wg.bar); }
     wg.wait();
     tc::ld64(wg.tm + kDA, v);
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
-    store_row<64>(act + kH2, wg.r, v);
+    if (fits) *fits &= row_fits<E, 64>(v);
+    store_row<E, 64>(act + kH2, wg.r, v);
     // layer 3
     wg.sync();
-    if (leader) { mma_kk(wg.tm + kDA, act + kH2, sw + kF3, 64, 64, false); tc::commit(wg.bar); }
+    if (leader) { mma_kk<E>(wg.tm + kDA, act + kH2, sw + kF3, 64, 64, false); tc::commit(wg.bar); }
     wg.wait();
     tc::ld64(wg.tm + kDA, v);
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
-    store_row<64>(act + kH3, wg.r, v);
+    if (fits) *fits &= row_fits<E, 64>(v);
+    store_row<E, 64>(act + kH3, wg.r, v);
     // layer 4
     wg.sync();
-    if (leader) { mma_kk(wg.tm + kDB, act + kH3, sw + kF4, 64, 16, false); tc::commit(wg.bar); }
+    if (leader) { mma_kk<E>(wg.tm + kDB, act + kH3, sw + kF4, 64, 16, false); tc::commit(wg.bar); }
     wg.wait();
     tc::ld16(wg.tm + kDB, v);
 #pragma unroll
     for (int c = 0; c < 3; ++c) rgb[c] = 1.f / (1.f + expf(-v[c]));
 }
 
-__device__ __forceinline__ void load_enc_row(const float *__restrict__ enc, std::size_t s, bool valid, float *v) {
+// One sample's encoding row, fetched ahead of its tile: FP32 values (rounded to the operand type
+// when staged) or, with kHalf, the operand type's 32 values as they are stored.
+template <class E, bool kHalf>
+struct EncRow;
+
+template <class E>
+struct EncRow<E, false> {
+    using In = float;
+    float v[32];
+    __device__ __forceinline__ void load(const float *__restrict__ enc, std::size_t s, bool valid) {
 #pragma unroll
-    for (int c = 0; c < 32; c += 4) {
-        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid) q = *reinterpret_cast<const float4 *>(enc + s * 32 + c);
-        v[c] = q.x;
-        v[c + 1] = q.y;
-        v[c + 2] = q.z;
-        v[c + 3] = q.w;
+        for (int c = 0; c < 32; c += 4) {
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) q = *reinterpret_cast<const float4 *>(enc + s * 32 + c);
+            v[c] = q.x;
+            v[c + 1] = q.y;
+            v[c + 2] = q.z;
+            v[c + 3] = q.w;
+        }
+    }
+    __device__ __forceinline__ void stage(typename E::T *buf, int r) const { store_row<E, 32>(buf, r, v); }
+};
+
+template <class E>
+struct EncRow<E, true> {
+    using In = typename E::T;
+    uint4 q[4];
+    __device__ __forceinline__ void load(const In *__restrict__ enc, std::size_t s, bool valid) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(enc + s * 32);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) q[c] = valid ? src[c] : make_uint4(0u, 0u, 0u, 0u);
+    }
+    __device__ __forceinline__ void stage(typename E::T *buf, int r) const {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4 *>(buf + rb(r, c * 8, 32)) = q[c];
+    }
+};
+
+// dL/denc row of one sample: FP32, or the operand type when kHalf.
+template <class E>
+__device__ __forceinline__ void write_denc(float *__restrict__ out, std::size_t s, const float *v) {
+#pragma unroll
+    for (int c = 0; c < 32; c += 4)
+        *reinterpret_cast<float4 *>(out + s * 32 + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+}
+
+template <class E>
+__device__ __forceinline__ void write_denc(typename E::T *__restrict__ out, std::size_t s, const float *v) {
+#pragma unroll
+    for (int c = 0; c < 32; c += 8) {
+        uint4 q;
+        q.x = E::pack(v[c + 0], v[c + 1]);
+        q.y = E::pack(v[c + 2], v[c + 3]);
+        q.z = E::pack(v[c + 4], v[c + 5]);
+        q.w = E::pack(v[c + 6], v[c + 7]);
+        *reinterpret_cast<uint4 *>(out + s * 32 + c) = q;
     }
 }
 
 // Row r of tile `tile`: encoding, direction (+z past the end) and, when `g` is given, dL/ddrgb.
-__device__ __forceinline__ void fetch_row(const float *__restrict__ enc, const float *__restrict__ dirs,
+template <class Row>
+__device__ __forceinline__ void fetch_row(const typename Row::In *__restrict__ enc, const float *__restrict__ dirs,
                                           const float *__restrict__ dL_ddrgb, std::uint32_t tile, int r,
-                                          std::uint32_t n_act, float *v, float *dir, float4 *g) {
+                                          std::uint32_t n_act, Row &row, float *dir, float4 *g) {
     const std::size_t s = (std::size_t)tile * kRows + r;
     const bool valid = s < n_act;
-    load_enc_row(enc, s, valid, v);
+    row.load(enc, s, valid);
     dir[0] = valid ? dirs[s * 3 + 0] : 0.f;
     dir[1] = valid ? dirs[s * 3 + 1] : 0.f;
     dir[2] = valid ? dirs[s * 3 + 2] : 1.f;
     if (g != nullptr) *g = valid ? reinterpret_cast<const float4 *>(dL_ddrgb)[s] : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-template <int NWG>
-__global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_forward_kernel(
-    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+template <class E, bool kHalf, int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_forward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const typename EncRow<E, kHalf>::In *__restrict__ enc,
     const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb) {
+    using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ std::uint64_t bars[NWG];
     __shared__ std::uint32_t tbase;
     __shared__ int fails[NWG];
-    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    T *sw = reinterpret_cast<T *>(smem_raw);
     const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
-    __nv_bfloat16 *act = sw + kFwdW + g * kFwdAct;
-    load_weights_bf16(weights, sw, false);
+    T *act = sw + kFwdW + g * kFwdAct;
+    load_weights_tc<E>(weights, sw, false);
     if (threadIdx.x == 0) {
         for (int k = 0; k < NWG; ++k) {
             tc::mbar_init(&bars[k], 1);
@@ -294,21 +362,18 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_forward_kernel(
     const std::uint32_t n_act = active_count(n, count);
     const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
     const std::uint32_t step = gridDim.x * NWG;
-    float nv[32], nd[3];  // the next tile's row, loaded while the current tile computes
-    fetch_row(enc, dirs, nullptr, blockIdx.x * NWG + g, r, n_act, nv, nd, nullptr);
+    EncRow<E, kHalf> next;  // the next tile's row, loaded while the current tile computes
+    float nd[3];
+    fetch_row(enc, dirs, nullptr, blockIdx.x * NWG + g, r, n_act, next, nd, nullptr);
     for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
-        float v[32], dir[3];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = nv[i];
-        dir[0] = nd[0];
-        dir[1] = nd[1];
-        dir[2] = nd[2];
-        fetch_row(enc, dirs, nullptr, tile + step, r, n_act, nv, nd, nullptr);
-        store_row<32>(act + kX0, r, v);
+        const EncRow<E, kHalf> cur = next;
+        const float dir[3] = {nd[0], nd[1], nd[2]};
+        fetch_row(enc, dirs, nullptr, tile + step, r, n_act, next, nd, nullptr);
+        cur.stage(act + kX0, r);
         float x0, rgb[3];
-        tile_forward(wg, sw, act, dir, x0, rgb);
+        tile_forward<E>(wg, sw, act, dir, x0, rgb, nullptr);
         if (valid) reinterpret_cast<float4 *>(drgb)[s] = make_float4(expf(x0), rgb[0], rgb[1], rgb[2]);
         tc::bar_sync(1 + g, 128);
         if (*wg.fail) break;
@@ -320,17 +385,19 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_forward_kernel(
 }
 
 // sigma only (NeRF.__call__ with dir=None, nerfs.py:71-72): layers 0 and 1.
-template <int NWG>
-__global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_density_kernel(
-    std::uint32_t n, const float *__restrict__ enc, const float *__restrict__ weights, float *__restrict__ sigma) {
+template <class E, bool kHalf, int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_density_kernel(
+    std::uint32_t n, const typename EncRow<E, kHalf>::In *__restrict__ enc, const float *__restrict__ weights,
+    float *__restrict__ sigma) {
+    using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ std::uint64_t bars[NWG];
     __shared__ std::uint32_t tbase;
     __shared__ int fails[NWG];
-    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    T *sw = reinterpret_cast<T *>(smem_raw);
     const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
-    __nv_bfloat16 *act = sw + kFwdW + g * kFwdAct;
-    load_weights_bf16(weights, sw, false);
+    T *act = sw + kFwdW + g * kFwdAct;
+    load_weights_tc<E>(weights, sw, false);
     if (threadIdx.x == 0) {
         for (int k = 0; k < NWG; ++k) {
             tc::mbar_init(&bars[k], 1);
@@ -349,17 +416,20 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_density_kernel(
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n;
         float v[64];
-        load_enc_row(enc, s, valid, v);
-        store_row<32>(act + kX0, r, v);
+        {
+            EncRow<E, kHalf> row;
+            row.load(enc, s, valid);
+            row.stage(act + kX0, r);
+        }
         wg.sync();
-        if (leader) { mma_kk(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
+        if (leader) { mma_kk<E>(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
 #pragma unroll
         for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
-        store_row<64>(act + kH1, r, v);
+        store_row<E, 64>(act + kH1, r, v);
         wg.sync();
-        if (leader) { mma_kk(wg.tm + kDB, act + kH1, sw + kF1, 64, 16, false); tc::commit(wg.bar); }
+        if (leader) { mma_kk<E>(wg.tm + kDB, act + kH1, sw + kF1, 64, 16, false); tc::commit(wg.bar); }
         wg.wait();
         tc::ld16(wg.tm + kDB, v);
         if (valid) sigma[s] = expf(v[0]);
@@ -372,21 +442,25 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_density_kernel(
     if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
 }
 
-// Backward.  `grad_scale` multiplies dL/ddrgb; `partials` receives one [9408] dL/dW partial per CTA.
-template <int NWG>
-__global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_backward_kernel(
-    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+// Backward.  `grad_scale` multiplies dL/ddrgb, and so does the loss scale when `ls` is given; with
+// `ls`, a layer input or gradient that does not fit the 16-bit type (or dL/denc its storage type)
+// sets ls->overflow.  `partials` receives one [9408] dL/dW partial per CTA.
+template <class E, bool kHalf, int NWG>
+__global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const typename EncRow<E, kHalf>::In *__restrict__ enc,
     const float *__restrict__ dirs, const float *__restrict__ weights, const float *__restrict__ dL_ddrgb,
-    const float *__restrict__ grad_scale, float *__restrict__ dL_denc, float *__restrict__ partials) {
+    const float *__restrict__ grad_scale, NgpLossScale *__restrict__ ls,
+    typename EncRow<E, kHalf>::In *__restrict__ dL_denc, float *__restrict__ partials) {
+    using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ std::uint64_t bars[NWG];
     __shared__ std::uint32_t tbase;
     __shared__ int fails[NWG];
     __shared__ int tiles_done[NWG];
-    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    T *sw = reinterpret_cast<T *>(smem_raw);
     const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
-    __nv_bfloat16 *act = sw + kAllW + g * kBwdAct;
-    load_weights_bf16(weights, sw, true);
+    T *act = sw + kAllW + g * kBwdAct;
+    load_weights_tc<E>(weights, sw, true);
     if (threadIdx.x == 0) {
         for (int k = 0; k < NWG; ++k) {
             tc::mbar_init(&bars[k], 1);
@@ -402,29 +476,30 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_backward_kernel(
     const std::uint32_t tm0 = tbase + (std::uint32_t)g * 256u;
     WarpGroup wg{g, r, tm0 + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
     const bool leader = r == 0;
-    const float gs = grad_scale != nullptr ? *grad_scale : 1.f;
+    float gs = grad_scale != nullptr ? *grad_scale : 1.f;
+    if (ls != nullptr) gs *= ls->scale;
+    bool fits = true;
+    bool *check = ls != nullptr ? &fits : nullptr;
 
     const std::uint32_t n_act = active_count(n, count);
     const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
     bool first = true;
     const std::uint32_t step = gridDim.x * NWG;
-    float nv[32], nd[3];  // the next tile's row, loaded while the current tile computes
+    EncRow<E, kHalf> next;  // the next tile's row, loaded while the current tile computes
+    float nd[3];
     float4 ng;
-    fetch_row(enc, dirs, dL_ddrgb, blockIdx.x * NWG + g, r, n_act, nv, nd, &ng);
+    fetch_row(enc, dirs, dL_ddrgb, blockIdx.x * NWG + g, r, n_act, next, nd, &ng);
     for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
-        float v[64], dir[3];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = nv[i];
-        dir[0] = nd[0];
-        dir[1] = nd[1];
-        dir[2] = nd[2];
+        float v[64];
+        const EncRow<E, kHalf> cur = next;
+        const float dir[3] = {nd[0], nd[1], nd[2]};
         const float4 go = ng;
-        fetch_row(enc, dirs, dL_ddrgb, tile + step, r, n_act, nv, nd, &ng);
-        store_row<32>(act + kX0, r, v);
+        fetch_row(enc, dirs, dL_ddrgb, tile + step, r, n_act, next, nd, &ng);
+        cur.stage(act + kX0, r);
         float x0, rgb[3];
-        tile_forward(wg, sw, act, dir, x0, rgb);
+        tile_forward<E>(wg, sw, act, dir, x0, rgb, check);
 
         // output layer: dL/da4 (3, padded to 16) and dL/dx0 through the truncated exponential
         const float dx0 = gs * go.x * expf(fminf(fmaxf(x0, -15.f), 15.f));
@@ -435,85 +510,90 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_bf16_backward_kernel(
             d[0] = gs * go.y * rgb[0] * (1.f - rgb[0]);
             d[1] = gs * go.z * rgb[1] * (1.f - rgb[1]);
             d[2] = gs * go.w * rgb[2] * (1.f - rgb[2]);
-            store_row<16>(act + kDY, r, d);
+            if (check) fits &= row_fits<E, 3>(d);
+            store_row<E, 16>(act + kDY, r, d);
         }
         // layer 4: dW4 += h3^T dA4;  dh3 = dA4 @ W4^T
         wg.sync();
         if (leader) {
-            mma_mn(tm0 + kA4, act + kH3, act + kDY, 16, !first);
-            mma_kk(tm0 + kDA, act + kDY, sw + kG4, 16, 64, false);
+            mma_mn<E>(tm0 + kA4, act + kH3, act + kDY, 16, !first);
+            mma_kk<E>(tm0 + kDA, act + kDY, sw + kG4, 16, 64, false);
             tc::commit(wg.bar);
         }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
         {
             float h[64];
-            load_row<64>(act + kH3, r, h);
+            load_row<E, 64>(act + kH3, r, h);
 #pragma unroll
             for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
         }
-        store_row<64>(act + kH3, r, v);  // dA3 over h3
+        if (check) fits &= row_fits<E, 64>(v);
+        store_row<E, 64>(act + kH3, r, v);  // dA3 over h3
         // layer 3: dW3^T += dA3^T h2;  dh2 = dA3 @ W3^T
         wg.sync();
         if (leader) {
-            mma_mn(tm0 + kA3, act + kH3, act + kH2, 64, !first);
-            mma_kk(tm0 + kDA, act + kH3, sw + kG3, 64, 64, false);
+            mma_mn<E>(tm0 + kA3, act + kH3, act + kH2, 64, !first);
+            mma_kk<E>(tm0 + kDA, act + kH3, sw + kG3, 64, 64, false);
             tc::commit(wg.bar);
         }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
         {
             float h[64];
-            load_row<64>(act + kH2, r, h);
+            load_row<E, 64>(act + kH2, r, h);
 #pragma unroll
             for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
         }
-        store_row<64>(act + kH2, r, v);  // dA2 over h2
+        if (check) fits &= row_fits<E, 64>(v);
+        store_row<E, 64>(act + kH2, r, v);  // dA2 over h2
         // layer 2: dW2^T += dA2^T [x, sh];  dx = dA2 @ W2[:16]^T
         wg.sync();
         if (leader) {
-            mma_mn(tm0 + kA2, act + kH2, act + kX2, 32, !first);
-            mma_kk(tm0 + kDB, act + kH2, sw + kG2, 64, 16, false);
+            mma_mn<E>(tm0 + kA2, act + kH2, act + kX2, 32, !first);
+            mma_kk<E>(tm0 + kDB, act + kH2, sw + kG2, 64, 16, false);
             tc::commit(wg.bar);
         }
         wg.wait();
         tc::ld16(wg.tm + kDB, v);
         v[0] += dx0;
-        store_row<16>(act + kX2, r, v);  // dx (16 columns) over [x, sh]
+        if (check) fits &= row_fits<E, 16>(v);
+        store_row<E, 16>(act + kX2, r, v);  // dx (16 columns) over [x, sh]
         // layer 1: dW1 += h1^T dx;  dh1 = dx @ W1^T
         wg.sync();
         if (leader) {
-            mma_mn(tm0 + kA1, act + kH1, act + kX2, 16, !first);
-            mma_kk(tm0 + kDA, act + kX2, sw + kG1, 16, 64, false);
+            mma_mn<E>(tm0 + kA1, act + kH1, act + kX2, 16, !first);
+            mma_kk<E>(tm0 + kDA, act + kX2, sw + kG1, 16, 64, false);
             tc::commit(wg.bar);
         }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
         {
             float h[64];
-            load_row<64>(act + kH1, r, h);
+            load_row<E, 64>(act + kH1, r, h);
 #pragma unroll
             for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
         }
-        store_row<64>(act + kH1, r, v);  // dA1 over h1
+        if (check) fits &= row_fits<E, 64>(v);
+        store_row<E, 64>(act + kH1, r, v);  // dA1 over h1
         // layer 0: dW0^T += dA1^T enc;  denc = dA1 @ W0^T
         wg.sync();
         if (leader) {
-            mma_mn(tm0 + kA0, act + kH1, act + kX0, 32, !first);
-            mma_kk(tm0 + kDA, act + kH1, sw + kG0, 64, 32, false);
+            mma_mn<E>(tm0 + kA0, act + kH1, act + kX0, 32, !first);
+            mma_kk<E>(tm0 + kDA, act + kH1, sw + kG0, 64, 32, false);
             tc::commit(wg.bar);
         }
         wg.wait();
         tc::ld32(wg.tm + kDA, v);
         if (valid) {
-#pragma unroll
-            for (int c = 0; c < 32; c += 4)
-                *reinterpret_cast<float4 *>(dL_denc + s * 32 + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+            if (check) fits &= kHalf ? row_fits<E, 32>(v) : row_fits<F32Op, 32>(v);
+            write_denc<E>(dL_denc, s, v);
         }
         first = false;
         tc::bar_sync(1 + g, 128);
         if (*wg.fail) break;
     }
+    if (check != nullptr && !fits) atomicOr(&ls->overflow, 1u);
     if (r == 0) {
         tiles_done[g] = first ? 0 : 1;
         if (*wg.fail) atomicOr(&g_device_error, 1u);
@@ -575,26 +655,6 @@ constexpr int kQX = 0, kQH1 = 2048, kQH2 = 10240, kQAct = 18432;  // per warpgro
 constexpr int kPropWgs = 4;
 constexpr std::size_t kPropSmem = (std::size_t)(kQW + kPropWgs * kQAct) * 2;
 
-template <int N>
-__device__ __forceinline__ void store_row_f16(__half *buf, int r, const float *v) {
-#pragma unroll
-    for (int c = 0; c < N; c += 8) {
-        uint4 q;
-        q.x = tc::pack_f16(v[c + 0], v[c + 1]);
-        q.y = tc::pack_f16(v[c + 2], v[c + 3]);
-        q.z = tc::pack_f16(v[c + 4], v[c + 5]);
-        q.w = tc::pack_f16(v[c + 6], v[c + 7]);
-        *reinterpret_cast<uint4 *>(buf + rb(r, c, N)) = q;
-    }
-}
-
-__device__ __forceinline__ void mma_kk_f16(std::uint32_t d, const __half *a, const __half *b, int K, int N) {
-    const std::uint32_t id = tc::idesc_f16(128, N);
-    const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), sbo = (std::uint32_t)K * 16;
-    for (int j = 0; j < K / 16; ++j)
-        tc::mma_bf16(d, tc::sdesc(sa + j * 256, 128, sbo), tc::sdesc(sb + j * 256, 128, sbo), id, j > 0);
-}
-
 template <int NWG>
 __global__ void __launch_bounds__(NWG * 128, 1) prop_f16_forward_kernel(
     std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
@@ -646,23 +706,23 @@ __global__ void __launch_bounds__(NWG * 128, 1) prop_f16_forward_kernel(
             const float4 b = reinterpret_cast<const float4 *>(enc + s * 8)[1];
             v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
         }
-        store_row_f16<16>(act + kQX, r, v);
+        store_row<F16Op, 16>(act + kQX, r, v);
         wg.sync();
-        if (leader) { mma_kk_f16(wg.tm + kDA, act + kQX, sw + kQ0, 16, 64); tc::commit(wg.bar); }
+        if (leader) { mma_kk<F16Op>(wg.tm + kDA, act + kQX, sw + kQ0, 16, 64, false); tc::commit(wg.bar); }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
 #pragma unroll
         for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
-        store_row_f16<64>(act + kQH1, r, v);
+        store_row<F16Op, 64>(act + kQH1, r, v);
         wg.sync();
-        if (leader) { mma_kk_f16(wg.tm + kDA, act + kQH1, sw + kQ1, 64, 64); tc::commit(wg.bar); }
+        if (leader) { mma_kk<F16Op>(wg.tm + kDA, act + kQH1, sw + kQ1, 64, 64, false); tc::commit(wg.bar); }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
 #pragma unroll
         for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
-        store_row_f16<64>(act + kQH2, r, v);
+        store_row<F16Op, 64>(act + kQH2, r, v);
         wg.sync();
-        if (leader) { mma_kk_f16(wg.tm + kDB, act + kQH2, sw + kQ2, 64, 16); tc::commit(wg.bar); }
+        if (leader) { mma_kk<F16Op>(wg.tm + kDB, act + kQH2, sw + kQ2, 64, 16, false); tc::commit(wg.bar); }
         wg.wait();
         tc::ld16(wg.tm + kDB, v);
         if (valid) x_out[s] = v[0];
@@ -684,57 +744,120 @@ static_assert(kBwdAct * 2 >= kNW * 4, "dW sums fit over a warpgroup's rows");
 
 // ------------------------------------------------------------------------------- launchers
 
-int launch_mlp_bf16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
-                            const float *dirs, const float *weights, float *drgb) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp (bf16): enc, weights and drgb must be 16-byte aligned");
+namespace {
+
+template <class E, bool kHalf>
+int launch_tc_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const void *enc,
+                      const float *dirs, const float *weights, float *drgb) {
+    using In = typename EncRow<E, kHalf>::In;
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp (tensor cores): enc, weights and drgb must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_bf16_forward_kernel<kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_forward_kernel<E, kHalf, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
         attr = true;
     }
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kRows - 1) / kRows;
     const unsigned want = (tiles + kFwdWgs - 1) / kFwdWgs;
     const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
-    mlp_bf16_forward_kernel<kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
+    mlp_tc_forward_kernel<E, kHalf, kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(
+        n, count, static_cast<const In *>(enc), dirs, weights, drgb);
     count_launches(1);
     return launch_status();
 }
 
-int launch_mlp_bf16_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp (bf16): enc and weights must be 16-byte aligned");
+template <class E, bool kHalf>
+int launch_tc_density(cudaStream_t stream, std::uint32_t n, const void *enc, const float *weights, float *sigma) {
+    using In = typename EncRow<E, kHalf>::In;
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp (tensor cores): enc and weights must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_bf16_density_kernel<kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_density_kernel<E, kHalf, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
         attr = true;
     }
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kRows - 1) / kRows;
     const unsigned want = (tiles + kFwdWgs - 1) / kFwdWgs;
     const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
-    mlp_bf16_density_kernel<kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(n, enc, weights, sigma);
+    mlp_tc_density_kernel<E, kHalf, kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(n, static_cast<const In *>(enc),
+                                                                                        weights, sigma);
     count_launches(1);
     return launch_status();
+}
+
+template <class E, bool kHalf>
+int launch_tc_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const void *enc,
+                       const float *dirs, const float *weights, const float *dL_ddrgb, const float *grad_scale,
+                       NgpLossScale *ls, void *dL_denc, float *partials, unsigned *grid_out) {
+    using In = typename EncRow<E, kHalf>::In;
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
+                  "mlp (tensor cores): buffers must be 16-byte aligned");
+    static bool attr = false;
+    if (!attr) {
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_backward_kernel<E, kHalf, kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        attr = true;
+    }
+    const unsigned grid = (unsigned)sm_count();
+    mlp_tc_backward_kernel<E, kHalf, kBwdWgs><<<grid, kBwdWgs * 128, kBwdSmem, stream>>>(
+        n, count, static_cast<const In *>(enc), dirs, weights, dL_ddrgb, grad_scale, ls, static_cast<In *>(dL_denc), partials);
+    count_launches(1);
+    *grid_out = grid;
+    return launch_status();
+}
+
+}  // namespace
+
+int launch_mlp_bf16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                            const float *dirs, const float *weights, float *drgb) {
+    return launch_tc_forward<Bf16Op, false>(stream, n, count, enc, dirs, weights, drgb);
+}
+
+int launch_mlp_bf16_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
+    return launch_tc_density<Bf16Op, false>(stream, n, enc, weights, sigma);
 }
 
 // `partials` holds at least sm_count() x 9408 floats; one partial per CTA, grid = sm_count().
 int launch_mlp_bf16_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
                              const float *dirs, const float *weights, const float *dL_ddrgb, const float *grad_scale,
                              float *dL_denc, float *partials, unsigned *grid_out) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
-                  "mlp (bf16): buffers must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_bf16_backward_kernel<kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
-        attr = true;
-    }
-    const unsigned grid = (unsigned)sm_count();
-    mlp_bf16_backward_kernel<kBwdWgs><<<grid, kBwdWgs * 128, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
-                                                                                grad_scale, dL_denc, partials);
-    count_launches(1);
-    *grid_out = grid;
-    return launch_status();
+    return launch_tc_backward<Bf16Op, false>(stream, n, count, enc, dirs, weights, dL_ddrgb, grad_scale, nullptr,
+                                             dL_denc, partials, grid_out);
 }
+
+// The mixed-precision forms: `operand` NGP_DTYPE_BF16 or NGP_DTYPE_F16; `half_act` keeps the
+// encodings and their gradient in the operand type instead of FP32.
+#define NGP_TC_DISPATCH(call)                                                                          \
+    do {                                                                                               \
+        NGP_CHECK_ARG(operand == NGP_DTYPE_BF16 || operand == NGP_DTYPE_F16,                           \
+                      "mlp (tensor cores): operand type must be NGP_DTYPE_BF16 or NGP_DTYPE_F16");     \
+        if (operand == NGP_DTYPE_BF16) return half_act ? call(Bf16Op, true) : call(Bf16Op, false);    \
+        return half_act ? call(F16Op, true) : call(F16Op, false);                                      \
+    } while (0)
+
+int launch_mlp_tc_forward(cudaStream_t stream, std::uint32_t operand, bool half_act, std::uint32_t n,
+                          const std::uint32_t *count, const void *enc, const float *dirs, const float *weights,
+                          float *drgb) {
+#define NGP_CALL(E, H) launch_tc_forward<E, H>(stream, n, count, enc, dirs, weights, drgb)
+    NGP_TC_DISPATCH(NGP_CALL);
+#undef NGP_CALL
+}
+
+int launch_mlp_tc_density(cudaStream_t stream, std::uint32_t operand, bool half_act, std::uint32_t n, const void *enc,
+                          const float *weights, float *sigma) {
+#define NGP_CALL(E, H) launch_tc_density<E, H>(stream, n, enc, weights, sigma)
+    NGP_TC_DISPATCH(NGP_CALL);
+#undef NGP_CALL
+}
+
+int launch_mlp_tc_backward(cudaStream_t stream, std::uint32_t operand, bool half_act, std::uint32_t n,
+                           const std::uint32_t *count, const void *enc, const float *dirs, const float *weights,
+                           const float *dL_ddrgb, const float *grad_scale, NgpLossScale *ls, void *dL_denc,
+                           float *partials, unsigned *grid_out) {
+#define NGP_CALL(E, H) launch_tc_backward<E, H>(stream, n, count, enc, dirs, weights, dL_ddrgb, grad_scale, ls, dL_denc, partials, grid_out)
+    NGP_TC_DISPATCH(NGP_CALL);
+#undef NGP_CALL
+}
+#undef NGP_TC_DISPATCH
 
 int launch_prop_f16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
                             const float *weights, float *x) {

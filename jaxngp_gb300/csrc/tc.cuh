@@ -31,16 +31,22 @@ __device__ __forceinline__ std::uint64_t sdesc(std::uint32_t saddr, std::uint32_
            ((std::uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((std::uint64_t)1 << 46);
 }
 
-// Instruction descriptor of kind::f16 with BF16 operands and an FP32 accumulator.
-__host__ __device__ constexpr std::uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+// Instruction descriptor of kind::f16 with an FP32 accumulator; `fmt` is the operand format of
+// both A and B (0 = FP16, 1 = BF16: one instruction never mixes them).
+__host__ __device__ constexpr std::uint32_t idesc_kf16(int M, int N, std::uint32_t fmt, bool a_mn, bool b_mn) {
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
            ((std::uint32_t)(N >> 3) << 17) | ((std::uint32_t)(M >> 4) << 24);
 }
 
-// Instruction descriptor of kind::f16 with FP16 operands and an FP32 accumulator.
-__host__ __device__ constexpr std::uint32_t idesc_f16(int M, int N) {
-    return (1u << 4) | ((std::uint32_t)(N >> 3) << 17) | ((std::uint32_t)(M >> 4) << 24);
+__host__ __device__ constexpr std::uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
+    return idesc_kf16(M, N, 1u, a_mn, b_mn);
 }
+
+__host__ __device__ constexpr std::uint32_t idesc_f16(int M, int N) { return idesc_kf16(M, N, 0u, false, false); }
+
+static_assert(idesc_f16(128, 64) == ((1u << 4) | (8u << 17) | (8u << 24)), "FP16 descriptor");
+static_assert(idesc_bf16(64, 16, true, true) == ((1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | (2u << 17) | (4u << 24)),
+              "BF16 descriptor");
 
 // kind::f16 MMA (BF16 or FP16 operands, as the instruction descriptor says).
 __device__ __forceinline__ void mma_bf16(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b, std::uint32_t idesc,

@@ -10,6 +10,7 @@
 //   occupancy grid:  utils/types.py:1149-1225 (decay, sampling, density max), :1227-1239
 //                    (threshold), :1241-1362 (marking cells no camera sees), :1385-1392
 #include "common.cuh"
+#include "half.cuh"
 
 namespace ngp {
 namespace {
@@ -369,6 +370,90 @@ __global__ void __launch_bounds__(256) adam_kernel(NgpAdamDescriptor d, float bc
     }
 }
 
+// adam_kernel on FP32 master parameters with a dynamic loss scale and a 16-bit working copy
+// (kHalf: 0 none, NGP_DTYPE_BF16 or NGP_DTYPE_F16).  With `ls`, a step whose overflow flag is set
+// changes nothing but the zeroed gradient; otherwise the gradient is divided by the scale (a power
+// of two: exact) and the bias corrections use the count of updates actually made.
+template <int kHalf>
+__device__ __forceinline__ void put_half(void *ph, std::size_t i, float x) {
+    if constexpr (kHalf == (int)NGP_DTYPE_BF16) reinterpret_cast<__nv_bfloat16 *>(ph)[i] = Bf16Op::cvt(x);
+    else if constexpr (kHalf == (int)NGP_DTYPE_F16) reinterpret_cast<__half *>(ph)[i] = F16Op::cvt(x);
+}
+
+template <int kHalf>
+__global__ void __launch_bounds__(256) adam_mixed_kernel(NgpAdamDescriptor d, float bc1, float bc2,
+                                                         float *__restrict__ p, float *__restrict__ g,
+                                                         float *__restrict__ m, float *__restrict__ v,
+                                                         const NgpLossScale *__restrict__ ls, void *__restrict__ ph) {
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    const std::size_t n4 = d.n / 4;
+    const std::size_t i0 = (std::size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float inv = 1.f;
+    if (ls != nullptr) {
+        if (ls->overflow != 0u) {
+            if (d.zero_grad) {
+                for (std::size_t i = i0; i < n4; i += stride) reinterpret_cast<float4 *>(g)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (std::size_t i = n4 * 4 + i0; i < d.n; i += stride) g[i] = 0.f;
+            }
+            return;
+        }
+        inv = 1.f / ls->scale;
+        const float t = (float)(d.step - ls->skipped_steps);
+        bc1 = 1.f - powf(d.beta1, t);
+        bc2 = 1.f - powf(d.beta2, t);
+    }
+    for (std::size_t i = i0; i < n4; i += stride) {
+        float4 pp = reinterpret_cast<float4 *>(p)[i];
+        float4 gg = reinterpret_cast<float4 *>(g)[i];
+        float4 mm = reinterpret_cast<float4 *>(m)[i];
+        float4 vv = reinterpret_cast<float4 *>(v)[i];
+        float *pa = &pp.x, *ga = &gg.x, *ma = &mm.x, *va = &vv.x;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float gc = ls != nullptr ? ga[c] * inv : ga[c];
+            ma[c] = d.beta1 * ma[c] + (1.f - d.beta1) * gc;
+            va[c] = d.beta2 * va[c] + (1.f - d.beta2) * gc * gc;
+            const float mh = ma[c] / bc1, vh = va[c] / bc2;
+            const float upd = -d.lr * (mh / (sqrtf(vh + d.eps_root) + d.eps)) + d.weight_decay * pa[c];
+            pa[c] = pa[c] + upd;
+        }
+        reinterpret_cast<float4 *>(p)[i] = pp;
+        reinterpret_cast<float4 *>(m)[i] = mm;
+        reinterpret_cast<float4 *>(v)[i] = vv;
+        if (d.zero_grad) reinterpret_cast<float4 *>(g)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (kHalf == (int)NGP_DTYPE_BF16) {
+            reinterpret_cast<uint2 *>(ph)[i] = make_uint2(Bf16Op::pack(pp.x, pp.y), Bf16Op::pack(pp.z, pp.w));
+        } else if constexpr (kHalf == (int)NGP_DTYPE_F16) {
+            reinterpret_cast<uint2 *>(ph)[i] = make_uint2(F16Op::pack(pp.x, pp.y), F16Op::pack(pp.z, pp.w));
+        }
+    }
+    for (std::size_t i = n4 * 4 + i0; i < d.n; i += stride) {
+        const float gi = ls != nullptr ? g[i] * inv : g[i];
+        float mm = d.beta1 * m[i] + (1.f - d.beta1) * gi;
+        float vv = d.beta2 * v[i] + (1.f - d.beta2) * gi * gi;
+        const float upd = -d.lr * ((mm / bc1) / (sqrtf(vv / bc2 + d.eps_root) + d.eps)) + d.weight_decay * p[i];
+        p[i] = p[i] + upd;
+        m[i] = mm;
+        v[i] = vv;
+        if (d.zero_grad) g[i] = 0.f;
+        put_half<kHalf>(ph, i, p[i]);
+    }
+}
+
+__global__ void loss_scale_update_kernel(NgpLossScaleDescriptor d, NgpLossScale *__restrict__ ls) {
+    NgpLossScale s = *ls;
+    if (s.overflow != 0u) {
+        s.scale = fmaxf(s.scale * d.backoff_factor, d.min_scale);
+        s.good_steps = 0u;
+        s.skipped_steps += 1u;
+    } else if (++s.good_steps >= d.growth_interval) {
+        s.scale = fminf(s.scale * d.growth_factor, d.max_scale);
+        s.good_steps = 0u;
+    }
+    s.overflow = 0u;
+    *ls = s;
+}
+
 __device__ __forceinline__ std::uint32_t morton_decode(std::uint32_t x) {
     x = x & 0x49249249u;
     x = (x | (x >> 2)) & 0xc30c30c3u;
@@ -615,6 +700,40 @@ int launch_adam(cudaStream_t stream, const NgpAdamDescriptor &d, float *p, float
         adam_kernel<<<grid_for(d.n / 4 + 1, 256, 8), 256, 0, stream>>>(d, bc1, bc2, p, g, m, v);
         count_launches(1);
     }
+    return launch_status();
+}
+
+int launch_adam_mixed(cudaStream_t stream, const NgpAdamDescriptor &d, std::uint32_t half_copy, float *p, float *g,
+                      float *m, float *v, const NgpLossScale *ls, void *ph) {
+    NGP_CHECK_ARG(d.step >= 1, "adam: step is 1-based");
+    NGP_CHECK_ARG((((std::uintptr_t)p | (std::uintptr_t)g | (std::uintptr_t)m | (std::uintptr_t)v) & 15u) == 0,
+                  "adam: buffers must be 16-byte aligned");
+    NGP_CHECK_ARG(half_copy == NGP_DTYPE_F32 || half_copy == NGP_DTYPE_BF16 || half_copy == NGP_DTYPE_F16,
+                  "adam: unknown half-copy type");
+    NGP_CHECK_ARG(half_copy == NGP_DTYPE_F32 || (ph != nullptr && ((std::uintptr_t)ph & 7u) == 0),
+                  "adam: the 16-bit copy must be given and 8-byte aligned");
+    const float bc1 = 1.f - powf(d.beta1, (float)d.step);
+    const float bc2 = 1.f - powf(d.beta2, (float)d.step);
+    if (d.n > 0) {
+        const unsigned grid = grid_for(d.n / 4 + 1, 256, 8);
+        if (half_copy == NGP_DTYPE_BF16)
+            adam_mixed_kernel<(int)NGP_DTYPE_BF16><<<grid, 256, 0, stream>>>(d, bc1, bc2, p, g, m, v, ls, ph);
+        else if (half_copy == NGP_DTYPE_F16)
+            adam_mixed_kernel<(int)NGP_DTYPE_F16><<<grid, 256, 0, stream>>>(d, bc1, bc2, p, g, m, v, ls, ph);
+        else
+            adam_mixed_kernel<0><<<grid, 256, 0, stream>>>(d, bc1, bc2, p, g, m, v, ls, ph);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+int launch_loss_scale_update(cudaStream_t stream, const NgpLossScaleDescriptor &d, NgpLossScale *ls) {
+    NGP_CHECK_ARG(ls != nullptr && ((std::uintptr_t)ls & 3u) == 0, "loss scale: state buffer missing or misaligned");
+    NGP_CHECK_ARG(d.growth_interval >= 1 && d.growth_factor >= 1.f && d.backoff_factor > 0.f && d.backoff_factor <= 1.f &&
+                      d.min_scale > 0.f && d.max_scale >= d.min_scale,
+                  "loss scale: bad descriptor");
+    loss_scale_update_kernel<<<1, 1, 0, stream>>>(d, ls);
+    count_launches(1);
     return launch_status();
 }
 

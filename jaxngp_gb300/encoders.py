@@ -16,6 +16,7 @@ from typing import List, Optional
 import torch
 
 from . import _lib as L
+from . import precision as P
 
 PARAM_NAME = "latent codes stored on grid vertices"
 
@@ -83,24 +84,57 @@ class LevelTable:
         return d
 
 
+def mixed_descriptor(desc: L.NgpHashGridDescriptor, table: int, encodings: int) -> L.NgpHashGridMixedDescriptor:
+    m = L.NgpHashGridMixedDescriptor()
+    m.grid, m.table, m.encodings = desc, table, encodings
+    return m
+
+
+def forward_call(desc: L.NgpHashGridDescriptor, latents: torch.Tensor, out: torch.Tensor):
+    """(entry point, descriptor) of the encoder forward for these storage types."""
+    if latents.dtype == torch.float32 and out.dtype == torch.float32:
+        return "ngp_hashgrid_forward", desc
+    return "ngp_hashgrid_forward_mixed", mixed_descriptor(desc, P.dtype_code(latents), P.dtype_code(out))
+
+
+def backward_call(desc: L.NgpHashGridDescriptor, dL_denc: torch.Tensor):
+    """(entry point, descriptor) of the encoder backward for this gradient type."""
+    if dL_denc.dtype == torch.float32:
+        return "ngp_hashgrid_backward", desc
+    return "ngp_hashgrid_backward_mixed", mixed_descriptor(desc, L.DTYPE_F32, P.dtype_code(dL_denc))
+
+
 def hashgrid_forward(table: LevelTable, pos: torch.Tensor, latents: torch.Tensor, bound: float,
-                     count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+                     count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None,
+                     enc_dtype: torch.dtype = torch.float32) -> torch.Tensor:
+    """Encodings of `pos`.  A 16-bit `latents` (a working copy of the FP32 table) and/or 16-bit
+    encodings go through ngp_hashgrid_forward_mixed."""
     pos = pos.contiguous()
     n = pos.shape[0]
     if out is None:
-        out = torch.empty(n, table.L * table.F, dtype=torch.float32, device=pos.device)
-    L.call("ngp_hashgrid_forward", [pos, latents, count, out], table.descriptor(n, bound))
+        out = torch.empty(n, table.L * table.F, dtype=enc_dtype, device=pos.device)
+    desc = table.descriptor(n, bound)
+    if latents.dtype == torch.float32 and out.dtype == torch.float32:
+        L.call("ngp_hashgrid_forward", [pos, latents, count, out], desc)
+    else:
+        L.call("ngp_hashgrid_forward_mixed", [pos, latents, count, out],
+               mixed_descriptor(desc, P.dtype_code(latents), P.dtype_code(out)))
     return out
 
 
 def hashgrid_backward(table: LevelTable, pos: torch.Tensor, dL_denc: torch.Tensor, bound: float,
                       count: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None,
                       accumulate: bool = False) -> torch.Tensor:
+    """FP32 dL/dlatents from FP32 or 16-bit dL/dencodings."""
     n = pos.shape[0]
     if out is None:
         out = torch.empty(table.n_params, table.F, dtype=torch.float32, device=pos.device)
-    L.call("ngp_hashgrid_backward", [pos.contiguous(), dL_denc.contiguous(), count, out],
-           table.descriptor(n, bound, accumulate))
+    desc = table.descriptor(n, bound, accumulate)
+    if dL_denc.dtype == torch.float32:
+        L.call("ngp_hashgrid_backward", [pos.contiguous(), dL_denc.contiguous(), count, out], desc)
+    else:
+        L.call("ngp_hashgrid_backward_mixed", [pos.contiguous(), dL_denc.contiguous(), count, out],
+               mixed_descriptor(desc, L.DTYPE_F32, P.dtype_code(dL_denc)))
     return out
 
 

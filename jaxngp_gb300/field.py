@@ -15,6 +15,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
+from . import precision as P
 from .encoders import PARAM_NAME, HashGridEncoder, hashgrid_backward, hashgrid_forward
 
 SHAPES = [("W0", (32, 64)), ("W1", (64, 16)), ("W2", (32, 64)), ("W3", (64, 64)), ("W4", (64, 3))]
@@ -38,15 +39,74 @@ def unpack_weights(flat: torch.Tensor) -> Dict[str, torch.Tensor]:
 
 # ------------------------------------------------------------------------------ raw entry points
 
-PRECISIONS = ("fp32", "bf16")
+PRECISIONS = ("fp32", "bf16", "fp16")
 
 
 def entry(name: str, precision: str) -> str:
-    """Entry point of a field op for a precision: "fp32" (SIMT, the parity path) or "bf16"
-    (tensor cores, BF16 operands with FP32 accumulation)."""
-    if precision not in PRECISIONS:
-        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
+    """Entry point of a field op for "fp32" (SIMT, the parity path) or "bf16" (tensor cores, BF16
+    operands with FP32 accumulation, FP32 encodings).  FP16 and 16-bit encodings go through the
+    ``*_mixed`` entries (FieldOps)."""
+    if precision not in ("fp32", "bf16"):
+        raise ValueError(f"entry() covers fp32 and bf16; use FieldOps for {precision!r}")
     return name if precision == "fp32" else f"{name}_{precision}"
+
+
+class FieldOps:
+    """The field's forward, density and backward at one operand precision.  The encodings'
+    storage type is read from the tensor given (FP32, or the operand type for 16-bit
+    activations); a loss scale (precision.LossScale) goes to the backward.  FP32, and BF16 with
+    FP32 encodings and no loss scale, use the plain entry points; everything else the
+    ``ngp_field_*_mixed`` ones."""
+
+    def __init__(self, precision: str = "fp32"):
+        self.precision = P.check(precision)
+        self.code = P.CODE[precision]
+        self._descs = {}
+
+    def _plain(self, enc: torch.Tensor, loss_scale=None) -> bool:
+        return self.precision == "fp32" or (self.precision == "bf16" and enc.dtype == torch.float32 and loss_scale is None)
+
+    def _mixed(self, n: int, enc: torch.Tensor, accumulate: bool = False) -> L.NgpFieldMixedDescriptor:
+        key = (n, enc.dtype, accumulate)
+        d = self._descs.get(key)
+        if d is None:
+            act = P.dtype_code(enc)
+            if self.precision == "fp32" or act not in (L.DTYPE_F32, self.code):
+                raise ValueError(f"encodings of type {enc.dtype} do not fit a {self.precision} field")
+            d = self._descs[key] = L.NgpFieldMixedDescriptor(n, 1 if accumulate else 0, self.code, act)
+        return d
+
+    def forward(self, enc, dirs, weights, count, out, n: Optional[int] = None):
+        n = enc.shape[0] if n is None else n
+        if self._plain(enc):
+            L.call(entry("ngp_field_forward", self.precision), [enc, dirs, weights, count, out], L.NgpMlpDescriptor(n, 0))
+        else:
+            L.call("ngp_field_forward_mixed", [enc, dirs, weights, count, out], self._mixed(n, enc))
+        return out
+
+    def density(self, enc, weights, out, n: Optional[int] = None):
+        n = enc.shape[0] if n is None else n
+        if self._plain(enc):
+            L.call(entry("ngp_field_density", self.precision), [enc, weights, out], L.NgpMlpDescriptor(n, 0))
+        else:
+            L.call("ngp_field_density_mixed", [enc, weights, out], self._mixed(n, enc))
+        return out
+
+    def backward(self, enc, dirs, weights, dL_ddrgb, count, grad_scale, scratch, dL_denc, dL_dw,
+                 accumulate: bool = False, loss_scale=None, n: Optional[int] = None):
+        n = enc.shape[0] if n is None else n
+        if self._plain(enc, loss_scale):
+            L.call(entry("ngp_field_backward", self.precision),
+                   [enc, dirs, weights, dL_ddrgb, count, grad_scale, scratch, dL_denc, dL_dw],
+                   L.NgpMlpDescriptor(n, 1 if accumulate else 0))
+        else:
+            if dL_denc.dtype != enc.dtype:
+                raise ValueError("dL_dencodings must have the encodings' type")
+            state = loss_scale.state if loss_scale is not None else None
+            L.call("ngp_field_backward_mixed",
+                   [enc, dirs, weights, dL_ddrgb, count, grad_scale, state, scratch, dL_denc, dL_dw],
+                   self._mixed(n, enc, accumulate))
+        return dL_denc, dL_dw
 
 
 def field_forward(enc: torch.Tensor, dirs: torch.Tensor, weights: torch.Tensor,
@@ -55,9 +115,7 @@ def field_forward(enc: torch.Tensor, dirs: torch.Tensor, weights: torch.Tensor,
     n = enc.shape[0]
     if out is None:
         out = torch.empty(n, 4, dtype=torch.float32, device=enc.device)
-    L.call(entry("ngp_field_forward", precision), [enc.contiguous(), dirs.contiguous(), weights, count, out],
-           L.NgpMlpDescriptor(n, 0))
-    return out
+    return FieldOps(precision).forward(enc.contiguous(), dirs.contiguous(), weights, count, out, n)
 
 
 def field_density(enc: torch.Tensor, weights: torch.Tensor, out: Optional[torch.Tensor] = None,
@@ -65,8 +123,7 @@ def field_density(enc: torch.Tensor, weights: torch.Tensor, out: Optional[torch.
     n = enc.shape[0]
     if out is None:
         out = torch.empty(n, dtype=torch.float32, device=enc.device)
-    L.call(entry("ngp_field_density", precision), [enc.contiguous(), weights, out], L.NgpMlpDescriptor(n, 0))
-    return out
+    return FieldOps(precision).density(enc.contiguous(), weights, out, n)
 
 
 _scratch: Dict[int, torch.Tensor] = {}
@@ -83,19 +140,18 @@ def backward_scratch(device) -> torch.Tensor:
 def field_backward(enc: torch.Tensor, dirs: torch.Tensor, weights: torch.Tensor, dL_ddrgb: torch.Tensor,
                    count: Optional[torch.Tensor] = None, grad_scale: Optional[torch.Tensor] = None,
                    dL_denc: Optional[torch.Tensor] = None, dL_dw: Optional[torch.Tensor] = None,
-                   accumulate: bool = False, scratch: Optional[torch.Tensor] = None, precision: str = "fp32"):
+                   accumulate: bool = False, scratch: Optional[torch.Tensor] = None, precision: str = "fp32",
+                   loss_scale=None):
     n = enc.shape[0]
     dev = enc.device
     if dL_denc is None:
-        dL_denc = torch.empty(n, 32, dtype=torch.float32, device=dev)
+        dL_denc = torch.empty(n, 32, dtype=enc.dtype, device=dev)
     if dL_dw is None:
         dL_dw = torch.zeros(L.MLP_WEIGHTS, dtype=torch.float32, device=dev)
     if scratch is None:
         scratch = backward_scratch(dev)
-    L.call(entry("ngp_field_backward", precision),
-           [enc.contiguous(), dirs.contiguous(), weights, dL_ddrgb.contiguous(), count, grad_scale, scratch, dL_denc,
-            dL_dw], L.NgpMlpDescriptor(n, 1 if accumulate else 0))
-    return dL_denc, dL_dw
+    return FieldOps(precision).backward(enc.contiguous(), dirs.contiguous(), weights, dL_ddrgb.contiguous(), count,
+                                        grad_scale, scratch, dL_denc, dL_dw, accumulate, loss_scale, n)
 
 
 class _FieldMlpFn(torch.autograd.Function):

@@ -16,19 +16,19 @@ from typing import Tuple
 import torch
 
 from . import _lib as L
-from .encoders import LevelTable
-from .field import entry as field_entry
+from .encoders import LevelTable, forward_call
+from .field import FieldOps
 
 
 class Renderer:
     def __init__(self, latents: torch.Tensor, weights: torch.Tensor, table: LevelTable, bitfield: torch.Tensor,
                  K: int, G: int, bound: float, stepsize_portion: float, diagonal_n_steps: int = 1024,
                  n_slots: int = 1 << 18, march_steps_cap: int = 8, poll_every: int = 4, precision: str = "fp32",
-                 compact: bool = True):
+                 compact: bool = True, activations: torch.dtype = torch.float32):
         self.latents, self.weights, self.table, self.bitfield = latents, weights, table, bitfield
         self.K, self.G, self.bound, self.sp, self.dns = K, G, float(bound), float(stepsize_portion), diagonal_n_steps
         self.n_slots, self.cap, self.poll_every = n_slots, march_steps_cap, poll_every
-        self.field_fwd = field_entry("ngp_field_forward", precision)
+        self.field = FieldOps(precision)
         self.compact = compact
         if compact and march_steps_cap > 16:
             raise ValueError("the compact renderer supports march_steps_cap <= 16")
@@ -39,7 +39,7 @@ class Renderer:
         self.dirs = torch.empty(n * c, 3, **f32)
         self.dss = torch.empty(n, c, **f32)
         self.zs = torch.empty(n, c, **f32)
-        self.enc = torch.empty(n * c, 32, **f32)
+        self.enc = torch.empty(n * c, 32, dtype=activations, device=dev)
         self.drgbs = torch.empty(n * c, 4, **f32)
         self.n_samples = torch.empty(n, dtype=torch.int32, device=dev)
         self.indices = torch.empty(n, dtype=torch.int32, device=dev)
@@ -54,7 +54,8 @@ class Renderer:
     @classmethod
     def from_trainer(cls, tr, **kw) -> "Renderer":
         kw.setdefault("precision", tr.cfg.mlp_precision)
-        return cls(tr.latents, tr.weights, tr.table, tr.bitfield, tr.K, tr.cfg.G, tr.bound, tr.sp,
+        kw.setdefault("activations", tr.enc.dtype)
+        return cls(tr.gather_table, tr.weights, tr.table, tr.bitfield, tr.K, tr.cfg.G, tr.bound, tr.sp,
                    tr.cfg.diagonal_n_steps, **kw)
 
     @torch.no_grad()
@@ -71,8 +72,7 @@ class Renderer:
         self.total.zero_()
         dm = L.MarchingInferenceDescriptor(N, n, self.dns, self.K, self.G, cap, self.bound, self.sp)
         di = L.IntegratingInferenceDescriptor(N, n, cap)
-        dh = self.table.descriptor(n * cap, self.bound)
-        df = L.NgpMlpDescriptor(n * cap, 0)
+        hg, dh = forward_call(self.table.descriptor(n * cap, self.bound), self.latents, self.enc)
         it = 0
         while it < max_iterations:
             for _ in range(self.poll_every):
@@ -82,8 +82,8 @@ class Renderer:
                            [rays_o, rays_d, t_starts, t_ends, self.bitfield, self.terminated, self.indices,
                             self.next_ray, self.n_samples, self.sample_start, self.sample_count, self.xyzs, self.dirs,
                             self.dss, self.zs], dm)
-                    L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, self.sample_count, self.enc], dh)
-                    L.call(self.field_fwd, [self.enc, self.dirs, self.weights, self.sample_count, self.drgbs], df)
+                    L.call(hg, [self.xyzs, self.latents, self.sample_count, self.enc], dh)
+                    self.field.forward(self.enc, self.dirs, self.weights, self.sample_count, self.drgbs)
                     L.call("ngp_integrate_rays_inference_compact",
                            [rays_bg, rgbd, T, self.n_samples, self.indices, self.dss, self.zs, self.drgbs,
                             self.sample_start, self.total, self.terminated], di)
@@ -91,8 +91,8 @@ class Renderer:
                     L.call("ngp_march_rays_inference_inplace",
                            [rays_o, rays_d, t_starts, t_ends, self.bitfield, self.terminated, self.indices,
                             self.next_ray, self.n_samples, self.xyzs, self.dirs, self.dss, self.zs], dm)
-                    L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, None, self.enc], dh)
-                    L.call(self.field_fwd, [self.enc, self.dirs, self.weights, None, self.drgbs], df)
+                    L.call(hg, [self.xyzs, self.latents, None, self.enc], dh)
+                    self.field.forward(self.enc, self.dirs, self.weights, None, self.drgbs)
                     L.call("ngp_integrate_rays_inference_inplace",
                            [rays_bg, rgbd, T, self.n_samples, self.indices, self.dss, self.zs, self.drgbs, self.total,
                             self.terminated], di)

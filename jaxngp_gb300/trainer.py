@@ -25,8 +25,9 @@ import numpy as np
 import torch
 
 from . import _lib as L
-from .encoders import LevelTable
-from .field import SHAPES, entry as field_entry, glorot_uniform, pack_weights
+from . import precision as MP
+from .encoders import LevelTable, backward_call, forward_call
+from .field import SHAPES, FieldOps, glorot_uniform, pack_weights
 from .scene import SceneData
 
 
@@ -47,7 +48,11 @@ class TrainConfig:
     near: float = 0.3
     huber_delta: float = 0.1
     seed: int = 0
-    mlp_precision: str = "fp32"        # "fp32" (SIMT parity path) or "bf16" (tensor cores)
+    mlp_precision: str = "fp32"        # "fp32" (SIMT parity path), "bf16" or "fp16" (tensor cores)
+    table_precision: str = "fp32"      # "bf16"/"fp16": the encoder gathers from a 16-bit copy of the
+                                       # FP32 table, which the table's Adam update rewrites
+    half_activations: bool = False     # encodings and their gradient in the MLP's 16-bit type
+    loss_scale: Optional[float] = None # initial dynamic loss scale; None: 2^16 with an FP16 MLP, else off
     sampler: str = "march"             # "march" (occupancy grid, the reference's) or "proposal"
     proposal_every: int = 4            # proposal updates every k steps
     proposal_distill: bool = True      # also regress the proposal at points drawn in occupied cells
@@ -94,6 +99,11 @@ class NGPTrainer:
         self.sp = stepsize_portion_for(bound)
         self.R = cfg.n_rays or cfg.total_samples
         self.S = cfg.total_samples
+        self.field = FieldOps(cfg.mlp_precision)
+        MP.check(cfg.table_precision)
+        if cfg.half_activations and cfg.mlp_precision == "fp32":
+            raise ValueError("half_activations needs a 16-bit MLP (mlp_precision bf16 or fp16)")
+        act = MP.TORCH_DTYPE[cfg.mlp_precision] if cfg.half_activations else torch.float32
         self.table = LevelTable(cfg.L, cfg.T, 2, cfg.N_min, cfg.N_max or int(2 ** 11 * bound), cfg.per_level_scale)
         P = self.table.n_params
         g = torch.Generator(device=self.dev)
@@ -129,20 +139,24 @@ class NGPTrainer:
         self.idcs = torch.empty(S, **i32)
         self.xyzs, self.dirs = torch.empty(S, 3, **f32), torch.empty(S, 3, **f32)
         self.dss, self.z_vals = torch.empty(S, **f32), torch.empty(S, **f32)
-        self.enc = torch.empty(S, 32, **f32)
+        self.enc = torch.empty(S, 32, dtype=act, device=self.dev)
         self.drgbs = torch.empty(S, 4, **f32)
         self.g_drgbs = torch.empty(S, 4, **f32)
-        self.g_enc = torch.empty(S, 32, **f32)
+        self.g_enc = torch.empty(S, 32, dtype=act, device=self.dev)
         self.stats = torch.zeros(4, **f32)
         self.grad_scale = torch.zeros(1, **f32)
         self.loss_scratch = torch.zeros(4 + R, **f32)
         self.mlp_scratch = torch.empty(L.field_backward_scratch_floats(), **f32)
+        # mixed precision: the 16-bit working copy of the table and the dynamic loss scale
+        self.lat_h = self.latents.to(MP.TORCH_DTYPE[cfg.table_precision]) if cfg.table_precision != "fp32" else None
+        ls0 = cfg.loss_scale if cfg.loss_scale is not None else (2.0 ** 16 if cfg.mlp_precision == "fp16" else 0.0)
+        self.loss_scale = MP.LossScale(self.dev, init=ls0) if ls0 > 0 else None
         self.step_count = 0
         self._seed = np.random.SeedSequence(cfg.seed)
         # descriptors that do not change between steps
         self._d_march = L.MarchingDescriptor(R, S, cfg.diagonal_n_steps, self.K, cfg.G, bound, self.sp)
-        self._d_hg = self.table.descriptor(S, bound)
-        self._d_hg_acc = self.table.descriptor(S, bound, accumulate=True)
+        self._hg_fwd = forward_call(self.table.descriptor(S, bound), self.gather_table, self.enc)
+        self._hg_bwd = backward_call(self.table.descriptor(S, bound, accumulate=True), self.g_enc)
         self._d_mlp = L.NgpMlpDescriptor(S, 0)
         self._d_loss = L.NgpIntegrateLossDescriptor(R, S, data.camera.near if hasattr(data.camera, "near") else cfg.near,
                                                     cfg.huber_delta)
@@ -164,8 +178,20 @@ class NGPTrainer:
         self.mark_untrained_grid()
 
     # ---------------------------------------------------------------------------- helpers
-    def _mlp(self, name: str) -> str:
-        return field_entry(name, self.cfg.mlp_precision)
+    @property
+    def gather_table(self) -> torch.Tensor:
+        """The table the encoder forward reads: the 16-bit copy when there is one."""
+        return self.lat_h if self.lat_h is not None else self.latents
+
+    def sync_half_table(self):
+        """Rewrites the 16-bit table copy from the FP32 table (after the latents were set from
+        outside; the Adam update keeps it current otherwise)."""
+        if self.lat_h is not None:
+            self.lat_h.copy_(self.latents)
+
+    def _encode(self, xyz: torch.Tensor, count, enc: torch.Tensor, n: int):
+        name, desc = forward_call(self.table.descriptor(n, self.bound), self.gather_table, enc)
+        L.call(name, [xyz, self.gather_table, count, enc], desc)
 
     def _next_seed(self) -> int:
         return int(self._seed.spawn(1)[0].generate_state(1, np.uint64)[0])
@@ -239,9 +265,9 @@ class NGPTrainer:
             sigma = torch.empty(M, dtype=torch.float32, device=self.dev)
             for s in range(0, M, chunk):
                 n = min(chunk, M - s)
-                enc = self.enc[:n] if n <= self.S else torch.empty(n, 32, dtype=torch.float32, device=self.dev)
-                L.call("ngp_hashgrid_forward", [xyz[s:s + n], self.latents, None, enc], self.table.descriptor(n, self.bound))
-                L.call(self._mlp("ngp_field_density"), [enc, self.weights, sigma[s:s + n]], L.NgpMlpDescriptor(n, 0))
+                enc = self.enc[:n] if n <= self.S else torch.empty(n, 32, dtype=self.enc.dtype, device=self.dev)
+                self._encode(xyz[s:s + n], None, enc, n)
+                self.field.density(enc, self.weights, sigma[s:s + n], n)
             L.call("ngp_ogrid_max", [cells, sigma, self.density], d)
         L.call("ngp_ogrid_threshold", [self.density, self.thr_scratch, self.threshold], self._ogrid_desc())
         L.call("ngp_packbits_scalar", [self.threshold, self.density, self.occ_mask, self.bitfield],
@@ -266,8 +292,8 @@ class NGPTrainer:
         M = xyz.shape[0]
         d = self._ogrid_desc(0, M, False, self._next_seed())
         L.call("ngp_ogrid_sample", [self.density, self.bitfield, self.prop.cells, xyz], d)
-        L.call("ngp_hashgrid_forward", [xyz, self.latents, None, self.enc_d], self.table.descriptor(M, self.bound))
-        L.call(self._mlp("ngp_field_density"), [self.enc_d, self.weights, sigma], L.NgpMlpDescriptor(M, 0))
+        self._encode(xyz, None, self.enc_d, M)
+        self.field.density(self.enc_d, self.weights, sigma, M)
 
     # ------------------------------------------------------------------------------- step
     def step(self, perm: Optional[torch.Tensor] = None) -> torch.Tensor:
@@ -293,8 +319,8 @@ class NGPTrainer:
             cnt = self.prop.sample(self.rays_o, self.rays_d, self.t0, self.t1, self.valid, self.n_samples,
                                    self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals, cfg.perturb,
                                    seed ^ 0x5BD1E9955BD1E995)
-        L.call("ngp_hashgrid_forward", [self.xyzs, self.latents, cnt, self.enc], self._d_hg)
-        L.call(self._mlp("ngp_field_forward"), [self.enc, self.dirs, self.weights, cnt, self.drgbs], self._d_mlp)
+        L.call(self._hg_fwd[0], [self.xyzs, self.gather_table, cnt, self.enc], self._hg_fwd[1])
+        self.field.forward(self.enc, self.dirs, self.weights, cnt, self.drgbs)
         if self.prop is not None and (use_march or self.step_count % cfg.proposal_every == 0):
             # march steps teach the proposal at the march's evenly spread samples
             self.prop.train(self.xyzs, self.drgbs, self._distill if cfg.proposal_distill else None, count=cnt,
@@ -302,15 +328,24 @@ class NGPTrainer:
         L.call("ngp_integrate_loss_backward", [self.valid, self.startidx, self.n_samples, self.bgs, self.gt, self.dss,
                                                self.z_vals, self.drgbs, cnt, self.loss_scratch, self.g_drgbs,
                                                self.stats, self.grad_scale], self._d_loss)
-        L.call(self._mlp("ngp_field_backward"), [self.enc, self.dirs, self.weights, self.g_drgbs, cnt, self.grad_scale,
-                                      self.mlp_scratch, self.g_enc, self.g_w], self._d_mlp)
-        L.call("ngp_hashgrid_backward", [self.xyzs, self.g_enc, cnt, self.g_lat], self._d_hg_acc)
+        self.field.backward(self.enc, self.dirs, self.weights, self.g_drgbs, cnt, self.grad_scale, self.mlp_scratch,
+                            self.g_enc, self.g_w, loss_scale=self.loss_scale)
+        L.call(self._hg_bwd[0], [self.xyzs, self.g_enc, cnt, self.g_lat], self._hg_bwd[1])
         count = self.step_count
         lr = lr_at(cfg.lr, count)
-        L.call("ngp_adam", [self.latents, self.g_lat, self.m_lat, self.v_lat],
-               L.NgpAdamDescriptor(self.latents.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 0.0, 1))
-        L.call("ngp_adam", [self.weights, self.g_w, self.m_w, self.v_w],
-               L.NgpAdamDescriptor(self.weights.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 1e-6, 1))
+        d_lat = L.NgpAdamDescriptor(self.latents.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 0.0, 1)
+        d_w = L.NgpAdamDescriptor(self.weights.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 1e-6, 1)
+        if self.loss_scale is None and self.lat_h is None:
+            L.call("ngp_adam", [self.latents, self.g_lat, self.m_lat, self.v_lat], d_lat)
+            L.call("ngp_adam", [self.weights, self.g_w, self.m_w, self.v_w], d_w)
+        else:
+            ls = self.loss_scale.state if self.loss_scale is not None else None
+            L.call("ngp_adam_mixed", [self.latents, self.g_lat, self.m_lat, self.v_lat, ls, self.lat_h],
+                   L.NgpAdamMixedDescriptor(d_lat, MP.CODE[cfg.table_precision]))
+            L.call("ngp_adam_mixed", [self.weights, self.g_w, self.m_w, self.v_w, ls, None],
+                   L.NgpAdamMixedDescriptor(d_w, L.DTYPE_F32))
+            if self.loss_scale is not None:
+                self.loss_scale.update()
         self.step_count += 1
         if self.ogrid_due(self.step_count + self.cadence_offset):
             self.update_ogrid()
@@ -339,10 +374,10 @@ class NGPTrainer:
             L.call("march_rays", [o, d, t0, t1, zero, self.bitfield, cnt[0:1], cnt[1:2], valid, ns, st, idc, xyz, dirs,
                                   dss, zs], dm)
             L.call("ngp_march_count", [cnt[0:1], cnt[1:2], count])
-            enc = torch.empty(max_samples, 32, device=self.dev)
-            L.call("ngp_hashgrid_forward", [xyz, self.latents, count, enc], self.table.descriptor(max_samples, self.bound))
+            enc = torch.empty(max_samples, 32, dtype=self.enc.dtype, device=self.dev)
+            self._encode(xyz, count, enc, max_samples)
             drgb = torch.zeros(max_samples, 4, device=self.dev)
-            L.call(self._mlp("ngp_field_forward"), [enc, dirs, self.weights, count, drgb], L.NgpMlpDescriptor(max_samples, 0))
+            self.field.forward(enc, dirs, self.weights, count, drgb, max_samples)
             m = torch.empty(1, **i32)
             rgbd = torch.empty(n, 4, device=self.dev)
             opac = torch.empty(n, device=self.dev)

@@ -121,56 +121,82 @@ def round_bf16(x) -> np.ndarray:
     return u.astype(np.uint32).view(np.float32).reshape(a.shape)
 
 
-def _bf(x):
-    return round_bf16(np.asarray(x, np.float32)).astype(np.float64)
+def round_f16(x) -> np.ndarray:
+    """float32 values rounded to IEEE half precision (nearest, ties to even; overflow to inf),
+    returned as float32."""
+    return np.asarray(x, np.float32).astype(np.float16).astype(np.float32)
 
 
-def forward_bf16(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray]):
-    """The BF16 tensor-core forward restated: every MMA operand (weights, encodings, layer inputs)
-    rounded to bfloat16, products accumulated exactly (FP64 here, FP32 on the GPU).  Returns
-    (drgb [S,4] float64, cache)."""
-    wb = {k: _bf(v) for k, v in w.items()}
-    enc_b = _bf(enc)
+ROUNDERS = {"bf16": round_bf16, "fp16": round_f16}
+
+
+def forward_half(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray], operand: str = "bf16"):
+    """The tensor-core forward restated for a 16-bit operand type: every MMA operand (weights,
+    encodings, layer inputs) rounded to that type, products accumulated exactly (FP64 here, FP32
+    on the GPU).  Returns (drgb [S,4] float64, cache)."""
+    rnd = ROUNDERS[operand]
+
+    def h(x):
+        return rnd(np.asarray(x, np.float32)).astype(np.float64)
+
+    wb = {k: h(v) for k, v in w.items()}
+    enc_b = h(enc)
     a1 = enc_b @ wb["W0"]
-    h1 = _bf(np.maximum(a1, 0))
+    h1 = h(np.maximum(a1, 0))
     x = h1 @ wb["W1"]
     sigma = np.exp(x[:, :1])
     sh = sh4(np.asarray(dirs, np.float32)).astype(np.float64)
-    c = _bf(np.concatenate([x, sh], axis=-1))
+    c = h(np.concatenate([x, sh], axis=-1))
     a2 = c @ wb["W2"]
-    h2 = _bf(np.maximum(a2, 0))
+    h2 = h(np.maximum(a2, 0))
     a3 = h2 @ wb["W3"]
-    h3 = _bf(np.maximum(a3, 0))
+    h3 = h(np.maximum(a3, 0))
     a4 = h3 @ wb["W4"]
     rgb = 1 / (1 + np.exp(-a4))
     drgb = np.concatenate([sigma, rgb], axis=-1)
-    return drgb, dict(enc=enc_b, h1=h1, x=x, c=c, h2=h2, h3=h3, rgb=rgb, wb=wb)
+    return drgb, dict(enc=enc_b, h1=h1, x=x, c=c, h2=h2, h3=h3, rgb=rgb, wb=wb, operand=operand)
 
 
-def backward_bf16(dL_ddrgb: np.ndarray, cache, grad_scale: float = 1.0):
-    """The BF16 tensor-core backward restated: each layer's output gradient is rounded to bfloat16
-    before it enters the data- and weight-gradient MMAs; relu masks come from the BF16 layer
-    inputs.  Returns (dL_denc [S,32], dict of dL_dW) in float64."""
+def backward_half(dL_ddrgb: np.ndarray, cache, grad_scale: float = 1.0):
+    """The tensor-core backward restated: each layer's output gradient (times grad_scale, which
+    includes any loss scale) is rounded to the operand type before it enters the data- and
+    weight-gradient MMAs; relu masks come from the 16-bit layer inputs.  Returns (dL_denc [S,32],
+    dict of dL_dW) in float64, both still multiplied by grad_scale."""
+    rnd = ROUNDERS[cache["operand"]]
+
+    def h(x):
+        return rnd(np.asarray(x, np.float32)).astype(np.float64)
+
     c, wb = cache, cache["wb"]
     g = np.asarray(dL_ddrgb, np.float64) * grad_scale
     dx0 = g[:, 0] * np.exp(np.clip(c["x"][:, 0], -15, 15))
     rgb = c["rgb"]
     d4 = np.zeros((g.shape[0], 3))
     d4[:] = g[:, 1:] * rgb * (1 - rgb)
-    d4 = _bf(d4)
+    d4 = h(d4)
     grads = {"W4": c["h3"].T @ d4}
-    d3 = _bf((d4 @ wb["W4"].T) * (c["h3"] > 0))
+    d3 = h((d4 @ wb["W4"].T) * (c["h3"] > 0))
     grads["W3"] = c["h2"].T @ d3
-    d2 = _bf((d3 @ wb["W3"].T) * (c["h2"] > 0))
+    d2 = h((d3 @ wb["W3"].T) * (c["h2"] > 0))
     grads["W2"] = c["c"].T @ d2
     dx = d2 @ wb["W2"][:16].T
     dx[:, 0] += dx0
-    dx = _bf(dx)
+    dx = h(dx)
     grads["W1"] = c["h1"].T @ dx
-    d1 = _bf((dx @ wb["W1"].T) * (c["h1"] > 0))
+    d1 = h((dx @ wb["W1"].T) * (c["h1"] > 0))
     grads["W0"] = c["enc"].T @ d1
     denc = d1 @ wb["W0"].T
     return denc, grads
+
+
+def forward_bf16(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray]):
+    """forward_half with BF16 operands."""
+    return forward_half(enc, dirs, w, "bf16")
+
+
+def backward_bf16(dL_ddrgb: np.ndarray, cache, grad_scale: float = 1.0):
+    """backward_half of a forward_bf16 cache."""
+    return backward_half(dL_ddrgb, cache, grad_scale)
 
 
 def density_only(enc: np.ndarray, w: Dict[str, np.ndarray], dtype=np.float32) -> np.ndarray:

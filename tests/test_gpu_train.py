@@ -46,6 +46,32 @@ def test_train_loss_decreases(small_scene, precision):
     assert 0 < (dens > thr).mean() < 1
 
 
+@pytest.mark.parametrize("form", ["bf16-mixed", "fp16-mixed"])
+def test_train_mixed_precision(small_scene, form):
+    """BF16/FP16 MLP with a 16-bit table copy and 16-bit encodings (FP16 under the dynamic loss
+    scale): the loss falls as in FP32, the 16-bit copy tracks the FP32 master table exactly, and
+    the loss scale rarely has to back off."""
+    from jaxngp_gb300.trainer import NGPTrainer, TrainConfig
+    prec = form.split("-")[0]
+    cfg = TrainConfig(total_samples=1 << 14, T=1 << 16, seed=1, mlp_precision=prec, table_precision=prec,
+                      half_activations=True)
+    tr = NGPTrainer(small_scene, cfg)
+    dt = torch.bfloat16 if prec == "bf16" else torch.float16
+    assert tr.enc.dtype == dt and tr.g_enc.dtype == dt and tr.lat_h.dtype == dt
+    assert (tr.loss_scale is not None) == (prec == "fp16")
+    losses = []
+    for it in range(300):
+        st = tr.step()
+        if it % 20 == 0 or it >= 280:
+            losses.append(st.cpu().numpy()[0])
+    assert np.isfinite(losses).all()
+    assert np.mean(losses[-5:]) < 0.5 * losses[0], losses
+    assert torch.equal(tr.lat_h, tr.latents.to(dt))
+    if tr.loss_scale is not None:
+        s = tr.loss_scale.read()
+        assert s["skipped_steps"] <= 3 and s["scale"] >= 2.0 ** 12, s
+
+
 def test_train_step_with_host_perm(small_scene):
     """The step accepts the reference's `perm` (pixel indices); with a sample budget no ray
     overflows, two runs agree up to the order of float atomics (which rays fit an overflowing
