@@ -40,6 +40,12 @@ FORMS = {"fp32-march": ("fp32", "march", "fp32", False), "bf16-march": ("bf16", 
 UNIT = "rays/s"
 WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
            "L16 F2 T2^19 Nmin16 Nmax2048, MLP 32-64-16 / 32-64-64-3, R=S=2^18, Adam lr1e-2, fp32"
+WORKLOAD4 = "config4: NGP train step on 512 Gaussian blobs + 8 thin shells (r~U[0.1,0.4], thickness 0.01), 200 cams " \
+            "800x800 fov40 r4, G=128 K=1 diag=1024, L16 F2 T2^19, R=S=2^20, Adam lr1e-2"
+# scene: blobs, shells, views, resolution, samples (= rays) per step, workload, metric
+SCENES = {"blobs64": (64, 0, 100, 800, 1 << 18, WORKLOAD, METRIC),
+          "config4": (512, 8, 200, 800, 1 << 20, WORKLOAD4,
+                      "train rays/s (plain FP32 hash-grid NeRF step, 512 blobs + 8 shells, 2^20 samples)")}
 
 
 def parse():
@@ -49,9 +55,15 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--pretrain", type=int, default=300, help="untimed training steps before warm-up")
-    p.add_argument("--samples", type=int, default=1 << 18)
-    p.add_argument("--views", type=int, default=100)
-    p.add_argument("--res", type=int, default=800)
+    p.add_argument("--scene", default="blobs64", choices=sorted(SCENES),
+                   help="blobs64: 64 blobs, 100 views, 2^18 samples (the headline); config4: 512 blobs + 8 shells, "
+                        "200 views, 2^20 samples")
+    p.add_argument("--samples", type=int, default=None, help="samples (= rays) per step; default from the scene")
+    p.add_argument("--views", type=int, default=None)
+    p.add_argument("--res", type=int, default=None)
+    p.add_argument("--equal-psnr-steps", type=int, default=2000,
+                   help="steps of the plain step whose held-out PSNR the fastest proposal form must reach (0: skip)")
+    p.add_argument("--equal-psnr-every", type=int, default=250)
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -63,7 +75,14 @@ def parse():
     p.add_argument("--render-frames", type=int, default=12, help="1920x1080 frames rendered on a 120-pose orbit")
     p.add_argument("--render-slots", type=int, default=1 << 18, help="rays in flight in the inference renderer")
     p.add_argument("--render-cap", type=int, default=8, help="march_steps_cap of the inference renderer")
-    return p.parse_args()
+    args = p.parse_args()
+    sc = SCENES[args.scene]
+    args.n_blobs, args.n_shells = sc[0], sc[1]
+    args.views = args.views or sc[2]
+    args.res = args.res or sc[3]
+    args.samples = args.samples or sc[4]
+    args.workload, args.metric = sc[5], sc[6]
+    return args
 
 
 # ------------------------------------------------------------------------------ clocks sampler
@@ -371,19 +390,21 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     quality = {"psnr_heldout": round(evaluate_psnr(tr, n_views=2), 3), "views": 2, "steps_trained": tr.step_count,
                "judge": "occupancy-grid inference renderer, white background, 4096-step quadrature ground truth"}
 
-    out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    out = {"metric": args.metric, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(form),
-           "data": "synthetic (procedural 64-blob scene, GT by 4096-step quadrature; NeRF-synthetic not used)",
-           "config": {"workload": WORKLOAD, "rays_per_step": R, "sample_budget": args.samples,
+           "data": f"synthetic (procedural scene: {args.n_blobs} blobs, {args.n_shells} shells; GT by 4096-step "
+                   "quadrature; NeRF-synthetic not used)",
+           "config": {"workload": args.workload, "rays_per_step": R, "sample_budget": args.samples,
                       "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,
                       "occupancy_init": "analytic scene density, then learned updates",
                       "mean_samples_per_step": round(samples_used, 1),
                       "mean_composited_samples_per_step": round(float(a[2]) / args.steps, 1),
                       "mean_samples_per_valid_ray": round(samples_used / max(rays / args.steps, 1), 2),
                       "valid_rays_per_step": round(rays / args.steps, 1),
-                      "l2": "per-step working set (table 46.5 MB + 2^18-sample buffers ~70 MB) is touched once per step; "
-                            "no flush", "parallelism": f"replicas x{world}"},
+                      "l2": f"per-step working set (table 46.5 MB + {args.samples}-sample buffers "
+                            f"~{args.samples * 280 // 2**20} MB) is touched once per step; no flush",
+                      "parallelism": f"replicas x{world}"},
            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": 4 * R,
                    "d2h_bytes_per_step": 16},
            "gpu_launches": int(launches), "roofline": roof, "kernels": breakdown, "clocks": clk.summary()}
@@ -447,6 +468,45 @@ def render_fps(args, tr, stream) -> dict:
             "ms_per_frame_by_entry": {k: round(v, 4) for k, v in sorted(per.items(), key=lambda kv: -kv[1])}}
 
 
+def equal_psnr(args, data, plain: str, fast: str) -> dict:
+    """Time to quality: trains the plain step for `equal_psnr_steps` steps and the fast form until
+    its held-out PSNR (checked every `equal_psnr_every` steps, outside the timed chunks) reaches the
+    plain step's final PSNR.  Training time is device time of the steps (CUDA events), occupancy-grid
+    refreshes included."""
+    import torch
+    from jaxngp_gb300.trainer import HeldOut, NGPTrainer, TrainConfig
+    ev = HeldOut(data, n_views=2)
+    curves, target = {}, None
+    for f in (plain, fast):
+        precision, sampler, table, half_act = FORMS[f]
+        tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
+                                          table_precision=table, half_activations=half_act))
+        tr.init_occupancy_analytic()
+        stream = torch.cuda.current_stream()
+        t, pts = 0.0, []
+        while tr.step_count < args.equal_psnr_steps:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.equal_psnr_every):
+                tr.step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t += e0.elapsed_time(e1) / 1e3
+            pts.append((tr.step_count, round(t, 4), round(ev.psnr(tr), 3)))
+            if target is not None and pts[-1][2] >= target:
+                break
+        curves[f] = pts
+        if target is None:
+            target = pts[-1][2]
+    hit = next((p for p in curves[fast] if p[2] >= target), None)
+    out = {"target_psnr": target, "plain": plain, "fast": fast,
+           "plain_steps": curves[plain][-1][0], "plain_seconds": curves[plain][-1][1],
+           "fast_steps": hit[0] if hit else None, "fast_seconds": hit[1] if hit else None,
+           "time_ratio": round(curves[plain][-1][1] / hit[1], 3) if hit else None,
+           "curves": {f: [list(p) for p in c] for f, c in curves.items()}}
+    return out
+
+
 def main():
     args = parse()
     import numpy as np
@@ -457,24 +517,25 @@ def main():
         if rank != 0:
             return 0
         from jaxngp_gb300.scene import BlobScene, PinholeCamera, hemisphere_poses, poses_to_transforms
-        blob = BlobScene.random(64, 0, 0)
+        blob = BlobScene.random(args.n_blobs, args.n_shells, 0)
         cam = PinholeCamera.from_fov(args.res, args.res, 40.0)
         transforms = poses_to_transforms(hemisphere_poses(args.views, 4.0, np.random.default_rng(1)))
         t = time.perf_counter()
         steps = max(1, args.steps // 10)
         args.cpu_steps = max(1, min(args.cpu_steps, steps))
         cb = cpu_baseline(args, (blob.blobs, cam, transforms, 1.0), cores)
-        out = {"metric": METRIC, "value": round(cb["value"], 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        out = {"metric": args.metric, "value": round(cb["value"], 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-               "config": {"workload": WORKLOAD}, "cpu_baseline": cb,
+               "config": {"workload": args.workload}, "cpu_baseline": cb,
                "e2e": {"value": round(cb["value"], 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                "wall_s": round(time.perf_counter() - t, 2)}
         print(json.dumps(out))
         return 0
     world, rank, _ = setup_device(args)
     from jaxngp_gb300.scene import make_scene_data
-    data = make_scene_data(n_views=args.views, width=args.res, height=args.res, seed=0)
+    data = make_scene_data(n_blobs=args.n_blobs, n_shells=args.n_shells, n_views=args.views, width=args.res,
+                           height=args.res, seed=0)
     forms = [f.strip() for f in args.forms.split(",") if f.strip()]
     results = {}
     for f in forms:
@@ -500,10 +561,13 @@ def main():
                           "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3)}
             if cmp:
                 out["learned_proposal_vs_plain"] = {"plain": "fp32-march", **cmp}
+            if cmp and args.equal_psnr_steps > 0:
+                fastest = max(cmp, key=lambda f: results[f]["value"])
+                out["learned_proposal_vs_plain"]["at_equal_psnr"] = equal_psnr(args, data, "fp32-march", fastest)
     if rank == 0:
         if not args.no_cpu_baseline:
             from jaxngp_gb300.scene import BlobScene, PinholeCamera, hemisphere_poses, poses_to_transforms
-            blob = BlobScene.random(64, 0, 0)
+            blob = BlobScene.random(args.n_blobs, args.n_shells, 0)
             cam = PinholeCamera.from_fov(args.res, args.res, 40.0)
             transforms = poses_to_transforms(hemisphere_poses(args.views, 4.0, np.random.default_rng(1)))
             out["cpu_baseline"] = cpu_baseline(args, (blob.blobs, cam, transforms, 1.0), cores)

@@ -45,16 +45,17 @@ __global__ void __launch_bounds__(128) render_blobs_kernel(NgpRenderBlobsDescrip
     }
     float R = 0.f, Gc = 0.f, B = 0.f, Tr = 1.f;
     if (t1 > t0) {
-        // cull blobs: keep those whose 5-sigma ball meets the ray segment
-        std::uint32_t keep[64];
+        // cull blobs: keep those whose 5-sigma ball meets the ray segment (a per-thread list in
+        // local memory, up to every blob)
+        std::uint16_t keep[kMaxBlobs];
         int n_keep = 0;
-        for (std::uint32_t k = 0; k < d.n_blobs && n_keep < 64; ++k) {
+        for (std::uint32_t k = 0; k < d.n_blobs; ++k) {
             const float *bl = blobs + (std::size_t)k * 8;
             const float vx = bl[0] - ox, vy = bl[1] - oy, vz = bl[2] - oz;
             const float tc = vx * dx + vy * dy + vz * dz;
             const float qx = vx - tc * dx, qy = vy - tc * dy, qz = vz - tc * dz;
             const float r = 5.f * bl[3];
-            if (qx * qx + qy * qy + qz * qz <= r * r && tc + r >= t0 && tc - r <= t1) keep[n_keep++] = k;
+            if (qx * qx + qy * qy + qz * qz <= r * r && tc + r >= t0 && tc - r <= t1) keep[n_keep++] = (std::uint16_t)k;
         }
         const float dt = (t1 - t0) / (float)d.n_steps;
         for (std::uint32_t s = 0; s < d.n_steps && Tr > 1e-6f; ++s) {

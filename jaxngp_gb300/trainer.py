@@ -420,23 +420,36 @@ def near_far(bound: float, o: torch.Tensor, d: torch.Tensor):
     return ts.contiguous(), te.contiguous()
 
 
-@torch.no_grad()
+class HeldOut:
+    """Held-out views of a synthetic scene -- poses on the training hemisphere drawn with another
+    seed -- with their quadrature ground truth blended over white, rendered once."""
+
+    @torch.no_grad()
+    def __init__(self, data: SceneData, n_views: int = 2, seed: int = 12345, n_steps: int = 4096, radius: float = 4.0,
+                 device="cuda"):
+        from .scene import hemisphere_poses, poses_to_transforms, render_views
+        cam = data.camera
+        self.cam, self.n_views = cam, n_views
+        poses = hemisphere_poses(n_views, radius, np.random.default_rng(seed))
+        self.transforms = torch.from_numpy(poses_to_transforms(poses)).to(device)
+        gt = render_views(data.scene, cam, self.transforms, n_steps).view(n_views, cam.height, cam.width, 4).float() / 255
+        self.gt_rgb = (gt[..., :3] * gt[..., 3:] + (1 - gt[..., 3:])).mul(255).round().to(torch.uint8)
+
+    @torch.no_grad()
+    def psnr(self, tr: "NGPTrainer") -> float:
+        """Mean PSNR (utils/data.py:407-410) of the trainer's field rendered by the occupancy-grid
+        inference renderer over a white background."""
+        from .renderer import Renderer
+        from .scene import psnr_u8
+        r = Renderer.from_trainer(tr, n_slots=1 << 18)
+        vals = []
+        for v in range(self.n_views):
+            rgb, _ = r.render_image(self.cam, self.transforms[v], bg=(1.0, 1.0, 1.0))
+            vals.append(psnr_u8(rgb, self.gt_rgb[v]))
+        return float(np.mean(vals))
+
+
 def evaluate_psnr(tr: "NGPTrainer", n_views: int = 2, seed: int = 12345, n_steps: int = 4096,
                   radius: float = 4.0) -> float:
-    """Mean PSNR (utils/data.py:407-410) over held-out views -- poses on the training hemisphere
-    drawn with another seed -- rendered by the occupancy-grid inference renderer over a white
-    background, against the scene's quadrature ground truth blended over white."""
-    from .renderer import Renderer
-    from .scene import hemisphere_poses, poses_to_transforms, psnr_u8, render_views
-    cam = tr.data.camera
-    poses = hemisphere_poses(n_views, radius, np.random.default_rng(seed))
-    transforms = torch.from_numpy(poses_to_transforms(poses)).to(tr.dev)
-    gt = render_views(tr.data.scene, cam, transforms, n_steps).view(n_views, cam.height, cam.width, 4).float() / 255
-    gt_rgb = (gt[..., :3] * gt[..., 3:] + (1 - gt[..., 3:])).mul(255).round().to(torch.uint8)
-    r = Renderer.from_trainer(tr, n_slots=1 << 18)
-    vals = []
-    for v in range(n_views):
-        rgb, _ = r.render_image(cam, transforms[v], bg=(1.0, 1.0, 1.0))
-        vals.append(psnr_u8(rgb, gt_rgb[v]))
-    return float(np.mean(vals))
-
+    """Mean PSNR over `n_views` held-out views (HeldOut)."""
+    return HeldOut(tr.data, n_views, seed, n_steps, radius, tr.dev).psnr(tr)
