@@ -104,20 +104,42 @@ __global__ void __launch_bounds__(256) train_rays_kernel(
 // Two passes.  The light pass (a thread per ray) finishes every ray without samples -- its
 // prediction is the background -- and appends the rays with samples to a list (one atomic per
 // warp).  The heavy pass gives each listed ray a whole warp, warps taking rays from the list in
-// turn: 32-sample chunks are loaded coalesced into shared memory, all lanes compute the chunk's
-// opacities in parallel, and one lane runs the compositing recurrence from shared memory in the
-// reference's order (so every rounding is the reference's); in the backward pass the same lane
-// writes per-sample gradients to shared memory and the warp stores them coalesced.  Taking rays
+// turn, and runs the ray as segments of 32 samples (lane = sample, loads and stores coalesced):
+// the transmittance before and after each sample comes from a warp product scan of 1 - alpha,
+// the running colour sums of the backward from warp sum scans, the ray's totals from warp
+// reductions, and the transmittance and sums carry from segment to segment.  Products and sums
+// are formed in tree order rather than the reference's left-to-right order (a few ulps apart;
+// the termination test is the reference's: a sample counts while the transmittance before it is
+// above 1e-4).  Taking rays
 // from a list keeps the warps evenly loaded however the rays with samples cluster in the batch
 // (which rays fit the sample budget follows the order of the allocation atomics).  The loss sums
 // are reduced per block before their one atomic each.
 constexpr int kIlbWarps = 4;
 
-struct IlbChunk {
-    float4 c[32];
-    float dt[32], z[32], a[32], om[32];
-    float4 g[32];
-};
+// Inclusive warp scans (product and sum) and a warp sum that every lane receives.
+__device__ __forceinline__ float warp_prod_incl(float v, unsigned lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane >= o) v *= t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_incl(float v, unsigned lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane >= o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 __device__ __forceinline__ float huber_grad(float e, float delta, float *loss) {
     const float ae = fabsf(e);
@@ -187,8 +209,6 @@ __global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_heavy_kernel(
     const float *__restrict__ bgs, const float *__restrict__ gt, const float *__restrict__ dss,
     const float *__restrict__ z_vals, const float *__restrict__ drgbs, const std::uint32_t *__restrict__ heavy_count,
     const std::uint32_t *__restrict__ heavy, float *__restrict__ dL_ddrgbs, float *__restrict__ acc) {
-    __shared__ IlbChunk chunks[kIlbWarps];
-    IlbChunk &ch = chunks[threadIdx.x >> 5];
     const unsigned lane = lane_id();
     const std::uint32_t n_heavy = *heavy_count;
     const std::uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -207,43 +227,40 @@ __global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_heavy_kernel(
             tg[c] = gt[ray * 3 + c];
         }
         const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + s;
-        // ---- forward (integrating.cu:61-78)
+        // ---- forward (integrating.cu:61-78) over 32-sample segments: lane q takes sample q of the
+        // segment, a warp product scan of (1 - alpha) gives each sample's transmittance, sums are
+        // warp reductions, and the transmittance is carried to the next segment.  A sample is
+        // composited while the transmittance before it is above the threshold (a prefix of the
+        // segment: the product never grows).
         float T = 1.f, r = 0.f, g = 0.f, b = 0.f, dep = 0.f;
         std::uint32_t used = 0;
         for (std::uint32_t base = 0; base < n; base += 32) {
             const std::uint32_t cnt = min(32u, n - base);
-            if (lane < cnt) {
-                const float4 c = rc[base + lane];
-                const float dt = dss[s + base + lane];
-                ch.c[lane] = c;
-                ch.dt[lane] = dt;
-                ch.z[lane] = z_vals[s + base + lane];
-                const float a = 1.f - expf(-c.x * dt);
-                ch.a[lane] = a;
-                ch.om[lane] = 1.f - a;
+            const bool in = lane < cnt;
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            float dt = 0.f, z = 0.f;
+            if (in) {
+                c = rc[base + lane];
+                dt = dss[s + base + lane];
+                z = z_vals[s + base + lane];
             }
-            __syncwarp();
-            if (lane == 0) {
-                for (std::uint32_t q = 0; q < cnt && T > kTThreshold; ++q) {
-                    const float w = T * ch.a[q];
-                    const float4 c = ch.c[q];
-                    r += w * c.y;
-                    g += w * c.z;
-                    b += w * c.w;
-                    dep += w * ch.z[q];
-                    T *= ch.om[q];
-                    ++used;
-                }
-            }
-            T = __shfl_sync(0xffffffffu, T, 0);
-            __syncwarp();
-            if (!(T > kTThreshold)) break;
+            const float a = in ? 1.f - expf(-c.x * dt) : 0.f;
+            const float P = warp_prod_incl(1.f - a, lane);
+            const float Pup = __shfl_up_sync(0xffffffffu, P, 1);   // every lane takes part
+            const float Pex = lane == 0 ? 1.f : Pup;
+            const float Tq = T * Pex;
+            const bool use = in && Tq > kTThreshold;
+            const std::uint32_t nu = __popc(__ballot_sync(0xffffffffu, use));
+            const float w = use ? Tq * a : 0.f;
+            r += warp_sum(w * c.y);
+            g += warp_sum(w * c.z);
+            b += warp_sum(w * c.w);
+            dep += warp_sum(w * z);
+            const float Pend = __shfl_sync(0xffffffffu, P, nu > 0 ? (int)nu - 1 : 0);
+            if (nu > 0) T *= Pend;
+            used += nu;
+            if (nu < cnt || !(T > kTThreshold)) break;
         }
-        r = __shfl_sync(0xffffffffu, r, 0);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        b = __shfl_sync(0xffffffffu, b, 0);
-        dep = __shfl_sync(0xffffffffu, dep, 0);
-        used = __shfl_sync(0xffffffffu, used, 0);
         const float fo = 1.f - T;
         float fr[4];
         if (T <= kTThreshold) {
@@ -265,45 +282,47 @@ __global__ void __launch_bounds__(32 * kIlbWarps) integrate_loss_heavy_kernel(
             }
             used_f += (float)used;
         }
-        // ---- backward (integrating.cu:173-233), recomputing the forward
+        // ---- backward (integrating.cu:173-233), recomputing the forward with the same scans:
+        // T_{k+1} from the product scan, the running colour/depth sums cur_k from inclusive sum
+        // scans, both carried across segments
         const bool terminated = fo >= 1.f - kTThreshold;
         const float bgterm = terminated ? 0.f : 1.f - fo;
         float4 *gc = reinterpret_cast<float4 *>(dL_ddrgbs) + s;
         float Tb = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, cd = 0.f;
         for (std::uint32_t base = 0; base < used; base += 32) {
             const std::uint32_t cnt = min(32u, used - base);
-            if (lane < cnt) {
-                const float4 c = rc[base + lane];
-                const float dt = dss[s + base + lane];
-                ch.c[lane] = c;
-                ch.dt[lane] = dt;
-                ch.z[lane] = z_vals[s + base + lane];
-                const float a = 1.f - expf(-c.x * dt);
-                ch.a[lane] = a;
-                ch.om[lane] = 1.f - a;
+            const bool in = lane < cnt;
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            float dt = 0.f, z = 0.f;
+            if (in) {
+                c = rc[base + lane];
+                dt = dss[s + base + lane];
+                z = z_vals[s + base + lane];
             }
-            __syncwarp();
-            if (lane == 0) {
-                for (std::uint32_t q = 0; q < cnt; ++q) {
-                    const float4 c = ch.c[q];
-                    const float z = ch.z[q], dt = ch.dt[q];
-                    const float w = Tb * ch.a[q];
-                    cr += w * c.y;
-                    cg += w * c.z;
-                    cb += w * c.w;
-                    cd += w * z;
-                    Tb *= ch.om[q];
-                    const float dsig = dt * (go[0] * (Tb * c.y - (fr[0] - cr) - bg[0] * bgterm)
-                                           + go[1] * (Tb * c.z - (fr[1] - cg) - bg[1] * bgterm)
-                                           + go[2] * (Tb * c.w - (fr[2] - cb) - bg[2] * bgterm)
-                                           + 0.f * (Tb * z - (fr[3] - cd)));
-                    const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
-                    ch.g[q] = make_float4(fminf(z * z, 1.f) * dsig + reg, w * go[0], w * go[1], w * go[2]);
-                }
+            const float a = in ? 1.f - expf(-c.x * dt) : 0.f;
+            const float P = warp_prod_incl(1.f - a, lane);
+            const float Pup = __shfl_up_sync(0xffffffffu, P, 1);   // every lane takes part
+            const float Pex = lane == 0 ? 1.f : Pup;
+            const float w = Tb * Pex * a;
+            const float Tn = Tb * P;
+            const float qr = cr + warp_sum_incl(w * c.y, lane);
+            const float qg = cg + warp_sum_incl(w * c.z, lane);
+            const float qb = cb + warp_sum_incl(w * c.w, lane);
+            const float qd = cd + warp_sum_incl(w * z, lane);
+            if (in) {
+                const float dsig = dt * (go[0] * (Tn * c.y - (fr[0] - qr) - bg[0] * bgterm)
+                                       + go[1] * (Tn * c.z - (fr[1] - qg) - bg[1] * bgterm)
+                                       + go[2] * (Tn * c.w - (fr[2] - qb) - bg[2] * bgterm)
+                                       + 0.f * (Tn * z - (fr[3] - qd)));
+                const float reg = ((double)c.x > 4e-5 && z < near_distance) ? 1e-4f : 0.0f;
+                gc[base + lane] = make_float4(fminf(z * z, 1.f) * dsig + reg, w * go[0], w * go[1], w * go[2]);
             }
-            __syncwarp();
-            if (lane < cnt) gc[base + lane] = ch.g[lane];
-            __syncwarp();
+            const int lastl = (int)cnt - 1;
+            Tb = __shfl_sync(0xffffffffu, Tn, lastl);
+            cr = __shfl_sync(0xffffffffu, qr, lastl);
+            cg = __shfl_sync(0xffffffffu, qg, lastl);
+            cb = __shfl_sync(0xffffffffu, qb, lastl);
+            cd = __shfl_sync(0xffffffffu, qd, lastl);
         }
         for (std::uint32_t k = used + lane; k < n; k += 32) gc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }

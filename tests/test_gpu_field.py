@@ -184,3 +184,35 @@ def test_hashgrid_points_outside_the_box():
     want = H.encode(pos, lat, 1.0, tab)
     got = hashgrid_forward(t, cu(pos), cu(lat), 1.0).cpu().numpy()
     assert np.array_equal(got, want)
+
+
+def test_hashgrid_paired_and_single_row_paths_agree():
+    """A table (or table gradient) whose base is not aligned to a pair of rows takes one load (one
+    atomic) per corner; an aligned one fetches the two x-neighbour corners of an aligned row pair
+    with one 16-byte load (atomic).  Both give the oracle's results; samples along rays make
+    neighbouring lanes share corners, so the backward's segmented runs are exercised too."""
+    from jaxngp_gb300.encoders import LevelTable, hashgrid_backward, hashgrid_forward
+    rng = np.random.default_rng(7)
+    tab_np = H.LevelTable(16, 2 ** 16, 2, 16, 2048)
+    tab = LevelTable(16, 2 ** 16, 2, 16, 2048)
+    R, m = 512, 64
+    o = rng.uniform(-0.9, 0.9, size=(R, 1, 3))
+    d = rng.normal(size=(R, 1, 3))
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    pos = (o + d * (0.01 * np.arange(m))[None, :, None]).reshape(-1, 3).astype(np.float32)
+    lat = rng.uniform(-1, 1, size=(tab_np.n_params, 2)).astype(np.float32)
+    store = torch.zeros(tab_np.n_params + 1, 2, device="cuda")
+    store[1:] = cu(lat)
+    single = store[1:]   # 8-byte aligned, not 16
+    assert single.data_ptr() % 16 == 8
+    a = hashgrid_forward(tab, cu(pos), cu(lat), 1.0)
+    b = hashgrid_forward(tab, cu(pos), single, 1.0)
+    assert torch.equal(a, b)
+    assert np.array_equal(a.cpu().numpy(), H.encode(pos, lat, 1.0, tab_np))
+    g = rng.normal(size=(R * m, 32)).astype(np.float32)
+    ref = H.encode_backward(pos, g, 1.0, tab_np, dtype=np.float64)
+    ga = hashgrid_backward(tab, cu(pos), cu(g), 1.0)
+    gstore = torch.zeros(tab_np.n_params + 1, 2, device="cuda")
+    gb = hashgrid_backward(tab, cu(pos), cu(g), 1.0, out=gstore[1:])
+    assert rel_err(ga.cpu().numpy(), ref) <= RTOL
+    assert rel_err(gb.cpu().numpy(), ref) <= RTOL
