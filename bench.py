@@ -36,7 +36,11 @@ METRIC = "train rays/s (plain FP32 hash-grid NeRF step, 64-blob scene)"
 FORMS = {"fp32-march": ("fp32", "march", "fp32", False), "bf16-march": ("bf16", "march", "fp32", False),
          "bf16-proposal": ("bf16", "proposal", "fp32", False),
          "bf16x-march": ("bf16", "march", "bf16", True), "fp16x-march": ("fp16", "march", "fp16", True),
-         "bf16x-proposal": ("bf16", "proposal", "bf16", True), "fp16x-proposal": ("fp16", "proposal", "fp16", True)}
+         "bf16x-proposal": ("bf16", "proposal", "bf16", True), "fp16x-proposal": ("fp16", "proposal", "fp16", True),
+         "bf16x-proposal-fb": ("bf16", "proposal", "bf16", True)}
+# forms whose proposal steps also march, per ray, the rays on which the proposal misses > 1% of the
+# transmittance the occupancy grid implies
+FALLBACK_FORMS = {"bf16x-proposal-fb"}
 UNIT = "rays/s"
 WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
            "L16 F2 T2^19 Nmin16 Nmax2048, MLP 32-64-16 / 32-64-64-3, R=S=2^18, Adam lr1e-2, fp32"
@@ -64,10 +68,14 @@ def parse():
     p.add_argument("--equal-psnr-steps", type=int, default=2000,
                    help="steps of the plain step whose held-out PSNR the fastest proposal form must reach (0: skip)")
     p.add_argument("--equal-psnr-every", type=int, default=250)
+    p.add_argument("--convergence-steps", type=int, default=0,
+                   help="quality study instead of the bench line: train each form this many steps and print "
+                        "held-out PSNR (4 views) against device training time every --convergence-every steps")
+    p.add_argument("--convergence-every", type=int, default=2500)
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--forms", default="fp32-march,bf16-march,bf16-proposal,bf16x-proposal,fp16x-proposal",
+    p.add_argument("--forms", default="fp32-march,bf16-march,bf16-proposal,bf16x-proposal,fp16x-proposal,bf16x-proposal-fb",
                    help="training forms to run, the first is the headline: fp32-march (the reference's "
                         "algorithm, FP32 SIMT field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
                         "(learned proposal sampler + BF16 MLP); the x forms (bf16x-*, fp16x-*) also gather from a "
@@ -271,7 +279,7 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     L.lib().ngp_kernel_launches.restype = __import__("ctypes").c_ulonglong
     precision, sampler, table, half_act = FORMS[form]
     cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=precision, sampler=sampler,
-                      table_precision=table, half_activations=half_act)
+                      table_precision=table, half_activations=half_act, proposal_fallback=form in FALLBACK_FORMS)
     tr = NGPTrainer(data, cfg)
     tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
@@ -409,6 +417,10 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
                    "d2h_bytes_per_step": 16},
            "gpu_launches": int(launches), "roofline": roof, "kernels": breakdown, "clocks": clk.summary()}
     out["quality"] = quality
+    if tr.prop is not None:
+        out["proposal"] = {"slots_per_step": tr.prop.slots, "samples_per_ray": tr.prop.spr,
+                           "fallback_rays_per_proposal_step": round(tr.prop.fallback_rate(), 1)
+                           if cfg.proposal_fallback else None, "march_every": cfg.march_every}
     if render is not None:
         out["render_1080p"] = render
     return out
@@ -480,7 +492,8 @@ def equal_psnr(args, data, plain: str, fast: str) -> dict:
     for f in (plain, fast):
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
-                                          table_precision=table, half_activations=half_act))
+                                          table_precision=table, half_activations=half_act,
+                                          proposal_fallback=f in FALLBACK_FORMS))
         tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()
         t, pts = 0.0, []
@@ -504,6 +517,37 @@ def equal_psnr(args, data, plain: str, fast: str) -> dict:
            "fast_steps": hit[0] if hit else None, "fast_seconds": hit[1] if hit else None,
            "time_ratio": round(curves[plain][-1][1] / hit[1], 3) if hit else None,
            "curves": {f: [list(p) for p in c] for f, c in curves.items()}}
+    return out
+
+
+def convergence(args, data, forms) -> dict:
+    """Held-out PSNR against device training time for each form, from the same initial state."""
+    import torch
+    from jaxngp_gb300.trainer import HeldOut, NGPTrainer, TrainConfig
+    ev = HeldOut(data, n_views=4)
+    out = {}
+    for f in forms:
+        precision, sampler, table, half_act = FORMS[f]
+        tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
+                                          table_precision=table, half_activations=half_act,
+                                          proposal_fallback=f in FALLBACK_FORMS))
+        tr.init_occupancy_analytic()
+        stream = torch.cuda.current_stream()
+        t, curve = 0.0, []
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            while tr.step_count < args.convergence_steps:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(args.convergence_every):
+                    tr.step()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                t += e0.elapsed_time(e1) / 1e3
+                curve.append([tr.step_count, round(t, 3), round(ev.psnr(tr), 3)])
+        out[f] = {"curve": curve, "final_psnr": curve[-1][2], "seconds": curve[-1][1], "clocks": clk.summary(),
+                  "loss_scale": tr.loss_scale.read() if tr.loss_scale is not None else None}
+        del tr
+        torch.cuda.empty_cache()
     return out
 
 
@@ -537,6 +581,13 @@ def main():
     data = make_scene_data(n_blobs=args.n_blobs, n_shells=args.n_shells, n_views=args.views, width=args.res,
                            height=args.res, seed=0)
     forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    if args.convergence_steps > 0:
+        if rank == 0:
+            print(json.dumps({"study": "convergence", "scene": args.scene, "steps": args.convergence_steps,
+                              "every": args.convergence_every, "psnr_views": 4,
+                              "judge": "occupancy-grid inference renderer, white background, 4096-step quadrature "
+                                       "ground truth", "forms": convergence(args, data, forms)}))
+        return 0
     results = {}
     for f in forms:
         results[f] = run_ours(args, data, f, with_render=True)
@@ -545,7 +596,7 @@ def main():
     out["config"] = dict(head["config"], form=forms[0])
     if len(forms) > 1:
         out["forms"] = {f: {k: r[k] for k in ("value", "ms_per_step", "dtype", "e2e", "gpu_launches", "quality",
-                                               "roofline", "clocks")} | {
+                                               "roofline", "clocks") if k in r} | {"proposal": r.get("proposal")} | {
                             "valid_rays_per_step": r["config"]["valid_rays_per_step"],
                             "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
                             "top_kernels": dict(list(r["kernels"].items())[:6])}

@@ -593,6 +593,39 @@ int ngp_proposal_bin_points_status(cudaStream_t stream, void **buffers, const ch
 void ngp_proposal_sample(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_sample_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* Per-ray fallback of the proposal sampler to the occupancy-grid march (no reference
+ * counterpart).  Where the grid marks a bin's cell occupied, the field's density is at least the
+ * grid's threshold; where the proposal's density is below it, the proposal misses mass the field
+ * has.  A slot whose ray misses more than 1% of its transmittance -- the sum over occupied bins of
+ * T_i (1 - exp(-max(0, threshold - sigma_i) delta)), T_i the proposal's transmittance before
+ * bin i -- is flagged and its ray appended to the fallback list.
+ * buffers: counts u32[3], rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins f32[slots*64],
+ * occupancy bitfield u8[G^3/8], threshold f32[1] -> slot_flag u8[slots], fallback_rays u32[R],
+ * fallback_count u32[1] (zeroed by the call), fallback_total u32[1] (accumulated across calls).
+ * opaque: NgpProposalDescriptor (n = R, total_samples, G, bound, samples_per_ray; K = 1). */
+void ngp_proposal_judge(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_judge_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* The training march (ngp_march_rays_train's probe form) over the rays fallback_rays[0 ..
+ * *fallback_count), allocating sample ranges from next_sample_write_location /
+ * number_of_exceeded_samples as they stand: the counters are not reset and the unwritten tail is
+ * not zeroed, because ngp_proposal_sample_alloc allocates after it.
+ * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call),
+ * fallback_rays u32[n], fallback_count u32[1].  opaque: MarchingDescriptor (n_rays bounds the list). */
+void ngp_march_rays_fallback(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_march_rays_fallback_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
+/* ngp_proposal_sample for the fallback flow: slots flagged by ngp_proposal_judge are skipped (their
+ * rays were marched); every other slot takes samples_per_ray samples from the same counters (rays
+ * past the budget are invalid, as in march_rays) and writes its ray's validity, count and start.
+ * counts[2] becomes the number of samples written and the buffers past it are zeroed.
+ * buffers: counts u32[3] (in/out), rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins,
+ * slot_flag u8[slots], next_sample_write_location u32[1], number_of_exceeded_samples u32[1] ->
+ * idcs, xyzs, dirs, dss, z_vals, ray_is_valid, rays_n_samples, rays_sample_startidx.
+ * opaque: NgpProposalDescriptor. */
+void ngp_proposal_sample_alloc(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_proposal_sample_alloc_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* Log-density regression: dL/dx = 2 w (x - log(sigma + 1e-3)) / n, w = 2 below the target, else 1.
  * buffers: counts u32[3] or NULL, x f32[n], sigma f32[n*stride] -> dL_dx f32[n], loss f32[1]
  * (the loss sum is added; the caller zeroes it). */

@@ -53,6 +53,18 @@ int launch_mlp_bf16_density(cudaStream_t, std::uint32_t, const float *, const fl
 int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                              const float *, const float *, const float *, float *, float *, unsigned *);
 int device_status();
+int launch_proposal_judge(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t, float, const float *,
+                          const float *, const float *, const std::uint32_t *, const float *, const float *, const float *,
+                          const std::uint8_t *, std::uint8_t *, std::uint32_t *, std::uint32_t *, std::uint32_t *);
+int launch_proposal_sample_alloc(cudaStream_t, std::uint32_t, std::uint32_t, std::uint32_t *, std::uint32_t, float, bool,
+                                 std::uint64_t, const float *, const float *, const std::uint32_t *, const float *,
+                                 const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *,
+                                 std::uint32_t *, float *, float *, float *, float *, bool *, std::uint32_t *,
+                                 std::uint32_t *);
+int launch_march_rays_list(cudaStream_t, const MarchingDescriptor &, const float *, const float *, const float *,
+                           const float *, const float *, const std::uint8_t *, std::uint32_t *, std::uint32_t *, bool *,
+                           std::uint32_t *, std::uint32_t *, std::uint32_t *, float *, float *, float *, float *,
+                           std::uint32_t *, const std::uint32_t *, const std::uint32_t *);
 int launch_mlp_tc_forward(cudaStream_t, std::uint32_t, bool, std::uint32_t, const std::uint32_t *, const void *,
                           const float *, const float *, float *);
 int launch_mlp_tc_density(cudaStream_t, std::uint32_t, bool, std::uint32_t, const void *, const float *, float *);
@@ -464,6 +476,28 @@ NGP_ENTRY(ngp_proposal_sample) {
                                   seed,
                                   CF32(1),
                                   CF32(2), CU32(3), CF32(4), CF32(5), CF32(6), U32(7), F32(8), F32(9), F32(10), F32(11));
+}
+
+NGP_ENTRY(ngp_proposal_judge) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    return launch_proposal_judge(stream, d.total_samples / proposal_spr(d), CU32(0), d.G, d.bound, CF32(8), CF32(1), CF32(2),
+                                 CU32(3), CF32(4), CF32(5), CF32(6), CU8(7), U8(9), U32(10), U32(11), U32(12));
+}
+
+NGP_ENTRY(ngp_proposal_sample_alloc) {
+    NGP_DESC(NgpProposalDescriptor, d);
+    const std::uint64_t seed = ((std::uint64_t)d.seed_hi << 32) | d.seed_lo;
+    return launch_proposal_sample_alloc(stream, d.total_samples / proposal_spr(d), d.total_samples, U32(0), proposal_spr(d),
+                                        d.mix, d.perturb != 0, seed, CF32(1), CF32(2), CU32(3), CF32(4), CF32(5), CF32(6),
+                                        CU8(7), U32(8), U32(9), U32(10), F32(11), F32(12), F32(13), F32(14), B8(15),
+                                        U32(16), U32(17));
+}
+
+NGP_ENTRY(ngp_march_rays_fallback) {
+    NGP_DESC(MarchingDescriptor, d);
+    return launch_march_rays_list(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
+                                  U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), U32(16), CU32(17),
+                                  CU32(18));
 }
 
 NGP_ENTRY(ngp_proposal_loss) {

@@ -208,8 +208,11 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
     std::uint32_t *__restrict__ queue, bool *__restrict__ ray_is_valid,
     std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
     std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
-    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse) {
+    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse,
+    const std::uint32_t *__restrict__ ray_list, const std::uint32_t *__restrict__ list_count) {
     __shared__ std::uint32_t expand[1024];  // expand_bits(v), v < G (G <= 1024)
+    // list form: the rays to march are ray_list[0 .. *list_count) (taken through the queue)
+    if (ray_list != nullptr) n_rays = min(n_rays, *list_count);
     for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
     __syncthreads();
     const unsigned lane = lane_id();
@@ -241,8 +244,9 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
             }
             if (phase == kIdle) {
                 const std::uint32_t q = base + (unsigned)__popc(idle & lt_mask);
-                const std::uint32_t r = queue != nullptr ? q : (((q >> 5) * n_warps + warp) << 5) + (q & 31u);
-                if (r < n_rays) {
+                const std::uint32_t qi = queue != nullptr ? q : (((q >> 5) * n_warps + warp) << 5) + (q & 31u);
+                if (qi < n_rays) {
+                    const std::uint32_t r = ray_list != nullptr ? ray_list[qi] : qi;
                     ray = r;
                     o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
                     d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
@@ -676,17 +680,48 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
         if (probe) {
             march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse,
+                nullptr, nullptr);
         } else {
             march_rays_kernel<false><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse,
+                nullptr, nullptr);
         }
         count_launches(1);
     }
     if (d.total_samples > 0) {
         zero_sample_tail_kernel<<<grid_for(d.total_samples, 256, 8), 256, 0, stream>>>(
             d.total_samples, next_loc, n_exceeded, idcs, xyzs, dirs, dss, z_vals);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+// The training march (probe form) over the rays ray_list[0 .. *list_count), allocating from the
+// counters as they stand (they are not reset, and the unwritten tail is not zeroed: the caller
+// allocates more samples after this and finishes the buffers itself).  d.n_rays bounds the list.
+int launch_march_rays_list(cudaStream_t stream, const MarchingDescriptor &d, const float *rays_o, const float *rays_d,
+                           const float *t_starts, const float *t_ends, const float *noises, const std::uint8_t *bits,
+                           std::uint32_t *next_loc, std::uint32_t *n_exceeded, bool *ray_is_valid,
+                           std::uint32_t *rays_n_samples, std::uint32_t *rays_startidx, std::uint32_t *idcs, float *xyzs,
+                           float *dirs, float *dss, float *z_vals, std::uint32_t *queue, const std::uint32_t *ray_list,
+                           const std::uint32_t *list_count) {
+    NGP_CHECK_ARG(d.K > 0 && d.G > 0 && d.diagonal_n_steps > 0, "march_rays: K, G and diagonal_n_steps must be positive");
+    NGP_CHECK_ARG(d.G <= 1024 && (d.G & (d.G - 1)) == 0, "march_rays: G must be a power of two <= 1024 (Morton codes of other sizes exceed G^3)");
+    NGP_CHECK_ARG(d.K <= 16, "march_rays: at most 16 cascades");
+    NGP_CHECK_ARG(d.bound > 0.f && d.stepsize_portion >= 0.f, "march_rays: bound must be positive, stepsize_portion non-negative");
+    NGP_CHECK_ARG(queue != nullptr && ray_list != nullptr && list_count != nullptr, "march_rays (list): queue, ray list and its count are required");
+    NGP_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(std::uint32_t), stream));
+    const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
+    if (d.n_rays > 0) {
+        const unsigned warps_needed = (d.n_rays + 31) / 32;
+        const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
+        const unsigned cap = (unsigned)sm_count() * kMarchBlocksPerSm;
+        const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
+        march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
+            d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc, n_exceeded, queue,
+            ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, nullptr, ray_list, list_count);
         count_launches(1);
     }
     return launch_status();

@@ -181,7 +181,10 @@ __global__ void __launch_bounds__(32 * kSampleWarps) proposal_sample_kernel(
     const float *__restrict__ rays_o,
     const float *__restrict__ rays_d, const std::uint32_t *__restrict__ ray_of_slot, const float *__restrict__ slot_ta,
     const float *__restrict__ slot_tb, const float *__restrict__ x_bins, std::uint32_t *__restrict__ idcs,
-    float *__restrict__ xyzs, float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals) {
+    float *__restrict__ xyzs, float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals,
+    const std::uint8_t *__restrict__ slot_flag, std::uint32_t total_samples, std::uint32_t *__restrict__ next_loc,
+    std::uint32_t *__restrict__ n_exceeded, bool *__restrict__ ray_is_valid, std::uint32_t *__restrict__ rays_n_samples,
+    std::uint32_t *__restrict__ rays_startidx) {
     __shared__ float cdf_s[kSampleWarps][kBins], pdf_s[kSampleWarps][kBins];
     float *cdf = cdf_s[threadIdx.x >> 5], *pdf = pdf_s[threadIdx.x >> 5];
     const unsigned lane = lane_id();
@@ -189,6 +192,23 @@ __global__ void __launch_bounds__(32 * kSampleWarps) proposal_sample_kernel(
     const std::uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
     for (std::uint32_t j = warp0; j < n_slots; j += n_warps) {
         const std::uint32_t r = ray_of_slot[j];
+        std::size_t s_base = (std::size_t)j * spr;
+        if (next_loc != nullptr) {
+            // allocating form: flagged slots were marched; the others take spr samples here
+            if (slot_flag[j]) continue;
+            std::uint32_t start = 0;
+            if (lane == 0) {
+                start = atomicAdd(next_loc, spr);
+                const bool fits = (std::uint64_t)start + spr <= total_samples;
+                if (!fits) atomicAdd(n_exceeded, spr);
+                ray_is_valid[r] = fits;
+                rays_n_samples[r] = fits ? spr : 0u;
+                rays_startidx[r] = fits ? start : 0u;
+            }
+            start = __shfl_sync(0xffffffffu, start, 0);
+            if ((std::uint64_t)start + spr > total_samples) continue;
+            s_base = start;
+        }
         const float ta = slot_ta[j], tb = slot_tb[j];
         const float delta = (tb - ta) / (float)kBins;
         const float2 xv = reinterpret_cast<const float2 *>(x_bins + (std::size_t)j * kBins)[lane];
@@ -209,7 +229,6 @@ __global__ void __launch_bounds__(32 * kSampleWarps) proposal_sample_kernel(
         __syncwarp();
         const float o[3] = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
         const float d[3] = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
-        const std::size_t s_base = (std::size_t)j * spr;
         for (int k = (int)lane; k < (int)spr; k += 32) {
             const float e_lo = proposal_edge(k, spr, ta, tb, delta, perturb != 0, seed, r, cdf, pdf);
             const float e_hi = proposal_edge(k + 1, spr, ta, tb, delta, perturb != 0, seed, r, cdf, pdf);
@@ -226,6 +245,85 @@ __global__ void __launch_bounds__(32 * kSampleWarps) proposal_sample_kernel(
             dss[s] = e_hi - e_lo;
         }
         __syncwarp();
+    }
+}
+
+// Fallback test (a warp per slot, lane l holding bins 2l and 2l + 1).  The occupancy grid says
+// where the field's density is at least the grid's threshold; where the proposal's density is
+// below that, the proposal misses mass the field has.  The transmittance it misses there is
+// sum over occupied bins i of T_i (1 - exp(-max(0, threshold - sigma_i) delta)), T_i the
+// proposal's transmittance before bin i.  A slot whose ray misses more than kMissLimit is flagged
+// and its ray appended to the fallback list, for the occupancy-grid march.
+constexpr float kMissLimit = 0.01f;
+
+__global__ void __launch_bounds__(32 * kSampleWarps) proposal_judge_kernel(
+    const std::uint32_t *__restrict__ counts, std::uint32_t G, float mb, const float *__restrict__ threshold,
+    const float *__restrict__ rays_o, const float *__restrict__ rays_d, const std::uint32_t *__restrict__ ray_of_slot,
+    const float *__restrict__ slot_ta, const float *__restrict__ slot_tb, const float *__restrict__ x_bins,
+    const std::uint8_t *__restrict__ bits, std::uint8_t *__restrict__ slot_flag, std::uint32_t *__restrict__ fb_rays,
+    std::uint32_t *__restrict__ fb_count, std::uint32_t *__restrict__ fb_total) {
+    const unsigned lane = lane_id();
+    const std::uint32_t n_slots = counts[0];
+    const float thr = *threshold;
+    const float Gf = (float)G;
+    const int Gi = (int)G - 1;
+    const std::uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (std::uint32_t j = warp0; j < n_slots; j += n_warps) {
+        const std::uint32_t r = ray_of_slot[j];
+        const float ta = slot_ta[j], tb = slot_tb[j];
+        const float delta = (tb - ta) / (float)kBins;
+        const float2 xv = reinterpret_cast<const float2 *>(x_bins + (std::size_t)j * kBins)[lane];
+        const float s[2] = {expf(fminf(fmaxf(xv.x, -15.f), 15.f)), expf(fminf(fmaxf(xv.y, -15.f), 15.f))};
+        const float acc0 = warp_inclusive_scan_f(s[0] + s[1]) - (s[0] + s[1]);
+        const float acc[2] = {acc0, acc0 + s[0]};
+        const float o[3] = {rays_o[(std::size_t)r * 3 + 0], rays_o[(std::size_t)r * 3 + 1], rays_o[(std::size_t)r * 3 + 2]};
+        const float d[3] = {rays_d[(std::size_t)r * 3 + 0], rays_d[(std::size_t)r * 3 + 1], rays_d[(std::size_t)r * 3 + 2]};
+        float miss = 0.f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float t = ta + ((float)(2 * lane + h) + 0.5f) * delta;
+            std::uint32_t c[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float g = (((o[a] + t * d[a]) / mb + 1.0f) * 0.5f) * Gf;
+                c[a] = (std::uint32_t)min(max((int)floorf(g), 0), Gi);
+            }
+            const std::uint32_t m = expand_bits(c[0]) | (expand_bits(c[1]) << 1) | (expand_bits(c[2]) << 2);
+            const bool occ = (__ldg(bits + (m >> 3)) >> (m & 7u)) & 1u;
+            if (occ && s[h] < thr) miss += expf(-(delta * acc[h])) * -expm1f(-((thr - s[h]) * delta));
+        }
+        miss = warp_sum_f(miss);
+        if (lane == 0) {
+            const bool fb = miss > kMissLimit;
+            slot_flag[j] = fb ? 1 : 0;
+            if (fb) {
+                fb_rays[atomicAdd(fb_count, 1u)] = r;
+                atomicAdd(fb_total, 1u);
+            }
+        }
+    }
+}
+
+// counts[2] = the samples written ([0, next_loc - n_exceeded), capped at the budget); the slots
+// past it are zeroed (as march_rays does).
+__global__ void proposal_finish_kernel(std::uint32_t total_samples, const std::uint32_t *__restrict__ next_loc,
+                                       const std::uint32_t *__restrict__ n_exceeded, std::uint32_t *__restrict__ counts,
+                                       std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
+                                       float *__restrict__ dss, float *__restrict__ z_vals) {
+    std::uint32_t used = *next_loc - *n_exceeded;
+    if (used > total_samples) used = total_samples;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[2] = used;
+    const std::size_t stride = (std::size_t)gridDim.x * blockDim.x;
+    for (std::size_t q = used + (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total_samples; q += stride) {
+        idcs[q] = 0;
+        dss[q] = 0.f;
+        z_vals[q] = 0.f;
+        xyzs[q * 3 + 0] = 0.f;
+        xyzs[q * 3 + 1] = 0.f;
+        xyzs[q * 3 + 2] = 0.f;
+        dirs[q * 3 + 0] = 0.f;
+        dirs[q * 3 + 1] = 0.f;
+        dirs[q * 3 + 2] = 0.f;
     }
 }
 
@@ -308,9 +406,51 @@ int launch_proposal_sample(cudaStream_t stream, std::uint32_t max_slots, const s
         const unsigned want = (max_slots + kSampleWarps - 1) / kSampleWarps;
         proposal_sample_kernel<<<grid_for(want, 1, 16), 32 * kSampleWarps, 0, stream>>>(
             counts, spr, mix, perturb ? 1 : 0, seed, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, idcs, xyzs, dirs, dss,
-            z_vals);
+            z_vals, nullptr, 0u, nullptr, nullptr, nullptr, nullptr, nullptr);
         count_launches(1);
     }
+    return launch_status();
+}
+
+int launch_proposal_judge(cudaStream_t stream, std::uint32_t max_slots, const std::uint32_t *counts, std::uint32_t G,
+                          float bound, const float *threshold, const float *rays_o, const float *rays_d,
+                          const std::uint32_t *ray_of_slot, const float *slot_ta, const float *slot_tb,
+                          const float *x_bins, const std::uint8_t *bits, std::uint8_t *slot_flag, std::uint32_t *fb_rays,
+                          std::uint32_t *fb_count, std::uint32_t *fb_total) {
+    NGP_CHECK_ARG(G >= 8 && G <= 1024 && (G & (G - 1)) == 0, "proposal judge: G must be a power of two in [8, 1024]");
+    NGP_CHECK_ARG(bound > 0.f, "proposal judge: bound must be positive");
+    NGP_CUDA_TRY(cudaMemsetAsync(fb_count, 0, sizeof(std::uint32_t), stream));
+    if (max_slots > 0) {
+        const unsigned want = (max_slots + kSampleWarps - 1) / kSampleWarps;
+        proposal_judge_kernel<<<grid_for(want, 1, 16), 32 * kSampleWarps, 0, stream>>>(
+            counts, G, fminf(1.0f, bound), threshold, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, bits, slot_flag,
+            fb_rays, fb_count, fb_total);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+// The allocating form: after the fallback rays were marched (allocating from next_loc /
+// n_exceeded), every unflagged slot takes spr samples from the same counters; counts[2] becomes
+// the samples written and the rest of the buffers is zeroed.
+int launch_proposal_sample_alloc(cudaStream_t stream, std::uint32_t max_slots, std::uint32_t total_samples,
+                                 std::uint32_t *counts, std::uint32_t spr, float mix, bool perturb, std::uint64_t seed,
+                                 const float *rays_o, const float *rays_d, const std::uint32_t *ray_of_slot,
+                                 const float *slot_ta, const float *slot_tb, const float *x_bins,
+                                 const std::uint8_t *slot_flag, std::uint32_t *next_loc, std::uint32_t *n_exceeded,
+                                 std::uint32_t *idcs, float *xyzs, float *dirs, float *dss, float *z_vals, bool *valid,
+                                 std::uint32_t *n_samples, std::uint32_t *startidx) {
+    NGP_CHECK_ARG(mix >= 0.f && mix <= 1.f, "proposal: mix must be in [0, 1]");
+    if (max_slots > 0) {
+        const unsigned want = (max_slots + kSampleWarps - 1) / kSampleWarps;
+        proposal_sample_kernel<<<grid_for(want, 1, 16), 32 * kSampleWarps, 0, stream>>>(
+            counts, spr, mix, perturb ? 1 : 0, seed, rays_o, rays_d, ray_of_slot, slot_ta, slot_tb, x_bins, idcs, xyzs, dirs, dss,
+            z_vals, slot_flag, total_samples, next_loc, n_exceeded, valid, n_samples, startidx);
+        count_launches(1);
+    }
+    proposal_finish_kernel<<<grid_for(total_samples > 0 ? total_samples : 1, 256, 8), 256, 0, stream>>>(
+        total_samples, next_loc, n_exceeded, counts, idcs, xyzs, dirs, dss, z_vals);
+    count_launches(1);
     return launch_status();
 }
 

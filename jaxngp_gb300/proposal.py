@@ -12,9 +12,11 @@ Per training step:
                occupied cells (ngp_proposal_loss), its own backward and Adam
 
 Every k-th training step (TrainConfig.march_every, 8 by default) marches the occupancy grid instead
--- the sampler's fallback: its evenly spread samples train the field's empty space, which the
-proposal's concentrated samples rarely visit, and teach the proposal where its density is wrong.
-Without it the field keeps density the occupancy-grid renderer (the judge) then shows.
+-- the sampler's fallback for whole steps: its evenly spread samples train the field's empty
+space, which the proposal's concentrated samples rarely visit, and teach the proposal where its
+density is wrong.  Without it the field keeps density the occupancy-grid renderer (the judge) then
+shows.  Per ray (TrainConfig.proposal_fallback), rays on which the proposal misses more than 1% of
+the transmittance the occupancy grid implies are marched within the step (sample()).
 
 Everything stays on the device; the sample count of a step is read by the kernels from `counts`.
 """
@@ -74,6 +76,15 @@ class ProposalSampler:
         self.coarse = torch.zeros(Gc ** 3, dtype=torch.uint8, device=self.dev)
         self.counters = torch.zeros(2, **i32)
         self.counts = torch.zeros(3, **i32)
+        # per-ray fallback to the occupancy-grid march: flagged slots, the list of their rays, and
+        # the sample counters the marched rays and then the proposal's rays allocate from
+        self.slot_flag = torch.zeros(self.slots, dtype=torch.uint8, device=self.dev)
+        self.fb_rays = torch.zeros(n_rays, **i32)
+        self.fb_count = torch.zeros(1, **i32)
+        self.fb_total = torch.zeros(1, **i32)
+        self.alloc = torch.zeros(2, **i32)
+        self.queue = torch.zeros(1, **i32)
+        self.sample_calls = 0
         self.ray_of_slot = torch.zeros(self.slots, **i32)
         self.slot_ta, self.slot_tb = torch.zeros(self.slots, **f32), torch.zeros(self.slots, **f32)
         nb = self.slots * BINS
@@ -111,18 +122,43 @@ class ProposalSampler:
                L.NgpMlpDescriptor(n, 0))
 
     def sample(self, rays_o, rays_d, t0, t1, valid, n_samples, startidx, idcs, xyzs, dirs, dss, z_vals,
-               perturb: bool, seed: int) -> torch.Tensor:
-        """Fills the march_rays-layout sample buffers; returns the device count of samples (u32[1])."""
+               perturb: bool, seed: int, fallback=None) -> torch.Tensor:
+        """Fills the march_rays-layout sample buffers; returns the device count of samples (u32[1]).
+
+        `fallback` = (occupancy bitfield, density threshold f32[1], noises f32[R], MarchingDescriptor)
+        turns on the per-ray fallback: rays on which the proposal misses more than 1% of the
+        transmittance the occupancy grid implies (ngp_proposal_judge) are marched instead
+        (ngp_march_rays_fallback, first, so they find room in the budget), and the other rays take
+        their proposal samples after them (ngp_proposal_sample_alloc)."""
         n = rays_o.shape[0]
+        self.sample_calls += 1
         L.call("ngp_proposal_rays", [rays_o, rays_d, t0, t1, self.coarse, self.counters[0:1], self.counters[1:2], valid,
                                      n_samples, startidx, self.ray_of_slot, self.slot_ta, self.slot_tb, self.counts],
                self._desc(n))
         L.call("ngp_proposal_bin_points", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb,
                                            self.points], self._desc())
         self.network(self.points, self.enc_b, self.x_b, self.counts[1:2], f16=self.f16)
-        L.call("ngp_proposal_sample", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb,
-                                       self.x_b, idcs, xyzs, dirs, dss, z_vals], self._desc(perturb=perturb, seed=seed))
+        if fallback is None:
+            L.call("ngp_proposal_sample", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb,
+                                           self.x_b, idcs, xyzs, dirs, dss, z_vals], self._desc(perturb=perturb, seed=seed))
+            return self.counts[2:3]
+        bits, threshold, noises, d_march = fallback
+        L.call("ngp_proposal_judge", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb, self.x_b,
+                                      bits, threshold, self.slot_flag, self.fb_rays, self.fb_count, self.fb_total],
+               self._desc(n))
+        self.alloc.zero_()
+        L.call("ngp_march_rays_fallback", [rays_o, rays_d, t0, t1, noises, bits, self.alloc[0:1], self.alloc[1:2], valid,
+                                           n_samples, startidx, idcs, xyzs, dirs, dss, z_vals, self.queue, self.fb_rays,
+                                           self.fb_count], d_march)
+        L.call("ngp_proposal_sample_alloc", [self.counts, rays_o, rays_d, self.ray_of_slot, self.slot_ta, self.slot_tb,
+                                             self.x_b, self.slot_flag, self.alloc[0:1], self.alloc[1:2], idcs, xyzs, dirs,
+                                             dss, z_vals, valid, n_samples, startidx],
+               self._desc(perturb=perturb, seed=seed))
         return self.counts[2:3]
+
+    def fallback_rate(self) -> float:
+        """Mean fallback rays per sampling call so far (reads the device counter)."""
+        return float(self.fb_total.item()) / max(self.sample_calls, 1)
 
     # ----------------------------------------------------------------------------- training
     def train(self, xyzs: torch.Tensor, drgbs: torch.Tensor, distill: Optional[Callable] = None, lr: Optional[float] = None,

@@ -59,6 +59,7 @@ class TrainConfig:
     proposal_samples: int = 48         # samples on each ray the proposal samples
     proposal_mix: float = 0.1          # share of a uniform pdf mixed into the proposal's
     march_every: int = 8               # proposal sampler: every k-th step marches the occupancy grid (0: never)
+    proposal_fallback: bool = False    # proposal sampler: march the rays whose proposal misses > 1% of transmittance
     proposal_train_points: int = 1 << 16   # field samples a proposal update regresses on (at most)
     march_coarse_skip: bool = False    # march: finish rays that cross no occupied coarse block at once
                                        # (exact; pays off on sparse grids, costs ~3% on dense ones)
@@ -316,9 +317,10 @@ class NGPTrainer:
             L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
             cnt = self.count
         else:
+            fb = (self.bitfield, self.threshold, self.noise, self._d_march) if cfg.proposal_fallback else None
             cnt = self.prop.sample(self.rays_o, self.rays_d, self.t0, self.t1, self.valid, self.n_samples,
                                    self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals, cfg.perturb,
-                                   seed ^ 0x5BD1E9955BD1E995)
+                                   seed ^ 0x5BD1E9955BD1E995, fallback=fb)
         L.call(self._hg_fwd[0], [self.xyzs, self.gather_table, cnt, self.enc], self._hg_fwd[1])
         self.field.forward(self.enc, self.dirs, self.weights, cnt, self.drgbs)
         if self.prop is not None and (use_march or self.step_count % cfg.proposal_every == 0):

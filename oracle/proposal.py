@@ -226,3 +226,29 @@ def sample_ray(x_bins: np.ndarray, ta: float, tb: float, xi: np.ndarray, n_sampl
     t = ((e[:-1] + e[1:]) * f(0.5)).astype(f)
     ds = (e[1:] - e[:-1]).astype(f)
     return t, ds
+
+
+MISS_LIMIT = 0.01
+
+
+def missed_transmittance(x_bins: np.ndarray, ta: float, tb: float, o, d, bits: np.ndarray, G: int, bound: float,
+                         threshold: float) -> float:
+    """The per-ray fallback test (ngp_proposal_judge), in float64: the occupancy grid marks the bins
+    whose cell holds density >= threshold; where the proposal's density sigma_i is below that the
+    proposal misses mass, and the transmittance it misses is
+    sum over occupied bins of T_i (1 - exp(-(threshold - sigma_i) delta)), T_i = exp(-delta
+    sum_{j<i} sigma_j).  A ray is marched instead when this exceeds MISS_LIMIT."""
+    f = np.float32
+    occ = np.unpackbits(np.asarray(bits, np.uint8), bitorder="little").astype(bool)
+    ta64, tb64 = float(f(ta)), float(f(tb))
+    delta = (tb64 - ta64) / N_BINS
+    s = np.exp(np.clip(np.asarray(x_bins, np.float64), -15, 15))
+    acc = np.concatenate([[0.0], np.cumsum(s)[:-1]])
+    T = np.exp(-delta * acc)
+    mb = min(1.0, float(bound))
+    t = ta64 + (np.arange(N_BINS) + 0.5) * delta
+    pos = np.asarray(o, np.float64)[None, :] + t[:, None] * np.asarray(d, np.float64)[None, :]
+    g = np.clip(np.floor((pos / mb + 1.0) * 0.5 * G), 0, G - 1).astype(np.int64)
+    cell_occ = occ[_morton3(g[:, 0], g[:, 1], g[:, 2])]
+    short = np.maximum(threshold - s, 0.0)
+    return float(np.sum(np.where(cell_occ, T * -np.expm1(-short * delta), 0.0)))
