@@ -25,6 +25,12 @@
 // Every mbarrier wait gives up after kWaitLimit polls; the warpgroup then stops, records
 // NGP_ERR_DEVICE for ngp_device_status(), and releases its tensor memory.
 #include "common.cuh"
+#include <cstring>
+#include <type_traits>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "half.cuh"
 #include "tc.cuh"
 
@@ -47,8 +53,9 @@ constexpr int kG4 = 10240, kG3 = 11264, kG2 = 15360, kG1 = 16384, kG0 = 17408, k
 
 // Per-warpgroup activation rows (element offsets): layer inputs of the tile, and the output-layer
 // gradient for the backward.
-constexpr int kX0 = 0, kH1 = 4096, kX2 = 12288, kH2 = 16384, kH3 = 24576, kDY = 32768;
-constexpr int kFwdAct = 32768, kBwdAct = 34816;
+constexpr int kX0 = 0, kH1 = 4096, kX2 = 12288, kH2 = 16384, kH3 = 24576, kDY = 32768, kX0b = 34816;
+constexpr int kFwdAct = 32768, kBwdAct = 38912;
+constexpr std::uint32_t kTileBytes = kRows * 32 * 2;   // one tile of 16-bit encodings
 
 // Tensor-memory columns of a warpgroup.
 constexpr std::uint32_t kDA = 0, kDB = 64;                                    // layer outputs
@@ -210,15 +217,17 @@ struct WarpGroup {
 // Forward through one tile; on return H1, X2, H2, H3 hold the layer inputs (16-bit), and x0 / rgb
 // this thread's pre-activation density and colour.  With `fits` given, every layer input is also
 // checked against the 16-bit range (loss scaling's overflow test).
-template <class E>
+template <class E, class After0>
 __device__ __forceinline__ void tile_forward(WarpGroup &wg, const typename E::T *sw, typename E::T *act,
-                                             const float dir[3], float &x0, float rgb[3], bool *fits) {
+                                             const typename E::T *x0in, const float dir[3], float &x0, float rgb[3],
+                                             bool *fits, After0 &&after0) {
     float v[64];
     const bool leader = wg.r == 0;
     // layer 0
     wg.sync();
-    if (leader) { mma_kk<E>(wg.tm + kDA, act + kX0, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
+    if (leader) { mma_kk<E>(wg.tm + kDA, x0in, sw + kF0, 32, 64, false); tc::commit(wg.bar); }
     wg.wait();
+    after0();   // the layer-0 operand may be refilled from here on
     tc::ld64(wg.tm + kDA, v);
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
@@ -319,27 +328,35 @@ __device__ __forceinline__ void write_denc(typename E::T *__restrict__ out, std:
     }
 }
 
-// Row r of tile `tile`: encoding, direction (+z past the end) and, when `g` is given, dL/ddrgb.
+// Row r of tile `tile`: encoding (unless `enc` is null), direction (+z past the end) and, when `g`
+// is given, dL/ddrgb.
 template <class Row>
 __device__ __forceinline__ void fetch_row(const typename Row::In *__restrict__ enc, const float *__restrict__ dirs,
                                           const float *__restrict__ dL_ddrgb, std::uint32_t tile, int r,
                                           std::uint32_t n_act, Row &row, float *dir, float4 *g) {
     const std::size_t s = (std::size_t)tile * kRows + r;
     const bool valid = s < n_act;
-    row.load(enc, s, valid);
+    if (enc != nullptr) row.load(enc, s, valid);   // null: the tile arrives by TMA
     dir[0] = valid ? dirs[s * 3 + 0] : 0.f;
     dir[1] = valid ? dirs[s * 3 + 1] : 0.f;
     dir[2] = valid ? dirs[s * 3 + 2] : 1.f;
     if (g != nullptr) *g = valid ? reinterpret_cast<const float4 *>(dL_ddrgb)[s] : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-template <class E, bool kHalf, int NWG>
+// TMA-fed tiles (kTma, 16-bit encodings only): a 4-D tensor map over enc [n][32] views it as
+// [n/8 row groups][4 column chunks][8 rows][8 columns] (strides 512, 16 and 64 bytes), so one
+// 128-row box lands in shared memory in exactly the operand's core-matrix layout; the leader
+// issues the next tile's copy as soon as the layer-0 MMA has consumed the current one, and the copy
+// overlaps layers 1-4.  Copy completion is an mbarrier transaction count; every wait is bounded.
+template <class E, bool kHalf, bool kTma, int NWG>
 __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_forward_kernel(
     std::uint32_t n, const std::uint32_t *__restrict__ count, const typename EncRow<E, kHalf>::In *__restrict__ enc,
-    const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb) {
+    const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb,
+    const __grid_constant__ CUtensorMap enc_map) {
+    static_assert(!kTma || kHalf, "TMA tiles carry 16-bit encodings");
     using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ std::uint64_t bars[NWG];
+    __shared__ std::uint64_t bars[NWG], tbars[NWG];
     __shared__ std::uint32_t tbase;
     __shared__ int fails[NWG];
     T *sw = reinterpret_cast<T *>(smem_raw);
@@ -349,6 +366,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_forward_kernel(
     if (threadIdx.x == 0) {
         for (int k = 0; k < NWG; ++k) {
             tc::mbar_init(&bars[k], 1);
+            tc::mbar_init(&tbars[k], 1);
             fails[k] = 0;
         }
         tc::fence_mbar_init();
@@ -358,26 +376,48 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_forward_kernel(
     __syncthreads();
     tc::fence_after();
     WarpGroup wg{g, r, tbase + (std::uint32_t)g * 128u + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
+    const bool leader = r == 0;
 
     const std::uint32_t n_act = active_count(n, count);
     const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
     const std::uint32_t step = gridDim.x * NWG;
+    std::uint32_t tphase = 0;
+    bool pending = false;   // a tile copy was issued and not yet waited for
+    auto issue = [&](std::uint32_t t) {
+        if (kTma && t < n_tiles) {
+            if (leader) {
+                tc::mbar_expect_tx(&tbars[g], kTileBytes);
+                tc::tma_load_4d(act + kX0, &enc_map, 0, 0, 0, (int)(t * (kRows / 8)), &tbars[g]);
+            }
+            pending = true;
+        }
+    };
     EncRow<E, kHalf> next;  // the next tile's row, loaded while the current tile computes
     float nd[3];
-    fetch_row(enc, dirs, nullptr, blockIdx.x * NWG + g, r, n_act, next, nd, nullptr);
+    issue(blockIdx.x * NWG + g);
+    fetch_row(kTma ? nullptr : enc, dirs, nullptr, blockIdx.x * NWG + g, r, n_act, next, nd, nullptr);
     for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
         const EncRow<E, kHalf> cur = next;
         const float dir[3] = {nd[0], nd[1], nd[2]};
-        fetch_row(enc, dirs, nullptr, tile + step, r, n_act, next, nd, nullptr);
-        cur.stage(act + kX0, r);
+        fetch_row(kTma ? nullptr : enc, dirs, nullptr, tile + step, r, n_act, next, nd, nullptr);
+        if (kTma) {
+            if (!tc::mbar_wait(&tbars[g], tphase, kWaitLimit)) *wg.fail = 1;
+            tphase ^= 1u;
+            pending = false;
+        } else {
+            cur.stage(act + kX0, r);
+        }
         float x0, rgb[3];
-        tile_forward<E>(wg, sw, act, dir, x0, rgb, nullptr);
+        tile_forward<E>(wg, sw, act, act + kX0, dir, x0, rgb, nullptr, [&] {
+            if (!*wg.fail) issue(tile + step);
+        });
         if (valid) reinterpret_cast<float4 *>(drgb)[s] = make_float4(expf(x0), rgb[0], rgb[1], rgb[2]);
         tc::bar_sync(1 + g, 128);
         if (*wg.fail) break;
     }
+    if (kTma && pending) tc::mbar_wait(&tbars[g], tphase, kWaitLimit);   // leave no copy in flight
     if (*wg.fail && r == 0) atomicOr(&g_device_error, 1u);
     tc::fence_before();
     __syncthreads();
@@ -445,15 +485,17 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_density_kernel(
 // Backward.  `grad_scale` multiplies dL/ddrgb, and so does the loss scale when `ls` is given; with
 // `ls`, a layer input or gradient that does not fit the 16-bit type (or dL/denc its storage type)
 // sets ls->overflow.  `partials` receives one [9408] dL/dW partial per CTA.
-template <class E, bool kHalf, int NWG>
+template <class E, bool kHalf, bool kTma, int NWG>
 __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     std::uint32_t n, const std::uint32_t *__restrict__ count, const typename EncRow<E, kHalf>::In *__restrict__ enc,
     const float *__restrict__ dirs, const float *__restrict__ weights, const float *__restrict__ dL_ddrgb,
     const float *__restrict__ grad_scale, NgpLossScale *__restrict__ ls,
-    typename EncRow<E, kHalf>::In *__restrict__ dL_denc, float *__restrict__ partials) {
+    typename EncRow<E, kHalf>::In *__restrict__ dL_denc, float *__restrict__ partials,
+    const __grid_constant__ CUtensorMap enc_map) {
+    static_assert(!kTma || kHalf, "TMA tiles carry 16-bit encodings");
     using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ std::uint64_t bars[NWG];
+    __shared__ std::uint64_t bars[NWG], tbars[NWG][2];
     __shared__ std::uint32_t tbase;
     __shared__ int fails[NWG];
     __shared__ int tiles_done[NWG];
@@ -464,6 +506,8 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     if (threadIdx.x == 0) {
         for (int k = 0; k < NWG; ++k) {
             tc::mbar_init(&bars[k], 1);
+            tc::mbar_init(&tbars[k][0], 1);
+            tc::mbar_init(&tbars[k][1], 1);
             fails[k] = 0;
             tiles_done[k] = 0;
         }
@@ -485,21 +529,44 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
     bool first = true;
     const std::uint32_t step = gridDim.x * NWG;
+    // TMA-fed tiles (kTma): two encoding buffers; tile i lands in buffer i % 2 while tile i - 1,
+    // whose MMAs have all completed, frees the other for tile i + 1.
+    std::uint32_t tphase[2] = {0u, 0u};
+    bool pending[2] = {false, false};
+    auto issue = [&](std::uint32_t t, int b) {
+        if (kTma && t < n_tiles) {
+            if (leader) {
+                tc::mbar_expect_tx(&tbars[g][b], kTileBytes);
+                tc::tma_load_4d(act + (b ? kX0b : kX0), &enc_map, 0, 0, 0, (int)(t * (kRows / 8)), &tbars[g][b]);
+            }
+            pending[b] = true;
+        }
+    };
     EncRow<E, kHalf> next;  // the next tile's row, loaded while the current tile computes
     float nd[3];
     float4 ng;
-    fetch_row(enc, dirs, dL_ddrgb, blockIdx.x * NWG + g, r, n_act, next, nd, &ng);
-    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step) {
+    issue(blockIdx.x * NWG + g, 0);
+    fetch_row(kTma ? nullptr : enc, dirs, dL_ddrgb, blockIdx.x * NWG + g, r, n_act, next, nd, &ng);
+    int buf = 0;
+    for (std::uint32_t tile = blockIdx.x * NWG + g; tile < n_tiles; tile += step, buf ^= 1) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
         float v[64];
         const EncRow<E, kHalf> cur = next;
         const float dir[3] = {nd[0], nd[1], nd[2]};
         const float4 go = ng;
-        fetch_row(enc, dirs, dL_ddrgb, tile + step, r, n_act, next, nd, &ng);
-        cur.stage(act + kX0, r);
+        fetch_row(kTma ? nullptr : enc, dirs, dL_ddrgb, tile + step, r, n_act, next, nd, &ng);
+        T *X0 = act + ((kTma && buf) ? kX0b : kX0);
+        if (kTma) {
+            if (!tc::mbar_wait(&tbars[g][buf], tphase[buf], kWaitLimit)) *wg.fail = 1;
+            tphase[buf] ^= 1u;
+            pending[buf] = false;
+            if (!*wg.fail) issue(tile + step, buf ^ 1);
+        } else {
+            cur.stage(X0, r);
+        }
         float x0, rgb[3];
-        tile_forward<E>(wg, sw, act, dir, x0, rgb, check);
+        tile_forward<E>(wg, sw, act, X0, dir, x0, rgb, check, [] {});
 
         // output layer: dL/da4 (3, padded to 16) and dL/dx0 through the truncated exponential
         const float dx0 = gs * go.x * expf(fminf(fmaxf(x0, -15.f), 15.f));
@@ -579,7 +646,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
         // layer 0: dW0^T += dA1^T enc;  denc = dA1 @ W0^T
         wg.sync();
         if (leader) {
-            mma_mn<E>(tm0 + kA0, act + kH1, act + kX0, 32, !first);
+            mma_mn<E>(tm0 + kA0, act + kH1, X0, 32, !first);
             mma_kk<E>(tm0 + kDA, act + kH1, sw + kG0, 64, 32, false);
             tc::commit(wg.bar);
         }
@@ -593,6 +660,9 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
         tc::bar_sync(1 + g, 128);
         if (*wg.fail) break;
     }
+#pragma unroll
+    for (int b = 0; b < 2; ++b)   // leave no copy in flight
+        if (kTma && pending[b]) tc::mbar_wait(&tbars[g][b], tphase[b], kWaitLimit);
     if (check != nullptr && !fits) atomicOr(&ls->overflow, 1u);
     if (r == 0) {
         tiles_done[g] = first ? 0 : 1;
@@ -746,6 +816,40 @@ static_assert(kBwdAct * 2 >= kNW * 4, "dW sums fit over a warpgroup's rows");
 
 namespace {
 
+// Tensor map of 16-bit encodings enc [n][32] (n a multiple of 8) as the 4-D view [n/8][4][8][8]
+// (row group, column chunk, row, column; byte strides 512, 16, 64) with a box of one 128-row tile:
+// the box lands in shared memory in the MMA operand's core-matrix layout.  False when the driver
+// entry point is unavailable or n does not qualify (the caller then loads the rows itself).
+template <class E>
+int encode_enc_map(CUtensorMap *map, const void *enc, std::uint32_t n, bool *ok) {
+    *ok = false;
+    std::memset(map, 0, sizeof(*map));
+    if (n == 0 || n % 8 != 0) return NGP_OK;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            (void)cudaGetLastError();
+    }
+    if (fn == nullptr) return NGP_OK;
+    const cuuint64_t dims[4] = {8, 8, 4, n / 8};
+    const cuuint64_t strides[3] = {64, 16, 512};   // bytes: next row, next 8-column chunk, next 8-row group
+    const cuuint32_t box[4] = {8, 8, 4, kRows / 8};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUtensorMapDataType dt = std::is_same<E, Bf16Op>::value ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    const CUresult r = fn(map, dt, 4, const_cast<void *>(enc), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    NGP_CHECK_ARG(r == CUDA_SUCCESS, "mlp (tensor cores): cuTensorMapEncodeTiled rejected the encodings' tensor map");
+    *ok = true;
+    return NGP_OK;
+}
+
 template <class E, bool kHalf>
 int launch_tc_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const void *enc,
                       const float *dirs, const float *weights, float *drgb) {
@@ -753,15 +857,29 @@ int launch_tc_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t 
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp (tensor cores): enc, weights and drgb must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_forward_kernel<E, kHalf, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_forward_kernel<E, kHalf, false, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+        if (kHalf)
+            NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_forward_kernel<E, kHalf, kHalf, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
         attr = true;
     }
     if (n == 0) return launch_status();
+    CUtensorMap map;
+    bool tma = false;
+    if (kHalf) {
+        const int st = encode_enc_map<E>(&map, enc, n, &tma);
+        if (st != NGP_OK) return st;
+    } else {
+        std::memset(&map, 0, sizeof(map));
+    }
     const unsigned tiles = (n + kRows - 1) / kRows;
     const unsigned want = (tiles + kFwdWgs - 1) / kFwdWgs;
     const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
-    mlp_tc_forward_kernel<E, kHalf, kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(
-        n, count, static_cast<const In *>(enc), dirs, weights, drgb);
+    if (tma)
+        mlp_tc_forward_kernel<E, kHalf, kHalf, kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(
+            n, count, static_cast<const In *>(enc), dirs, weights, drgb, map);
+    else
+        mlp_tc_forward_kernel<E, kHalf, false, kFwdWgs><<<grid, kFwdWgs * 128, kFwdSmem, stream>>>(
+            n, count, static_cast<const In *>(enc), dirs, weights, drgb, map);
     count_launches(1);
     return launch_status();
 }
@@ -794,12 +912,28 @@ int launch_tc_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t
                   "mlp (tensor cores): buffers must be 16-byte aligned");
     static bool attr = false;
     if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_backward_kernel<E, kHalf, kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_backward_kernel<E, kHalf, false, kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
+        if (kHalf)
+            NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_backward_kernel<E, kHalf, kHalf, kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
         attr = true;
     }
+    CUtensorMap map;
+    bool tma = false;
+    if (kHalf) {
+        const int st = encode_enc_map<E>(&map, enc, n, &tma);
+        if (st != NGP_OK) return st;
+    } else {
+        std::memset(&map, 0, sizeof(map));
+    }
     const unsigned grid = (unsigned)sm_count();
-    mlp_tc_backward_kernel<E, kHalf, kBwdWgs><<<grid, kBwdWgs * 128, kBwdSmem, stream>>>(
-        n, count, static_cast<const In *>(enc), dirs, weights, dL_ddrgb, grad_scale, ls, static_cast<In *>(dL_denc), partials);
+    if (tma)
+        mlp_tc_backward_kernel<E, kHalf, kHalf, kBwdWgs><<<grid, kBwdWgs * 128, kBwdSmem, stream>>>(
+            n, count, static_cast<const In *>(enc), dirs, weights, dL_ddrgb, grad_scale, ls, static_cast<In *>(dL_denc),
+            partials, map);
+    else
+        mlp_tc_backward_kernel<E, kHalf, false, kBwdWgs><<<grid, kBwdWgs * 128, kBwdSmem, stream>>>(
+            n, count, static_cast<const In *>(enc), dirs, weights, dL_ddrgb, grad_scale, ls, static_cast<In *>(dL_denc),
+            partials, map);
     count_launches(1);
     *grid_out = grid;
     return launch_status();

@@ -82,6 +82,22 @@ __device__ __forceinline__ bool mbar_wait(std::uint64_t *bar, std::uint32_t pari
     return false;
 }
 
+// The next phase of `bar` also waits for `bytes` of asynchronous copies (one arrival).
+__device__ __forceinline__ void mbar_expect_tx(std::uint64_t *bar, std::uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// Tensor-map tile load (TMA) of a 4-D box at coordinates {c0, c1, c2, c3} into shared memory;
+// completion is signalled on `bar` as transferred bytes.  `map` is the address of a
+// __grid_constant__ CUtensorMap kernel parameter.  c0, the innermost coordinate, must keep the
+// copy's start 16-byte aligned (callers pass 0).
+__device__ __forceinline__ void tma_load_4d(void *dst, const void *map, int c0, int c1, int c2, int c3,
+                                            std::uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        :: "r"(smem_addr(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar)) : "memory");
+}
+
 // Generic-proxy shared-memory writes become visible to the tensor cores.
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

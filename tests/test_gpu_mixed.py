@@ -384,3 +384,25 @@ def test_chain_fp16_needs_the_loss_scale():
     scaled = chain_errors("fp16-mixed")
     plain = chain_errors("fp16-mixed-unscaled")
     assert scaled["dL_dlatents"] * 2 < plain["dL_dlatents"], (scaled, plain)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_tma_tiles_equal_register_tiles(prec):
+    """16-bit encodings of a buffer whose row count is a multiple of 8 reach the MMAs through TMA
+    tile copies (a 4-D tensor map whose box lands in the operand's core-matrix layout); other row
+    counts through per-thread loads.  The same rows give bit-identical outputs, dL/denc and
+    weight gradients either way (the active count keeps the work the same)."""
+    from jaxngp_gb300.field import field_backward, field_forward
+    n = 3 * 8192 + 40   # several tiles per warpgroup, a partial last tile
+    enc, dirs, g = inputs(n + 1, 31)
+    wt = packed(Fd.init_weights(32))
+    eh = cu(enc).to(HALF[prec])
+    act = torch.tensor([n], dtype=torch.int32, device="cuda")
+    a = field_forward(eh[:n].contiguous(), cu(dirs[:n]), wt, precision=prec)            # n % 8 == 0: TMA
+    b = field_forward(eh, cu(dirs), wt, count=act, precision=prec)                     # n + 1 rows: loads
+    assert torch.equal(a, b[:n])
+    da, wa = field_backward(eh[:n].contiguous(), cu(dirs[:n]), wt, cu(g[:n]), precision=prec)
+    db, wb = field_backward(eh, cu(dirs), wt, cu(g), count=act, precision=prec)
+    assert torch.equal(da, db[:n]) and torch.equal(wa, wb)
+    from jaxngp_gb300 import _lib as L
+    assert L.lib().ngp_device_status() == 0
