@@ -37,7 +37,10 @@ FORMS = {"fp32-march": ("fp32", "march", "fp32", False), "bf16-march": ("bf16", 
          "bf16-proposal": ("bf16", "proposal", "fp32", False),
          "bf16x-march": ("bf16", "march", "bf16", True), "fp16x-march": ("fp16", "march", "fp16", True),
          "bf16x-proposal": ("bf16", "proposal", "bf16", True), "fp16x-proposal": ("fp16", "proposal", "fp16", True),
-         "bf16x-proposal-fb": ("bf16", "proposal", "bf16", True)}
+         "bf16x-proposal-fb": ("bf16", "proposal", "bf16", True),
+         "fp32-march-pipe": ("fp32", "march", "fp32", False), "bf16x-march-pipe": ("bf16", "march", "bf16", True)}
+# forms that march the next batch on a second stream while the current step trains (same results)
+PIPELINE_FORMS = {"fp32-march-pipe", "bf16x-march-pipe"}
 # forms whose proposal steps also march, per ray, the rays on which the proposal misses > 1% of the
 # transmittance the occupancy grid implies
 FALLBACK_FORMS = {"bf16x-proposal-fb"}
@@ -279,7 +282,8 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     L.lib().ngp_kernel_launches.restype = __import__("ctypes").c_ulonglong
     precision, sampler, table, half_act = FORMS[form]
     cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=precision, sampler=sampler,
-                      table_precision=table, half_activations=half_act, proposal_fallback=form in FALLBACK_FORMS)
+                      table_precision=table, half_activations=half_act, proposal_fallback=form in FALLBACK_FORMS,
+                      pipeline=form in PIPELINE_FORMS)
     tr = NGPTrainer(data, cfg)
     tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
@@ -354,12 +358,15 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
         s1.record()
         times.setdefault(name, []).append((s0, s1))
     L.call = timed_call
+    pipelined = tr.pipeline
+    tr.pipeline = False   # per-entry device times from the serial step (a second stream would blur them)
     try:
         for _ in range(args.steps):
             tr.step()
         torch.cuda.synchronize()
     finally:
         L.call = orig_call
+        tr.pipeline = pipelined
     per = {k: [a_.elapsed_time(b_) for a_, b_ in v] for k, v in times.items()}
     total = sum(sum(v) for v in per.values())
     breakdown = {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 5), "share": round(sum(v) / total, 4)}

@@ -46,6 +46,11 @@ unsigned long long ngp_kernel_launches(void);
  * recorded a device-side error since the last call -- a tensor-core kernel whose bounded wait for
  * its MMAs ran out -- else NGP_OK, or NGP_ERR_CUDA if the synchronisation failed. */
 int ngp_device_status(void);
+/* CTAs per SM the training march (march_rays, ngp_march_rays_train, ngp_march_rays_fallback)
+ * launches for every later call on any thread; 0 restores the default (10, the register limit).
+ * A caller that runs the march on a second stream, beside other kernels, lowers it so those
+ * kernels find room on every SM.  Returns the previous value, or -1 for n outside [0, 10]. */
+int ngp_set_march_blocks_per_sm(int n);
 
 /* ------------------------------------------------------- volrendjax descriptors (byte-exact) */
 /* deps/volume-rendering-jax/lib/impl/volrend.h:23-29 */

@@ -15,6 +15,8 @@
 // launcher never blocks the host (the reference synchronises the stream at marching.cu:562).
 #include <cstring>
 
+#include <atomic>
+
 #include "common.cuh"
 #include "coarse.cuh"
 
@@ -173,6 +175,7 @@ __device__ __forceinline__ bool no_sample_possible(const MarchParams &m, const V
 
 constexpr int kMarchBlock = 128;
 constexpr int kMarchBlocksPerSm = 10;   // 40 warps per SM at <= 48 registers
+std::atomic<int> g_march_blocks_per_sm{kMarchBlocksPerSm};
 
 enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
 
@@ -658,6 +661,11 @@ MarchParams make_params(std::uint32_t dns, std::uint32_t K, std::uint32_t G, flo
 
 // ----------------------------------------------------------------------------- launchers
 
+int set_march_blocks_per_sm(int n) {
+    if (n < 0 || n > kMarchBlocksPerSm) return -1;
+    return g_march_blocks_per_sm.exchange(n == 0 ? kMarchBlocksPerSm : n);
+}
+
 int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const float *rays_o,
                       const float *rays_d, const float *t_starts, const float *t_ends,
                       const float *noises, const std::uint8_t *bits, std::uint32_t *next_loc,
@@ -675,7 +683,7 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
     if (d.n_rays > 0) {
         const unsigned warps_needed = (d.n_rays + 31) / 32;
         const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
-        const unsigned cap = (unsigned)sm_count() * kMarchBlocksPerSm;
+        const unsigned cap = (unsigned)sm_count() * (unsigned)g_march_blocks_per_sm.load(std::memory_order_relaxed);
         const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
         if (probe) {
             march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
@@ -717,7 +725,7 @@ int launch_march_rays_list(cudaStream_t stream, const MarchingDescriptor &d, con
     if (d.n_rays > 0) {
         const unsigned warps_needed = (d.n_rays + 31) / 32;
         const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
-        const unsigned cap = (unsigned)sm_count() * kMarchBlocksPerSm;
+        const unsigned cap = (unsigned)sm_count() * (unsigned)g_march_blocks_per_sm.load(std::memory_order_relaxed);
         const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
         march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
             d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc, n_exceeded, queue,

@@ -68,6 +68,8 @@ struct Strip {
     static constexpr int RPT = ROWS >= R ? ROWS / R : 1;
     static constexpr bool kIdle = R > ROWS;
     static_assert(NT % G == 0 && (kIdle || ROWS % R == 0), "tile shape");
+    static __device__ __forceinline__ int col0(int t) { return (t % G) * 4; }
+    static __device__ __forceinline__ int row0(int t) { return t / G; }
 };
 
 // acc[q][j] += sum over k in [k0, k0 + 4) of A[row_q][k] * B[k][c0 + j], A read as one float4
@@ -106,7 +108,7 @@ template <int NT, int K, int N, bool kRelu>
 __device__ __forceinline__ void mm(const float *A, int lda, const float *B, float *C, int ldc) {
     using S = Strip<NT, kTile, N>;
     static_assert(K % 4 == 0, "K must be a multiple of 4");
-    const int t = threadIdx.x, c0 = (t % S::G) * 4, r0 = t / S::G;
+    const int t = threadIdx.x, c0 = S::col0(t), r0 = S::row0(t);
     if (S::kIdle && r0 >= kTile) return;
     int rows[S::RPT];
     float acc[S::RPT][4];
@@ -115,7 +117,7 @@ __device__ __forceinline__ void mm(const float *A, int lda, const float *B, floa
         rows[q] = r0 + q * S::R;
         acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
     }
-#pragma unroll 2
+#pragma unroll
     for (int k = 0; k < K; k += 4) fma4<S::RPT>(acc, A, lda, rows, B, N, k, c0);
 #pragma unroll
     for (int q = 0; q < S::RPT; ++q) {
@@ -131,7 +133,7 @@ template <int NT, int K, int N>
 __device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const float *B, float *M, int ldm) {
     using S = Strip<NT, kTile, N>;
     static_assert(K % 4 == 0, "K must be a multiple of 4");
-    const int t = threadIdx.x, c0 = (t % S::G) * 4, r0 = t / S::G;
+    const int t = threadIdx.x, c0 = S::col0(t), r0 = S::row0(t);
     if (S::kIdle && r0 >= kTile) return;
     int rows[S::RPT];
     float acc[S::RPT][4];
@@ -140,7 +142,7 @@ __device__ __forceinline__ void mm_mask_inplace(const float *A, int lda, const f
         rows[q] = r0 + q * S::R;
         acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
     }
-#pragma unroll 2
+#pragma unroll
     for (int k = 0; k < K; k += 4) fma4<S::RPT>(acc, A, lda, rows, B, N, k, c0);
 #pragma unroll
     for (int q = 0; q < S::RPT; ++q) {
@@ -158,14 +160,14 @@ struct WGrad {
     using S = Strip<NT, M, N>;
     static constexpr bool kVec = S::RPT == 4;
     float acc[S::RPT][4];
-    __device__ __forceinline__ bool owner() const { return !S::kIdle || (int)threadIdx.x / S::G < M; }
+    __device__ __forceinline__ bool owner() const { return !S::kIdle || S::row0((int)threadIdx.x) < M; }
     __device__ __forceinline__ int row(int m0, int q) const { return kVec ? m0 * 4 + q : m0 + q * S::R; }
     __device__ __forceinline__ void zero() {
 #pragma unroll
         for (int q = 0; q < S::RPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
     }
     __device__ __forceinline__ void add(const float *A, int lda, const float *D, int ldd, int rows) {
-        const int t = threadIdx.x, c0 = (t % S::G) * 4, m0 = t / S::G;
+        const int t = threadIdx.x, c0 = S::col0(t), m0 = S::row0(t);
         if (!owner()) return;
 #pragma unroll 4
         for (int s = 0; s < rows; ++s) {
@@ -193,7 +195,7 @@ struct WGrad {
         }
     }
     __device__ __forceinline__ void store(float *out) const {  // out: [M][N] row-major
-        const int t = threadIdx.x, c0 = (t % S::G) * 4, m0 = t / S::G;
+        const int t = threadIdx.x, c0 = S::col0(t), m0 = S::row0(t);
         if (!owner()) return;
 #pragma unroll
         for (int q = 0; q < S::RPT; ++q)

@@ -61,6 +61,9 @@ class TrainConfig:
     march_every: int = 8               # proposal sampler: every k-th step marches the occupancy grid (0: never)
     proposal_fallback: bool = False    # proposal sampler: march the rays whose proposal misses > 1% of transmittance
     proposal_train_points: int = 1 << 16   # field samples a proposal update regresses on (at most)
+    pipeline: bool = False             # march sampler: march the next step's batch on a second stream while
+                                       # this step's field, integrator, backwards and Adam run (same results)
+    pipeline_march_blocks: int = 10    # CTAs per SM of that march (measured: 8-10 best; fewer starve it)
     march_coarse_skip: bool = False    # march: finish rays that cross no occupied coarse block at once
                                        # (exact; pays off on sparse grids, costs ~3% on dense ones)
 
@@ -127,19 +130,14 @@ class NGPTrainer:
         self.threshold = torch.zeros(1, **f32)
         self.thr_scratch = torch.zeros(2, **f32)
         self.thr_step = 0.01 * cfg.diagonal_n_steps / (2 * min(bound, 1) * 3 ** 0.5)
-        # batch buffers
+        # batch buffers (rays and their samples): two sets when the next batch is marched ahead
         R, S = self.R, self.S
-        self.rays_o, self.rays_d = torch.empty(R, 3, **f32), torch.empty(R, 3, **f32)
-        self.t0, self.t1, self.noise = torch.empty(R, **f32), torch.empty(R, **f32), torch.empty(R, **f32)
-        self.bgs, self.gt = torch.empty(R, 3, **f32), torch.empty(R, 3, **f32)
-        self.counters = torch.zeros(2, **i32)
-        self.queue = torch.zeros(1, **i32)
-        self.count = torch.zeros(1, **i32)
-        self.valid = torch.empty(R, dtype=torch.bool, device=self.dev)
-        self.n_samples, self.startidx = torch.empty(R, **i32), torch.empty(R, **i32)
-        self.idcs = torch.empty(S, **i32)
-        self.xyzs, self.dirs = torch.empty(S, 3, **f32), torch.empty(S, 3, **f32)
-        self.dss, self.z_vals = torch.empty(S, **f32), torch.empty(S, **f32)
+        self.pipeline = bool(cfg.pipeline) and cfg.sampler == "march"
+        self._batches = [self._new_batch(R, S) for _ in range(2 if self.pipeline else 1)]
+        self._use_batch(0)
+        self._side = torch.cuda.Stream(device=self.dev) if self.pipeline else None
+        self._prepared = [None, None]   # events after which a batch prepared on the side stream is ready
+        self._ready = None              # the batch prepared for the next step
         self.enc = torch.empty(S, 32, dtype=act, device=self.dev)
         self.drgbs = torch.empty(S, 4, **f32)
         self.g_drgbs = torch.empty(S, 4, **f32)
@@ -179,6 +177,24 @@ class NGPTrainer:
         self.mark_untrained_grid()
 
     # ---------------------------------------------------------------------------- helpers
+    BATCH_FIELDS = ("rays_o", "rays_d", "t0", "t1", "noise", "bgs", "gt", "counters", "queue", "count", "valid",
+                    "n_samples", "startidx", "idcs", "xyzs", "dirs", "dss", "z_vals")
+
+    def _new_batch(self, R: int, S: int) -> dict:
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        i32 = dict(dtype=torch.int32, device=self.dev)
+        return dict(rays_o=torch.empty(R, 3, **f32), rays_d=torch.empty(R, 3, **f32), t0=torch.empty(R, **f32),
+                    t1=torch.empty(R, **f32), noise=torch.empty(R, **f32), bgs=torch.empty(R, 3, **f32),
+                    gt=torch.empty(R, 3, **f32), counters=torch.zeros(2, **i32), queue=torch.zeros(1, **i32),
+                    count=torch.zeros(1, **i32), valid=torch.empty(R, dtype=torch.bool, device=self.dev),
+                    n_samples=torch.empty(R, **i32), startidx=torch.empty(R, **i32), idcs=torch.empty(S, **i32),
+                    xyzs=torch.empty(S, 3, **f32), dirs=torch.empty(S, 3, **f32), dss=torch.empty(S, **f32),
+                    z_vals=torch.empty(S, **f32))
+
+    def _use_batch(self, i: int):
+        for k in self.BATCH_FIELDS:
+            setattr(self, k, self._batches[i][k])
+
     @property
     def gather_table(self) -> torch.Tensor:
         """The table the encoder forward reads: the 16-bit copy when there is one."""
@@ -297,30 +313,100 @@ class NGPTrainer:
         self.field.density(self.enc_d, self.weights, sigma, M)
 
     # ------------------------------------------------------------------------------- step
-    def step(self, perm: Optional[torch.Tensor] = None) -> torch.Tensor:
-        """One training step.  `perm`: int32 pixel indices [n_rays] on the device (as the
-        reference's `perm`), or None to draw them on the device.  Returns the device tensor
-        [loss, n_valid_rays, measured_batch_size, measured_batch_size_before_compaction]."""
+    def _rays(self, b: dict, perm, stream=None) -> int:
+        """ngp_train_rays into batch `b`; returns the step seed."""
         cfg, c = self.cfg, self.data.camera
         seed = self._next_seed()
         d_rays = L.NgpTrainRaysDescriptor(self.R, c.width, c.height, self.data.n_views, c.fx, c.fy, c.cx, c.cy,
                                           self.bound, int(cfg.perturb), int(cfg.random_bg), (L.c_f32 * 3)(1, 1, 1), seed)
-        L.call("ngp_train_rays", [self.data.transforms, self.data.rgbas, perm, self.rays_o, self.rays_d, self.t0,
-                                  self.t1, self.noise, self.bgs, self.gt], d_rays)
+        L.call("ngp_train_rays", [self.data.transforms, self.data.rgbas, perm, b["rays_o"], b["rays_d"], b["t0"],
+                                  b["t1"], b["noise"], b["bgs"], b["gt"]], d_rays, stream=stream)
+        return seed
+
+    def _march(self, b: dict, stream=None):
+        """The training march of batch `b` and its sample count."""
+        L.call("ngp_march_rays_train", [b["rays_o"], b["rays_d"], b["t0"], b["t1"], b["noise"], self.bitfield,
+                                        b["counters"][0:1], b["counters"][1:2], b["valid"], b["n_samples"],
+                                        b["startidx"], b["idcs"], b["xyzs"], b["dirs"], b["dss"], b["z_vals"],
+                                        b["queue"], self.coarse if self.cfg.march_coarse_skip else None],
+               self._d_march, stream=stream)
+        L.call("ngp_march_count", [b["counters"][0:1], b["counters"][1:2], b["count"]], stream=stream)
+
+    def _prepare_ahead(self, i: int, perm):
+        """Rays and march of batch i on the side stream, after everything queued on this stream so
+        far (the previous user of batch i, the copy of `perm`), with the march kept to
+        pipeline_march_blocks CTAs per SM so that this stream's kernels run beside it."""
+        main = torch.cuda.current_stream(self.dev)
+        entry = torch.cuda.Event()
+        entry.record(main)
+        self._side.wait_event(entry)
+        side = self._side.cuda_stream
+        self._rays(self._batches[i], perm, side)
+        prev = L.lib().ngp_set_march_blocks_per_sm(int(self.cfg.pipeline_march_blocks))
+        try:
+            self._march(self._batches[i], side)
+        finally:
+            L.lib().ngp_set_march_blocks_per_sm(prev)
+        ev = torch.cuda.Event()
+        ev.record(self._side)
+        self._prepared[i] = ev
+
+    def step(self, perm: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """One training step.  `perm`: int32 pixel indices [n_rays] on the device (as the
+        reference's `perm`), or None to draw them on the device.  Returns the device tensor
+        [loss, n_valid_rays, measured_batch_size, measured_batch_size_before_compaction].
+
+        With TrainConfig.pipeline (march sampler) each call trains on the batch the previous call
+        marched and marches the next one on a second stream meanwhile; `perm` then selects the
+        pixels of that next batch (the first call draws its own batch on the device).  The
+        results are the serial step's: the march reads only the occupancy grid, and a step that
+        ends with a grid refresh marches the next batch after the refresh."""
+        cfg = self.cfg
+        if self.pipeline:
+            if self._ready is None:
+                b = self._batches[0]
+                self._rays(b, None)
+                self._march(b)
+                self._ready = 0
+            cur, nxt = self._ready, 1 - self._ready
+            self._use_batch(cur)
+            if self._prepared[cur] is not None:
+                torch.cuda.current_stream(self.dev).wait_event(self._prepared[cur])
+                self._prepared[cur] = None
+            refresh = self.ogrid_due(self.step_count + 1 + self.cadence_offset)
+            if not refresh:
+                self._prepare_ahead(nxt, perm)
+            cnt = self.count
+            self._train_on(cnt, use_march=True)
+            if refresh:
+                self._rays(self._batches[nxt], perm)
+                self._march(self._batches[nxt])
+            self._ready = nxt
+            return self.stats
+        if self._ready is not None:   # leaving pipelined mode: let a batch still being marched finish
+            for i, ev in enumerate(self._prepared):
+                if ev is not None:
+                    torch.cuda.current_stream(self.dev).wait_event(ev)
+                    self._prepared[i] = None
+            self._ready = None
+            self._use_batch(0)
+        seed = self._rays(self._batches[0], perm)
         use_march = self.prop is None or (cfg.march_every > 0 and self.step_count % cfg.march_every == cfg.march_every - 1)
         if use_march:
-            L.call("ngp_march_rays_train", [self.rays_o, self.rays_d, self.t0, self.t1, self.noise, self.bitfield,
-                                            self.counters[0:1], self.counters[1:2], self.valid, self.n_samples,
-                                            self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals,
-                                            self.queue, self.coarse if cfg.march_coarse_skip else None],
-                   self._d_march)
-            L.call("ngp_march_count", [self.counters[0:1], self.counters[1:2], self.count])
+            self._march(self._batches[0])
             cnt = self.count
         else:
             fb = (self.bitfield, self.threshold, self.noise, self._d_march) if cfg.proposal_fallback else None
             cnt = self.prop.sample(self.rays_o, self.rays_d, self.t0, self.t1, self.valid, self.n_samples,
                                    self.startidx, self.idcs, self.xyzs, self.dirs, self.dss, self.z_vals, cfg.perturb,
                                    seed ^ 0x5BD1E9955BD1E995, fallback=fb)
+        self._train_on(cnt, use_march)
+        return self.stats
+
+    def _train_on(self, cnt: torch.Tensor, use_march: bool):
+        """The rest of the step on the current batch: encoder, field, (proposal update), fused
+        integrator + loss, backwards, Adam, and the occupancy-grid refresh when due."""
+        cfg = self.cfg
         L.call(self._hg_fwd[0], [self.xyzs, self.gather_table, cnt, self.enc], self._hg_fwd[1])
         self.field.forward(self.enc, self.dirs, self.weights, cnt, self.drgbs)
         if self.prop is not None and (use_march or self.step_count % cfg.proposal_every == 0):
@@ -351,7 +437,6 @@ class NGPTrainer:
         self.step_count += 1
         if self.ogrid_due(self.step_count + self.cadence_offset):
             self.update_ogrid()
-        return self.stats
 
     # -------------------------------------------------------------------------- rendering
     @torch.no_grad()

@@ -93,3 +93,28 @@ def test_render_view(small_scene):
     tr = NGPTrainer(small_scene, TrainConfig(total_samples=1 << 14, T=1 << 16, seed=1))
     img = tr.render_view(0)
     assert img.shape == (64, 64, 3) and img.dtype == torch.uint8
+
+
+def test_pipelined_march_matches_serial(small_scene):
+    """TrainConfig.pipeline marches the next batch on a second stream while the current step
+    trains; the batches are the serial trainer's, ray for ray (the march reads only the
+    occupancy grid, which no step between refreshes changes), and the step across a grid refresh
+    marches after it.  Losses agree to float-atomics order."""
+    from jaxngp_gb300.trainer import NGPTrainer, TrainConfig
+    # 64 rays cannot fill a 2^16-sample budget (at most 1024 samples each), so which rays fit does
+    # not depend on the order in which concurrent warps allocate (near a full budget it does, in
+    # the reference too)
+    cfgs = [TrainConfig(total_samples=1 << 16, n_rays=64, T=1 << 16, seed=4, pipeline=p) for p in (False, True)]
+    a, b = NGPTrainer(small_scene, cfgs[0]), NGPTrainer(small_scene, cfgs[1])
+    assert b.pipeline and not a.pipeline
+    for tr in (a, b):
+        tr.init_occupancy_analytic()
+        tr.cadence_offset = 1009   # refreshes every 16 steps, the first after step 15
+    for it in range(24):
+        sa, sb = a.step().cpu().numpy(), b.step().cpu().numpy()
+        assert sa[3] <= 64 * 1024   # nothing overflowed
+        if it < 15:   # before the first refresh both grids are the analytic one
+            assert torch.equal(a.valid, b.valid) and torch.equal(a.n_samples, b.n_samples), it
+            assert sa[1] == sb[1] and sa[2] == sb[2] and sa[3] == sb[3], (it, sa, sb)
+        assert abs(sa[0] - sb[0]) <= 1e-3 * abs(sa[0]) + 1e-7, (it, sa[0], sb[0])
+    torch.cuda.synchronize()
