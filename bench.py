@@ -401,9 +401,15 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
             roof["frac_of_fp32_simt_nominal"] = round(achieved / FP32_SIMT_NOMINAL_TFLOPS, 4)
 
     render = render_fps(args, tr, stream) if (with_render and args.render_frames > 0) else None
-    from jaxngp_gb300.trainer import evaluate_psnr
-    quality = {"psnr_heldout": round(evaluate_psnr(tr, n_views=2), 3), "views": 2, "steps_trained": tr.step_count,
+    render_prop = render_fps(args, tr, stream, proposal=True) if (
+        with_render and args.render_frames > 0 and tr.prop is not None) else None
+    from jaxngp_gb300.trainer import HeldOut
+    held = HeldOut(data, n_views=2)
+    quality = {"psnr_heldout": round(held.psnr(tr), 3), "views": 2, "steps_trained": tr.step_count,
                "judge": "occupancy-grid inference renderer, white background, 4096-step quadrature ground truth"}
+    if tr.prop is not None:
+        from jaxngp_gb300.renderer import ProposalRenderer
+        quality["psnr_heldout_proposal_renderer"] = round(held.psnr(tr, ProposalRenderer(tr)), 3)
 
     out = {"metric": args.metric, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
@@ -430,21 +436,25 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
                            if cfg.proposal_fallback else None, "march_every": cfg.march_every}
     if render is not None:
         out["render_1080p"] = render
+    if render_prop is not None:
+        out["render_1080p_proposal"] = render_prop
     return out
 
 
-def render_fps(args, tr, stream) -> dict:
-    """1920x1080 frames of the trained field on a 120-pose orbit (render_image_inference,
-    models/renderers/cuda.py:244-373), each frame's u8 image copied to pinned host memory inside
-    the timed region."""
+def render_fps(args, tr, stream, proposal: bool = False) -> dict:
+    """1920x1080 frames of the trained field on a 120-pose orbit, each frame's u8 image copied to
+    pinned host memory inside the timed region: by the occupancy-grid inference renderer
+    (render_image_inference, models/renderers/cuda.py:244-373) or, with `proposal`, by the
+    learned proposal's sampler (ProposalRenderer)."""
     import torch
     from jaxngp_gb300 import _lib as L
-    from jaxngp_gb300.renderer import Renderer
+    from jaxngp_gb300.renderer import ProposalRenderer, Renderer
     from jaxngp_gb300.scene import PinholeCamera, orbit_poses, poses_to_transforms
 
     cam = PinholeCamera.from_fov(1920, 1080, 40.0)
     poses = torch.from_numpy(poses_to_transforms(orbit_poses(120, 4.0))).cuda()
-    rnd = Renderer.from_trainer(tr, n_slots=args.render_slots, march_steps_cap=args.render_cap)
+    rnd = ProposalRenderer(tr) if proposal else Renderer.from_trainer(tr, n_slots=args.render_slots,
+                                                                      march_steps_cap=args.render_cap)
     host_img = torch.empty(cam.height, cam.width, 3, dtype=torch.uint8).pin_memory()
     for f in range(2):
         rnd.render_image(cam, poses[f])
@@ -457,7 +467,7 @@ def render_fps(args, tr, stream) -> dict:
     for f in range(n):
         rgb, _ = rnd.render_image(cam, poses[(f * 120) // n])
         host_img.copy_(rgb, non_blocking=True)
-        iters += rnd.iterations
+        iters += getattr(rnd, "iterations", 0)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
@@ -479,7 +489,8 @@ def render_fps(args, tr, stream) -> dict:
     finally:
         L.call = orig_call
     per = {k: sum(a.elapsed_time(b) for a, b in v) for k, v in times.items()}
-    return {"fps": round(n / (ms / 1e3), 2), "ms_per_frame": round(ms / n, 3), "frames": n,
+    return {"renderer": "learned proposal (48 samples per ray crossing occupied blocks)" if proposal
+            else "occupancy-grid march", "fps": round(n / (ms / 1e3), 2), "ms_per_frame": round(ms / n, 3), "frames": n,
             "width": cam.width, "height": cam.height, "poses": "120-pose orbit, radius 4, elevation 25 deg, fov 40",
             "slots": args.render_slots, "march_steps_cap": args.render_cap,
             "iterations_per_frame": round(iters / n, 1), "gpu_launches": int(launches),
@@ -606,6 +617,7 @@ def main():
                                                "roofline", "clocks") if k in r} | {"proposal": r.get("proposal")} | {
                             "valid_rays_per_step": r["config"]["valid_rays_per_step"],
                             "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
+                            "render_1080p_fps_proposal_renderer": (r.get("render_1080p_proposal") or {}).get("fps"),
                             "top_kernels": dict(list(r["kernels"].items())[:6])}
                         for f, r in results.items()}
         if "fp32-march" in results:
@@ -617,6 +629,12 @@ def main():
                 cmp[f] = {"train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
                           "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
                           "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3)}
+                ra, rp = a.get("render_1080p"), b.get("render_1080p_proposal")
+                if ra and rp:
+                    # 1080p inference: the proposal renderer against the plain step's march renderer
+                    cmp[f]["render_1080p_fps_ratio"] = round(rp["fps"] / ra["fps"], 3)
+                    cmp[f]["render_delta_psnr_db"] = round(
+                        b["quality"]["psnr_heldout_proposal_renderer"] - a["quality"]["psnr_heldout"], 3)
             if cmp:
                 out["learned_proposal_vs_plain"] = {"plain": "fp32-march", **cmp}
             if cmp and args.equal_psnr_steps > 0:

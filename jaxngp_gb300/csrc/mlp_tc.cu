@@ -307,6 +307,15 @@ struct EncRow<E, true> {
     }
 };
 
+// Zeroes row r of a 32-column 16-bit operand buffer (a tile row past the active count: a TMA copy
+// brings whatever the buffer holds there, and a NaN in it would reach the weight gradients as
+// NaN x 0).
+template <class T>
+__device__ __forceinline__ void zero_row32(T *buf, int r) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4 *>(buf + rb(r, c * 8, 32)) = make_uint4(0u, 0u, 0u, 0u);
+}
+
 // dL/denc row of one sample: FP32, or the operand type when kHalf.
 template <class E>
 __device__ __forceinline__ void write_denc(float *__restrict__ out, std::size_t s, const float *v) {
@@ -406,6 +415,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_forward_kernel(
             if (!tc::mbar_wait(&tbars[g], tphase, kWaitLimit)) *wg.fail = 1;
             tphase ^= 1u;
             pending = false;
+            if (!valid) zero_row32(act + kX0, r);
         } else {
             cur.stage(act + kX0, r);
         }
@@ -561,6 +571,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
             if (!tc::mbar_wait(&tbars[g][buf], tphase[buf], kWaitLimit)) *wg.fail = 1;
             tphase[buf] ^= 1u;
             pending[buf] = false;
+            if (!valid) zero_row32(X0, r);
             if (!*wg.fail) issue(tile + step, buf ^ 1);
         } else {
             cur.stage(X0, r);

@@ -44,7 +44,8 @@ def proposal_table() -> LevelTable:
 
 class ProposalSampler:
     def __init__(self, n_rays: int, total_samples: int, G: int, bound: float, device="cuda", seed: int = 0,
-                 lr: float = 1e-2, distill_points: int = 1 << 14, samples_per_ray: int = SAMPLES, mix: float = 0.1):
+                 lr: float = 1e-2, distill_points: int = 1 << 14, samples_per_ray: int = SAMPLES, mix: float = 0.1,
+                 inference_only: bool = False):
         if G % 8 != 0:
             raise ValueError("the proposal sampler needs an occupancy grid resolution divisible by 8")
         self.R, self.S, self.G, self.bound = n_rays, total_samples, G, float(bound)
@@ -91,7 +92,7 @@ class ProposalSampler:
         self.points = torch.zeros(nb, 3, **f32)
         self.enc_b = torch.zeros(nb, 8, **f32)
         self.x_b = torch.zeros(nb, **f32)
-        n_train = max(self.S, self.M)
+        n_train = 1 if inference_only else max(self.S, self.M)   # sampling only: no training buffers
         self.enc_t = torch.zeros(n_train, 8, **f32)
         self.x_t = torch.zeros(n_train, **f32)
         self.g_x = torch.zeros(n_train, **f32)
@@ -155,6 +156,14 @@ class ProposalSampler:
                                              dss, z_vals, valid, n_samples, startidx],
                self._desc(perturb=perturb, seed=seed))
         return self.counts[2:3]
+
+    def for_rendering(self, n_rays: int) -> "ProposalSampler":
+        """A sampler for inference that shares this one's proposal field (table, weights) and
+        coarse blocks, with a slot for every one of `n_rays` rays per call."""
+        r = ProposalSampler(n_rays, n_rays * self.spr, self.G, self.bound, self.dev, samples_per_ray=self.spr,
+                            mix=self.mix, inference_only=True)
+        r.latents, r.weights, r.coarse, r.f16 = self.latents, self.weights, self.coarse, self.f16
+        return r
 
     def fallback_rate(self) -> float:
         """Mean fallback rays per sampling call so far (reads the device counter)."""

@@ -114,3 +114,64 @@ class Renderer:
         rgbd, _ = self.render_rays(o, d, t0.contiguous(), t1, bgt)
         rgb = (rgbd[:, :3].clamp(0, 1) * 255).round().to(torch.uint8).view(camera.height, camera.width, 3)
         return rgb, rgbd[:, 3].view(camera.height, camera.width)
+
+
+class ProposalRenderer:
+    """Inference with the learned proposal instead of the occupancy-grid march (no reference
+    counterpart): rays in chunks; per chunk the proposal places samples_per_ray samples on every
+    ray that crosses an occupied coarse block (ngp_proposal_rays, _bin_points, the FP16 proposal
+    MLP, ngp_proposal_sample), the field evaluates them (encoder and field MLP at the trainer's
+    precision) and integrate_rays composites them; rays that cross no occupied block show the
+    background.  The trained proposal and field are shared with the trainer, not copied."""
+
+    def __init__(self, tr, chunk: int = 1 << 16):
+        if tr.prop is None:
+            raise ValueError("the trainer has no proposal sampler")
+        self.tr = tr
+        self.chunk = chunk
+        self.ps = tr.prop.for_rendering(chunk)
+        dev = tr.dev
+        S = self.ps.S
+        f32 = dict(dtype=torch.float32, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.valid = torch.zeros(chunk, dtype=torch.bool, device=dev)
+        self.n_samples, self.startidx = torch.zeros(chunk, **i32), torch.zeros(chunk, **i32)
+        self.idcs = torch.zeros(S, **i32)
+        self.xyzs, self.dirs = torch.zeros(S, 3, **f32), torch.zeros(S, 3, **f32)
+        self.dss, self.zs = torch.zeros(S, **f32), torch.zeros(S, **f32)
+        self.enc = torch.empty(S, 32, dtype=tr.enc.dtype, device=dev)
+        self.drgbs = torch.zeros(S, 4, **f32)
+        self.measured = torch.zeros(1, **i32)
+        self.opacity = torch.zeros(chunk, **f32)
+        self.hg = forward_call(tr.table.descriptor(S, tr.bound), tr.gather_table, self.enc)
+
+    @torch.no_grad()
+    def render_rays(self, rays_o, rays_d, t_starts, t_ends, rays_bg) -> torch.Tensor:
+        """rays_rgbd [N, 4]."""
+        tr, ps = self.tr, self.ps
+        N = rays_o.shape[0]
+        out = torch.empty(N, 4, dtype=torch.float32, device=rays_o.device)
+        for s0 in range(0, N, self.chunk):
+            n = min(self.chunk, N - s0)
+            sl = slice(s0, s0 + n)
+            o, d = rays_o[sl].contiguous(), rays_d[sl].contiguous()
+            t0, t1 = t_starts[sl].contiguous(), t_ends[sl].contiguous()
+            cnt = ps.sample(o, d, t0, t1, self.valid[:n], self.n_samples[:n], self.startidx[:n], self.idcs, self.xyzs,
+                            self.dirs, self.dss, self.zs, False, 0)
+            L.call(self.hg[0], [self.xyzs, tr.gather_table, cnt, self.enc], self.hg[1])
+            tr.field.forward(self.enc, self.dirs, tr.weights, cnt, self.drgbs)
+            L.call("integrate_rays", [self.startidx[:n], self.n_samples[:n], rays_bg[sl].contiguous(), self.dss, self.zs,
+                                      self.drgbs, self.measured, out[sl], self.opacity[:n]],
+                   L.IntegratingDescriptor(n, ps.S))
+        return out
+
+    @torch.no_grad()
+    def render_image(self, camera, transform: torch.Tensor, bg=(1.0, 1.0, 1.0)) -> Tuple[torch.Tensor, torch.Tensor]:
+        """(rgb u8 [H, W, 3], depth f32 [H, W]) of one pinhole view."""
+        from .trainer import camera_rays, near_far
+        o, d = camera_rays(camera, transform)
+        t0, t1 = near_far(self.tr.bound, o, d)
+        bgt = torch.as_tensor(bg, dtype=torch.float32, device=o.device).expand(o.shape[0], 3).contiguous()
+        rgbd = self.render_rays(o, d, t0, t1, bgt)
+        rgb = (rgbd[:, :3].clamp(0, 1) * 255).round().to(torch.uint8).view(camera.height, camera.width, 3)
+        return rgb, rgbd[:, 3].view(camera.height, camera.width)

@@ -523,12 +523,12 @@ class HeldOut:
         self.gt_rgb = (gt[..., :3] * gt[..., 3:] + (1 - gt[..., 3:])).mul(255).round().to(torch.uint8)
 
     @torch.no_grad()
-    def psnr(self, tr: "NGPTrainer") -> float:
-        """Mean PSNR (utils/data.py:407-410) of the trainer's field rendered by the occupancy-grid
-        inference renderer over a white background."""
+    def psnr(self, tr: "NGPTrainer", renderer=None) -> float:
+        """Mean PSNR (utils/data.py:407-410) of the trainer's field rendered over a white
+        background, by the occupancy-grid inference renderer unless `renderer` is given."""
         from .renderer import Renderer
         from .scene import psnr_u8
-        r = Renderer.from_trainer(tr, n_slots=1 << 18)
+        r = renderer if renderer is not None else Renderer.from_trainer(tr, n_slots=1 << 18)
         vals = []
         for v in range(self.n_views):
             rgb, _ = r.render_image(self.cam, self.transforms[v], bg=(1.0, 1.0, 1.0))

@@ -391,7 +391,8 @@ def test_tma_tiles_equal_register_tiles(prec):
     """16-bit encodings of a buffer whose row count is a multiple of 8 reach the MMAs through TMA
     tile copies (a 4-D tensor map whose box lands in the operand's core-matrix layout); other row
     counts through per-thread loads.  The same rows give bit-identical outputs, dL/denc and
-    weight gradients either way (the active count keeps the work the same)."""
+    weight gradients either way (the active count keeps the work the same), whatever the buffer
+    holds past the active count."""
     from jaxngp_gb300.field import field_backward, field_forward
     n = 3 * 8192 + 40   # several tiles per warpgroup, a partial last tile
     enc, dirs, g = inputs(n + 1, 31)
@@ -404,5 +405,15 @@ def test_tma_tiles_equal_register_tiles(prec):
     da, wa = field_backward(eh[:n].contiguous(), cu(dirs[:n]), wt, cu(g[:n]), precision=prec)
     db, wb = field_backward(eh, cu(dirs), wt, cu(g), count=act, precision=prec)
     assert torch.equal(da, db[:n]) and torch.equal(wa, wb)
+    # a TMA-eligible buffer whose rows past the active count hold NaN (stale memory): the tile's
+    # inactive rows are zeroed before the MMAs, so nothing of them reaches the outputs
+    pad = torch.full((8, 32), float("nan"), dtype=HALF[prec], device="cuda")
+    en = torch.cat([eh[:n], pad]).contiguous()
+    dn = torch.cat([cu(dirs[:n]), torch.zeros(8, 3, device="cuda")]).contiguous()
+    gn = torch.cat([cu(g[:n]), torch.full((8, 4), float("nan"), device="cuda")]).contiguous()
+    c = field_forward(en, dn, wt, count=act, precision=prec)
+    assert torch.equal(c[:n], a)
+    dc, wc = field_backward(en, dn, wt, gn, count=act, precision=prec)
+    assert torch.equal(dc[:n], da) and torch.equal(wc, wa) and bool(torch.isfinite(wc).all())
     from jaxngp_gb300 import _lib as L
     assert L.lib().ngp_device_status() == 0
