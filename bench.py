@@ -5,7 +5,8 @@ on the synthetic 64-blob scene: 100 views at 800x800, 2^18 rays and a 2^18-sampl
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--forms ...]
 
 Prints one JSON line.  The headline (`value`) is the first form, by default the plain step --
-the reference's algorithm (occupancy-grid march, FP32 field MLP) -- in train rays/s (sum of
+the reference's algorithm (occupancy-grid march, FP32 field MLP; the next batch is marched on a
+second stream while the current step trains, with the serial step's results) -- in train rays/s (sum of
 n_valid_rays over the timed steps / time, the reference's own throughput count,
 app/nerf/train.py:59) with every input resident on the GPU; `e2e` is the same step driven through
 the public API with the pixel indices copied from pinned host memory and the step's metrics copied
@@ -38,12 +39,13 @@ FORMS = {"fp32-march": ("fp32", "march", "fp32", False), "bf16-march": ("bf16", 
          "bf16x-march": ("bf16", "march", "bf16", True), "fp16x-march": ("fp16", "march", "fp16", True),
          "bf16x-proposal": ("bf16", "proposal", "bf16", True), "fp16x-proposal": ("fp16", "proposal", "fp16", True),
          "bf16x-proposal-fb": ("bf16", "proposal", "bf16", True),
-         "fp32-march-pipe": ("fp32", "march", "fp32", False), "bf16x-march-pipe": ("bf16", "march", "bf16", True)}
-# forms that march the next batch on a second stream while the current step trains (same results)
-PIPELINE_FORMS = {"fp32-march-pipe", "bf16x-march-pipe"}
+         "fp32-march-serial": ("fp32", "march", "fp32", False)}
 # forms whose proposal steps also march, per ray, the rays on which the proposal misses > 1% of the
 # transmittance the occupancy grid implies
 FALLBACK_FORMS = {"bf16x-proposal-fb"}
+# march-sampler forms march the next batch on a second stream while the current step trains (the
+# same results as the serial step, which fp32-march-serial keeps)
+PIPELINE_FORMS = {f for f, v in FORMS.items() if v[1] == "march" and not f.endswith("-serial")}
 UNIT = "rays/s"
 WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
            "L16 F2 T2^19 Nmin16 Nmax2048, MLP 32-64-16 / 32-64-64-3, R=S=2^18, Adam lr1e-2, fp32"
@@ -511,7 +513,7 @@ def equal_psnr(args, data, plain: str, fast: str) -> dict:
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
                                           table_precision=table, half_activations=half_act,
-                                          proposal_fallback=f in FALLBACK_FORMS))
+                                          proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS))
         tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()
         t, pts = 0.0, []
@@ -548,7 +550,7 @@ def convergence(args, data, forms) -> dict:
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
                                           table_precision=table, half_activations=half_act,
-                                          proposal_fallback=f in FALLBACK_FORMS))
+                                          proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS))
         tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()
         t, curve = 0.0, []
