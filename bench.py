@@ -620,6 +620,8 @@ def main():
                             "valid_rays_per_step": r["config"]["valid_rays_per_step"],
                             "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
                             "render_1080p_fps_proposal_renderer": (r.get("render_1080p_proposal") or {}).get("fps"),
+                            "render_1080p_proposal_ms_by_entry": (r.get("render_1080p_proposal") or {}).get(
+                                "ms_per_frame_by_entry"),
                             "top_kernels": dict(list(r["kernels"].items())[:6])}
                         for f, r in results.items()}
         if "fp32-march" in results:

@@ -96,31 +96,43 @@ __device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, st
     }
 }
 
-// enc[n, l*2 + f] for n < n_points (n_points read from `count` when given).  A CTA takes tiles of
-// 32 points; warp w computes levels w, w + 8, ... for them and the tile's rows [32][L] leave
-// through shared memory as one contiguous block.
-constexpr int kHgTile = 32, kHgRow = NGP_MAX_LEVELS + 1;   // padded row: lanes hit different banks
+// enc[n, l*2 + f] for n < n_points (n_points read from `count` when given).  A CTA of 8 warps takes
+// tiles of 32 S points, S = max(1, 8 / L) sub-tiles of 32: with S = 1 warp w computes levels
+// w, w + 8, ... of the tile's 32 points (lane = point); with fewer levels than warps (the 4-level
+// proposal table: S = 2), warp w computes level w % L of sub-tile w / L, so no warp idles.  The
+// tile's rows [32 S][L] leave through shared memory as one contiguous block.
+constexpr int kHgTile = 32, kHgWarps = 8, kHgRows = kHgTile * (NGP_MAX_LEVELS + 1);
 
 template <class Tab, class Enc, bool kPaired>
-__global__ void __launch_bounds__(256) hashgrid_forward_kernel(
+__global__ void __launch_bounds__(kHgWarps * 32) hashgrid_forward_kernel(
     NgpHashGridDescriptor d, std::uint32_t n_points, const std::uint32_t *__restrict__ count,
     const float *__restrict__ pos, const void *__restrict__ latents, void *__restrict__ enc) {
-    __shared__ float2 rows[kHgTile * kHgRow];
+    // rows[p * (L + 1) + l]: the padded row stride puts the lanes of a warp in different banks.
+    // It needs 32 S (L + 1) entries: 32 (L + 1) <= kHgRows when S = 1, and 32 S L + 32 S <= 512
+    // when S > 1 (then S L <= 8 and S <= 8).
+    __shared__ float2 rows[kHgRows];
     std::uint32_t n_active = n_points;
     if (count != nullptr) n_active = min(n_active, *count);
     const std::uint32_t L = d.L, tmask = (d.T & (d.T - 1u)) == 0u ? d.T - 1u : 0u, last = d.n_params - 1u;
-    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
-    const std::uint32_t n_tiles = (n_active + kHgTile - 1) / kHgTile;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const std::uint32_t S = L < (std::uint32_t)kHgWarps ? (std::uint32_t)kHgWarps / L : 1u;
+    const std::uint32_t sub = S > 1u ? warp / L : 0u;              // this warp's sub-tile
+    const std::uint32_t l0 = S > 1u ? warp % L : warp;              // and its first level
+    const std::uint32_t l_step = S > 1u ? L : (std::uint32_t)kHgWarps;
+    const bool busy = sub < S;                                       // warps past S L idle
+    const std::uint32_t tile_pts = kHgTile * S, Lp = L + 1u;
+    const std::uint32_t n_tiles = (n_active + tile_pts - 1) / tile_pts;
     for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const std::uint32_t n = tile * kHgTile + lane;
-        const bool in = n < n_active;
+        const std::uint32_t p = sub * kHgTile + lane;                // point within the tile
+        const std::uint32_t n = tile * tile_pts + p;
+        const bool in = busy && n < n_active;
         float px = 0.f, py = 0.f, pz = 0.f;
         if (in) {
             px = pos[(std::size_t)n * 3 + 0];
             py = pos[(std::size_t)n * 3 + 1];
             pz = pos[(std::size_t)n * 3 + 2];
         }
-        for (std::uint32_t l = warp; l < L; l += n_warps) {
+        for (std::uint32_t l = l0; busy && l < L; l += l_step) {
             float2 r = make_float2(0.f, 0.f);
             if (in) {
                 Corner8 c;
@@ -155,12 +167,12 @@ __global__ void __launch_bounds__(256) hashgrid_forward_kernel(
                 }
                 r = make_float2(a0, a1);
             }
-            rows[lane * kHgRow + l] = r;
+            rows[p * Lp + l] = r;
         }
         __syncthreads();
-        const std::uint32_t n_rows = min((std::uint32_t)kHgTile, n_active - tile * kHgTile);
-        const std::size_t dst = (std::size_t)tile * kHgTile * L;
-        for (std::uint32_t i = threadIdx.x; i < n_rows * L; i += blockDim.x) Enc::put(enc, dst + i, rows[(i / L) * kHgRow + i % L]);
+        const std::uint32_t n_rows = min(tile_pts, n_active - tile * tile_pts);
+        const std::size_t dst = (std::size_t)tile * tile_pts * L;
+        for (std::uint32_t i = threadIdx.x; i < n_rows * L; i += blockDim.x) Enc::put(enc, dst + i, rows[(i / L) * Lp + i % L]);
         __syncthreads();
     }
 }
@@ -256,11 +268,11 @@ template <class Tab, bool kPaired>
 void forward_for_table(cudaStream_t stream, std::uint32_t enc_type, unsigned grid, const NgpHashGridDescriptor &d,
                        const std::uint32_t *count, const float *pos, const void *latents, void *enc) {
     if (enc_type == NGP_DTYPE_BF16)
-        hashgrid_forward_kernel<Tab, PairHalf<Bf16Op>, kPaired><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
+        hashgrid_forward_kernel<Tab, PairHalf<Bf16Op>, kPaired><<<grid, kHgWarps * 32, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
     else if (enc_type == NGP_DTYPE_F16)
-        hashgrid_forward_kernel<Tab, PairHalf<F16Op>, kPaired><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
+        hashgrid_forward_kernel<Tab, PairHalf<F16Op>, kPaired><<<grid, kHgWarps * 32, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
     else
-        hashgrid_forward_kernel<Tab, PairF32, kPaired><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
+        hashgrid_forward_kernel<Tab, PairF32, kPaired><<<grid, kHgWarps * 32, 0, stream>>>(d, d.n_coords, count, pos, latents, enc);
 }
 
 // Paired loads are used for 16-bit tables (a pair of rows is 8 bytes; measured 12% faster on the
@@ -287,7 +299,8 @@ int launch_hashgrid_forward_mixed(cudaStream_t stream, const NgpHashGridDescript
     const std::uintptr_t a = table_type == NGP_DTYPE_F32 ? 7u : 3u, b = enc_type == NGP_DTYPE_F32 ? 7u : 3u;
     NGP_CHECK_ARG(((std::uintptr_t)latents & a) == 0 && ((std::uintptr_t)enc & b) == 0,
                   "hashgrid: latents and encodings must be aligned to one row of two features");
-    const std::size_t tiles = ((std::size_t)d.n_coords + kHgTile - 1) / kHgTile;
+    const std::size_t tile_pts = (std::size_t)kHgTile * (d.L < (std::uint32_t)kHgWarps ? kHgWarps / d.L : 1u);
+    const std::size_t tiles = ((std::size_t)d.n_coords + tile_pts - 1) / tile_pts;
     if (tiles > 0) {
         const unsigned grid = grid_for(tiles, 1, 8);
         if (table_type == NGP_DTYPE_BF16)

@@ -115,8 +115,10 @@ class ProposalSampler:
 
     def network(self, points: torch.Tensor, enc: torch.Tensor, x: torch.Tensor, count: Optional[torch.Tensor],
                 f16: bool = False):
-        """Log density at `points`: FP32 (training, consistent with its backward) or, for the
-        sampler's bins, FP16 tensor cores."""
+        """Log density at `points`: FP32, or FP16 tensor cores (FP16 operands, FP32 accumulation).
+        The sampler's bins and, with `f16` set on the sampler, the training forward use the FP16
+        form; the training backward recomputes its own FP32 activations either way, so FP16 only
+        rounds the loss's x (relative error ~1e-3 against a regression residual far larger)."""
         n = points.shape[0]
         L.call("ngp_hashgrid_forward", [points, self.latents, count, enc], self.table.descriptor(n, self.bound))
         L.call("ngp_proposal_mlp_forward_f16" if f16 else "ngp_proposal_mlp_forward", [enc, self.weights, count, x],
@@ -179,7 +181,7 @@ class ProposalSampler:
         S = xyzs.shape[0] if max_points is None else min(xyzs.shape[0], max_points)
         cnt = self.counts[2:3] if count is None else count
         self.loss.zero_()
-        self.network(xyzs, self.enc_t[:S], self.x_t[:S], cnt)
+        self.network(xyzs, self.enc_t[:S], self.x_t[:S], cnt, f16=self.f16)
         L.call("ngp_proposal_loss", [cnt, self.x_t[:S], drgbs, self.g_x[:S], self.loss[0:1]],
                self._desc(S, count_index=0, sigma_stride=4))
         L.call("ngp_proposal_mlp_backward", [self.enc_t[:S], self.weights, self.g_x[:S], cnt, self.scratch,
@@ -188,7 +190,7 @@ class ProposalSampler:
         if distill is not None:
             M = self.M
             distill(self.xyz_d, self.sigma_d)
-            self.network(self.xyz_d, self.enc_t[:M], self.x_t[:M], None)
+            self.network(self.xyz_d, self.enc_t[:M], self.x_t[:M], None, f16=self.f16)
             L.call("ngp_proposal_loss", [None, self.x_t[:M], self.sigma_d, self.g_x[:M], self.loss[1:2]],
                    self._desc(M, count_index=3, sigma_stride=1))
             L.call("ngp_proposal_mlp_backward", [self.enc_t[:M], self.weights, self.g_x[:M], None, self.scratch,

@@ -43,6 +43,30 @@ def test_hashgrid_forward_golden(case):
     assert np.array_equal(enc, load(f"hashgrid_{case['tag']}")["encodings"])
 
 
+@pytest.mark.parametrize("L", [1, 2, 3, 5, 8, 12])
+def test_hashgrid_forward_level_counts(L):
+    """Tables with fewer levels than the kernel's 8 warps split a tile into sub-tiles of 32 points
+    (L = 1, 2, 3: 8, 4, 2 sub-tiles; L = 3 leaves two warps idle); L >= 8 loops warps over levels.
+    Ragged point counts and a device count below n: bit-exact against the oracle, rows past the
+    count untouched; the 16-bit encodings are the FP32 ones rounded."""
+    from jaxngp_gb300.encoders import LevelTable, hashgrid_forward
+    rng = np.random.default_rng(40 + L)
+    n = 32 * 8 * 5 + 37
+    pos = rng.uniform(-1, 1, size=(n, 3)).astype(np.float32)
+    tab = H.LevelTable(L, 2 ** 12, 2, 4, 256, per_level_scale=1.5)   # explicit scale: L = 1 has no ratio
+    lat = rng.uniform(-1, 1, size=(tab.n_params, 2)).astype(np.float32)
+    ref = H.encode(pos, lat, 1.0, tab)
+    t = LevelTable(L, 2 ** 12, 2, 4, 256, per_level_scale=1.5)
+    assert np.array_equal(hashgrid_forward(t, cu(pos), cu(lat), 1.0).cpu().numpy(), ref)
+    m = n - 301
+    out = torch.full((n, 2 * L), 7.0, device="cuda")
+    hashgrid_forward(t, cu(pos), cu(lat), 1.0, count=torch.tensor([m], dtype=torch.int32, device="cuda"), out=out)
+    got = out.cpu().numpy()
+    assert np.array_equal(got[:m], ref[:m]) and (got[m:] == 7.0).all()
+    h = hashgrid_forward(t, cu(pos), cu(lat), 1.0, enc_dtype=torch.bfloat16)
+    assert torch.equal(h, torch.from_numpy(ref).cuda().to(torch.bfloat16))
+
+
 def test_hashgrid_forward_large_bitexact():
     """2^18 points at the training configuration (config 0): bit-exact against the oracle."""
     from jaxngp_gb300.encoders import LevelTable, hashgrid_forward
