@@ -267,6 +267,24 @@ int ngp_hashgrid_forward_status(cudaStream_t stream, void **buffers, const char 
 void ngp_hashgrid_backward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_hashgrid_backward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* The total-variation term HashGridEncoder returns with tv_scale > 0 (models/encoders.py:236-254):
+ * tv = tv_scale * mean over levels and points of the sum, over the six axis neighbours of the
+ * point's corner 0 and the features, of (lat[neighbour] - lat[corner 0])^2.  Every point counts
+ * (no active count: the reference averages over the whole sample buffer).  tv_scale <= 0 writes
+ * tv = 0 and adds no gradient, as the reference returns 0.
+ * buffers: pos f32[N,3], latents f32[P,2], grad_scale f32[1] or NULL -> tv f32[1], dL_dlatents
+ * f32[P,2] (with_grad: d tv / d latents, times *grad_scale when given, ADDED to the buffer; NULL
+ * otherwise), scratch f64[1] (overwritten).  opaque: NgpHashGridTVDescriptor (grid.n_coords = N;
+ * grid.accumulate is ignored). */
+typedef struct NgpHashGridTVDescriptor {
+    NgpHashGridDescriptor grid;
+    float tv_scale;
+    uint32_t with_grad;
+} NgpHashGridTVDescriptor;
+
+void ngp_hashgrid_tv(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_hashgrid_tv_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* ------------------------------------------------------------------------- field MLP */
 #define NGP_MLP_WEIGHTS 9408 /* W0[32,64] W1[64,16] W2[32,64] W3[64,64] W4[64,3], packed */
 

@@ -127,6 +127,10 @@ class NgpHashGridMixedDescriptor(_Desc):
     _fields_ = [("grid", NgpHashGridDescriptor), ("table", c_u32), ("encodings", c_u32)]
 
 
+class NgpHashGridTVDescriptor(_Desc):
+    _fields_ = [("grid", NgpHashGridDescriptor), ("tv_scale", c_f32), ("with_grad", c_u32)]
+
+
 class NgpAdamMixedDescriptor(_Desc):
     _fields_ = [("adam", NgpAdamDescriptor), ("half_copy", c_u32)]
 

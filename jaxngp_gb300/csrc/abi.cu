@@ -39,6 +39,8 @@ int launch_hashgrid_forward(cudaStream_t, const NgpHashGridDescriptor &, const s
                             const float *, float *);
 int launch_hashgrid_backward(cudaStream_t, const NgpHashGridDescriptor &, const std::uint32_t *, const float *,
                              const float *, float *, bool);
+int launch_hashgrid_tv(cudaStream_t, const NgpHashGridDescriptor &, float, const float *, const float *, const float *,
+                       float *, float *, double *);
 int launch_mlp_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                        const float *, float *);
 int launch_mlp_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
@@ -301,6 +303,12 @@ NGP_ENTRY(ngp_hashgrid_forward) {
 NGP_ENTRY(ngp_hashgrid_backward) {
     NGP_DESC(NgpHashGridDescriptor, d);
     return launch_hashgrid_backward(stream, d, CU32(2), CF32(0), CF32(1), F32(3), d.accumulate != 0);
+}
+
+NGP_ENTRY(ngp_hashgrid_tv) {
+    NGP_DESC(NgpHashGridTVDescriptor, d);
+    return launch_hashgrid_tv(stream, d.grid, d.tv_scale, CF32(0), CF32(1), CF32(2), F32(3),
+                              d.with_grad != 0 ? F32(4) : nullptr, static_cast<double *>(buffers[5]));
 }
 
 NGP_ENTRY(ngp_render_blobs) {

@@ -11,7 +11,8 @@
 // encodings agree bit for bit with its float32 evaluation:
 //   pos01  = (pos + bound) / (2*bound)                      encoders.py:87
 //   ps     = pos01 * float32(scale_l) + 0.5                 encoders.py:216-218
-//   corner = floor(ps) + {0,1}^3 as uint32                  encoders.py:116-123
+//   corner = floor(ps) + {0,1}^3, converted to uint32       encoders.py:116-123
+//            (saturating, as XLA converts on the GPU: a coordinate below the grid becomes 0)
 //   index  = x + y*res + z*res^2           (dense levels)   encoders.py:134-155
 //          = x ^ y*2654435761 ^ z*805459861 (hashed levels) encoders.py:157-177
 //            then mod T, + offsets[l]; clamped to the table  encoders.py:179-189
@@ -61,7 +62,22 @@ struct PairHalf {
     }
 };
 
+// Float grid coordinate to uint32 as the reference's astype(jnp.uint32) runs on the GPU: negative
+// and NaN give 0, values past the range 2^32 - 1; integral values in range convert exactly.
+__device__ __forceinline__ std::uint32_t coord_u32(float v) {
+    return v > 0.f ? (v < 4294967296.f ? (std::uint32_t)v : 0xFFFFFFFFu) : 0u;
+}
+
+// Table row of grid vertex (x, y, z) at level l, clamped to the table (encoders.py:134-189).
 // `tmask` = T - 1 when T is a power of two (then h mod T = h & tmask), else 0.
+__device__ __forceinline__ std::uint32_t level_row(const NgpHashGridDescriptor &d, std::uint32_t l, std::uint32_t tmask,
+                                                   std::uint32_t x, std::uint32_t y, std::uint32_t z) {
+    const std::uint32_t res = d.resolutions[l];
+    const std::uint32_t h = l < d.first_hash_level ? (x + y * res + z * (res * res)) : (x ^ (y * 2654435761u) ^ (z * 805459861u));
+    const std::uint32_t idx = (tmask != 0u ? (h & tmask) : h % d.T) + d.offsets[l];
+    return idx < d.n_params - 1u ? idx : d.n_params - 1u;
+}
+
 __device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, std::uint32_t l, std::uint32_t tmask,
                                               float px, float py, float pz, Corner8 &c) {
     const float b = d.bound;
@@ -75,23 +91,20 @@ __device__ __forceinline__ void level_corners(const NgpHashGridDescriptor &d, st
     const float sy = __fadd_rn(__fmul_rn(uy, s), 0.5f);
     const float sz = __fadd_rn(__fmul_rn(uz, s), 0.5f);
     const float fx = floorf(sx), fy = floorf(sy), fz = floorf(sz);
-    const std::uint32_t bx = (std::uint32_t)(int)fx, by = (std::uint32_t)(int)fy, bz = (std::uint32_t)(int)fz;
+    // floor + {0, 1} in float, then converted (both corners of an axis below the grid become 0)
+    const std::uint32_t xs[2] = {coord_u32(fx), coord_u32(__fadd_rn(fx, 1.f))};
+    const std::uint32_t ys[2] = {coord_u32(fy), coord_u32(__fadd_rn(fy, 1.f))};
+    const std::uint32_t zs[2] = {coord_u32(fz), coord_u32(__fadd_rn(fz, 1.f))};
     // modf's fractional part (the sign of the coordinate) and the clip to [0, 1] of
     // encoders.py:204-212: a point below the grid gives all its weight to the lower corner
     const float rx = __fsub_rn(sx, truncf(sx)), ry = __fsub_rn(sy, truncf(sy)), rz = __fsub_rn(sz, truncf(sz));
     const float wx[2] = {fminf(fmaxf(__fsub_rn(1.f, rx), 0.f), 1.f), fminf(fmaxf(rx, 0.f), 1.f)};
     const float wy[2] = {fminf(fmaxf(__fsub_rn(1.f, ry), 0.f), 1.f), fminf(fmaxf(ry, 0.f), 1.f)};
     const float wz[2] = {fminf(fmaxf(__fsub_rn(1.f, rz), 0.f), 1.f), fminf(fmaxf(rz, 0.f), 1.f)};
-    const bool dense = l < d.first_hash_level;
-    const std::uint32_t res = d.resolutions[l], res2 = res * res;
-    const std::uint32_t off = d.offsets[l], last = d.n_params - 1u, T = d.T;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const std::uint32_t ox = (k >> 2) & 1, oy = (k >> 1) & 1, oz = k & 1;
-        const std::uint32_t x = bx + ox, y = by + oy, z = bz + oz;
-        const std::uint32_t h = dense ? (x + y * res + z * res2) : (x ^ (y * 2654435761u) ^ (z * 805459861u));
-        std::uint32_t idx = (tmask != 0u ? (h & tmask) : h % T) + off;
-        c.idx[k] = idx < last ? idx : last;
+        c.idx[k] = level_row(d, l, tmask, xs[ox], ys[oy], zs[oz]);
         c.w[k] = __fmul_rn(__fmul_rn(wx[ox], wy[oy]), wz[oz]);
     }
 }
@@ -249,6 +262,72 @@ __global__ void __launch_bounds__(256) hashgrid_backward_kernel(
     }
 }
 
+// Total variation of the table (encoders.py:236-254):
+//   tv = tv_scale * mean over (level, point) of sum over the six axis neighbours a of the point's
+//        corner 0 and the two features of (lat[a] - lat[corner 0])^2,
+// the neighbours floor(pos_scaled) + (0,0,1), (0,1,0), (1,0,0), (0,0,-1), (0,-1,0), (-1,0,0)
+// converted and indexed like the corners.  A warp takes 32 points at one level; each lane sums its
+// squared differences in FP32, the warp sums its lanes and adds the total into a double
+// accumulator.  With `dL_dlat`, 2 g (lat[a] - lat[c0]) is added to each neighbour's row and
+// subtracted from corner 0's, g = tv_scale / (L n) times *grad_scale when given.
+__global__ void __launch_bounds__(256) hashgrid_tv_kernel(NgpHashGridDescriptor d, std::uint32_t n_points,
+                                                          const float *__restrict__ pos, const float2 *__restrict__ lat,
+                                                          float tv_scale, const float *__restrict__ grad_scale,
+                                                          float2 *__restrict__ dL_dlat, double *__restrict__ acc) {
+    const std::uint32_t tmask = (d.T & (d.T - 1u)) == 0u ? d.T - 1u : 0u;
+    const unsigned lane = lane_id();
+    const std::size_t n_groups = (std::size_t)((n_points + 31) / 32) * d.L;
+    const std::size_t warp0 = ((std::size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const std::size_t n_warps = ((std::size_t)gridDim.x * blockDim.x) >> 5;
+    const float g2 = dL_dlat != nullptr
+                         ? 2.f * (float)((double)tv_scale / ((double)d.L * (double)n_points)) *
+                               (grad_scale != nullptr ? *grad_scale : 1.f)
+                         : 0.f;
+    float sum = 0.f;
+    for (std::size_t wg = warp0; wg < n_groups; wg += n_warps) {
+        const std::uint32_t l = (std::uint32_t)(wg % d.L);
+        const std::uint32_t n = (std::uint32_t)(wg / d.L) * 32u + lane;
+        if (n >= n_points) continue;
+        const float s = d.scales[l];
+        float f[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float u = __fdiv_rn(__fadd_rn(pos[(std::size_t)n * 3 + a], d.bound), d.two_bound);
+            f[a] = floorf(__fadd_rn(__fmul_rn(u, s), 0.5f));
+        }
+        const std::uint32_t c0 = level_row(d, l, tmask, coord_u32(f[0]), coord_u32(f[1]), coord_u32(f[2]));
+        const float2 v0 = __ldg(lat + c0);
+        float sx = 0.f, sy = 0.f;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            // neighbour j of encoders.py:41-48: axis z, y, x, then the same axes at -1
+            const int axis = 2 - (j % 3);
+            const float step = j < 3 ? 1.f : -1.f;
+            const std::uint32_t x = coord_u32(axis == 0 ? __fadd_rn(f[0], step) : f[0]);
+            const std::uint32_t y = coord_u32(axis == 1 ? __fadd_rn(f[1], step) : f[1]);
+            const std::uint32_t z = coord_u32(axis == 2 ? __fadd_rn(f[2], step) : f[2]);
+            const std::uint32_t r = level_row(d, l, tmask, x, y, z);
+            const float2 v = __ldg(lat + r);
+            const float dx = v.x - v0.x, dy = v.y - v0.y;
+            sum += dx * dx + dy * dy;
+            if (dL_dlat != nullptr) {
+                atomicAdd(dL_dlat + r, make_float2(g2 * dx, g2 * dy));
+                sx += dx;
+                sy += dy;
+            }
+        }
+        if (dL_dlat != nullptr) atomicAdd(dL_dlat + c0, make_float2(-g2 * sx, -g2 * sy));
+    }
+    const float w = warp_sum(sum);
+    if (lane == 0 && w != 0.f) atomicAdd(acc, (double)w);
+}
+
+// tv = tv_scale * sum / (L n): 0 / 0 for n = 0, as the mean of an empty array.
+__global__ void hashgrid_tv_finish_kernel(const double *__restrict__ acc, float tv_scale, std::uint32_t L,
+                                          std::uint32_t n_points, float *__restrict__ tv) {
+    tv[0] = (float)((double)tv_scale * (acc[0] / ((double)L * (double)n_points)));
+}
+
 }  // namespace
 
 int check_hashgrid_descriptor(const NgpHashGridDescriptor &d) {
@@ -342,6 +421,33 @@ int launch_hashgrid_backward_mixed(cudaStream_t stream, const NgpHashGridDescrip
             hashgrid_backward_kernel<PairF32><<<grid, 256, 0, stream>>>(d, d.n_coords, count, pos, dL_denc, out);
         count_launches(1);
     }
+    return launch_status();
+}
+
+// tv[0] <- the TV term of `latents` at d.n_coords points (0 when tv_scale <= 0); with dL_dlatents,
+// its gradient (times *grad_scale when given) is added there.  `acc` is one double of scratch.
+int launch_hashgrid_tv(cudaStream_t stream, const NgpHashGridDescriptor &d, float tv_scale, const float *pos,
+                       const float *latents, const float *grad_scale, float *tv, float *dL_dlatents, double *acc) {
+    int st = check_hashgrid_descriptor(d);
+    if (st != NGP_OK) return st;
+    NGP_CHECK_ARG(tv != nullptr && acc != nullptr, "hashgrid tv: tv and scratch buffers are required");
+    NGP_CHECK_ARG(((std::uintptr_t)acc & 7u) == 0, "hashgrid tv: the scratch double must be 8-byte aligned");
+    NGP_CHECK_ARG(((std::uintptr_t)latents & 7u) == 0 && ((std::uintptr_t)dL_dlatents & 7u) == 0,
+                  "hashgrid tv: latents and gradients must be aligned to one row of two features");
+    if (!(tv_scale > 0.f)) {   // encoders.py:253-254: no term, no gradient
+        NGP_CUDA_TRY(cudaMemsetAsync(tv, 0, sizeof(float), stream));
+        return launch_status();
+    }
+    NGP_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(double), stream));
+    const std::size_t items = (std::size_t)((d.n_coords + 31) / 32) * 32 * d.L;
+    if (items > 0) {
+        hashgrid_tv_kernel<<<grid_for(items, 256, 8), 256, 0, stream>>>(d, d.n_coords, pos,
+                                                                      reinterpret_cast<const float2 *>(latents), tv_scale,
+                                                                      grad_scale, reinterpret_cast<float2 *>(dL_dlatents), acc);
+        count_launches(1);
+    }
+    hashgrid_tv_finish_kernel<<<1, 1, 0, stream>>>(acc, tv_scale, d.L, d.n_coords, tv);
+    count_launches(1);
     return launch_status();
 }
 

@@ -138,6 +138,38 @@ def hashgrid_backward(table: LevelTable, pos: torch.Tensor, dL_denc: torch.Tenso
     return out
 
 
+def hashgrid_tv(table: LevelTable, pos: torch.Tensor, latents: torch.Tensor, bound: float, tv_scale: float,
+                grad: Optional[torch.Tensor] = None, grad_scale: Optional[torch.Tensor] = None,
+                out: Optional[torch.Tensor] = None, scratch: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """The TV term of encoders.py:236-254 as a device f32[1] (0 when tv_scale <= 0).  With `grad`
+    ([P, F] FP32), d tv / d latents -- times the device scalar `grad_scale` when given -- is added
+    into it."""
+    pos = pos.contiguous()
+    if out is None:
+        out = torch.empty(1, dtype=torch.float32, device=pos.device)
+    if scratch is None:
+        scratch = torch.empty(1, dtype=torch.float64, device=pos.device)
+    desc = L.NgpHashGridTVDescriptor(table.descriptor(pos.shape[0], bound), float(tv_scale), int(grad is not None))
+    L.call("ngp_hashgrid_tv", [pos, latents, grad_scale, out, grad, scratch], desc)
+    return out
+
+
+class _HashGridTVFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pos, latents, table, bound, tv_scale):
+        ctx.table, ctx.bound, ctx.tv_scale = table, bound, tv_scale
+        ctx.save_for_backward(pos, latents)
+        return hashgrid_tv(table, pos, latents, bound, tv_scale)[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        pos, latents = ctx.saved_tensors
+        grad = torch.zeros_like(latents)
+        g1 = g.reshape(1).to(torch.float32).contiguous()   # the upstream scalar stays on the device
+        hashgrid_tv(ctx.table, pos, latents, ctx.bound, ctx.tv_scale, grad=grad, grad_scale=g1)
+        return None, grad, None, None, None
+
+
 class _HashGridFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, pos, latents, table, bound):
@@ -176,9 +208,11 @@ class HashGridEncoder(torch.nn.Module):
         return self.table.b
 
     def forward(self, pos: torch.Tensor, bound: float):
-        if self.tv_scale > 0:
-            raise NotImplementedError("the total-variation term (tv_scale > 0) is not implemented on the GPU")
+        """(encodings [N, L*F], tv): tv is a differentiable device scalar when tv_scale > 0, else 0
+        (encoders.py:236-256)."""
         if pos.dtype != torch.float32 or pos.dim() != 2 or pos.shape[-1] != 3:
             raise ValueError("pos must be float32 [N, 3]")
         enc = _HashGridFn.apply(pos, self.latents, self.table, float(bound))
-        return enc, 0.0
+        tv = _HashGridTVFn.apply(pos, self.latents, self.table, float(bound), float(self.tv_scale)) \
+            if self.tv_scale > 0 else 0.0
+        return enc, tv

@@ -66,6 +66,8 @@ class TrainConfig:
     pipeline_march_blocks: int = 10    # CTAs per SM of that march (measured: 8-10 best; fewer starve it)
     march_coarse_skip: bool = False    # march: finish rays that cross no occupied coarse block at once
                                        # (exact; pays off on sparse grids, costs ~3% on dense ones)
+    tv_scale: float = 0.0              # the encoder's total-variation term (encoders.py:236-254), added to
+                                       # the loss and its gradient to the table's (0: off, the reference's default)
 
 
 def cascades_for(bound: float) -> int:
@@ -156,6 +158,10 @@ class NGPTrainer:
         self._d_march = L.MarchingDescriptor(R, S, cfg.diagonal_n_steps, self.K, cfg.G, bound, self.sp)
         self._hg_fwd = forward_call(self.table.descriptor(S, bound), self.gather_table, self.enc)
         self._hg_bwd = backward_call(self.table.descriptor(S, bound, accumulate=True), self.g_enc)
+        # the TV term over the whole sample buffer (the reference evaluates the field on all of it)
+        self._d_tv = L.NgpHashGridTVDescriptor(self.table.descriptor(S, bound), float(cfg.tv_scale), 1)
+        self.tv = torch.zeros(1, **f32)
+        self.tv_acc = torch.zeros(1, dtype=torch.float64, device=self.dev)
         self._d_mlp = L.NgpMlpDescriptor(S, 0)
         self._d_loss = L.NgpIntegrateLossDescriptor(R, S, data.camera.near if hasattr(data.camera, "near") else cfg.near,
                                                     cfg.huber_delta)
@@ -419,6 +425,10 @@ class NGPTrainer:
         self.field.backward(self.enc, self.dirs, self.weights, self.g_drgbs, cnt, self.grad_scale, self.mlp_scratch,
                             self.g_enc, self.g_w, loss_scale=self.loss_scale)
         L.call(self._hg_bwd[0], [self.xyzs, self.g_enc, cnt, self.g_lat], self._hg_bwd[1])
+        if cfg.tv_scale > 0:   # loss = rgb + tv (_utils.py:150-158); its gradient in the loss scale's units
+            gs = self.loss_scale.state[0:1].view(torch.float32) if self.loss_scale is not None else None
+            L.call("ngp_hashgrid_tv", [self.xyzs, self.latents, gs, self.tv, self.g_lat, self.tv_acc], self._d_tv)
+            self.stats[0:1] += self.tv
         count = self.step_count
         lr = lr_at(cfg.lr, count)
         d_lat = L.NgpAdamDescriptor(self.latents.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 0.0, 1)

@@ -23,8 +23,27 @@ HASHGRID_CASES = [
     dict(tag="ngp_b2", L=16, T=2**16, F=2, N_min=16, N_max=4096, bound=2.0, n=1024, seed=13),
 ]
 
+# Total-variation cases (encoders.py:236-254 with tv_scale > 0): a small table with dense and hashed
+# levels and the training configuration.  Points keep clear of the grid's low faces, where the -1
+# neighbour's float-to-uint32 conversion is the platform's (the tests cover that case separately).
+TV_CASES = [
+    dict(tag="tv_small", L=8, T=2**12, F=2, N_min=16, N_max=512, bound=1.0, n=1024, seed=31, tv_scale=0.37),
+    dict(tag="tv_ngp", L=16, T=2**19, F=2, N_min=16, N_max=2048, bound=1.0, n=2048, seed=32, tv_scale=1e-3),
+]
+
 FIELD_CASE = dict(L=16, T=2**19, F=2, N_min=16, N_max=2048, bound=1.0, n=1024, seed=21,
                   weight_seed=22)
+
+
+def tv_inputs(case):
+    """Returns (positions [n,3], latents [P,F], LevelTable, bound) for a TV case: positions with
+    (pos + bound) / (2 bound) >= 0.075, so floor(pos_scaled) >= 1 at every level (N_min = 16)."""
+    tab = LevelTable(case["L"], case["T"], case["F"], case["N_min"], case["N_max"])
+    rng = np.random.default_rng(case["seed"])
+    b = case["bound"]
+    pos = rng.uniform(-0.85 * b, 0.95 * b, size=(case["n"], 3)).astype(np.float32)
+    latents = rng.uniform(-1, 1, size=(tab.n_params, tab.F)).astype(np.float32)
+    return pos, latents, tab, b
 
 
 def hashgrid_inputs(case):

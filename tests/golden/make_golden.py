@@ -10,6 +10,9 @@ TEST INFRASTRUCTURE ONLY; run in a container that holds the reference checkout:
 * ``hashgrid_*.npz`` and ``field_*.npz``: outputs of the reference's ``HashGridEncoder``
   (models/encoders.py) and ``make_nerf_ngp`` field (models/nerfs.py), executed unmodified on the
   NumPy stand-in for jax/flax in ``jax_numpy_shim.py``.
+* ``tv_*.npz``: the total-variation term the same ``HashGridEncoder`` returns with tv_scale > 0.
+
+``python tests/golden/make_golden.py REF tv`` regenerates only the ``tv_*`` files.
 
 Large inputs (hash tables, MLP weights) are not stored: the tests regenerate them from the seeds
 recorded in each file with ``golden_inputs.py``.
@@ -26,8 +29,8 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from golden_inputs import (FIELD_CASE, HASHGRID_CASES, field_inputs, hashgrid_inputs,  # noqa: E402
-                           make_rays, random_bitfield)
+from golden_inputs import (FIELD_CASE, HASHGRID_CASES, TV_CASES, field_inputs, hashgrid_inputs,  # noqa: E402
+                           make_rays, random_bitfield, tv_inputs)
 
 
 def _save(name, **arrays):
@@ -169,7 +172,26 @@ def field(ref_root: str):
           density=np.asarray(density, np.float32), **{k: v for k, v in FIELD_CASE.items()})
 
 
+def total_variation(ref_root: str):
+    import jax_numpy_shim as shim
+    shim.install()
+    enc_mod = shim.load_reference_module("models.encoders",
+                                         os.path.join(ref_root, "models", "encoders.py"))
+    for case in TV_CASES:
+        pos, latents, tab, bound = tv_inputs(case)
+        enc = enc_mod.HashGridEncoder(L=tab.L, T=tab.T, F=tab.F, N_min=tab.N_min, N_max=tab.N_max,
+                                      tv_scale=case["tv_scale"])
+        enc.bind({"latent codes stored on grid vertices": latents})
+        _, tv = enc(pos, bound)
+        _save(f"{case['tag']}.npz", tv=np.asarray(tv, np.float32), **{k: v for k, v in case.items() if k != "tag"})
+
+
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    volrend(ref)
-    field(ref)
+    parts = sys.argv[2:] or ["volrend", "field", "tv"]
+    if "volrend" in parts:
+        volrend(ref)
+    if "field" in parts:
+        field(ref)
+    if "tv" in parts:
+        total_variation(ref)

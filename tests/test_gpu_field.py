@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 import torch
 
-from golden_inputs import FIELD_CASE, HASHGRID_CASES, field_inputs, hashgrid_inputs
+from golden_inputs import FIELD_CASE, HASHGRID_CASES, TV_CASES, field_inputs, hashgrid_inputs, tv_inputs
 from oracle import field as Fd
 from oracle import hashgrid as H
 from tests.golden_util import load
@@ -65,6 +65,66 @@ def test_hashgrid_forward_level_counts(L):
     assert np.array_equal(got[:m], ref[:m]) and (got[m:] == 7.0).all()
     h = hashgrid_forward(t, cu(pos), cu(lat), 1.0, enc_dtype=torch.bfloat16)
     assert torch.equal(h, torch.from_numpy(ref).cuda().to(torch.bfloat16))
+
+
+@pytest.mark.parametrize("case", TV_CASES, ids=lambda c: c["tag"])
+def test_hashgrid_tv_golden(case):
+    """The TV term against the reference's HashGridEncoder (fixtures made by running encoders.py)."""
+    from jaxngp_gb300.encoders import LevelTable, hashgrid_tv
+    pos, lat, tab, b = tv_inputs(case)
+    t = LevelTable(tab.L, tab.T, tab.F, tab.N_min, tab.N_max)
+    tv = float(hashgrid_tv(t, cu(pos), cu(lat), b, case["tv_scale"]))
+    want = float(load(case["tag"])["tv"])
+    assert abs(tv - want) <= RTOL * abs(want)
+
+
+def test_hashgrid_tv_vs_fp64():
+    """Value and gradient against the FP64 oracle on points inside, on and outside the box (the
+    saturating coordinate conversion at the low faces); the gradient is scaled by a device scalar
+    and added to what the buffer holds; tv_scale = 0 writes 0 and leaves the gradient alone."""
+    from jaxngp_gb300.encoders import LevelTable, hashgrid_tv
+    rng = np.random.default_rng(17)
+    n = 40000
+    pos = rng.uniform(-1.2, 1.2, size=(n, 3)).astype(np.float32)
+    pos[:64] = np.float32(-1.0)                       # the low corner of the box
+    tab = H.LevelTable(16, 2 ** 16, 2, 16, 2048)
+    t = LevelTable(16, 2 ** 16, 2, 16, 2048)
+    lat = rng.uniform(-1, 1, size=(tab.n_params, 2)).astype(np.float32)
+    s = 0.05
+    want = H.total_variation(pos, lat, 1.0, tab, s, dtype=np.float64)
+    gwant = H.total_variation_grad(pos, lat, 1.0, tab, s)
+    grad = torch.zeros(tab.n_params, 2, device="cuda")
+    three = torch.tensor([3.0], device="cuda")
+    tv = hashgrid_tv(t, cu(pos), cu(lat), 1.0, s, grad=grad, grad_scale=three)
+    assert abs(float(tv) - want) <= RTOL * want
+    first = grad.cpu().numpy()
+    assert rel_err(first, 3.0 * gwant) <= RTOL
+    hashgrid_tv(t, cu(pos), cu(lat), 1.0, s, grad=grad, grad_scale=three)   # adds to what is there
+    assert rel_err(grad.cpu().numpy(), 2.0 * first) <= RTOL
+    before = grad.clone()
+    tv0 = hashgrid_tv(t, cu(pos), cu(lat), 1.0, 0.0, grad=grad)
+    assert float(tv0) == 0.0 and torch.equal(grad, before)
+
+
+def test_hashgrid_encoder_module_tv():
+    """HashGridEncoder(tv_scale > 0) returns (encodings, tv) with tv differentiable w.r.t. the table,
+    as the reference's flax module; the upstream gradient of tv scales the table gradient."""
+    from jaxngp_gb300.encoders import HashGridEncoder
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    enc_mod = HashGridEncoder(16, 2 ** 14, 2, 16, 2048, tv_scale=0.2, generator=g)
+    with torch.no_grad():
+        enc_mod.latents.uniform_(-1, 1, generator=g)
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(-1, 1, size=(5000, 3)).astype(np.float32)
+    enc, tv = enc_mod(cu(pos), 1.0)
+    lat = enc_mod.latents.detach().cpu().numpy()
+    tab = H.LevelTable(16, 2 ** 14, 2, 16, 2048)
+    tv_value = float(tv.detach())
+    assert abs(tv_value - H.total_variation(pos, lat, 1.0, tab, 0.2, dtype=np.float64)) <= RTOL * tv_value
+    (2.5 * tv).backward()
+    gw = H.total_variation_grad(pos, lat, 1.0, tab, 0.2)
+    assert rel_err(enc_mod.latents.grad.cpu().numpy(), 2.5 * gw) <= RTOL
 
 
 def test_hashgrid_forward_large_bitexact():

@@ -74,6 +74,31 @@ def test_train_mixed_precision(small_scene, form):
         assert s["skipped_steps"] <= 3 and s["scale"] >= 2.0 ** 12, s
 
 
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+def test_train_with_total_variation(small_scene, prec):
+    """TrainConfig.tv_scale > 0 (encoders.py:236-254): the step's loss is the TV-free step's plus the
+    TV term of the initial table at the step's whole sample buffer (the oracle's value), and
+    training with it stays finite -- under FP16 the TV gradient joins the table's in the loss
+    scale's units."""
+    from oracle import hashgrid as H
+    from jaxngp_gb300.trainer import NGPTrainer, TrainConfig
+    # a budget no ray overflows, no jitter, the same pixels: both trainers see the same batch (the
+    # table starts at +-1e-4, so a large tv_scale lifts the term far above the loss's float noise)
+    kw = dict(total_samples=1 << 18, n_rays=512, T=1 << 16, seed=2, perturb=False, random_bg=False,
+              mlp_precision=prec, table_precision=prec, half_activations=prec != "fp32")
+    s = 10.0
+    perm = torch.randint(0, small_scene.n_pixels, (512,), dtype=torch.int32, device="cuda")
+    a, b = NGPTrainer(small_scene, TrainConfig(**kw)), NGPTrainer(small_scene, TrainConfig(tv_scale=s, **kw))
+    lat0 = b.latents.detach().cpu().numpy().copy()
+    la, lb = a.step(perm).cpu().numpy(), b.step(perm).cpu().numpy()
+    tab = H.LevelTable(b.table.L, b.table.T, b.table.F, b.table.N_min, b.table.N_max)
+    want = H.total_variation(b.xyzs.cpu().numpy(), lat0, b.bound, tab, s, dtype=np.float64)
+    assert abs(float(b.tv) - want) <= 1e-5 * want
+    assert abs((float(lb[0]) - float(la[0])) - want) <= 1e-5 * want + 8 * float(np.spacing(la[0]))
+    losses = [float(b.step().cpu().numpy()[0]) for _ in range(40)]
+    assert np.isfinite(losses).all()
+
+
 def test_train_step_with_host_perm(small_scene):
     """The step accepts the reference's `perm` (pixel indices); with a sample budget no ray
     overflows, two runs agree up to the order of float atomics (which rays fit an overflowing
