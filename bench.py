@@ -412,6 +412,7 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     if tr.prop is not None:
         from jaxngp_gb300.renderer import ProposalRenderer
         quality["psnr_heldout_proposal_renderer"] = round(held.psnr(tr, ProposalRenderer(tr)), 3)
+    quality["error_vs_fp64"] = fp64_errors(tr)
 
     out = {"metric": args.metric, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
@@ -440,6 +441,42 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
         out["render_1080p"] = render
     if render_prop is not None:
         out["render_1080p_proposal"] = render_prop
+    return out
+
+
+def fp64_errors(tr) -> dict:
+    """Errors of the form's colours against FP64 on a whole training batch (the last one trained,
+    at the trained weights).  The reference is the FP32 field (FP32 table, FP32 SIMT MLP)
+    composited in FP64 on the GPU (ngp_integrate_rays_fp64).  `chain`: the form's own encoder and
+    field composited by the float integrator.  `integrator`: the FP32 field's samples composited
+    in float.  Norm-relative over the batch's rays with samples (rgb, then opacity); rays whose
+    float and double compositing stop at different samples are counted apart."""
+    import torch
+    from jaxngp_gb300 import _lib as L
+    from jaxngp_gb300 import volrendjax as vr
+    from jaxngp_gb300.encoders import hashgrid_forward
+    from jaxngp_gb300.precision import integrate_rays_fp64
+    S = tr.S
+    with torch.no_grad():
+        L.call(tr._hg_fwd[0], [tr.xyzs, tr.gather_table, None, tr.enc], tr._hg_fwd[1])
+        d_form = torch.empty(S, 4, dtype=torch.float32, device=tr.dev)
+        tr.field.forward(tr.enc, tr.dirs, tr.weights, None, d_form)
+        enc32 = hashgrid_forward(tr.table, tr.xyzs, tr.latents, tr.bound)
+        d32 = torch.empty(S, 4, dtype=torch.float32, device=tr.dev)
+        L.call("ngp_field_forward", [enc32, tr.dirs, tr.weights, None, d32], L.NgpMlpDescriptor(S, 0))
+        args = (tr.startidx, tr.n_samples, tr.bgs, tr.dss, tr.z_vals)
+        _, c_form, o_form = vr.integrate_rays(0.0, *args, d_form)
+        _, c32, o32 = vr.integrate_rays(0.0, *args, d32)
+        c64, T64, used64 = integrate_rays_fp64(*args, d32)
+        rays = (tr.n_samples > 0) & tr.valid
+        ref = torch.cat([c64[:, :3], (1.0 - T64)[:, None]], 1)[rays]
+
+        def rel(c, o):
+            x = torch.cat([c[:, :3].double(), o.double()[:, None]], 1)[rays]
+            return float((x - ref).norm() / ref.norm())
+        out = {"rays": int(rays.sum()), "chain": round(rel(c_form, o_form), 9),
+               "integrator": round(rel(c32, o32), 9),
+               "reference": "FP32 field composited in FP64 on the GPU (ngp_integrate_rays_fp64)"}
     return out
 
 

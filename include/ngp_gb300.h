@@ -207,6 +207,16 @@ int integrate_rays_backward_status(cudaStream_t stream, void **buffers, const ch
 void ngp_integrate_rays_backward_exact(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_integrate_rays_backward_exact_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* FP64 checker of integrate_rays (no reference counterpart; used to state errors, not by any
+ * training or rendering path): the same forward loop in double on the float inputs -- transmittance
+ * product, colour and depth sums, termination once T <= 1e-4, opacity normalisation of terminated
+ * rays, else + T bg.
+ * buffers: rays_sample_startidx u32[R], rays_n_samples u32[R], bgs f32[R,3], dss f32[S], z_vals f32[S],
+ * drgbs f32[S,4] -> rgbds f64[R,4], transmittance f64[R] (after the last composited sample),
+ * n_used u32[R] (samples composited).  opaque: IntegratingDescriptor. */
+void ngp_integrate_rays_fp64(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int ngp_integrate_rays_fp64_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+
 /* Replaces volrendjax::integrate_rays_inference (volrend.h:170-175; integrating.cu:530-537).
  * buffers: rays_bg f32[N,3], rays_rgbd f32[N,4], rays_T f32[N], n_samples u32[n],
  * indices u32[n], dss f32[n,cap], z_vals f32[n,cap], drgbs f32[n,cap,4] -> terminate_cnt u32[1],

@@ -39,6 +39,9 @@ int launch_hashgrid_forward(cudaStream_t, const NgpHashGridDescriptor &, const s
                             const float *, float *);
 int launch_hashgrid_backward(cudaStream_t, const NgpHashGridDescriptor &, const std::uint32_t *, const float *,
                              const float *, float *, bool);
+int launch_integrate_rays_fp64(cudaStream_t, const IntegratingDescriptor &, const std::uint32_t *, const std::uint32_t *,
+                               const float *, const float *, const float *, const float *, double *, double *,
+                               std::uint32_t *);
 int launch_hashgrid_tv(cudaStream_t, const NgpHashGridDescriptor &, float, const float *, const float *, const float *,
                        float *, float *, double *);
 int launch_mlp_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
@@ -276,6 +279,12 @@ NGP_ENTRY(ngp_integrate_rays_backward_exact) {
                   "integrate_rays_backward_exact: drgbs, final_rgbds, dL_dfinal_rgbds and dL_ddrgbs must be 16-byte aligned");
     return launch_integrate_rays_backward(stream, d, CU32(0), CU32(1), CF32(2), CF32(3), CF32(4), CF32(5), CF32(6),
                                           CF32(7), CF32(8), F32(9), F32(10), F32(11), true);
+}
+
+NGP_ENTRY(ngp_integrate_rays_fp64) {
+    NGP_DESC(IntegratingDescriptor, d);
+    return launch_integrate_rays_fp64(stream, d, CU32(0), CU32(1), CF32(2), CF32(3), CF32(4), CF32(5),
+                                      static_cast<double *>(buffers[6]), static_cast<double *>(buffers[7]), U32(8));
 }
 
 NGP_ENTRY(integrate_rays_inference) {

@@ -64,6 +64,47 @@ __global__ void __launch_bounds__(256) integrate_rays_kernel(
     if (lane_id() == 0 && used > 0) atomicAdd(measured, used);
 }
 
+// FP64 checker of integrate_rays (not used by any training or rendering path): the same loop --
+// alpha = 1 - exp(-sigma ds), w = T alpha, colour and depth sums, T *= 1 - alpha, stop once
+// T <= 1e-4, normalise a terminated ray by its opacity, else add T bg -- evaluated in double on the
+// float inputs widened exactly.  It states the error of the float integrators (and of everything
+// that feeds them) at full batch sizes.  Outputs per ray: colour and depth, the transmittance
+// after the last composited sample, and the number of samples composited (a ray whose float and
+// double transmittances cross 1e-4 at different samples composites different counts).
+__global__ void __launch_bounds__(256) integrate_rays_fp64_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, const std::uint32_t *__restrict__ startidx,
+    const std::uint32_t *__restrict__ n_samples, const float *__restrict__ bgs,
+    const float *__restrict__ dss, const float *__restrict__ z_vals, const float *__restrict__ drgbs,
+    double *__restrict__ rgbds, double *__restrict__ trans, std::uint32_t *__restrict__ used) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_rays) return;
+    const std::uint32_t s = startidx[i], n = clamp_range(s, n_samples[i], total_samples);
+    const float *rd = dss + s, *rz = z_vals + s;
+    const float4 *rc = reinterpret_cast<const float4 *>(drgbs) + s;
+    double depth = 0.0, T = 1.0, r = 0.0, g = 0.0, b = 0.0;
+    std::uint32_t k = 0;
+    for (; T > (double)kTThreshold && k < n; ++k) {
+        const float4 c = rc[k];
+        const double alpha = 1.0 - exp(-(double)c.x * (double)rd[k]);
+        const double w = T * alpha;
+        r += w * (double)c.y;
+        g += w * (double)c.z;
+        b += w * (double)c.w;
+        depth += w * (double)rz[k];
+        T *= 1.0 - alpha;
+    }
+    double *o = rgbds + (std::size_t)i * 4;
+    if (T <= (double)kTThreshold) {
+        const double opacity = 1.0 - T;
+        o[0] = r / opacity, o[1] = g / opacity, o[2] = b / opacity, o[3] = depth / opacity;
+    } else {
+        o[0] = r + T * (double)bgs[i * 3 + 0], o[1] = g + T * (double)bgs[i * 3 + 1];
+        o[2] = b + T * (double)bgs[i * 3 + 2], o[3] = depth;
+    }
+    trans[i] = T;
+    used[i] = k;
+}
+
 // kExact = false: the reference's gradient (integrating.cu:173-233): density gradients scaled by
 // min(z^2, 1), the near-plane penalty added, the background counted in (final - cur) and again in
 // bg * (1 - opacity), the opacity normalisation of terminated rays not differentiated.
@@ -248,6 +289,19 @@ int launch_integrate_rays(cudaStream_t stream, const IntegratingDescriptor &d,
     if (d.n_rays > 0) {
         integrate_rays_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(
             d.n_rays, d.total_samples, startidx, n_samples, bgs, dss, z_vals, drgbs, measured, final_rgbds, final_opacities);
+        count_launches(1);
+    }
+    return launch_status();
+}
+
+int launch_integrate_rays_fp64(cudaStream_t stream, const IntegratingDescriptor &d, const std::uint32_t *startidx,
+                               const std::uint32_t *n_samples, const float *bgs, const float *dss, const float *z_vals,
+                               const float *drgbs, double *rgbds, double *trans, std::uint32_t *used) {
+    NGP_CHECK_ARG(((std::uintptr_t)drgbs & 15u) == 0 && ((std::uintptr_t)rgbds & 7u) == 0 && ((std::uintptr_t)trans & 7u) == 0,
+                  "integrate_rays_fp64: drgbs must be 16-byte and the double outputs 8-byte aligned");
+    if (d.n_rays > 0) {
+        integrate_rays_fp64_kernel<<<(d.n_rays + 255) / 256, 256, 0, stream>>>(d.n_rays, d.total_samples, startidx, n_samples,
+                                                                             bgs, dss, z_vals, drgbs, rgbds, trans, used);
         count_launches(1);
     }
     return launch_status();

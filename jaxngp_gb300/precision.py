@@ -51,3 +51,19 @@ class LossScale:
         s = self.state.cpu()
         return {"scale": float(s[0:1].view(torch.float32).item()), "overflow": int(s[1]),
                 "good_steps": int(s[2]), "skipped_steps": int(s[3])}
+
+
+def integrate_rays_fp64(rays_sample_startidx: torch.Tensor, rays_n_samples: torch.Tensor, bgs: torch.Tensor,
+                        dss: torch.Tensor, z_vals: torch.Tensor, drgbs: torch.Tensor):
+    """FP64 checker of integrate_rays on the GPU (ngp_integrate_rays_fp64): the same compositing in
+    double on the float inputs.  Returns (rgbd f64[R,4], transmittance f64[R], n_used int32[R]).
+    For stating errors only; no training or rendering path calls it."""
+    R = rays_sample_startidx.shape[0]
+    dev = dss.device
+    rgbd = torch.empty(R, 4, dtype=torch.float64, device=dev)
+    trans = torch.empty(R, dtype=torch.float64, device=dev)
+    used = torch.empty(R, dtype=torch.int32, device=dev)
+    bgs = bgs.expand(R, 3).contiguous() if bgs.dim() == 1 else bgs.contiguous()
+    L.call("ngp_integrate_rays_fp64", [rays_sample_startidx, rays_n_samples, bgs, dss, z_vals, drgbs.contiguous(),
+                                       rgbd, trans, used], L.IntegratingDescriptor(R, dss.shape[0]))
+    return rgbd, trans, used
