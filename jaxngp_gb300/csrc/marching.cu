@@ -211,11 +211,8 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
     std::uint32_t *__restrict__ queue, bool *__restrict__ ray_is_valid,
     std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
     std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
-    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse,
-    const std::uint32_t *__restrict__ ray_list, const std::uint32_t *__restrict__ list_count) {
+    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse) {
     __shared__ std::uint32_t expand[1024];  // expand_bits(v), v < G (G <= 1024)
-    // list form: the rays to march are ray_list[0 .. *list_count) (taken through the queue)
-    if (ray_list != nullptr) n_rays = min(n_rays, *list_count);
     for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
     __syncthreads();
     const unsigned lane = lane_id();
@@ -249,7 +246,7 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
                 const std::uint32_t q = base + (unsigned)__popc(idle & lt_mask);
                 const std::uint32_t qi = queue != nullptr ? q : (((q >> 5) * n_warps + warp) << 5) + (q & 31u);
                 if (qi < n_rays) {
-                    const std::uint32_t r = ray_list != nullptr ? ray_list[qi] : qi;
+                    const std::uint32_t r = qi;
                     ray = r;
                     o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
                     d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
@@ -359,6 +356,204 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
             if (lane == 0 && over > 0) atomicAdd(n_exceeded, over);
         }
         if (phase == kWrite && !(k < n && t < t1 && it < kMaxMarchIters)) phase = kIdle;
+    }
+}
+
+// ------------------------------------------------------------- march_rays, a warp per ray
+
+// Lane j's view of a 32-step lookahead from t: its candidate t after j occupied steps (the
+// additions the sequential march makes, in its order), whether the march loop's condition still
+// holds there (`live`, given the lane's part of it in `cond`), and whether the cell is occupied.
+struct Lookahead {
+    float t, ds, mb;
+    V3 pos, g;
+    bool live, occ;
+};
+
+__device__ __forceinline__ void look_ahead(const MarchParams &m, float t, unsigned lane, V3 o, V3 d, float t1,
+                                           bool cond, const std::uint8_t *__restrict__ bits,
+                                           const std::uint32_t *expand, Lookahead &a) {
+    float tj = t;
+    for (unsigned i = 0; i < lane; ++i) tj = tj + calc_ds(tj, m);
+    a.t = tj;
+    a.pos = at(o, d, tj);
+    a.ds = calc_ds(tj, m);
+    a.live = cond && tj < t1;
+    a.occ = a.live && occupied_at(m, a.pos, a.ds, bits, a.g, a.mb, expand);
+}
+
+// After a lookahead that accepted k occupied steps: the t the sequential march reaches next, or
+// false when its loop ends at lane k (k < 32 and the condition fails there).  An empty cell at
+// lane k is skipped by that lane exactly as marching.cu:182-189 skips it.
+__device__ __forceinline__ bool advance(const MarchParams &m, const Lookahead &a, unsigned lane, unsigned k, V3 d,
+                                        V3 inv_d, float &t) {
+    if (k < 32u) {
+        if (!__shfl_sync(0xffffffffu, a.live, k)) return false;
+        const float nt = lane == k ? skip_empty(m, a.t, a.g, a.mb, a.pos, d, inv_d) : 0.f;
+        t = __shfl_sync(0xffffffffu, nt, k);
+    } else {
+        const float nt = lane == 31u ? a.t + a.ds : 0.f;
+        t = __shfl_sync(0xffffffffu, nt, 31);
+    }
+    return true;
+}
+
+constexpr int kWarpTrips = 256;   // trips with samples the count pass records per ray (per warp)
+
+// The list form of the training march (the proposal sampler's per-ray fallback) marches a few
+// thousand rays of a batch, each through occupied space.  With a lane per ray, each ray's chain of
+// dependent steps would run alone while most of the GPU idled; here a warp takes one ray and looks
+// 32 steps ahead.  All lanes test their candidate cells at once, and the warp accepts the samples
+// up to the first lane whose cell is empty or whose step ends the ray.  Both passes (count, then
+// write from the first occupied sample) follow march_rays_kernel's sequence, so each ray's count,
+// validity and samples are bit-identical to it.  The budget probe checks the counter once per trip
+// that reaches the ray's first occupied sample or every 16th after it, if the ray goes on.  The
+// count pass records, per trip that took samples, the trip's starting t and how many it took
+// (up to kWarpTrips trips); the write pass then replays those trips -- the same additions from
+// the same t -- without looking at the grid again, and re-marches only a ray with more trips.
+// Few warps are busy at once (one per listed ray), so no minimum residency is asked of the
+// register allocator.
+__global__ void __launch_bounds__(kMarchBlock) march_rays_warp_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, MarchParams m,
+    const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+    const float *__restrict__ t_starts, const float *__restrict__ t_ends,
+    const float *__restrict__ noises, const std::uint8_t *__restrict__ bits,
+    std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded,
+    std::uint32_t *__restrict__ queue, bool *__restrict__ ray_is_valid,
+    std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
+    std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
+    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint32_t *__restrict__ ray_list,
+    const std::uint32_t *__restrict__ list_count) {
+    __shared__ std::uint32_t expand[1024];  // expand_bits(v), v < G (G <= 1024)
+    __shared__ float trip_t[kMarchBlock / 32][kWarpTrips];
+    __shared__ std::uint8_t trip_k[kMarchBlock / 32][kWarpTrips];
+    n_rays = min(n_rays, *list_count);
+    for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
+    __syncthreads();
+    const unsigned lane = lane_id(), wib = threadIdx.x >> 5;
+    const float n_cap = (float)m.dns * m.bound;
+    for (;;) {
+        std::uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(queue, 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n_rays) break;
+        const std::uint32_t r = ray_list[q];
+        const V3 o{rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
+        const V3 d{rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
+        const float t0 = t_starts[r], t1 = t_ends[r];
+        if (!(t1 > t0)) {  // marching.cu:151
+            if (lane == 0) {
+                ray_is_valid[r] = false;
+                rays_n_samples[r] = 0;
+                rays_startidx[r] = 0;
+            }
+            continue;
+        }
+        const V3 inv_d{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+        // ---- count pass (marching.cu:162-192)
+        float t = t0 + calc_ds(t0, m) * noises[r], t_hit = 0.f;
+        std::uint32_t n = 0, it = 0, trips = 0;
+        bool dropped = false;
+        for (;;) {
+            Lookahead a;
+            look_ahead(m, t, lane, o, d, t1, (float)(n + lane) < n_cap && it + lane < kMaxMarchIters, bits, expand, a);
+            const unsigned stop = __ballot_sync(0xffffffffu, !a.occ);
+            const unsigned k = stop != 0u ? (unsigned)__ffs(stop) - 1u : 32u;
+            if (n == 0 && k > 0) t_hit = t;
+            if (k > 0) {
+                if (lane == 0 && trips < (std::uint32_t)kWarpTrips) {
+                    trip_t[wib][trips] = t;
+                    trip_k[wib][trips] = (std::uint8_t)k;
+                }
+                ++trips;
+            }
+            const std::uint32_t n0 = n;
+            n += k;
+            it += k;
+            const bool more = advance(m, a, lane, k, d, inv_d, t);
+            if (!more) break;
+            if (k < 32u) ++it;   // the skip is a step of its own
+            // a sample numbered 1, 17, 33, ... was taken in this trip: probe the budget (lane 0
+            // reads the counter, so the whole warp takes the same decision)
+            if (k > 0 && ((n0 + 15u) >> 4) != ((n + 15u) >> 4)) {
+                int full = 0;
+                if (lane == 0) full = *((volatile std::uint32_t *)next_loc) >= total_samples;
+                if (__shfl_sync(0xffffffffu, full, 0)) {
+                    dropped = true;
+                    break;
+                }
+            }
+        }
+        if (dropped || n == 0) {  // over budget, or marching.cu:196-199: valid with no samples
+            if (lane == 0) {
+                ray_is_valid[r] = !dropped;
+                rays_n_samples[r] = 0;
+                rays_startidx[r] = 0;
+            }
+            continue;
+        }
+        std::uint32_t start = 0;
+        if (lane == 0) start = atomicAdd(next_loc, n);
+        start = __shfl_sync(0xffffffffu, start, 0);
+        const bool fits = (std::uint64_t)start + n <= total_samples;
+        if (lane == 0) {
+            ray_is_valid[r] = fits;
+            rays_n_samples[r] = fits ? n : 0u;
+            rays_startidx[r] = fits ? start : 0u;
+            if (!fits) atomicAdd(n_exceeded, n);
+        }
+        if (!fits) continue;
+        // ---- write pass from the first occupied sample (marching.cu:224-267)
+        __syncwarp();
+        if (trips <= (std::uint32_t)kWarpTrips) {   // replay the recorded trips
+            std::uint32_t w = 0;
+            for (std::uint32_t e = 0; e < trips; ++e) {
+                const unsigned k = trip_k[wib][e];
+                if (lane < k) {
+                    float tj = trip_t[wib][e];
+                    for (unsigned i = 0; i < lane; ++i) tj = tj + calc_ds(tj, m);
+                    const V3 pos = at(o, d, tj);
+                    const std::uint32_t s = start + w + lane;
+                    idcs[s] = r;
+                    xyzs[(std::size_t)s * 3 + 0] = pos.x;
+                    xyzs[(std::size_t)s * 3 + 1] = pos.y;
+                    xyzs[(std::size_t)s * 3 + 2] = pos.z;
+                    dirs[(std::size_t)s * 3 + 0] = d.x;
+                    dirs[(std::size_t)s * 3 + 1] = d.y;
+                    dirs[(std::size_t)s * 3 + 2] = d.z;
+                    dss[s] = calc_ds(tj, m);
+                    z_vals[s] = tj;
+                }
+                w += k;
+            }
+            __syncwarp();   // the next ray's count pass overwrites the records
+            continue;
+        }
+        t = t_hit;
+        std::uint32_t w = 0;
+        it = 0;
+        for (;;) {
+            Lookahead a;
+            look_ahead(m, t, lane, o, d, t1, w + lane < n && it + lane < kMaxMarchIters, bits, expand, a);
+            const unsigned stop = __ballot_sync(0xffffffffu, !a.occ);
+            const unsigned k = stop != 0u ? (unsigned)__ffs(stop) - 1u : 32u;
+            if (lane < k) {
+                const std::uint32_t s = start + w + lane;
+                idcs[s] = r;
+                xyzs[(std::size_t)s * 3 + 0] = a.pos.x;
+                xyzs[(std::size_t)s * 3 + 1] = a.pos.y;
+                xyzs[(std::size_t)s * 3 + 2] = a.pos.z;
+                dirs[(std::size_t)s * 3 + 0] = d.x;
+                dirs[(std::size_t)s * 3 + 1] = d.y;
+                dirs[(std::size_t)s * 3 + 2] = d.z;
+                dss[s] = a.ds;
+                z_vals[s] = a.t;
+            }
+            w += k;
+            it += k;
+            if (!advance(m, a, lane, k, d, inv_d, t)) break;
+            if (k < 32u) ++it;
+        }
     }
 }
 
@@ -688,13 +883,11 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
         if (probe) {
             march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse,
-                nullptr, nullptr);
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
         } else {
             march_rays_kernel<false><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse,
-                nullptr, nullptr);
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
         }
         count_launches(1);
     }
@@ -723,13 +916,13 @@ int launch_march_rays_list(cudaStream_t stream, const MarchingDescriptor &d, con
     NGP_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(std::uint32_t), stream));
     const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
     if (d.n_rays > 0) {
-        const unsigned warps_needed = (d.n_rays + 31) / 32;
+        const unsigned warps_needed = d.n_rays;   // a warp per listed ray, at most n_rays of them
         const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
         const unsigned cap = (unsigned)sm_count() * (unsigned)g_march_blocks_per_sm.load(std::memory_order_relaxed);
         const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
-        march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
+        march_rays_warp_kernel<<<grid, kMarchBlock, 0, stream>>>(
             d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc, n_exceeded, queue,
-            ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, nullptr, ray_list, list_count);
+            ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, ray_list, list_count);
         count_launches(1);
     }
     return launch_status();

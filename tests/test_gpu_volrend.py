@@ -369,3 +369,71 @@ def test_march_rays_train_coarse_shortcut(vr, budget_frac):
         assert np.array_equal(ns, full_n) and np.array_equal(valid, ref[1])
         without = _march_train(z, total)
         assert np.array_equal(without[3], ns) and np.array_equal(without[2], valid)
+
+
+def _march_list(o, d, t0, t1, noise, bits, listed, n, total, K, G, bound, sp, start_at=17):
+    """ngp_march_rays_fallback over `listed`; counters start at (start_at, 0), ray outputs at -1."""
+    from jaxngp_gb300 import _lib as L
+    i32 = dict(dtype=torch.int32, device="cuda")
+    ctr = torch.tensor([start_at, 0], **i32)
+    out = [torch.zeros(n, dtype=torch.bool, device="cuda"), torch.full((n,), -1, **i32), torch.full((n,), -1, **i32),
+           torch.zeros(total, **i32), torch.zeros(total, 3, device="cuda"), torch.zeros(total, 3, device="cuda"),
+           torch.zeros(total, device="cuda"), torch.zeros(total, device="cuda")]
+    extra = [torch.zeros(1, **i32), dev(listed), torch.tensor([len(listed)], **i32)]
+    L.call("ngp_march_rays_fallback", [dev(o), dev(d), dev(t0), dev(t1), dev(noise), dev(bits), ctr[0:1], ctr[1:2]]
+           + out + extra, L.MarchingDescriptor(n, total, 1024, K, G, bound, sp))
+    return host(ctr), [host(x) for x in out]
+
+
+@pytest.mark.parametrize("K,G,bound,sp,occ", [(1, 128, 1.0, 0.0, 0.3), (1, 64, 1.0, 0.0, 1.0),
+                                              (3, 64, 4.0, 1 / 256, 0.25)])
+def test_march_list_vs_oracle(K, G, bound, sp, occ):
+    """The list form of the training march (a warp per listed ray, 32-step lookahead): every listed
+    ray's count, validity and samples are the oracle march's bit for bit -- through a fully
+    occupied grid (runs of up to 1024 samples) and with cascades and a t-dependent step too; slots
+    are allocated after what the counters already hold; rays not listed are left alone."""
+    rng = np.random.default_rng(40 + K + G)
+    n = 3000
+    o, d, t0, t1 = make_rays(rng, n, bound)
+    noise = rng.uniform(size=n).astype(np.float32)
+    bits = random_bitfield(rng, K, G, occ)
+    total = 1 << 22
+    a = V.march_rays(total, 1024, K, G, bound, sp, o, d, t0, t1, noise, bits)
+    listed = rng.permutation(n)[:1000].astype(np.uint32)
+    ctr, (valid, ns, st, idcs, X, _, Ds, Z) = _march_list(o, d, t0, t1, noise, bits, listed, n, total, K, G, bound, sp)
+    unlisted = np.setdiff1d(np.arange(n), listed)
+    assert (ns[unlisted] == 0xFFFFFFFF).all() and (st[unlisted] == 0xFFFFFFFF).all()
+    assert np.array_equal(valid[listed], a[1][listed]) and np.array_equal(ns[listed], a[2][listed])
+    assert ctr[0] == 17 + a[2][listed].sum() and ctr[1] == 0
+    if occ == 1.0:
+        assert a[2][listed].max() > 256
+    for r in listed[a[2][listed] > 0]:
+        x0, y0, k = st[r], a[3][r], ns[r]
+        assert x0 >= 17 and (idcs[x0:x0 + k] == r).all()
+        assert np.array_equal(Z[x0:x0 + k], a[8][y0:y0 + k]) and np.array_equal(Ds[x0:x0 + k], a[7][y0:y0 + k])
+        assert np.array_equal(X[x0:x0 + k], a[5][y0:y0 + k])
+
+
+def test_march_list_over_budget():
+    """A budget of half the listed rays' demand: each listed ray is either valid with exactly the
+    oracle's samples inside the budget, or invalid with none; the counters keep
+    next - exceeded = the samples written."""
+    rng = np.random.default_rng(77)
+    n, K, G = 3000, 1, 128
+    o, d, t0, t1 = make_rays(rng, n, 1.0)
+    noise = rng.uniform(size=n).astype(np.float32)
+    bits = random_bitfield(rng, K, G, 0.3)
+    a = V.march_rays(1 << 22, 1024, K, G, 1.0, 0.0, o, d, t0, t1, noise, bits)
+    listed = rng.permutation(n)[:1500].astype(np.uint32)
+    total = int(a[2][listed].sum()) // 2
+    ctr, (valid, ns, st, _, _, _, _, Z) = _march_list(o, d, t0, t1, noise, bits, listed, n, total, K, G, 1.0, 0.0,
+                                                      start_at=0)
+    written = 0
+    for r in listed:
+        if valid[r] and ns[r] > 0:
+            assert ns[r] == a[2][r] and st[r] + ns[r] <= total
+            assert np.array_equal(Z[st[r]:st[r] + ns[r]], a[8][a[3][r]:a[3][r] + a[2][r]])
+            written += int(ns[r])
+        elif not valid[r]:   # over the budget (or, as in the oracle, an empty interval)
+            assert ns[r] == 0 and (a[2][r] > 0 or not a[1][r])
+    assert 0 < written <= total and int(ctr[0]) - int(ctr[1]) == written
