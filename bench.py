@@ -47,13 +47,13 @@ FALLBACK_FORMS = {"bf16x-proposal-fb"}
 # same results as the serial step, which fp32-march-serial keeps)
 PIPELINE_FORMS = {f for f, v in FORMS.items() if v[1] == "march" and not f.endswith("-serial")}
 UNIT = "rays/s"
-WORKLOAD = "config1: plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
+WORKLOAD = "plain NGP train step, 64 Gaussian blobs, 100 cams 800x800 fov40 r4, G=128 K=1 diag=1024, " \
            "L16 F2 T2^19 Nmin16 Nmax2048, MLP 32-64-16 / 32-64-64-3, R=S=2^18, Adam lr1e-2, fp32"
-WORKLOAD4 = "config4: NGP train step on 512 Gaussian blobs + 8 thin shells (r~U[0.1,0.4], thickness 0.01), 200 cams " \
+WORKLOAD4 = "NGP train step on 512 Gaussian blobs + 8 thin shells (r~U[0.1,0.4], thickness 0.01), 200 cams " \
             "800x800 fov40 r4, G=128 K=1 diag=1024, L16 F2 T2^19, R=S=2^20, Adam lr1e-2"
 # scene: blobs, shells, views, resolution, samples (= rays) per step, workload, metric
 SCENES = {"blobs64": (64, 0, 100, 800, 1 << 18, WORKLOAD, METRIC),
-          "config4": (512, 8, 200, 800, 1 << 20, WORKLOAD4,
+          "blobs512-shells8": (512, 8, 200, 800, 1 << 20, WORKLOAD4,
                       "train rays/s (plain FP32 hash-grid NeRF step, 512 blobs + 8 shells, 2^20 samples)")}
 
 
@@ -65,7 +65,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--pretrain", type=int, default=300, help="untimed training steps before warm-up")
     p.add_argument("--scene", default="blobs64", choices=sorted(SCENES),
-                   help="blobs64: 64 blobs, 100 views, 2^18 samples (the headline); config4: 512 blobs + 8 shells, "
+                   help="blobs64: 64 blobs, 100 views, 2^18 samples (the headline); blobs512-shells8: 512 blobs + 8 shells, "
                         "200 views, 2^20 samples")
     p.add_argument("--samples", type=int, default=None, help="samples (= rays) per step; default from the scene")
     p.add_argument("--views", type=int, default=None)

@@ -84,8 +84,9 @@ class BlobScene:
 
     @staticmethod
     def random(n_blobs: int = 64, n_shells: int = 0, seed: int = 0) -> "BlobScene":
-        """BASELINE configs 1-3: centres ~U[-0.5,0.5]^3, sigma ~U[0.03,0.15], peak ~U[10,200],
-        RGB ~U[0,1]; config 4 adds shells with radius ~U[0.1,0.4] and thickness 0.01."""
+        """Blobs with centres ~U[-0.5,0.5]^3, sigma ~U[0.03,0.15], peak ~U[10,200], RGB ~U[0,1]
+        (the 64-blob training scene), plus thin shells with radius ~U[0.1,0.4] and thickness 0.01
+        (the harder 512-blob + 8-shell scene)."""
         rng = np.random.default_rng(seed)
         b = np.zeros((n_blobs, 8), np.float32)
         b[:, 0:3] = rng.uniform(-0.5, 0.5, (n_blobs, 3))
@@ -135,8 +136,8 @@ class SceneData:
 def make_scene_data(n_blobs: int = 64, n_shells: int = 0, n_views: int = 100, width: int = 800, height: int = 800,
                     fov_deg: float = 40.0, radius: float = 4.0, n_steps: int = 4096, seed: int = 0,
                     device="cuda") -> SceneData:
-    """The synthetic training set of BASELINE config 1 (64 blobs, 100 views at 800x800, fov 40,
-    radius 4, 4096 quadrature steps) by default."""
+    """The synthetic training set; by default the 64-blob scene seen from 100 views at 800x800,
+    fov 40, radius 4, with targets from 4096-step quadrature."""
     scene = BlobScene.random(n_blobs, n_shells, seed)
     cam = PinholeCamera.from_fov(width, height, fov_deg)
     poses = hemisphere_poses(n_views, radius, np.random.default_rng(seed + 1))

@@ -128,7 +128,7 @@ def test_hashgrid_encoder_module_tv():
 
 
 def test_hashgrid_forward_large_bitexact():
-    """2^18 points at the training configuration (config 0): bit-exact against the oracle."""
+    """2^18 points at the training configuration (L=16, T=2^19, N_max=2048): bit-exact against the oracle."""
     from jaxngp_gb300.encoders import LevelTable, hashgrid_forward
     rng = np.random.default_rng(0)
     n = 1 << 18
