@@ -330,17 +330,38 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     g = np.random.default_rng(123 + rank)
     perms = torch.from_numpy(g.integers(0, n_pix, (args.steps, R)).astype(np.int32)).pin_memory()
     host_stats = torch.empty(args.steps, 4, dtype=torch.float32).pin_memory()
-    perm_dev = torch.empty(R, dtype=torch.int32, device="cuda")
+    # Step k+1's indices are copied on a copy stream while step k trains (still inside the timed
+    # region).  Three buffers: step j's indices are read while step j runs -- by the side stream
+    # that marches the next batch, in the pipelined step, which the main stream awaits in step
+    # j+1 -- so a buffer is overwritten only after the step following its reader.
+    perm_dev = [torch.empty(R, dtype=torch.int32, device="cuda") for _ in range(3)]
+    copied = [torch.cuda.Event() for _ in range(3)]
+    free = [torch.cuda.Event() for _ in range(3)]
+    copy_stream = torch.cuda.Stream()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
+
+    def upload(k):
+        b = k % 3
+        copy_stream.wait_event(free[b])
+        with torch.cuda.stream(copy_stream):
+            perm_dev[b].copy_(perms[k], non_blocking=True)
+        copied[b].record(copy_stream)
+
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
+    upload(0)
     for k in range(args.steps):
-        perm_dev.copy_(perms[k], non_blocking=True)
-        st = tr.step(perm_dev)
+        if k + 1 < args.steps:
+            upload(k + 1)
+        stream.wait_event(copied[k % 3])
+        st = tr.step(perm_dev[k % 3])
         host_stats[k].copy_(st, non_blocking=True)
+        if k >= 1:
+            free[(k - 1) % 3].record(stream)   # step k has awaited step k-1's readers
     e1.record(stream)
+    copy_stream.synchronize()
     torch.cuda.synchronize()
     ms_e2e = torch.tensor([e0.elapsed_time(e1)], device="cuda")
     rays_e2e = torch.tensor([float(host_stats[:, 1].double().sum())], device="cuda", dtype=torch.float64)
