@@ -370,11 +370,35 @@ struct Lookahead {
     bool live, occ;
 };
 
+// t after j occupied steps from t0 (j <= 31): the sequential additions t <- fl(t + calc_ds(t)).
+// With the constant step c of a bound <= 1 march, and t0 > 0 normal with ulp u, every addition
+// whose exact sum stays below the next power of two T adds the same multiple of u: the sum
+// (t/u + c/u) u rounds to (t/u + round(c/u)) u for integral t/u, unless c/u lies exactly half
+// way between integers (a round-to-even tie, whose result depends on t).  Then
+// t_j = t0 + j delta with delta = fl(t0 + c) - t0, each operation exact.  The fast form is taken
+// only when c/u is no tie and t0 + 32 (delta + c) < T (a margin over the largest sum,
+// t0 + 30 delta + c); otherwise the additions are made one by one.
+__device__ __forceinline__ float chain_t(const MarchParams &m, float t0, unsigned j) {
+    if (m.const_ds && t0 > 0.f) {
+        const std::uint32_t e = __float_as_uint(t0) & 0x7F800000u;
+        if (e > (24u << 23) && e < (253u << 23)) {
+            const float u = __uint_as_float(e - (23u << 23));      // ulp of t0 (a power of two)
+            const float top = __uint_as_float(e + (1u << 23));     // the next power of two
+            const float c = m.ds_const;
+            const float x = __fdiv_rn(c, u);                       // exact: u is a power of two
+            const float delta = (t0 + c) - t0;                     // round(c / u) u, exact
+            if (x - floorf(x) != 0.5f && t0 + 32.f * (delta + c) < top) return t0 + (float)j * delta;
+        }
+    }
+    float tj = t0;
+    for (unsigned i = 0; i < j; ++i) tj = tj + calc_ds(tj, m);
+    return tj;
+}
+
 __device__ __forceinline__ void look_ahead(const MarchParams &m, float t, unsigned lane, V3 o, V3 d, float t1,
                                            bool cond, const std::uint8_t *__restrict__ bits,
                                            const std::uint32_t *expand, Lookahead &a) {
-    float tj = t;
-    for (unsigned i = 0; i < lane; ++i) tj = tj + calc_ds(tj, m);
+    const float tj = chain_t(m, t, lane);
     a.t = tj;
     a.pos = at(o, d, tj);
     a.ds = calc_ds(tj, m);
@@ -510,8 +534,7 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_warp_kernel(
             for (std::uint32_t e = 0; e < trips; ++e) {
                 const unsigned k = trip_k[wib][e];
                 if (lane < k) {
-                    float tj = trip_t[wib][e];
-                    for (unsigned i = 0; i < lane; ++i) tj = tj + calc_ds(tj, m);
+                    const float tj = chain_t(m, trip_t[wib][e], lane);
                     const V3 pos = at(o, d, tj);
                     const std::uint32_t s = start + w + lane;
                     idcs[s] = r;
