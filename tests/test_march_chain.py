@@ -64,3 +64,4 @@ def test_closed_form_equals_the_sequential_additions():
         naive = np.array([f32(t0 + f32(j) * delta) for j in range(32)], np.float32)
         assert not np.array_equal(naive, sequential(t0, c))
         assert closed_form(t0, c) is None
+
