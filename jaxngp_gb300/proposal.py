@@ -180,6 +180,7 @@ class ProposalSampler:
         `distill(xyz, sigma)` is given, at points drawn in occupied cells."""
         S = xyzs.shape[0] if max_points is None else min(xyzs.shape[0], max_points)
         cnt = self.counts[2:3] if count is None else count
+        xyzs = xyzs[:S]   # the forward evaluates only the points the update regresses on
         self.loss.zero_()
         self.network(xyzs, self.enc_t[:S], self.x_t[:S], cnt, f16=self.f16)
         L.call("ngp_proposal_loss", [cnt, self.x_t[:S], drgbs, self.g_x[:S], self.loss[0:1]],
