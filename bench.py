@@ -394,9 +394,11 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     total = sum(sum(v) for v in per.values())
     breakdown = {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 5), "share": round(sum(v) / total, 4)}
                  for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1]))}
-    top = next(iter(breakdown))
-    bound_kind, units = algorithmic(top, R, int(samples_used), tr.table.n_params, cfg.G,
-                                    2 if table != "fp32" else 4, 2 if half_act else 4)
+    # the roofline's kernel: the most expensive entry point that has an algorithmic count
+    tb_, eb_ = (2 if table != "fp32" else 4), (2 if half_act else 4)
+    top = next((k for k in breakdown if algorithmic(k, R, int(samples_used), tr.table.n_params, cfg.G, tb_, eb_)[1] > 0),
+               next(iter(breakdown)))
+    bound_kind, units = algorithmic(top, R, int(samples_used), tr.table.n_params, cfg.G, tb_, eb_)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     avg_s = breakdown[top]["avg_ms"] / 1e3
