@@ -642,7 +642,9 @@ int ngp_proposal_judge_status(cudaStream_t stream, void **buffers, const char *o
 /* The training march (ngp_march_rays_train's probe form) over the rays fallback_rays[0 ..
  * *fallback_count), allocating sample ranges from next_sample_write_location /
  * number_of_exceeded_samples as they stand: the counters are not reset and the unwritten tail is
- * not zeroed, because ngp_proposal_sample_alloc allocates after it.
+ * not zeroed, because ngp_proposal_sample_alloc allocates after it.  A warp marches one listed ray
+ * (32-step lookahead); each ray's count, validity and samples are those ngp_march_rays_train gives
+ * it.
  * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call),
  * fallback_rays u32[n], fallback_count u32[1].  opaque: MarchingDescriptor (n_rays bounds the list). */
 void ngp_march_rays_fallback(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
