@@ -270,6 +270,20 @@ def setup_device(args):
     return world, rank, local
 
 
+def job_rate(ms: float, units: float, world: int, device) -> tuple:
+    """The whole job's rate over `world` replicas: (the slowest rank's ms, the units all ranks
+    processed, units per second).  All ranks call it together (all_reduce of MAX and SUM)."""
+    import torch
+    import torch.distributed as dist
+    ms_t = torch.tensor([ms], device=device, dtype=torch.float64)
+    units_t = torch.tensor([units], device=device, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(units_t)
+    ms_max, total = float(ms_t.item()), float(units_t.item())
+    return ms_max, total, total / (ms_max / 1e3)
+
+
 def run_ours(args, data, form: str, with_render: bool) -> dict:
     import numpy as np
     import torch
@@ -316,13 +330,7 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     a = acc.cpu().numpy()
     rays = float(a[1])
     samples_used = float(a[3]) / args.steps
-    ms_t = torch.tensor([ms], device="cuda")
-    rays_t = torch.tensor([rays], device="cuda", dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(rays_t)
-    ms_max = ms_t.item()
-    value = rays_t.item() / (ms_max / 1e3)
+    ms_max, _, value = job_rate(ms, rays, world, "cuda")
 
     # ---- end to end through the public API: host pixel indices in, metrics out, every step
     R = tr.R
@@ -363,12 +371,7 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     e1.record(stream)
     copy_stream.synchronize()
     torch.cuda.synchronize()
-    ms_e2e = torch.tensor([e0.elapsed_time(e1)], device="cuda")
-    rays_e2e = torch.tensor([float(host_stats[:, 1].double().sum())], device="cuda", dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(ms_e2e, op=dist.ReduceOp.MAX)
-        dist.all_reduce(rays_e2e)
-    e2e_value = rays_e2e.item() / (ms_e2e.item() / 1e3)
+    _, _, e2e_value = job_rate(e0.elapsed_time(e1), float(host_stats[:, 1].double().sum()), world, "cuda")
 
     # ---- per-entry-point device time (events around each call, on the launching stream)
     times = {}
