@@ -299,6 +299,8 @@ NGP_ENTRY(ngp_march_count) {
     (void)opaque;
     (void)opaque_len;
     NGP_CHECK_ARG(buffers != nullptr, "buffers is NULL");
+    NGP_CHECK_ARG(buffers[0] != nullptr && buffers[1] != nullptr && buffers[2] != nullptr,
+                  "ngp_march_count: the two counters and the result are required");
     march_count_kernel<<<1, 1, 0, stream>>>(CU32(0), CU32(1), U32(2));
     count_launches(1);
     return launch_status();

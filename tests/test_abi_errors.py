@@ -75,3 +75,24 @@ def test_legacy_signature_records_the_status(lib):
     assert lib.ngp_last_status() == OPAQUE_SIZE
     lib.ngp_last_status_message.restype = ctypes.c_char_p
     assert b"length" in lib.ngp_last_status_message()
+
+
+def test_every_entry_rejects_missing_buffers_and_bad_descriptors(lib):
+    """Every `_status` entry the header declares returns INVALID for a NULL buffer array; every
+    entry that takes a descriptor returns OPAQUE_SIZE for an opaque of the wrong length; the one
+    without a descriptor (ngp_march_count) returns INVALID for missing buffers -- all before any
+    CUDA call."""
+    import os
+    import re
+    header = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                               "ngp_gb300.h")).read()
+    names = re.findall(r"int (\w+)_status\(cudaStream_t stream, void \*\*buffers, const char \*opaque, "
+                       r"size_t opaque_len\);", header)
+    assert len(names) >= 50
+    nulls = (ctypes.c_void_p * 32)()
+    for n in names:
+        f = getattr(lib, n + "_status")
+        f.restype = ctypes.c_int
+        assert f(ctypes.c_void_p(0), None, ctypes.c_char_p(b"x"), ctypes.c_size_t(1)) == INVALID, n
+        want = INVALID if n == "ngp_march_count" else OPAQUE_SIZE
+        assert f(ctypes.c_void_p(0), nulls, ctypes.c_char_p(b"x"), ctypes.c_size_t(1)) == want, n
