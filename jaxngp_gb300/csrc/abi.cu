@@ -3,6 +3,9 @@
 // (deps/volume-rendering-jax/src/volrendjax/*/lowering.py): operands, then results.
 #include <atomic>
 #include <cstdio>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 #include "common.cuh"
 
@@ -141,15 +144,28 @@ void set_last_status(int status, const char *msg) {
 }
 
 int sm_count() {
-    static int cached[64] = {0};
+    static std::atomic<int> cached[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-    if (cached[dev] == 0) {
-        int n = 0;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
-        cached[dev] = n;
+    int v = cached[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cached[dev].store(v, std::memory_order_relaxed);
     }
-    return cached[dev];
+    return v;
+}
+
+int set_smem_limit(const void *kernel, std::size_t bytes) {
+    static std::mutex mu;
+    static std::set<std::tuple<int, const void *, std::size_t>> done;
+    int dev = 0;
+    NGP_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(dev, kernel, bytes);
+    if (done.count(key) != 0) return NGP_OK;
+    NGP_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    done.insert(key);
+    return NGP_OK;
 }
 
 }  // namespace ngp

@@ -27,6 +27,16 @@ inline unsigned grid_for(std::size_t n, unsigned block, unsigned per_sm) {
     return want == 0 ? 1u : (unsigned)want;
 }
 
+// Raises `kernel`'s dynamic shared-memory limit to `bytes` on the current device, once per
+// (device, kernel, size); thread-safe.  Returns a status.
+int set_smem_limit(const void *kernel, std::size_t bytes);
+
+#define NGP_SMEM_LIMIT(kernel, bytes)                                                      \
+    do {                                                                                   \
+        const int s_ = ::ngp::set_smem_limit(reinterpret_cast<const void *>(kernel), (bytes)); \
+        if (s_ != NGP_OK) return s_;                                                       \
+    } while (0)
+
 // Process-wide count of kernel launches made by this library (ngp_kernel_launches()).
 void count_launches(unsigned n);
 

@@ -596,15 +596,18 @@ constexpr std::size_t kDensSmem = (std::size_t)(kNW + 3 * kTile * kLd) * sizeof(
 // that cannot allocate device memory -- an XLA custom call bound through the legacy signature
 // receives only its operand and result buffers, and embedders that run with a fixed,
 // pre-reserved memory budget may not call cudaMalloc or any allocating library routine -- use
-// ngp_field_backward_noalloc instead, whose partials live in the array below.  Every CTA owns a
-// fixed span of kNoAllocSamplesPerPart samples, so the number of partials, and therefore the
-// batch, is bounded: at most kNoAllocMaxParts * kNoAllocSamplesPerPart = 524288 samples, and the
-// array is 256 * 9408 floats = 9.6 MB, held by every GPU that loads the library until the process
-// exits.  Each call overwrites every partial it later reads, so nothing has to be cleared between
-// calls; but all calls share the one array, so calls that overlap on the GPU (on different
-// streams) race on it and must be ordered by the caller.
-constexpr std::uint32_t kNoAllocSamplesPerPart = 2048;
+// ngp_field_backward_noalloc instead, whose partials live in the array below: room for
+// kNoAllocMaxParts partials (256 x 9408 floats = 9.6 MB), held by every GPU that loads the library
+// until the process exits.  The kernel strides its CTAs over the batch's tiles, so a call launches
+// min(SM count, kNoAllocMaxParts, tiles) CTAs and any batch would fit the array; the batch limit
+// NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES is a deliberate, published bound of this entry point (a
+// caller sizes its batches against it), not a property of the array.  Each call overwrites every
+// partial it later reads, so nothing has to be cleared between calls; but all calls share the one
+// array, so calls that overlap on the GPU (on different streams) race on it and must be ordered by
+// the caller.
 constexpr std::uint32_t kNoAllocMaxParts = 256;
+constexpr std::uint32_t kNoAllocMaxSamples = NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES;
+static_assert(kNoAllocMaxSamples == 524288u, "the published limit of ngp_field_backward_noalloc");
 __device__ __align__(256) float g_noalloc_partials[kNoAllocMaxParts * kNW];
 
 int mlp_partials_count() { return sm_count(); }
@@ -615,11 +618,7 @@ static bool aligned16(const void *p) { return ((std::uintptr_t)p & 15u) == 0; }
 int launch_mlp_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
                        const float *enc, const float *dirs, const float *weights, float *drgb) {
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp: enc, weights and drgb must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_forward_kernel<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_forward_kernel<kFwdThreads>), kFwdSmem);
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 2 ? tiles : (unsigned)sm_count() * 2;
@@ -630,11 +629,7 @@ int launch_mlp_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t
 
 int launch_mlp_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp: enc and weights must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_density_kernel<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDensSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_density_kernel<kFwdThreads>), kDensSmem);
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
@@ -650,11 +645,7 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
                         float *dL_dweights, float *partials, bool accumulate) {
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
                   "mlp: buffers must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel<kBwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_backward_kernel<kBwdThreads>), kBwdSmem);
     const unsigned grid = (unsigned)mlp_partials_count();
     mlp_backward_kernel<kBwdThreads><<<grid, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
     count_launches(1);
@@ -670,11 +661,7 @@ int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_
 int launch_prop_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
                         const float *weights, float *x) {
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "proposal mlp: enc and weights must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(prop_forward_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropFwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((prop_forward_kernel<256>), kPropFwdSmem);
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kTile - 1) / kTile;
     const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
@@ -691,11 +678,7 @@ int launch_prop_backward(cudaStream_t stream, std::uint32_t n, const std::uint32
                          bool accumulate) {
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_denc) && aligned16(partials),
                   "proposal mlp: buffers must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(prop_backward_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropBwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((prop_backward_kernel<256>), kPropBwdSmem);
     const unsigned grid = (unsigned)sm_count();
     prop_backward_kernel<256><<<grid, 256, kPropBwdSmem, stream>>>(n, count, enc, weights, dL_dx, dL_denc, partials);
     count_launches(1);
@@ -744,28 +727,26 @@ int launch_mlp_backward_noalloc(cudaStream_t stream, std::uint32_t n, const std:
                                 float *dL_dweights, bool accumulate) {
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc),
                   "mlp: buffers must be 16-byte aligned");
-    const std::uint64_t parts = ((std::uint64_t)n + kNoAllocSamplesPerPart - 1) / kNoAllocSamplesPerPart;
-    if (parts > kNoAllocMaxParts) {
+    if (n > kNoAllocMaxSamples) {
         set_last_status(NGP_ERR_CAPACITY,
-                        "ngp_field_backward_noalloc: n_samples exceeds 524288, the capacity of its static scratch; "
-                        "use ngp_field_backward with a caller-provided scratch buffer");
+                        "ngp_field_backward_noalloc: n_samples exceeds 524288, the published limit of this entry "
+                        "point; use ngp_field_backward with a caller-provided scratch buffer");
         return NGP_ERR_CAPACITY;
     }
     float *scratch = nullptr;
     int st = noalloc_scratch(&scratch);
     if (st != NGP_OK) return st;
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel<kBwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_backward_kernel<kBwdThreads>), kBwdSmem);
+    const std::uint32_t tiles = (n + kTile - 1) / kTile;
+    std::uint32_t parts = (std::uint32_t)sm_count();
+    if (parts > kNoAllocMaxParts) parts = kNoAllocMaxParts;
+    if (parts > tiles) parts = tiles;
     if (parts > 0) {
-        mlp_backward_kernel<kBwdThreads><<<(unsigned)parts, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
-                                                                             grad_scale, dL_denc, scratch);
+        mlp_backward_kernel<kBwdThreads><<<parts, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
+                                                                                   grad_scale, dL_denc, scratch);
         count_launches(1);
     }
-    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>((std::uint32_t)parts, scratch, dL_dweights,
-                                                                  accumulate ? 1 : 0);
+    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(parts, scratch, dL_dweights, accumulate ? 1 : 0);
     count_launches(1);
     if (count != nullptr && n > 0) {
         zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);

@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_forward_kernel(
         tc::bar_sync(1 + g, 128);
         if (*wg.fail) break;
     }
-    if (kTma && pending) tc::mbar_wait(&tbars[g], tphase, kWaitLimit);   // leave no copy in flight
+    if (kTma && pending && !tc::mbar_wait(&tbars[g], tphase, kWaitLimit)) *wg.fail = 1;   // leave no copy in flight
     if (*wg.fail && r == 0) atomicOr(&g_device_error, 1u);
     tc::fence_before();
     __syncthreads();
@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     }
 #pragma unroll
     for (int b = 0; b < 2; ++b)   // leave no copy in flight
-        if (kTma && pending[b]) tc::mbar_wait(&tbars[g][b], tphase[b], kWaitLimit);
+        if (kTma && pending[b] && !tc::mbar_wait(&tbars[g][b], tphase[b], kWaitLimit)) *wg.fail = 1;
     if (check != nullptr && !fits) atomicOr(&ls->overflow, 1u);
     if (r == 0) {
         tiles_done[g] = first ? 0 : 1;
@@ -836,18 +836,16 @@ int encode_enc_map(CUtensorMap *map, const void *enc, std::uint32_t n, bool *ok)
     *ok = false;
     std::memset(map, 0, sizeof(*map));
     if (n == 0 || n % 8 != 0) return NGP_OK;
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool looked = false;
-    if (!looked) {
-        looked = true;
+    // looked up once per process (a function-local static is initialised exactly once, thread-safely)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        else
-            (void)cudaGetLastError();
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        (void)cudaGetLastError();
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     if (fn == nullptr) return NGP_OK;
     const cuuint64_t dims[4] = {8, 8, 4, n / 8};
     const cuuint64_t strides[3] = {64, 16, 512};   // bytes: next row, next 8-column chunk, next 8-row group
@@ -866,13 +864,8 @@ int launch_tc_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t 
                       const float *dirs, const float *weights, float *drgb) {
     using In = typename EncRow<E, kHalf>::In;
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp (tensor cores): enc, weights and drgb must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_forward_kernel<E, kHalf, false, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
-        if (kHalf)
-            NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_forward_kernel<E, kHalf, kHalf, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_tc_forward_kernel<E, kHalf, false, kFwdWgs>), kFwdSmem);
+    if (kHalf) NGP_SMEM_LIMIT((mlp_tc_forward_kernel<E, kHalf, kHalf, kFwdWgs>), kFwdSmem);
     if (n == 0) return launch_status();
     CUtensorMap map;
     bool tma = false;
@@ -899,11 +892,7 @@ template <class E, bool kHalf>
 int launch_tc_density(cudaStream_t stream, std::uint32_t n, const void *enc, const float *weights, float *sigma) {
     using In = typename EncRow<E, kHalf>::In;
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp (tensor cores): enc and weights must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_density_kernel<E, kHalf, kFwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_tc_density_kernel<E, kHalf, kFwdWgs>), kFwdSmem);
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kRows - 1) / kRows;
     const unsigned want = (tiles + kFwdWgs - 1) / kFwdWgs;
@@ -921,13 +910,8 @@ int launch_tc_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t
     using In = typename EncRow<E, kHalf>::In;
     NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
                   "mlp (tensor cores): buffers must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_backward_kernel<E, kHalf, false, kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
-        if (kHalf)
-            NGP_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_backward_kernel<E, kHalf, kHalf, kBwdWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((mlp_tc_backward_kernel<E, kHalf, false, kBwdWgs>), kBwdSmem);
+    if (kHalf) NGP_SMEM_LIMIT((mlp_tc_backward_kernel<E, kHalf, kHalf, kBwdWgs>), kBwdSmem);
     CUtensorMap map;
     bool tma = false;
     if (kHalf) {
@@ -1007,11 +991,7 @@ int launch_mlp_tc_backward(cudaStream_t stream, std::uint32_t operand, bool half
 int launch_prop_f16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
                             const float *weights, float *x) {
     NGP_CHECK_ARG(aligned16(enc), "proposal mlp (fp16): encodings must be 16-byte aligned");
-    static bool attr = false;
-    if (!attr) {
-        NGP_CUDA_TRY(cudaFuncSetAttribute(prop_f16_forward_kernel<kPropWgs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropSmem));
-        attr = true;
-    }
+    NGP_SMEM_LIMIT((prop_f16_forward_kernel<kPropWgs>), kPropSmem);
     if (n == 0) return launch_status();
     const unsigned tiles = (n + kRows - 1) / kRows;
     const unsigned want = (tiles + kPropWgs - 1) / kPropWgs;

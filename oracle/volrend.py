@@ -37,9 +37,10 @@ def build_oracle() -> str:
     return _ORACLE_SO
 
 
-def build_ref(reference_root: str = "/root/reference") -> str:
-    """Compile the reference's kernels for the CPU into oracle/_ref/."""
-    subprocess.run([os.path.join(_HERE, "build_ref.sh"), reference_root], check=True,
+def build_ref(reference_root: str | None = None) -> str:
+    """Compile the reference's kernels for the CPU into oracle/_ref/ (oracle/build_ref.sh finds
+    the checkout itself unless `reference_root` is given, and builds nothing without one)."""
+    subprocess.run([os.path.join(_HERE, "build_ref.sh")] + ([reference_root] if reference_root else []), check=True,
                    stdout=subprocess.DEVNULL)
     return _REF_SO
 

@@ -12,15 +12,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
-REFERENCE_ROOT = os.environ.get("NGP_REFERENCE_ROOT", "/root/reference")
-
-
 @pytest.fixture(scope="session")
 def ref_backend():
-    """The reference's own kernels compiled for the CPU (only where the checkout exists)."""
+    """The reference's own kernels compiled for the CPU (only where the reference checkout exists:
+    oracle/build_ref.sh locates it and builds nothing without one)."""
     from oracle import volrend as V
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "deps", "volume-rendering-jax")):
-        pytest.skip("reference checkout not present")
     if not V.ref_available():
-        V.build_ref(REFERENCE_ROOT)
+        V.build_ref()
+    if not V.ref_available():
+        pytest.skip("reference checkout not present")
     return "ref"

@@ -2,7 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY; run in a container that holds the reference checkout:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py REFERENCE_ROOT [volrend] [field] [tv]
+
+(REFERENCE_ROOT may be left out when the environment variable NGP_REFERENCE_ROOT names it.)
 
 * ``volrend_*.npz``: inputs and outputs of the reference's ``marching.cu``, ``integrating.cu`` and
   ``packbits.cu`` kernels, compiled for the CPU by ``oracle/build_ref.sh`` and run thread by
@@ -187,8 +189,14 @@ def total_variation(ref_root: str):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    parts = sys.argv[2:] or ["volrend", "field", "tv"]
+    args = sys.argv[1:]
+    if args and args[0] not in ("volrend", "field", "tv"):
+        ref = args.pop(0)
+    elif os.environ.get("NGP_REFERENCE_ROOT"):
+        ref = os.environ["NGP_REFERENCE_ROOT"]
+    else:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [volrend] [field] [tv]  (or set NGP_REFERENCE_ROOT)")
+    parts = args or ["volrend", "field", "tv"]
     if "volrend" in parts:
         volrend(ref)
     if "field" in parts:
