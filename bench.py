@@ -14,7 +14,13 @@ back every step.  `forms` repeats the measurement for the BF16 tensor-core field
 learned proposal sampler with it (also with a 16-bit table copy and 16-bit encodings, BF16 or
 FP16 under a dynamic loss scale), each with the held-out PSNR of the trained field and 1080p
 inference FPS, and `learned_proposal_vs_plain` gives each proposal form's throughput ratio and
-PSNR difference against the plain step.
+PSNR difference against the plain step (with samples/s and rays-with-samples/s beside rays/s).
+The occupancy grid starts as the reference's does (mark_untrained_density_grid, then the learned
+refresh on its cadence) unless --occupancy-init analytic.  Three further blocks: `config0_encoder`
+(the hash-grid encoder alone at 2^18 points, both level tables, with its roofline and a NumPy
+baseline), `kernels_vs_reference` (the drop-in march/integrate/packbits kernels against the
+reference's own kernels built for sm_103a, same batch, same GPU) and `config4_learned_proposal`
+(512 blobs + 8 shells at 2^20 samples: the plain step against the learned proposal).
 `--impl reference` times the CPU restatement of the plain step (the reference has no CPU path for
 its volume-rendering ops) on the host's cores, on a bounded sample of the batch, extrapolated to
 the full batch.
@@ -75,7 +81,7 @@ def parse():
     p.add_argument("--equal-psnr-every", type=int, default=250)
     p.add_argument("--convergence-steps", type=int, default=0,
                    help="quality study instead of the bench line: train each form this many steps and print "
-                        "held-out PSNR (4 views) against device training time every --convergence-every steps")
+                        "held-out PSNR (--psnr-views views) against device training time every --convergence-every steps")
     p.add_argument("--convergence-every", type=int, default=2500)
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
@@ -85,6 +91,18 @@ def parse():
                         "algorithm, FP32 SIMT field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
                         "(learned proposal sampler + BF16 MLP); the x forms (bf16x-*, fp16x-*) also gather from a "
                         "16-bit copy of the table and keep the encodings in 16 bits (fp16 under a dynamic loss scale)")
+    p.add_argument("--occupancy-init", default="reference", choices=["reference", "analytic"],
+                   help="reference: the reference's initialisation (mark_untrained_density_grid, then the learned "
+                        "refresh on its cadence, utils/types.py:1149-1392) before the untimed pretraining; analytic: "
+                        "the grid starts from the scene's analytic density (a converged grid's stand-in)")
+    p.add_argument("--psnr-views", type=int, default=8, help="held-out views the PSNR is averaged over")
+    p.add_argument("--no-encoder-block", action="store_true", help="skip the standalone encoder block (config 0)")
+    p.add_argument("--no-kernels-vs-reference", action="store_true",
+                   help="skip timing the drop-in kernels against the reference's own sm_103a build")
+    p.add_argument("--config4-steps", type=int, default=60,
+                   help="timed steps per form of the 512-blob + 8-shell block at 2^20 samples (0: skip the block)")
+    p.add_argument("--config4-equal-psnr-steps", type=int, default=1000,
+                   help="steps of the plain step whose PSNR the proposal form must reach in the 512-blob block (0: skip)")
     p.add_argument("--render-frames", type=int, default=12, help="1920x1080 frames rendered on a 120-pose orbit")
     p.add_argument("--render-slots", type=int, default=1 << 18, help="rays in flight in the inference renderer")
     p.add_argument("--render-cap", type=int, default=8, help="march_steps_cap of the inference renderer")
@@ -250,6 +268,19 @@ def dtype_of(form: str) -> str:
     return "f32 (" + "; ".join(parts) + ")"
 
 
+def static_config(args, world: int) -> dict:
+    """The workload as configured (the same dict on both arms; measured batch statistics are
+    reported apart, under `batch`)."""
+    return {"workload": args.workload, "rays_per_step": args.samples, "sample_budget": args.samples,
+            "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,
+            "occupancy_init": ("reference: mark_untrained_density_grid, then the learned refresh on the reference's "
+                               "cadence" if args.occupancy_init == "reference" else
+                               "analytic scene density, then the learned refresh"),
+            "l2": f"no flush: the per-step working set (table 46.5 MB + {args.samples}-sample buffers "
+                  f"~{args.samples * 280 // 2**20} MB) is rewritten every step",
+            "parallelism": f"replicas x{world}", "form": args.forms.split(",")[0].strip()}
+
+
 FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # SMs x FP32 lanes x FMA x max clock
 
 
@@ -284,7 +315,7 @@ def job_rate(ms: float, units: float, world: int, device) -> tuple:
     return ms_max, total, total / (ms_max / 1e3)
 
 
-def run_ours(args, data, form: str, with_render: bool) -> dict:
+def run_ours(args, data, form: str, with_render: bool, on_trainer=None) -> dict:
     import numpy as np
     import torch
     import torch.distributed as dist
@@ -301,13 +332,17 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
                       table_precision=table, half_activations=half_act, proposal_fallback=form in FALLBACK_FORMS,
                       pipeline=form in PIPELINE_FORMS)
     tr = NGPTrainer(data, cfg)
-    tr.init_occupancy_analytic()
+    if args.occupancy_init == "analytic":
+        tr.init_occupancy_analytic()
     for _ in range(args.pretrain):
         tr.step()
     torch.cuda.synchronize()
+    # rays that carry samples, per step: the fused loss pass lists them (its scratch word 3)
+    heavy = tr.loss_scratch[3:4].view(torch.int32)
 
     # ---- timed region: device-resident inputs (pixel indices drawn on the device)
     acc = torch.zeros(4, dtype=torch.float64, device="cuda")
+    acc_heavy = torch.zeros(1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -321,6 +356,7 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
         ev0.record(stream)
         for _ in range(args.steps):
             acc += tr.step()
+            acc_heavy += heavy
         ev1.record(stream)
         torch.cuda.synchronize()
         if world > 1:
@@ -331,6 +367,8 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     rays = float(a[1])
     samples_used = float(a[3]) / args.steps
     ms_max, _, value = job_rate(ms, rays, world, "cuda")
+    _, _, samples_rate = job_rate(ms, float(a[3]), world, "cuda")
+    _, _, heavy_rate = job_rate(ms, float(acc_heavy.item()), world, "cuda")
 
     # ---- end to end through the public API: host pixel indices in, metrics out, every step
     R = tr.R
@@ -432,8 +470,8 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
     render_prop = render_fps(args, tr, stream, proposal=True) if (
         with_render and args.render_frames > 0 and tr.prop is not None) else None
     from jaxngp_gb300.trainer import HeldOut
-    held = HeldOut(data, n_views=2)
-    quality = {"psnr_heldout": round(held.psnr(tr), 3), "views": 2, "steps_trained": tr.step_count,
+    held = HeldOut(data, n_views=args.psnr_views)
+    quality = {"psnr_heldout": round(held.psnr(tr), 3), "views": args.psnr_views, "steps_trained": tr.step_count,
                "judge": "occupancy-grid inference renderer, white background, 4096-step quadrature ground truth"}
     if tr.prop is not None:
         from jaxngp_gb300.renderer import ProposalRenderer
@@ -445,16 +483,13 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
            "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(form),
            "data": f"synthetic (procedural scene: {args.n_blobs} blobs, {args.n_shells} shells; GT by 4096-step "
                    "quadrature; NeRF-synthetic not used)",
-           "config": {"workload": args.workload, "rays_per_step": R, "sample_budget": args.samples,
-                      "views": args.views, "resolution": args.res, "pretrain_steps": args.pretrain,
-                      "occupancy_init": "analytic scene density, then learned updates",
-                      "mean_samples_per_step": round(samples_used, 1),
-                      "mean_composited_samples_per_step": round(float(a[2]) / args.steps, 1),
-                      "mean_samples_per_valid_ray": round(samples_used / max(rays / args.steps, 1), 2),
-                      "valid_rays_per_step": round(rays / args.steps, 1),
-                      "l2": f"per-step working set (table 46.5 MB + {args.samples}-sample buffers "
-                            f"~{args.samples * 280 // 2**20} MB) is touched once per step; no flush",
-                      "parallelism": f"replicas x{world}"},
+           "config": static_config(args, world),
+           "batch": {"mean_samples_per_step": round(samples_used, 1),
+                     "mean_composited_samples_per_step": round(float(a[2]) / args.steps, 1),
+                     "mean_samples_per_valid_ray": round(samples_used / max(rays / args.steps, 1), 2),
+                     "valid_rays_per_step": round(rays / args.steps, 1),
+                     "rays_with_samples_per_step": round(float(acc_heavy.item()) / args.steps, 1),
+                     "samples_per_s": round(samples_rate, 1), "rays_with_samples_per_s": round(heavy_rate, 1)},
            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": 4 * R,
                    "d2h_bytes_per_step": 16},
            "gpu_launches": int(launches), "roofline": roof, "kernels": breakdown, "clocks": clk.summary()}
@@ -467,6 +502,187 @@ def run_ours(args, data, form: str, with_render: bool) -> dict:
         out["render_1080p"] = render
     if render_prop is not None:
         out["render_1080p_proposal"] = render_prop
+    if on_trainer is not None:
+        on_trainer(tr)
+    return out
+
+
+def _event_ms(fn, iters: int = 20, warmup: int = 3, flush=None) -> float:
+    """Median device time of fn() in ms (CUDA events on the current stream around each call;
+    `flush`, when given, is rewritten before every call to evict L2)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    evs = []
+    for _ in range(iters):
+        if flush is not None:
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    ts = sorted(a.elapsed_time(b) for a, b in evs)
+    return ts[len(ts) // 2]
+
+
+def encoder_block(args, cores: int) -> dict:
+    """Config 0: the hash-grid encoder alone -- forward and the table-gradient backward (zeroed
+    table gradient, then the scatter) on 2^18 points ~U[0,1)^3 (numpy PCG64 seed 0), a table
+    ~U(-1e-4, 1e-4) (seed 1) and upstream gradients ~N(0,1) [2^18, 32] (seed 2), L=16, F=2,
+    T=2^19, N_min=16, for both level tables the configuration names (b from N_max=2048: 1.38191;
+    and b=1.447).  L2 is flushed (a 256 MB write) before every timed launch.  Roofline: HBM, with
+    algorithmic bytes fwd = N(12 + 4LF) + 4FP and bwd = N(12 + 4LF) + 8FP (zero-fill and final
+    write of the gradient table).  cpu_baseline: the NumPy restatement of encoders.py:77-256
+    (oracle/hashgrid.py, one thread) on 2^14 of the points, extrapolated per point."""
+    import numpy as np
+    import torch
+    from jaxngp_gb300 import _lib as L
+    from jaxngp_gb300.encoders import LevelTable
+    N = 1 << 18
+    u = np.random.default_rng(0).uniform(size=(N, 3)).astype(np.float32)
+    pos = torch.from_numpy(u * np.float32(2) - np.float32(1)).cuda()   # bound 1: (pos + 1) / 2 = u
+    g = torch.from_numpy(np.random.default_rng(2).standard_normal((N, 32)).astype(np.float32)).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    traffic = json.load(open(tfile)) if os.path.exists(tfile) else {}
+    out = {"workload": "hash-grid encoder fwd + bwd, 2^18 points ~U[0,1)^3, L16 F2 T2^19 Nmin16, table ~U(-1e-4,1e-4), "
+                       "upstream ~N(0,1), seeds 0/1/2", "l2": "flushed before every timed launch (256 MB write)",
+           "tables": {}}
+    for tag, tab in (("b=1.38191 (Nmax 2048)", LevelTable(16, 1 << 19, 2, 16, 2048)),
+                     ("b=1.447", LevelTable(16, 1 << 19, 2, 16, 2048, 1.447))):
+        P = tab.n_params
+        lat = torch.from_numpy(np.random.default_rng(1).uniform(-1e-4, 1e-4, (P, 2)).astype(np.float32)).cuda()
+        enc = torch.empty(N, 32, device="cuda")
+        glat = torch.empty(P, 2, device="cuda")
+        d_f, d_b = tab.descriptor(N, 1.0), tab.descriptor(N, 1.0, accumulate=False)
+        ms_f = _event_ms(lambda: L.call("ngp_hashgrid_forward", [pos, lat, None, enc], d_f), flush=flush)
+        ms_b = _event_ms(lambda: L.call("ngp_hashgrid_backward", [pos, g, None, glat], d_b), flush=flush)
+        bf, bb = N * (12 + 4 * 32) + 4 * 2 * P, N * (12 + 4 * 32) + 8 * 2 * P
+        ent = {"n_params": P, "max_resolution": tab.levels()[1][-1]}
+        for name, ms, by in (("forward", ms_f, bf), ("backward", ms_b, bb)):
+            gbs = by / (ms / 1e3) / 1e9
+            tr_ = traffic.get(f"config0 {tag} {name}")
+            ent[name] = {"ms": round(ms, 4), "points_per_s": round(N / (ms / 1e3), 1),
+                         "roofline": {"bound": "hbm", "achieved": round(gbs, 2), "peak": hbm, "unit": "GB/s",
+                                      "frac": round(gbs / hbm, 4), "traffic": tr_, "algorithmic_bytes_per_launch": by,
+                                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks
+                                                     else "fallback 6800 GB/s"}}
+        out["tables"][tag] = ent
+        del lat, glat, enc
+    if not args.no_cpu_baseline:
+        from oracle import hashgrid as H
+        n = 1 << 14
+        tab = H.LevelTable(16, 1 << 19, 2, 16, 2048)
+        lat = np.random.default_rng(1).uniform(-1e-4, 1e-4, (tab.n_params, 2)).astype(np.float32)
+        p_np, g_np = pos[:n].cpu().numpy(), g[:n].cpu().numpy()
+        t = time.perf_counter()
+        H.encode(p_np, lat, 1.0, tab)
+        t_f = time.perf_counter() - t
+        t = time.perf_counter()
+        H.encode_backward(p_np, g_np, 1.0, tab, dtype=np.float32)
+        t_b = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": round(n / (t_f + t_b), 1), "unit": "points/s (forward + backward)",
+                               "cores": 1, "kind": "port",
+                               "sample": f"NumPy restatement of encoders.py:77-256 on {n} of the 2^18 points, table "
+                                         "b=1.38191; fwd {:.3f} s, bwd {:.3f} s".format(t_f, t_b)}
+    return out
+
+
+def kernels_vs_reference(tr) -> dict:
+    """The drop-in volume-rendering kernels against the reference's own kernels built unmodified
+    for sm_103a (baseline/_ref/libvolrend_ref_gpu.so), on the same GPU and the same config-1 batch:
+    the trainer's last batch of rays, its occupancy grid, and its marched samples and field values.
+    Median of 20 launches each (CUDA events), after 3 warm-up launches."""
+    import torch
+    from jaxngp_gb300 import _lib as L
+    try:
+        from baseline import volrend_gpu as RG
+    except ImportError:
+        RG = None
+    if RG is None or not RG.available():
+        return {"unavailable": "the reference's sm_103a build is absent (baseline/volrend_gpu.sh stages its sources "
+                               "where the reference checkout exists)"}
+    R, S = tr.R, tr.S
+    i32 = dict(dtype=torch.int32, device="cuda")
+    out = {"batch": f"{R} rays, {S}-sample budget, G={tr.cfg.G} K={tr.K}", "kernels": {}}
+
+    def march_bufs():
+        cnt = torch.zeros(2, **i32)
+        return [tr.rays_o, tr.rays_d, tr.t0, tr.t1, tr.noise, tr.bitfield, cnt[0:1], cnt[1:2],
+                torch.empty(R, dtype=torch.bool, device="cuda"), torch.empty(R, **i32), torch.empty(R, **i32),
+                torch.empty(S, **i32), torch.empty(S, 3, device="cuda"), torch.empty(S, 3, device="cuda"),
+                torch.empty(S, device="cuda"), torch.empty(S, device="cuda")]
+    dm = L.MarchingDescriptor(R, S, tr.cfg.diagonal_n_steps, tr.K, tr.cfg.G, tr.bound, tr.sp)
+    g = torch.randn(R, 4, device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))
+    fwd_out = lambda: [torch.zeros(1, **i32), torch.empty(R, 4, device="cuda"), torch.empty(R, device="cuda")]
+    bwd_out = lambda: [torch.empty(R, 3, device="cuda"), torch.empty(S, device="cuda"), torch.empty(S, 4, device="cuda")]
+    ins = [tr.startidx, tr.n_samples, tr.bgs, tr.dss, tr.z_vals, tr.drgbs]
+    rgbd, opac = torch.empty(R, 4, device="cuda"), torch.empty(R, device="cuda")
+    m = torch.zeros(1, **i32)
+    L.call("integrate_rays", ins + [m, rgbd, opac], L.IntegratingDescriptor(R, S))
+    n_cells = tr.density.numel()
+    thr = torch.full((n_cells,), float(tr.threshold.item()), device="cuda")
+    pk_out = lambda: [torch.empty(n_cells, dtype=torch.bool, device="cuda"),
+                      torch.empty(n_cells // 8, dtype=torch.uint8, device="cuda")]
+    cases = {
+        "march_rays": (march_bufs, dm, "marching.cu:101-268"),
+        "integrate_rays": (lambda: ins + fwd_out(), L.IntegratingDescriptor(R, S), "integrating.cu:24-104"),
+        "integrate_rays_backward": (lambda: ins + [rgbd, opac, g] + bwd_out(),
+                                    L.IntegratingBackwardDescriptor(R, S, tr.data.camera.near), "integrating.cu:106-240"),
+        "pack_density_into_bits": (lambda: [thr, tr.density] + pk_out(), L.PackbitsDescriptor(n_cells // 8),
+                                   "packbits.cu:9-34"),
+    }
+    for name, (mk, desc, where) in cases.items():
+        b_ours, b_ref = mk(), mk()
+        ms_o = _event_ms(lambda: L.call(name, b_ours, desc))
+        ms_r = _event_ms(lambda: RG.call(name, b_ref, desc))
+        out["kernels"][name] = {"ours_ms": round(ms_o, 4), "reference_ms": round(ms_r, 4),
+                                "speedup": round(ms_r / ms_o, 2), "reference_kernel": where}
+    return out
+
+
+def config4_block(args, cores: int) -> dict:
+    """The learned proposal on the harder scene, shortened for the default run: 512 Gaussian blobs +
+    8 thin shells, 200 views at 800x800, 2^20 samples (= rays) per step; the plain FP32 step
+    against the fastest proposal form: train rays/s, samples/s, held-out PSNR at equal steps, time
+    to the plain step's PSNR, and 1080p FPS."""
+    import copy
+    import torch
+    from jaxngp_gb300.scene import make_scene_data
+    sc = SCENES["blobs512-shells8"]
+    a4 = copy.copy(args)
+    a4.n_blobs, a4.n_shells, a4.views, a4.res, a4.samples = sc[0], sc[1], sc[2], sc[3], sc[4]
+    a4.workload, a4.metric = sc[5], sc[6]
+    a4.steps, a4.warmup, a4.pretrain = args.config4_steps, 5, 200
+    a4.render_frames = 4
+    a4.forms = "fp32-march,bf16x-proposal"
+    a4.equal_psnr_steps = args.config4_equal_psnr_steps
+    t = time.perf_counter()
+    data4 = make_scene_data(n_blobs=sc[0], n_shells=sc[1], n_views=sc[2], width=sc[3], height=sc[3], seed=0)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t
+    res = {f: run_ours(a4, data4, f, with_render=True) for f in ("fp32-march", "bf16x-proposal")}
+    a, b = res["fp32-march"], res["bf16x-proposal"]
+    keep = ("value", "ms_per_step", "e2e", "batch", "quality", "roofline", "gpu_launches", "clocks")
+    out = {"workload": sc[5], "config": static_config(a4, 1), "scene_generation_s": round(t_gen, 2),
+           "forms": {f: {k: r[k] for k in keep if k in r} | {
+               "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
+               "render_1080p_fps_proposal_renderer": (r.get("render_1080p_proposal") or {}).get("fps")}
+               for f, r in res.items()},
+           "bf16x-proposal_vs_plain": {
+               "train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
+               "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
+               "samples_per_s_ratio": round(b["batch"]["samples_per_s"] / a["batch"]["samples_per_s"], 3),
+               "delta_psnr_db_equal_steps": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3)}}
+    if a4.equal_psnr_steps > 0:
+        out["bf16x-proposal_vs_plain"]["at_equal_psnr"] = equal_psnr(a4, data4, "fp32-march", "bf16x-proposal")
+    del data4
+    torch.cuda.empty_cache()
     return out
 
 
@@ -570,14 +786,15 @@ def equal_psnr(args, data, plain: str, fast: str) -> dict:
     refreshes included."""
     import torch
     from jaxngp_gb300.trainer import HeldOut, NGPTrainer, TrainConfig
-    ev = HeldOut(data, n_views=2)
+    ev = HeldOut(data, n_views=args.psnr_views)
     curves, target = {}, None
     for f in (plain, fast):
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
                                           table_precision=table, half_activations=half_act,
                                           proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS))
-        tr.init_occupancy_analytic()
+        if args.occupancy_init == "analytic":
+            tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()
         t, pts = 0.0, []
         while tr.step_count < args.equal_psnr_steps:
@@ -607,14 +824,15 @@ def convergence(args, data, forms) -> dict:
     """Held-out PSNR against device training time for each form, from the same initial state."""
     import torch
     from jaxngp_gb300.trainer import HeldOut, NGPTrainer, TrainConfig
-    ev = HeldOut(data, n_views=4)
+    ev = HeldOut(data, n_views=args.psnr_views)
     out = {}
     for f in forms:
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
                                           table_precision=table, half_activations=half_act,
                                           proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS))
-        tr.init_occupancy_analytic()
+        if args.occupancy_init == "analytic":
+            tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()
         t, curve = 0.0, []
         with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
@@ -654,7 +872,7 @@ def main():
         out = {"metric": args.metric, "value": round(cb["value"], 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-               "config": {"workload": args.workload}, "cpu_baseline": cb,
+               "config": static_config(args, world), "cpu_baseline": cb,
                "e2e": {"value": round(cb["value"], 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                "wall_s": round(time.perf_counter() - t, 2)}
         print(json.dumps(out))
@@ -667,20 +885,25 @@ def main():
     if args.convergence_steps > 0:
         if rank == 0:
             print(json.dumps({"study": "convergence", "scene": args.scene, "steps": args.convergence_steps,
-                              "every": args.convergence_every, "psnr_views": 4,
+                              "every": args.convergence_every, "psnr_views": args.psnr_views,
+                              "occupancy_init": args.occupancy_init,
                               "judge": "occupancy-grid inference renderer, white background, 4096-step quadrature "
                                        "ground truth", "forms": convergence(args, data, forms)}))
         return 0
-    results = {}
-    for f in forms:
-        results[f] = run_ours(args, data, f, with_render=True)
+    results, extra = {}, {}
+    for i, f in enumerate(forms):
+        cb = None
+        if i == 0 and args.scene == "blobs64" and not args.no_kernels_vs_reference:
+            cb = lambda tr: extra.__setitem__("kernels_vs_reference", kernels_vs_reference(tr))
+        results[f] = run_ours(args, data, f, with_render=True, on_trainer=cb)
     head = results[forms[0]]
     out = dict(head)
-    out["config"] = dict(head["config"], form=forms[0])
+    out.update(extra)
+    out["config"] = dict(head["config"])
     if len(forms) > 1:
         out["forms"] = {f: {k: r[k] for k in ("value", "ms_per_step", "dtype", "e2e", "gpu_launches", "quality",
                                                "roofline", "clocks") if k in r} | {"proposal": r.get("proposal")} | {
-                            "valid_rays_per_step": r["config"]["valid_rays_per_step"],
+                            "batch": r["batch"],
                             "render_1080p_fps": (r.get("render_1080p") or {}).get("fps"),
                             "render_1080p_fps_proposal_renderer": (r.get("render_1080p_proposal") or {}).get("fps"),
                             "render_1080p_proposal_ms_by_entry": (r.get("render_1080p_proposal") or {}).get(
@@ -695,6 +918,9 @@ def main():
                     continue
                 cmp[f] = {"train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
                           "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
+                          "samples_per_s_ratio": round(b["batch"]["samples_per_s"] / a["batch"]["samples_per_s"], 3),
+                          "rays_with_samples_per_s_ratio": round(
+                              b["batch"]["rays_with_samples_per_s"] / max(a["batch"]["rays_with_samples_per_s"], 1), 3),
                           "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3)}
                 ra, rp = a.get("render_1080p"), b.get("render_1080p_proposal")
                 if ra and rp:
@@ -707,6 +933,13 @@ def main():
             if cmp and args.equal_psnr_steps > 0:
                 fastest = max(cmp, key=lambda f: results[f]["value"])
                 out["learned_proposal_vs_plain"]["at_equal_psnr"] = equal_psnr(args, data, "fp32-march", fastest)
+    if rank == 0 and not args.no_encoder_block:
+        out["config0_encoder"] = encoder_block(args, cores)
+    if args.scene == "blobs64" and args.config4_steps > 0:
+        del data
+        import torch
+        torch.cuda.empty_cache()
+        out["config4_learned_proposal"] = config4_block(args, cores)
     if rank == 0:
         if not args.no_cpu_baseline:
             from jaxngp_gb300.scene import BlobScene, PinholeCamera, hemisphere_poses, poses_to_transforms

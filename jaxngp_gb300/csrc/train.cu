@@ -351,7 +351,7 @@ __global__ void zero_tail4_kernel(std::uint32_t total, const std::uint32_t *__re
 
 // optax.adam (scale_by_adam, then scale by -lr) chained with add_decayed_weights, in that order
 // (app/nerf/_utils.py:45-77), then optax.apply_updates:
-//   m = b1 m + (1-b1) g;  v = b2 v + (1-b2) g^2;  mh = m / (1-b1^t);  vh = v / (1-b2^t)
+//   m = b1 m + (1-b1) g;  v = b2 v + (1-b2) (g g);  mh = m / (1-b1^t);  vh = v / (1-b2^t)
 //   update = -lr * mh / (sqrt(vh + eps_root) + eps) + wd * p;  p = p + update
 // (the decay term is added after the learning-rate scaling, exactly as the reference chains it).
 __global__ void __launch_bounds__(256) adam_kernel(NgpAdamDescriptor d, float bc1, float bc2,
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(256) adam_kernel(NgpAdamDescriptor d, float bc
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             ma[c] = d.beta1 * ma[c] + (1.f - d.beta1) * ga[c];
-            va[c] = d.beta2 * va[c] + (1.f - d.beta2) * ga[c] * ga[c];
+            va[c] = d.beta2 * va[c] + (1.f - d.beta2) * (ga[c] * ga[c]);
             const float mh = ma[c] / bc1, vh = va[c] / bc2;
             const float upd = -d.lr * (mh / (sqrtf(vh + d.eps_root) + d.eps)) + d.weight_decay * pa[c];
             pa[c] = pa[c] + upd;
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(256) adam_kernel(NgpAdamDescriptor d, float bc
     }
     for (std::size_t i = n4 * 4 + (std::size_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += stride) {
         float mm = d.beta1 * m[i] + (1.f - d.beta1) * g[i];
-        float vv = d.beta2 * v[i] + (1.f - d.beta2) * g[i] * g[i];
+        float vv = d.beta2 * v[i] + (1.f - d.beta2) * (g[i] * g[i]);
         const float upd = -d.lr * ((mm / bc1) / (sqrtf(vv / bc2 + d.eps_root) + d.eps)) + d.weight_decay * p[i];
         p[i] = p[i] + upd;
         m[i] = mm;
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(256) adam_mixed_kernel(NgpAdamDescriptor d, fl
         for (int c = 0; c < 4; ++c) {
             const float gc = ls != nullptr ? ga[c] * inv : ga[c];
             ma[c] = d.beta1 * ma[c] + (1.f - d.beta1) * gc;
-            va[c] = d.beta2 * va[c] + (1.f - d.beta2) * gc * gc;
+            va[c] = d.beta2 * va[c] + (1.f - d.beta2) * (gc * gc);
             const float mh = ma[c] / bc1, vh = va[c] / bc2;
             const float upd = -d.lr * (mh / (sqrtf(vh + d.eps_root) + d.eps)) + d.weight_decay * pa[c];
             pa[c] = pa[c] + upd;
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(256) adam_mixed_kernel(NgpAdamDescriptor d, fl
     for (std::size_t i = n4 * 4 + i0; i < d.n; i += stride) {
         const float gi = ls != nullptr ? g[i] * inv : g[i];
         float mm = d.beta1 * m[i] + (1.f - d.beta1) * gi;
-        float vv = d.beta2 * v[i] + (1.f - d.beta2) * gi * gi;
+        float vv = d.beta2 * v[i] + (1.f - d.beta2) * (gi * gi);
         const float upd = -d.lr * ((mm / bc1) / (sqrtf(vv / bc2 + d.eps_root) + d.eps)) + d.weight_decay * p[i];
         p[i] = p[i] + upd;
         m[i] = mm;

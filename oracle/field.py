@@ -199,6 +199,74 @@ def backward_bf16(dL_ddrgb: np.ndarray, cache, grad_scale: float = 1.0):
     return backward_half(dL_ddrgb, cache, grad_scale)
 
 
+def _fma32(a, b, c):
+    """round_f32(a * b + c) with one rounding: the product of two float32 values is exact in
+    float64, so only the sum rounds twice (float64, then float32), which differs from a fused
+    multiply-add only when the float64 sum lands exactly halfway between two float32 values."""
+    return (np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64)).astype(np.float32)
+
+
+def _fma_chain(A: np.ndarray, W: np.ndarray) -> np.ndarray:
+    """C[s][n] = sum_k A[s][k] W[k][n] as a float32 multiply-add chain in k order, from 0."""
+    A64, W64 = np.asarray(A, np.float32).astype(np.float64), np.asarray(W, np.float32).astype(np.float64)
+    acc = np.zeros((A64.shape[0], W64.shape[1]), np.float32)
+    for k in range(A64.shape[1]):
+        acc = (acc.astype(np.float64) + A64[:, k:k + 1] * W64[k][None, :]).astype(np.float32)
+    return acc
+
+
+def sh4_fma32(d: np.ndarray) -> np.ndarray:
+    """sh4 in float32 with each a*b + c formed as one multiply-add, as a GPU compiler that
+    contracts multiply-adds evaluates encoders.py:375-406's expressions."""
+    d = np.asarray(d, np.float32)
+    t = np.float32
+    x, y, z = d[:, 0], d[:, 1], d[:, 2]
+    xy, xz, yz = x * y, x * z, y * z
+    x2, y2, z2 = x * x, y * y, z * z
+    out = np.empty((d.shape[0], 16), np.float32)
+    out[:, 0] = t(0.28209479177387814)
+    out[:, 1] = t(-0.48860251190291987) * y
+    out[:, 2] = t(0.48860251190291987) * z
+    out[:, 3] = t(-0.48860251190291987) * x
+    out[:, 4] = t(1.0925484305920792) * xy
+    out[:, 5] = t(-1.0925484305920792) * yz
+    out[:, 6] = _fma32(t(0.94617469575755997), z2, -t(0.31539156525251999))
+    out[:, 7] = t(-1.0925484305920792) * xz
+    out[:, 8] = _fma32(t(0.54627421529603959), x2, -(t(0.54627421529603959) * y2))
+    out[:, 9] = (t(0.59004358992664352) * y) * _fma32(t(-3.0), x2, y2)
+    out[:, 10] = (t(2.8906114426405538) * xy) * z
+    out[:, 11] = (t(0.45704579946446572) * y) * _fma32(t(-5.0), z2, t(1.0))
+    out[:, 12] = (t(0.3731763325901154) * z) * _fma32(t(5.0), z2, t(-3.0))
+    out[:, 13] = (t(0.45704579946446572) * x) * _fma32(t(-5.0), z2, t(1.0))
+    out[:, 14] = (t(1.4453057213202769) * z) * (x2 - y2)
+    out[:, 15] = (t(0.59004358992664352) * x) * _fma32(t(3.0), y2, -x2)
+    return out
+
+
+def forward_fma32(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray]):
+    """The field forward in float32 evaluated the way the FP32 SIMT kernel (mlp.cu) does: every
+    layer output a multiply-add chain over its inputs in order, SH with contracted multiply-adds.
+    Its pre-activations, and so its ReLU decisions, are the kernel's; a backward in float64 on
+    this cache (`backward(..., cache)`) is the kernel's gradient without its rounding, which is how
+    gradient parity is judged on whole batches where some pre-activations sit within float32
+    rounding of a ReLU kink.  Returns (drgb [S,4] float32, cache)."""
+    w = {k: np.asarray(v, np.float32) for k, v in w.items()}
+    enc = np.asarray(enc, np.float32)
+    a1 = _fma_chain(enc, w["W0"])
+    h1 = np.maximum(a1, np.float32(0))
+    x = _fma_chain(h1, w["W1"])
+    c = np.concatenate([x, sh4_fma32(dirs)], axis=-1)
+    a2 = _fma_chain(c, w["W2"])
+    h2 = np.maximum(a2, np.float32(0))
+    a3 = _fma_chain(h2, w["W3"])
+    h3 = np.maximum(a3, np.float32(0))
+    a4 = _fma_chain(h3, w["W4"])
+    rgb = (np.float32(1) / (np.float32(1) + np.exp(-a4))).astype(np.float32)
+    drgb = np.concatenate([np.exp(x[:, :1]), rgb], axis=-1).astype(np.float32)
+    cache = dict(enc=enc, a1=a1, h1=h1, x=x, c=c, a2=a2, h2=h2, a3=a3, h3=h3, rgb=rgb)
+    return drgb, cache
+
+
 def density_only(enc: np.ndarray, w: Dict[str, np.ndarray], dtype=np.float32) -> np.ndarray:
     """NeRF.__call__ with dir=None (nerfs.py:71-72): sigma [S]."""
     w = {k: np.asarray(v, dtype) for k, v in w.items()}
