@@ -611,13 +611,37 @@ def kernels_vs_reference(tr) -> dict:
     i32 = dict(dtype=torch.int32, device="cuda")
     out = {"batch": f"{R} rays, {S}-sample budget, G={tr.cfg.G} K={tr.K}", "kernels": {}}
 
-    def march_bufs():
+    def march_bufs(S_):
         cnt = torch.zeros(2, **i32)
         return [tr.rays_o, tr.rays_d, tr.t0, tr.t1, tr.noise, tr.bitfield, cnt[0:1], cnt[1:2],
                 torch.empty(R, dtype=torch.bool, device="cuda"), torch.empty(R, **i32), torch.empty(R, **i32),
-                torch.empty(S, **i32), torch.empty(S, 3, device="cuda"), torch.empty(S, 3, device="cuda"),
-                torch.empty(S, device="cuda"), torch.empty(S, device="cuda")]
+                torch.empty(S_, **i32), torch.empty(S_, 3, device="cuda"), torch.empty(S_, 3, device="cuda"),
+                torch.empty(S_, device="cuda"), torch.empty(S_, device="cuda")]
+    # the march twice: with a budget no ray overflows (both kernels march every ray in full), and
+    # with the step's budget, where both drop the rays taken up after the buffer filled
+    # (marching.cu:135), so which rays fit depends on each kernel's schedule
+    for label, S_ in (("march_rays (no overflow)", 1 << 25), ("march_rays (step budget)", S)):
+        dm_ = L.MarchingDescriptor(R, S_, tr.cfg.diagonal_n_steps, tr.K, tr.cfg.G, tr.bound, tr.sp)
+        b_ours, b_ref = march_bufs(S_), march_bufs(S_)
+        ms_o = _event_ms(lambda: L.call("march_rays", b_ours, dm_))
+        ms_r = _event_ms(lambda: RG.call("march_rays", b_ref, dm_))
+        stats = {}
+        for who, bb in (("ours", b_ours), ("reference", b_ref)):
+            c = bb[6].item(), bb[7].item()
+            stats[who] = {"valid_rays": int(bb[8].sum().item()), "samples_written": int(c[0] - c[1]),
+                          "rays_with_samples": int((bb[9] > 0).sum().item())}
+        out["kernels"][label] = {"ours_ms": round(ms_o, 4), "reference_ms": round(ms_r, 4),
+                                 "speedup": round(ms_r / ms_o, 2), "reference_kernel": "marching.cu:101-268",
+                                 "budget": S_, "results": stats}
+        del b_ours, b_ref
+    # the training march on the same batch and grid: ray-order fitting, coarse-block skips
+    q = torch.zeros(1, **i32)
     dm = L.MarchingDescriptor(R, S, tr.cfg.diagonal_n_steps, tr.K, tr.cfg.G, tr.bound, tr.sp)
+    bt = march_bufs(S)
+    out["kernels"]["ngp_march_rays_train (step budget)"] = {
+        "ours_ms": round(_event_ms(lambda: L.call("ngp_march_rays_train", bt + [q, tr.coarse], dm)), 4),
+        "results": {"valid_rays": int(bt[8].sum().item()), "samples_written": int((bt[6] - bt[7]).item()),
+                    "rays_with_samples": int((bt[9] > 0).sum().item())}}
     g = torch.randn(R, 4, device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))
     fwd_out = lambda: [torch.zeros(1, **i32), torch.empty(R, 4, device="cuda"), torch.empty(R, device="cuda")]
     bwd_out = lambda: [torch.empty(R, 3, device="cuda"), torch.empty(S, device="cuda"), torch.empty(S, 4, device="cuda")]
@@ -630,7 +654,6 @@ def kernels_vs_reference(tr) -> dict:
     pk_out = lambda: [torch.empty(n_cells, dtype=torch.bool, device="cuda"),
                       torch.empty(n_cells // 8, dtype=torch.uint8, device="cuda")]
     cases = {
-        "march_rays": (march_bufs, dm, "marching.cu:101-268"),
         "integrate_rays": (lambda: ins + fwd_out(), L.IntegratingDescriptor(R, S), "integrating.cu:24-104"),
         "integrate_rays_backward": (lambda: ins + [rgbd, opac, g] + bwd_out(),
                                     L.IntegratingBackwardDescriptor(R, S, tr.data.camera.near), "integrating.cu:106-240"),

@@ -227,13 +227,16 @@ int integrate_rays_inference_status(cudaStream_t stream, void **buffers, const c
 
 /* march_rays for the training step: the same per-ray outputs as march_rays for every ray that
  * fits the sample budget, with every sample-less ray valid and every ray that does not fit
- * invalid; but a ray that meets its first occupied sample after the budget is full stops there
- * (it could only overflow) and is left out of both counters, whose difference -- the samples
- * written -- stays exact.  Rays are taken from a work queue in index order.  With coarse
- * occupancy blocks (ngp_proposal_coarse of the same bitfield; K = 1, G a multiple of 8), a ray
- * whose segment crosses no occupied block is finished at once -- valid, no samples -- instead of
- * being marched through empty cells: the same result, since every cell the march could look up
- * lies in such a block.
+ * invalid, where the rays fit in ray order -- ray r fits when the counts of rays 0..r end within
+ * the budget, at the start their sum gives -- so the result is deterministic and the rays that fit
+ * are a prefix of the batch (march_rays, like the reference, fits rays in the order in which they
+ * finish counting).  The counters hold the samples requested and those left out; their
+ * difference is the samples written.  The block sums of the allocation borrow the last
+ * ceil(n_rays / 1024) words of idcs (overwritten by the samples and the zeroed tail); with fewer
+ * sample slots than that the call allocates as march_rays does.  With coarse occupancy blocks
+ * (ngp_proposal_coarse of the same bitfield; K = 1, G a multiple of 8) the march crosses empty
+ * blocks in one step each and finishes a ray whose segment crosses no occupied block at once --
+ * valid, no samples -- with the same samples as the cell-by-cell march.
  * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call), then
  * coarse u8[(G/8)^3] or NULL.  opaque: MarchingDescriptor. */
 void ngp_march_rays_train(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);

@@ -131,6 +131,22 @@ __device__ __forceinline__ bool occupied_at(const MarchParams &m, V3 pos, float 
     return (__ldg(bits + (idx >> 3)) >> (idx & 7u)) & 1u;
 }
 
+// K == 1: the clamped integer cell of a position, packed (10 bits per axis), as occupied_at finds
+// it -- the same operations in the same order -- so two positions with equal keys read the same
+// occupancy bit.
+__device__ __forceinline__ std::uint32_t cell_key(const MarchParams &m, V3 g) {
+    const int Gi = (int)m.G - 1;
+    return (std::uint32_t)clampi((int)floorf(g.x), 0, Gi) | ((std::uint32_t)clampi((int)floorf(g.y), 0, Gi) << 10) |
+           ((std::uint32_t)clampi((int)floorf(g.z), 0, Gi) << 20);
+}
+__device__ __forceinline__ std::uint32_t cell_key_at(const MarchParams &m, V3 pos) {
+    const float Gf = (float)m.G;
+    const V3 g{((div_mb(pos.x, m.mb0, m.inv_mb0, m.pow2_0) + 1.0f) * 0.5f) * Gf,
+               ((div_mb(pos.y, m.mb0, m.inv_mb0, m.pow2_0) + 1.0f) * 0.5f) * Gf,
+               ((div_mb(pos.z, m.mb0, m.inv_mb0, m.pow2_0) + 1.0f) * 0.5f) * Gf};
+    return cell_key(m, g);
+}
+
 // The march's constant step c from t > 0 in closed form: while every exact sum t + k c stays
 // below t's next power of two `top` and c / ulp(t) is not an exact round-to-even tie, each rounded
 // addition adds the same delta = fl(t + c) - t (a multiple of the ulp), so t after k additions is
@@ -172,6 +188,60 @@ __device__ __forceinline__ float skip_empty(const MarchParams &m, float t, V3 g,
 
 __device__ __forceinline__ V3 at(V3 o, V3 d, float t) { return {o.x + t * d.x, o.y + t * d.y, o.z + t * d.z}; }
 
+// Skipping an empty coarse block in one step (K = 1, constant step, G a multiple of 8, with the
+// coarse grid of coarse.cuh: a block is marked when a cell of it, grown by one cell, is occupied).
+//
+// Inside an unmarked block every cell the march can look up is empty, even with its positions
+// rounded (the one-cell growth), so the reference (marching.cu:174-190) goes from landing to
+// landing -- each the first step of the chain t <- t + c at or past the exit of the landing's cell
+// -- until it lands past the block.  Its last landing inside lies in the cell through which the
+// ray leaves the block, whose exit plane is the block's face, so its next landing is the first
+// chain point at or past `next_t` computed from that landing with the block's face plane.  Here
+// the same formula is evaluated from the current point instead; the two values of next_t differ
+// only by rounding, bounded by eps (the roundings of pos = o + t d, of plane - pos, 1/d, the
+// product and the sum, for either point, with a factor of 4 to spare).  When no chain point lies
+// within eps of the block's exit every landing the reference could make there is the same chain
+// point, the one returned; otherwise (and when the chain would cross a power of two, where its
+// step changes) this returns false and the march takes the cell-by-cell path.
+__device__ __forceinline__ bool skip_block(const MarchParams &m, float t, V3 g, V3 pos, V3 o, V3 d, V3 inv_d,
+                                           const std::uint8_t *__restrict__ coarse, float &t_land) {
+    const int Gi = (int)m.G - 1, Gc = (int)(m.G >> 3);
+    const int bx = clampi((int)floorf(g.x), 0, Gi) >> 3, by = clampi((int)floorf(g.y), 0, Gi) >> 3,
+              bz = clampi((int)floorf(g.z), 0, Gi) >> 3;
+    if (coarse[bx + by * Gc + bz * Gc * Gc] != 0) return false;
+    if (d.x == 0.f || d.y == 0.f || d.z == 0.f) return false;
+    const float u = 5.9604645e-8f;   // 2^-24
+    const int b3[3] = {bx, by, bz};
+    const float p3[3] = {pos.x, pos.y, pos.z}, o3[3] = {o.x, o.y, o.z}, d3[3] = {d.x, d.y, d.z},
+                id3[3] = {inv_d.x, inv_d.y, inv_d.z};
+    float dmin = __int_as_float(0x7f800000), err = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int nb = d3[a] > 0.f ? (b3[a] + 1) * 8 : b3[a] * 8;
+        const float plane = (((float)nb * m.inv_G - 0.5f) * 2.0f) * m.mb0;
+        const float dist = (plane - p3[a]) * id3[a];
+        // rounding bound of t + dist from any point of the block's last cell on this ray (|t| <= t + dist)
+        const float e = u * (fabsf(id3[a]) * (fabsf(o3[a]) + 2.0f * fabsf((t + fabsf(dist)) * d3[a]) + fabsf(plane)) +
+                             4.0f * fabsf(dist) + 2.0f * (fabsf(t) + fabsf(dist)));
+        dmin = fminf(dmin, dist);
+        err = fmaxf(err, e);   // every axis: covers the axis that decides the minimum, ties included
+    }
+    if (!(err < 1e30f)) return false;
+    const float eps = 4.0f * err;
+    const float tx = t + fmaxf(0.0f, dmin);
+    float delta, top;
+    if (!chain_step(t, m.ds_const, delta, top)) return false;
+    // the first chain point at or past tx + eps: j steps of delta from t (exact below `top`)
+    float jf = ceilf((tx + eps - t) / delta);
+    if (!(jf >= 2.0f && jf < 1.0e6f)) return false;
+    for (int k = 0; k < 4 && t + (jf - 1.0f) * delta >= tx + eps; ++k) jf -= 1.0f;
+    for (int k = 0; k < 4 && t + jf * delta < tx + eps; ++k) jf += 1.0f;
+    const float tl = t + jf * delta, tp = t + (jf - 1.0f) * delta;
+    if (!(tl >= tx + eps) || !(tp < tx - eps) || !(tl < top) || jf < 2.0f) return false;
+    t_land = tl;
+    return true;
+}
+
 // ------------------------------------------------------------------------------- march_rays
 
 // True when the ray cannot take a sample: every cell the march could look up on [t0, t1) lies in
@@ -201,26 +271,36 @@ enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
 // Marches rays with lane refill: every lane of a warp carries one ray and advances it by one
 // march iteration per trip of the loop; a lane whose ray is finished takes the next ray at once,
 // so a warp keeps all 32 lanes busy until the rays run out (one thread per ray, as in the
-// reference, leaves most lanes of a warp idle behind the warp's longest ray).
+// reference, leaves most lanes of a warp idle behind the warp's longest ray).  With one cascade,
+// an occupied sample's cell is followed through in a tight loop (below), and with a coarse grid
+// an empty coarse block is crossed in one step (skip_block).
 //
 // Rays come from a global queue counter when `queue` is given, else from a fixed interleaving:
 // warp w takes 32-ray chunks w, w + n_warps, w + 2 n_warps, ...
 //
 // Per ray the arithmetic and the two passes (count, then write) are the reference's
-// (marching.cu:162-192, :224-267), except that the write pass resumes at the t of the first
-// occupied sample the count pass met instead of re-marching the empty space before it: the march
-// state is t alone, so the samples from there on are the same.  Slots are allocated once per trip for all lanes that finished
-// counting in it (one atomic).  A ray with no sample is valid (marching.cu:196-199); a ray that
-// does not fit the budget is not (:206-209).  The reference also drops a ray whose thread starts
-// after the buffer filled (:135), which only happens when its grid does not fit on the GPU at
-// once; here every ray is treated as started before that.
+// (marching.cu:162-192, :224-267).  A ray with no sample is valid (marching.cu:196-199); a ray
+// that does not fit the budget is not (:206-209).  Three modes:
 //
-// kProbe (training): a ray that finds the sample budget already full while counting (checked at
-// its first occupied sample and every 16 after) stops there -- it can only overflow -- and adds
-// nothing to the counters, so
-// next_sample_write_location - number_of_exceeded_samples (the samples written) is exact while
-// the two counters themselves leave out such rays.
-template <bool kProbe>
+// kMarchAlloc (the drop-in march_rays): the write pass resumes at the t of the first occupied
+// sample the count pass met instead of re-marching the empty space before it (the march state is
+// t alone, so the samples from there on are the same).  Slots are allocated once per trip for all
+// lanes that finished counting in it (one atomic), so which rays fit an overflowing budget follows
+// the order in which they finish counting, as in the reference; and, as in the reference (:135),
+// a ray that a lane takes up after the buffer filled is dropped (invalid) without being marched --
+// a legal schedule of the reference's kernel, whose result depends on when each ray's thread
+// starts.
+//
+// kMarchCount, kMarchWrite (the training march, launch_march_rays with `ordered`): rays fit the
+// budget in ray order -- the schedule in which every ray's thread starts at once and the rays
+// finish counting in index order.  The count pass stores every ray's count and validity; a scan
+// over the rays in index order gives each ray its start and decides which fit; the write pass then
+// marches the rays that fit from their start and writes their samples.  The rays that fit are a
+// prefix of the batch (its pixel indices are drawn at random, so an unbiased sample of the rays
+// that carry samples) whatever the order of the counting, and the result is deterministic.
+enum : int { kMarchAlloc = 0, kMarchCount = 1, kMarchWrite = 2 };
+
+template <int kMode>
 __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_kernel(
     std::uint32_t n_rays, std::uint32_t total_samples, MarchParams m,
     const float *__restrict__ rays_o, const float *__restrict__ rays_d,
@@ -239,6 +319,7 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
     const std::uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const std::uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
     const float n_cap = (float)m.dns * m.bound;
+    const bool block_skip = coarse != nullptr && m.K == 1 && m.const_ds && (m.G & 7u) == 0u;
 
     int phase = kIdle;
     std::uint32_t ray = 0, n = 0, k = 0, start = 0, it = 0;
@@ -264,7 +345,29 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
             if (phase == kIdle) {
                 const std::uint32_t q = base + (unsigned)__popc(idle & lt_mask);
                 const std::uint32_t qi = queue != nullptr ? q : (((q >> 5) * n_warps + warp) << 5) + (q & 31u);
-                if (qi < n_rays) {
+                if (kMode == kMarchAlloc && qi < n_rays && *((volatile std::uint32_t *)next_loc) >= total_samples) {
+                    // marching.cu:135: a ray that starts after the sample buffer filled is dropped
+                    ray_is_valid[qi] = false;
+                    rays_n_samples[qi] = 0;
+                    rays_startidx[qi] = 0;
+                } else if (kMode == kMarchWrite && qi < n_rays) {
+                    // the write pass of a ray that fits (its count and start come from the scan)
+                    const std::uint32_t r = qi;
+                    n = rays_n_samples[r];
+                    if (n > 0u) {
+                        ray = r;
+                        start = rays_startidx[r];
+                        o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
+                        d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
+                        inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                        const float t0 = t_starts[r];
+                        t1 = t_ends[r];
+                        t = t0 + calc_ds(t0, m) * noises[r];
+                        k = 0;
+                        it = 0;
+                        phase = kWrite;
+                    }
+                } else if (qi < n_rays) {
                     const std::uint32_t r = qi;
                     ray = r;
                     o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
@@ -298,46 +401,74 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
         const bool active = phase != kIdle;
         if (__ballot_sync(0xffffffffu, active) == 0u) break;
 
-        // ---- one march iteration (marching.cu:166-191 / :231-266)
-        bool first_hit = false;
+        // ---- one march iteration (marching.cu:166-191 / :231-266).  With one cascade, an
+        // occupied sample's cell is followed through: the next steps are taken in a tight loop for
+        // as long as their positions stay in that cell, whose bit they share (positions move
+        // monotonically along the ray, so it is never re-entered) -- the reference's additions and
+        // positions, without a lookup or a trip of the refill machinery per sample.
         if (active) {
             const V3 pos = at(o, d, t);
             const float ds = calc_ds(t, m);
             V3 g;
             float mb;
             if (occupied_at(m, pos, ds, bits, g, mb, expand)) {
+                const std::uint32_t key = m.K == 1 ? cell_key(m, g) : 0u;
                 if (phase == kWrite) {
-                    const std::uint32_t s = start + k;
-                    idcs[s] = ray;
-                    xyzs[(std::size_t)s * 3 + 0] = pos.x;
-                    xyzs[(std::size_t)s * 3 + 1] = pos.y;
-                    xyzs[(std::size_t)s * 3 + 2] = pos.z;
-                    dirs[(std::size_t)s * 3 + 0] = d.x;
-                    dirs[(std::size_t)s * 3 + 1] = d.y;
-                    dirs[(std::size_t)s * 3 + 2] = d.z;
-                    dss[s] = ds;
-                    z_vals[s] = t;
-                    ++k;
+                    auto put = [&](V3 p, float dsj, float tj) {
+                        const std::uint32_t s = start + k;
+                        idcs[s] = ray;
+                        xyzs[(std::size_t)s * 3 + 0] = p.x;
+                        xyzs[(std::size_t)s * 3 + 1] = p.y;
+                        xyzs[(std::size_t)s * 3 + 2] = p.z;
+                        dirs[(std::size_t)s * 3 + 0] = d.x;
+                        dirs[(std::size_t)s * 3 + 1] = d.y;
+                        dirs[(std::size_t)s * 3 + 2] = d.z;
+                        dss[s] = dsj;
+                        z_vals[s] = tj;
+                        ++k;
+                    };
+                    put(pos, ds, t);
+                    t = t + ds;
+                    if (m.K == 1) {
+                        while (k < n && t < t1 && it < kMaxMarchIters) {   // marching.cu:231
+                            const V3 p2 = at(o, d, t);
+                            if (cell_key_at(m, p2) != key) break;
+                            const float ds2 = calc_ds(t, m);
+                            put(p2, ds2, t);
+                            t = t + ds2;
+                            ++it;
+                        }
+                    }
                 } else {
                     if (n == 0) t_hit = t;
                     ++n;
-                    first_hit = (n & 15u) == 1u;  // at the first occupied sample and every 16 after
+                    t = t + ds;
+                    if (m.K == 1) {
+                        while ((float)n < n_cap && t < t1 && it < kMaxMarchIters) {   // marching.cu:164
+                            if (cell_key_at(m, at(o, d, t)) != key) break;
+                            ++n;
+                            t = t + calc_ds(t, m);
+                            ++it;
+                        }
+                    }
                 }
-                t = t + ds;
             } else {
-                t = skip_empty(m, t, g, mb, pos, d, inv_d);
+                float tb;
+                if (block_skip && skip_block(m, t, g, pos, o, d, inv_d, coarse, tb))
+                    t = tb;
+                else
+                    t = skip_empty(m, t, g, mb, pos, d, inv_d);
             }
             ++it;
         }
 
         // ---- phase changes
         bool count_done = phase == kCount && !((float)n < n_cap && t < t1 && it < kMaxMarchIters);
-        if (kProbe && phase == kCount && first_hit && !count_done &&
-            *((volatile std::uint32_t *)next_loc) >= total_samples) {
-            ray_is_valid[ray] = false;  // can only overflow: decided without finishing the count
-            rays_n_samples[ray] = 0;
-            rays_startidx[ray] = 0;
+        if (kMode == kMarchCount && count_done) {   // the count and the ray's validity so far; the scan decides
+            ray_is_valid[ray] = true;
+            rays_n_samples[ray] = n;
             phase = kIdle;
+            count_done = false;
         }
         if (count_done && n == 0) {  // marching.cu:196-199
             ray_is_valid[ray] = true;
@@ -348,7 +479,7 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
         }
         const bool want = count_done;  // n > 0
         const unsigned wm = __ballot_sync(0xffffffffu, want);
-        if (wm != 0u) {
+        if (kMode == kMarchAlloc && wm != 0u) {
             const std::uint32_t incl = warp_inclusive_scan(want ? n : 0u);
             const std::uint32_t total_w = __shfl_sync(0xffffffffu, incl, 31);
             const int leader = __ffs(wm) - 1;
@@ -375,6 +506,74 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
             if (lane == 0 && over > 0) atomicAdd(n_exceeded, over);
         }
         if (phase == kWrite && !(k < n && t < t1 && it < kMaxMarchIters)) phase = kIdle;
+    }
+}
+
+// Ray-order allocation of the training march (between its count and write passes).  Rays are
+// taken in blocks of kScanRays; block b sums the counts of rays [b kScanRays, (b+1) kScanRays).
+constexpr int kScanRays = 1024;
+
+__global__ void __launch_bounds__(kScanRays) ray_block_sums_kernel(std::uint32_t n_rays,
+                                                                   const std::uint32_t *__restrict__ counts,
+                                                                   std::uint32_t *__restrict__ sums) {
+    __shared__ std::uint32_t ws[kScanRays / 32];
+    const std::uint32_t r = blockIdx.x * kScanRays + threadIdx.x;
+    const std::uint32_t v = warp_sum(r < n_rays ? counts[r] : 0u);
+    if (lane_id() == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const std::uint32_t x = warp_sum(ws[threadIdx.x]);
+        if (threadIdx.x == 0) sums[blockIdx.x] = x;
+    }
+}
+
+// Ray r's first sample slot is the sum of the counts of the rays before it; it fits when its
+// samples end within the budget (marching.cu:206-209).  A ray with samples that does not fit is
+// invalid, with no samples; the counters receive the samples requested and those left out (their
+// difference is the samples written, as march_rays' counters give it).
+__global__ void __launch_bounds__(kScanRays) ray_scan_fit_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, const std::uint32_t *__restrict__ sums,
+    bool *__restrict__ valid, std::uint32_t *__restrict__ counts, std::uint32_t *__restrict__ startidx,
+    std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded) {
+    __shared__ unsigned long long s_prefix;
+    __shared__ std::uint32_t ws[kScanRays / 32], wt[kScanRays / 32], wo[kScanRays / 32];
+    if (threadIdx.x < 32) {
+        unsigned long long a = 0;
+        for (std::uint32_t b = threadIdx.x; b < blockIdx.x; b += 32) a += sums[b];
+        a = warp_sum(a);
+        if (threadIdx.x == 0) s_prefix = a;
+    }
+    const std::uint32_t r = blockIdx.x * kScanRays + threadIdx.x;
+    const std::uint32_t n = r < n_rays ? counts[r] : 0u;
+    const std::uint32_t incl = warp_inclusive_scan(n);
+    if (lane_id() == 31) ws[threadIdx.x >> 5] = incl;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const std::uint32_t x = ws[threadIdx.x];
+        ws[threadIdx.x] = warp_inclusive_scan(x) - x;
+    }
+    __syncthreads();
+    const unsigned long long start = s_prefix + ws[threadIdx.x >> 5] + (incl - n);
+    const bool fits = start + n <= (unsigned long long)total_samples;
+    if (r < n_rays) {
+        if (n > 0u) {
+            valid[r] = fits;
+            counts[r] = fits ? n : 0u;
+        }
+        startidx[r] = (n > 0u && fits) ? (std::uint32_t)start : 0u;
+    }
+    const std::uint32_t tot = warp_sum(n), over = warp_sum((n > 0u && !fits) ? n : 0u);
+    if (lane_id() == 0) {
+        wt[threadIdx.x >> 5] = tot;
+        wo[threadIdx.x >> 5] = over;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const std::uint32_t a = warp_sum(wt[threadIdx.x]), o = warp_sum(wo[threadIdx.x]);
+        if (threadIdx.x == 0) {
+            if (a > 0u) atomicAdd(next_loc, a);
+            if (o > 0u) atomicAdd(n_exceeded, o);
+        }
     }
 }
 
@@ -900,7 +1099,7 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
                       const float *noises, const std::uint8_t *bits, std::uint32_t *next_loc,
                       std::uint32_t *n_exceeded, bool *ray_is_valid, std::uint32_t *rays_n_samples,
                       std::uint32_t *rays_startidx, std::uint32_t *idcs, float *xyzs, float *dirs,
-                      float *dss, float *z_vals, std::uint32_t *queue, bool probe, const std::uint8_t *coarse) {
+                      float *dss, float *z_vals, std::uint32_t *queue, bool ordered, const std::uint8_t *coarse) {
     NGP_CHECK_ARG(d.K > 0 && d.G > 0 && d.diagonal_n_steps > 0, "march_rays: K, G and diagonal_n_steps must be positive");
     NGP_CHECK_ARG(d.G <= 1024 && (d.G & (d.G - 1)) == 0, "march_rays: G must be a power of two <= 1024 (Morton codes of other sizes exceed G^3)");
     NGP_CHECK_ARG(d.K <= 16, "march_rays: at most 16 cascades");
@@ -914,16 +1113,29 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
         const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
         const unsigned cap = (unsigned)sm_count() * (unsigned)g_march_blocks_per_sm.load(std::memory_order_relaxed);
         const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
-        if (probe) {
-            march_rays_kernel<true><<<grid, kMarchBlock, 0, stream>>>(
+        const std::uint32_t nb = (d.n_rays + kScanRays - 1) / kScanRays;
+        if (ordered && queue != nullptr && nb <= d.total_samples) {
+            // count every ray; allocate in ray order (the block sums borrow the sample-index
+            // buffer's last nb words, which the write pass and the tail zeroing overwrite later);
+            // write the rays that fit
+            march_rays_kernel<kMarchCount><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
                 n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+            std::uint32_t *sums = idcs + (d.total_samples - nb);
+            ray_block_sums_kernel<<<nb, kScanRays, 0, stream>>>(d.n_rays, rays_n_samples, sums);
+            ray_scan_fit_kernel<<<nb, kScanRays, 0, stream>>>(d.n_rays, d.total_samples, sums, ray_is_valid,
+                                                               rays_n_samples, rays_startidx, next_loc, n_exceeded);
+            NGP_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(std::uint32_t), stream));
+            march_rays_kernel<kMarchWrite><<<grid, kMarchBlock, 0, stream>>>(
+                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
+                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+            count_launches(4);
         } else {
-            march_rays_kernel<false><<<grid, kMarchBlock, 0, stream>>>(
+            march_rays_kernel<kMarchAlloc><<<grid, kMarchBlock, 0, stream>>>(
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
                 n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+            count_launches(1);
         }
-        count_launches(1);
     }
     if (d.total_samples > 0) {
         zero_sample_tail_kernel<<<grid_for(d.total_samples, 256, 8), 256, 0, stream>>>(

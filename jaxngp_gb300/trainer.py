@@ -64,8 +64,8 @@ class TrainConfig:
     pipeline: bool = False             # march sampler: march the next step's batch on a second stream while
                                        # this step's field, integrator, backwards and Adam run (same results)
     pipeline_march_blocks: int = 10    # CTAs per SM of that march (measured: 8-10 best; fewer starve it)
-    march_coarse_skip: bool = False    # march: finish rays that cross no occupied coarse block at once
-                                       # (exact; pays off on sparse grids, costs ~3% on dense ones)
+    march_coarse_skip: bool = True     # march: skip empty coarse blocks (8^3 cells) in one step and finish
+                                       # rays that cross no occupied block at once (exact: the same samples)
     tv_scale: float = 0.0              # the encoder's total-variation term (encoders.py:236-254), added to
                                        # the loss and its gradient to the table's (0: off, the reference's default)
 

