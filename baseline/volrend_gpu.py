@@ -1,5 +1,6 @@
 """ctypes loader of baseline/_ref/libvolrend_ref_gpu.so: the reference's own volume-rendering
-kernels (deps/volume-rendering-jax/lib/impl/*.cu) built unmodified for sm_103a by
+kernels (deps/volume-rendering-jax/lib/impl/*.cu) and spherical-harmonics kernel
+(deps/spherical-harmonics-encoding-jax/lib/impl/*.cu) built unmodified for sm_103a by
 baseline/volrend_gpu.sh.  The GPU tests use it as an oracle and bench.py as the per-kernel bar;
 the product (jaxngp_gb300/) never loads it.
 
@@ -19,7 +20,8 @@ import torch
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libvolrend_ref_gpu.so")
 NAMES = ("pack_density_into_bits", "march_rays", "march_rays_inference", "morton3d", "morton3d_invert",
-         "integrate_rays", "integrate_rays_backward", "integrate_rays_inference")
+         "integrate_rays", "integrate_rays_backward", "integrate_rays_inference",
+         "spherical_harmonics_encoding_cuda_f32")
 # the reference's integrators return before a __syncthreads() in a partial last block
 # (integrating.cu:45/:100, :263/:318); callers keep n_rays a multiple of their 512-thread block
 INTEGRATOR_BLOCK = 512
@@ -59,6 +61,8 @@ def call(name: str, buffers: Sequence, desc, stream=None) -> None:
         if n % INTEGRATOR_BLOCK != 0:
             raise ValueError(f"{name}: n_rays must be a multiple of {INTEGRATOR_BLOCK} for the reference's kernel")
     L = lib()
+    if not hasattr(L, "ref_" + name):
+        raise RuntimeError(f"the reference's GPU build has no {name}")
     arr = (ctypes.c_void_p * max(1, len(buffers)))(*[_ptr(b) for b in buffers])
     opaque = desc.to_bytes()
     if stream is None:

@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # The reference's own volume-rendering kernels (deps/volume-rendering-jax/lib/impl/{marching,
-# integrating,packbits}.cu), compiled unmodified for sm_103a with nvcc's default floating point
+# integrating,packbits}.cu) and its spherical-harmonics kernel (deps/spherical-harmonics-encoding-
+# jax/lib/impl/spherical_harmonics_encoding.cu), compiled unmodified for sm_103a with nvcc's default floating point
 # (--fmad=true, as the reference's CMakeLists.txt builds them), into
 # baseline/_ref/libvolrend_ref_gpu.so.  It is the GPU bar the new kernels are timed against and a
 # GPU oracle for their parity tests; nothing in jaxngp_gb300/ loads it.
@@ -31,6 +32,11 @@ stage)
     mkdir -p "$src/impl" "$src/serde-helper"
     cp "$impl/marching.cu" "$impl/integrating.cu" "$impl/packbits.cu" "$impl/volrend.h" "$src/impl/"
     cp "$ref/deps/serde-helper/serde.h" "$src/serde-helper/"
+    shsrc="$ref/deps/spherical-harmonics-encoding-jax/lib/impl"
+    if [ -f "$shsrc/spherical_harmonics_encoding.cu" ]; then
+        mkdir -p "$src/shjax"
+        cp "$shsrc/spherical_harmonics_encoding.cu" "$shsrc/spherical_harmonics_encoding.h" "$src/shjax/"
+    fi
     echo "staged $src"
     ;;
 build)
@@ -46,7 +52,12 @@ build)
     for k in marching integrating packbits; do
         "$nvcc" "${flags[@]}" -c "$src/impl/$k.cu" -o "$out/obj/$k.o" & pids+=($!)
     done
-    "$nvcc" "${flags[@]}" -c "$here/volrend_gpu_exports.cu" -o "$out/obj/exports.o" & pids+=($!)
+    shflag=()
+    if [ -f "$src/shjax/spherical_harmonics_encoding.cu" ]; then
+        "$nvcc" "${flags[@]}" -I "$src/shjax" -c "$src/shjax/spherical_harmonics_encoding.cu" -o "$out/obj/shjax.o" & pids+=($!)
+        shflag=(-DNGP_REF_SHJAX -I "$src/shjax")
+    fi
+    "$nvcc" "${flags[@]}" "${shflag[@]}" -c "$here/volrend_gpu_exports.cu" -o "$out/obj/exports.o" & pids+=($!)
     for p in "${pids[@]}"; do wait "$p"; done
     "$nvcc" -gencode arch=compute_103a,code=sm_103a -shared -o "$out/libvolrend_ref_gpu.so.tmp" "$out"/obj/*.o
     mv "$out/libvolrend_ref_gpu.so.tmp" "$out/libvolrend_ref_gpu.so"

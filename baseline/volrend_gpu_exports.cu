@@ -38,4 +38,11 @@ REF_ENTRY(integrate_rays)
 REF_ENTRY(integrate_rays_backward)
 REF_ENTRY(integrate_rays_inference)
 
+#ifdef NGP_REF_SHJAX
+#include "spherical_harmonics_encoding.h"
+extern "C" int ref_spherical_harmonics_encoding_cuda_f32(cudaStream_t s, void **b, const char *o, std::size_t n) {
+    return guarded([&] { shjax::spherical_harmonics_encoding_cuda_f32(s, b, o, n); });
+}
+#endif
+
 extern "C" const char *ref_last_error() { return g_err; }

@@ -46,8 +46,9 @@ unsigned long long ngp_kernel_launches(void);
  * recorded a device-side error since the last call -- a tensor-core kernel whose bounded wait for
  * its MMAs ran out -- else NGP_OK, or NGP_ERR_CUDA if the synchronisation failed. */
 int ngp_device_status(void);
-/* CTAs per SM the training march (march_rays, ngp_march_rays_train, ngp_march_rays_fallback)
- * launches for every later call on any thread; 0 restores the default (10, the register limit).
+/* At most this many CTAs per SM for the marches (march_rays, ngp_march_rays_train,
+ * ngp_march_rays_fallback) on every later call on any thread -- they stride over the rest of the
+ * rays; 0 restores the default (10: no limit below what fits).
  * A caller that runs the march on a second stream, beside other kernels, lowers it so those
  * kernels find room on every SM.  Returns the previous value, or -1 for n outside [0, 10]. */
 int ngp_set_march_blocks_per_sm(int n);
@@ -182,6 +183,24 @@ int morton3d_status(cudaStream_t stream, void **buffers, const char *opaque, siz
 void morton3d_invert(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int morton3d_invert_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
+/* ------------------------------------------------ shjax (spherical-harmonics direction encoding) */
+/* deps/spherical-harmonics-encoding-jax/lib/impl/spherical_harmonics_encoding.h:6-9 */
+typedef struct SphericalHarmonicsEncodingDescriptor {
+    uint32_t n;       /* directions */
+    uint32_t degree;  /* L: outputs are the L^2 real harmonics of degrees 0..L-1, L in 1..8 */
+} SphericalHarmonicsEncodingDescriptor;
+
+/* Replaces shjax::spherical_harmonics_encoding_cuda_f32 (spherical_harmonics_encoding.h:11-16;
+ * spherical_harmonics_encoding.cu:120-167), the custom-call target of
+ * shjax.spherical_harmonics_encoding (src/shjax/__init__.py:120-134).
+ * buffers: coord f32[n,3] (unit directions) -> encodings f32[n, L^2].
+ * opaque: SphericalHarmonicsEncodingDescriptor.  The values equal the reference's flax
+ * SphericalHarmonicsEncoder (models/encoders.py:361-406) bit for bit; L outside 1..8 returns
+ * NGP_ERR_INVALID_ARGUMENT (the reference writes at most 64 values per direction). */
+void spherical_harmonics_encoding_cuda_f32(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
+int spherical_harmonics_encoding_cuda_f32_status(cudaStream_t stream, void **buffers, const char *opaque,
+                                                 size_t opaque_len);
+
 /* Replaces volrendjax::integrate_rays (volrend.h:156-161; integrating.cu:512-519).
  * buffers: rays_sample_startidx u32[R], rays_n_samples u32[R], bgs f32[R,3], dss f32[S],
  * z_vals f32[S], drgbs f32[S,4] -> measured_batch_size u32[1], final_rgbds f32[R,4],
@@ -225,20 +244,27 @@ int ngp_integrate_rays_fp64_status(cudaStream_t stream, void **buffers, const ch
 void integrate_rays_inference(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int integrate_rays_inference_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
-/* march_rays for the training step: the same per-ray outputs as march_rays for every ray that
- * fits the sample budget, with every sample-less ray valid and every ray that does not fit
- * invalid, where the rays fit in ray order -- ray r fits when the counts of rays 0..r end within
- * the budget, at the start their sum gives -- so the result is deterministic and the rays that fit
- * are a prefix of the batch (march_rays, like the reference, fits rays in the order in which they
- * finish counting).  The counters hold the samples requested and those left out; their
- * difference is the samples written.  The block sums of the allocation borrow the last
- * ceil(n_rays / 1024) words of idcs (overwritten by the samples and the zeroed tail); with fewer
- * sample slots than that the call allocates as march_rays does.  With coarse occupancy blocks
- * (ngp_proposal_coarse of the same bitfield; K = 1, G a multiple of 8) the march crosses empty
- * blocks in one step each and finishes a ray whose segment crosses no occupied block at once --
- * valid, no samples -- with the same samples as the cell-by-cell march.
- * buffers: the 16 buffers of march_rays, then queue u32[1] (scratch, zeroed by the call), then
- * coarse u8[(G/8)^3] or NULL.  opaque: MarchingDescriptor. */
+/* march_rays for the training step: march_rays' result under one schedule of the reference
+ * kernel (marching.cu:101-268) -- its threads run one at a time, in ray order -- so every buffer
+ * and both counters are deterministic.  Ray r starts with the counter at the sum of the counts of
+ * the rays before it; it is dropped (invalid, no samples) if that reaches the budget
+ * (marching.cu:135), else it is valid without samples, or fits, or is the one ray that does not
+ * fit (invalid; the counters' difference leaves its samples out); every later ray is dropped.
+ * The valid rays are thus a prefix of the batch (march_rays, like the reference, fits rays in the
+ * order in which they finish counting).  The rays past that prefix are not marched.  With coarse
+ * occupancy blocks (ngp_proposal_coarse of the same bitfield; K = 1, G a multiple of 8) the march
+ * crosses empty blocks in one step each and finishes a ray whose segment crosses no occupied block
+ * at once -- valid, no samples -- with the same samples as the cell-by-cell march.  The pass's sums
+ * per 256 rays, their done flags and its progress word borrow the last 2 ceil(n_rays / 256) + 3
+ * words of idcs (overwritten by the samples and the zeroed tail); with fewer sample slots than
+ * that the call allocates as march_rays does.
+ * queue: in, the word the previous call on this batch size left (0 on a first call); out, the
+ * index of the first ray dropped or unfit (0xFFFFFFFF when none is).  The leading rays -- 1.25
+ * times that index plus 512 (8192 for 0), at most 16384 -- are counted alone, a warp per ray,
+ * before the rest, which then find the budget full and are dropped unmarched: a caller that passes
+ * the word back from call to call keeps the lead just above the rays the budget takes.
+ * buffers: the 16 buffers of march_rays, then queue u32[1], then coarse u8[(G/8)^3] or NULL.
+ * opaque: MarchingDescriptor. */
 void ngp_march_rays_train(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_march_rays_train_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 
@@ -616,7 +642,8 @@ int ngp_proposal_coarse_status(cudaStream_t stream, void **buffers, const char *
 /* buffers: rays_o f32[R,3], rays_d f32[R,3], t_starts f32[R], t_ends f32[R], coarse u8[(G/8)^3]
  * -> next_sample_write_location u32[1], number_of_exceeded_samples u32[1], ray_is_valid bool[R],
  * rays_n_samples u32[R], rays_sample_startidx u32[R], ray_of_slot u32[S/spr], slot_t_start f32[S/spr],
- * slot_t_end f32[S/spr], counts u32[3] (slots, bin points, samples). */
+ * slot_t_end f32[S/spr], counts u32[3] (slots, bin points, samples).  A ray without an interval
+ * is valid with no samples unless it is taken up (a warp at a time) after the slots filled. */
 void ngp_proposal_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_proposal_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 

@@ -66,6 +66,10 @@ class PackbitsDescriptor(_Desc):
     _fields_ = [("n_bytes", c_u32)]
 
 
+class SphericalHarmonicsEncodingDescriptor(_Desc):
+    _fields_ = [("n", c_u32), ("degree", c_u32)]
+
+
 class NgpHashGridDescriptor(_Desc):
     _fields_ = [("n_coords", c_u32), ("L", c_u32), ("F", c_u32), ("T", c_u32), ("first_hash_level", c_u32),
                 ("n_params", c_u32), ("bound", c_f32), ("two_bound", c_f32), ("accumulate", c_u32),

@@ -23,9 +23,9 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", 
 # so that their float arithmetic is the reference's source arithmetic, one rounding per operation
 # (sample counts and early-termination steps then agree exactly with the reference built that way).
 EXTRA = {"marching.cu": ["--fmad=false"], "integrating.cu": ["--fmad=false"], "train.cu": ["--fmad=false"],
-         "proposal.cu": ["--fmad=false"]}
+         "proposal.cu": ["--fmad=false"], "sh.cu": ["--fmad=false"]}
 SOURCES = ["abi.cu", "marching.cu", "integrating.cu", "packbits.cu", "hashgrid.cu", "mlp.cu", "mlp_tc.cu", "proposal.cu", "train.cu",
-           "scene.cu"]
+           "scene.cu", "sh.cu"]
 
 
 def nvcc() -> str:

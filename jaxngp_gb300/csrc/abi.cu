@@ -38,6 +38,7 @@ int launch_integrate_rays_inference(cudaStream_t, const IntegratingInferenceDesc
                                     const float *, const std::uint32_t *, const std::uint32_t *, const float *,
                                     const float *, const float *, std::uint32_t *, bool *, float *, float *);
 int launch_packbits(cudaStream_t, std::uint32_t, const float *, const float *, bool *, std::uint8_t *, bool);
+int launch_sh_encoding(cudaStream_t, std::uint32_t, std::uint32_t, const float *, float *);
 int launch_hashgrid_forward(cudaStream_t, const NgpHashGridDescriptor &, const std::uint32_t *, const float *,
                             const float *, float *);
 int launch_hashgrid_backward(cudaStream_t, const NgpHashGridDescriptor &, const std::uint32_t *, const float *,
@@ -261,6 +262,11 @@ NGP_ENTRY(ngp_integrate_rays_inference_compact) {
     NGP_CHECK_ARG(buffers[8] != nullptr, "integrate_rays_inference_compact: sample_start is required");
     return launch_integrate_rays_inference_inplace(stream, d, CF32(0), F32(1), F32(2), CU32(3), CU32(4), CF32(5),
                                                    CF32(6), CF32(7), CU32(8), U32(9), B8(10));
+}
+
+NGP_ENTRY(spherical_harmonics_encoding_cuda_f32) {
+    NGP_DESC(SphericalHarmonicsEncodingDescriptor, d);
+    return launch_sh_encoding(stream, d.n, d.degree, CF32(0), F32(1));
 }
 
 NGP_ENTRY(morton3d) {

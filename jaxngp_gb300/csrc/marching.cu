@@ -268,188 +268,160 @@ std::atomic<int> g_march_blocks_per_sm{kMarchBlocksPerSm};
 
 enum : int { kIdle = 0, kCount = 1, kWrite = 2 };
 
-// Marches rays with lane refill: every lane of a warp carries one ray and advances it by one
-// march iteration per trip of the loop; a lane whose ray is finished takes the next ray at once,
-// so a warp keeps all 32 lanes busy until the rays run out (one thread per ray, as in the
-// reference, leaves most lanes of a warp idle behind the warp's longest ray).  With one cascade,
-// an occupied sample's cell is followed through in a tight loop (below), and with a coarse grid
-// an empty coarse block is crossed in one step (skip_block).
-//
-// Rays come from a global queue counter when `queue` is given, else from a fixed interleaving:
-// warp w takes 32-ray chunks w, w + n_warps, w + 2 n_warps, ...
+enum : int { kMarchAlloc = 0, kMarchCount = 1 };
+
+// The march, one thread per ray (the reference's structure, marching.cu:101-268), with the
+// arithmetic of occupied_at/skip_empty, same-cell loops (below) and, with a coarse grid, one-step
+// skips of empty coarse blocks (skip_block).  Rays are visited in index order by a block-uniform
+// grid-stride loop.  (A lane-refill design -- a lane that finishes its ray takes the next one
+// from a queue -- measured 1.5x slower on the same work: the march is issue-bound at about 7 of
+// 32 active threads per instruction either way, and the refill adds instructions without making
+// the lanes more coherent; ordering the rays by camera and direction did not help either.)
 //
 // Per ray the arithmetic and the two passes (count, then write) are the reference's
 // (marching.cu:162-192, :224-267).  A ray with no sample is valid (marching.cu:196-199); a ray
-// that does not fit the budget is not (:206-209).  Three modes:
+// that does not fit the budget is not (:206-209).  Two modes:
 //
-// kMarchAlloc (the drop-in march_rays): the write pass resumes at the t of the first occupied
-// sample the count pass met instead of re-marching the empty space before it (the march state is
-// t alone, so the samples from there on are the same).  Slots are allocated once per trip for all
-// lanes that finished counting in it (one atomic), so which rays fit an overflowing budget follows
-// the order in which they finish counting, as in the reference; and, as in the reference (:135),
-// a ray that a lane takes up after the buffer filled is dropped (invalid) without being marched --
-// a legal schedule of the reference's kernel, whose result depends on when each ray's thread
-// starts.
+// kMarchAlloc (the drop-in march_rays): after counting, the rays of a warp take their slots with
+// one atomic (a warp prefix sum of their counts), so which rays fit an overflowing budget follows
+// the order in which warps finish counting, as in the reference, and the write pass resumes at
+// the t of the ray's first occupied sample (the march state is t alone).  As in the reference
+// (:135), a ray whose thread starts after the buffer filled is dropped (invalid) unmarched.
 //
-// kMarchCount, kMarchWrite (the training march, launch_march_rays with `ordered`): rays fit the
-// budget in ray order -- the schedule in which every ray's thread starts at once and the rays
-// finish counting in index order.  The count pass stores every ray's count and validity; a scan
-// over the rays in index order gives each ray its start and decides which fit; the write pass then
-// marches the rays that fit from their start and writes their samples.  The rays that fit are a
-// prefix of the batch (its pixel indices are drawn at random, so an unbiased sample of the rays
-// that carry samples) whatever the order of the counting, and the result is deterministic.
-enum : int { kMarchAlloc = 0, kMarchCount = 1, kMarchWrite = 2 };
+// kMarchCount: the count pass of the training march (launch_march_rays with `ordered`) for the
+// rays after its leading ones; see below.
+//
+// The training march gives the reference kernel's result under one schedule: its threads run one
+// at a time, in ray order.  Then ray r starts with the counter at P(r), the sum of the counts of
+// the rays before it; it is dropped unmarched if P(r) >= budget (marching.cu:135), else it is
+// valid with no samples, or fits (P(r) + n(r) <= budget), or is the one ray that does not fit
+// (:206-209), after which every ray is dropped.  The rays that fit are a prefix of the batch's
+// rays with samples, and the valid rays a prefix of the batch (its pixel indices are drawn at
+// random, so an unbiased sample), and the result is deterministic.  The passes:
+//
+//  - the leading rays (march_lead_kernel, a warp per ray): counted in full, their counts summed
+//    per chunk of kThreadBlock rays;
+//  - the other rays (march_rays_kernel<kMarchCount>, a thread per ray), in chunks: each chunk
+//    publishes the sum of its counts when done, and a frontier word holds (F, P): chunks [0, F)
+//    are done and their counts sum to P.  A ray of chunk c >= F that reads P >= budget stops (or
+//    never starts): it is dropped.  Its published count is then a lower bound of its count; see
+//    ray_scan_fit_kernel for why the result stays exact;
+//  - ray_scan_fit_kernel: the prefix sums P(r), the fit, the counters;
+//  - march_write_kernel (a warp per ray): the samples of the rays that fit.
+//
+// Resident rays share the SMs round-robin, so the leading chunks of one launch over the whole
+// batch finish only about when all of its first wave does, too late for the frontier to spare
+// anything; hence the leading rays' launch of their own, where each ray runs at the speed of its
+// chain of steps, shortened 32-fold by the warp's lookahead.  How many rays lead comes from the
+// previous call: the index of its first dropped ray, which the call leaves in its `queue` word;
+// this call leads with 1.25 times that many rays and 512 more (8192 on a first call, whose word
+// is 0), at most kLeadMax.  A lead that falls short costs time, not exactness.  Once the leading
+// rays fill the budget, a chunk of the others only records that its rays have no count.
+constexpr int kThreadBlock = 256;
+constexpr std::uint32_t kFrontierCheck = 32;   // a counting ray reads the frontier every this many steps
+constexpr std::uint32_t kLeadMax = 16384;      // leading rays at most (a multiple of kThreadBlock)
+static_assert(kLeadMax % kThreadBlock == 0, "the leading rays are whole chunks");
 
+// The chunks of kThreadBlock rays the leading launch takes, given the previous call's word.
+__device__ __forceinline__ std::uint32_t lead_chunks(std::uint32_t word, std::uint32_t n_rays) {
+    std::uint64_t w = word == 0u ? 8192ull : (std::uint64_t)word + word / 4u + 512u;
+    if (w > kLeadMax) w = kLeadMax;
+    if (w > n_rays) w = n_rays;
+    return (std::uint32_t)((w + kThreadBlock - 1) / kThreadBlock);
+}
+
+// The frontier word: F in the high half, P (saturated at 2^32 - 1, which no budget exceeds) in
+// the low half.
+__device__ __forceinline__ unsigned long long frontier_pack(std::uint32_t F, std::uint64_t P) {
+    return ((unsigned long long)F << 32) | (P > 0xffffffffull ? 0xffffffffull : P);
+}
+__device__ __forceinline__ std::uint32_t frontier_sum(const unsigned long long *frontier) {
+    return (std::uint32_t)*((const volatile unsigned long long *)frontier);
+}
+
+// Publishes chunk c's count sum and moves the frontier over the chunks done (one thread).  The
+// attempts are bounded; a frontier left behind is moved on by the next chunk that finishes, and
+// only ever lowers what the rays can skip.
+__device__ __forceinline__ void publish_chunk(std::uint32_t c, std::uint32_t sum, std::uint32_t n_chunks,
+                                              std::uint32_t total_samples,
+                                              std::uint32_t *chunk_sums, std::uint32_t *chunk_done,
+                                              unsigned long long *frontier) {
+    *((volatile std::uint32_t *)(chunk_sums + c)) = sum;
+    __threadfence();
+    *((volatile std::uint32_t *)(chunk_done + c)) = 1u;
+    __threadfence();
+    if (frontier_sum(frontier) >= total_samples) return;   // full already: nothing more to skip
+    for (int k = 0; k < 256; ++k) {
+        const unsigned long long w = *((volatile unsigned long long *)frontier);
+        const std::uint32_t F = (std::uint32_t)(w >> 32), P = (std::uint32_t)w;
+        if (F >= n_chunks || *((volatile std::uint32_t *)(chunk_done + F)) == 0u) break;
+        __threadfence();
+        const std::uint32_t v = *((volatile std::uint32_t *)(chunk_sums + F));
+        atomicCAS(frontier, w, frontier_pack(F + 1u, (std::uint64_t)P + v));   // on failure: look again
+    }
+}
+
+// One ray of march_rays_kernel (every lane of the warp calls it together; r >= n_rays idles).
+// Returns the ray's count (as far as it was counted) in kMarchCount mode, else 0.
 template <int kMode>
-__global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_kernel(
-    std::uint32_t n_rays, std::uint32_t total_samples, MarchParams m,
+__device__ __forceinline__ std::uint32_t march_one(
+    std::uint32_t r, std::uint32_t n_rays, std::uint32_t total_samples, const MarchParams &m, float n_cap, bool block_skip,
     const float *__restrict__ rays_o, const float *__restrict__ rays_d,
     const float *__restrict__ t_starts, const float *__restrict__ t_ends,
     const float *__restrict__ noises, const std::uint8_t *__restrict__ bits,
-    std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded,
-    std::uint32_t *__restrict__ queue, bool *__restrict__ ray_is_valid,
+    std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded, bool *__restrict__ ray_is_valid,
     std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
     std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
-    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse) {
-    __shared__ std::uint32_t expand[1024];  // expand_bits(v), v < G (G <= 1024)
-    for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
-    __syncthreads();
-    const unsigned lane = lane_id();
-    const unsigned lt_mask = (1u << lane) - 1u;
-    const std::uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const std::uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-    const float n_cap = (float)m.dns * m.bound;
-    const bool block_skip = coarse != nullptr && m.K == 1 && m.const_ds && (m.G & 7u) == 0u;
-
-    int phase = kIdle;
-    std::uint32_t ray = 0, n = 0, k = 0, start = 0, it = 0;
+    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse,
+    const std::uint32_t *expand, const unsigned long long *frontier) {
+    bool march = false;
+    std::uint32_t n = 0, start = 0, it = 0;
     V3 o{0.f, 0.f, 0.f}, d{1.f, 1.f, 1.f}, inv_d{1.f, 1.f, 1.f};
     float t = 0.f, t1 = 0.f, t_hit = 0.f;
-    std::uint32_t cursor = 0;   // static interleaving: rays handed out so far by this warp
-    bool exhausted = false;     // warp-uniform
-
-    for (;;) {
-        // ---- hand the next rays to idle lanes until all lanes march or the rays run out
-        for (;;) {
-            const unsigned idle = __ballot_sync(0xffffffffu, phase == kIdle);
-            if (idle == 0u || exhausted) break;
-            const unsigned cnt = (unsigned)__popc(idle);
-            std::uint32_t base = 0;
-            if (queue != nullptr) {
-                if (lane == 0) base = atomicAdd(queue, cnt);
-                base = __shfl_sync(0xffffffffu, base, 0);
+    if (r < n_rays) {
+        if (kMode == kMarchAlloc && *((volatile std::uint32_t *)next_loc) >= total_samples) {
+            ray_is_valid[r] = false;   // marching.cu:135
+            rays_n_samples[r] = 0;
+            rays_startidx[r] = 0;
+        } else {
+            o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
+            d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
+            const float t0 = t_starts[r];
+            t1 = t_ends[r];
+            if (t1 > t0 && !(coarse != nullptr && no_sample_possible(m, o, d, t0, t1, coarse))) {
+                march = true;
+                inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                t = t0 + calc_ds(t0, m) * noises[r];
             } else {
-                base = cursor;
-                cursor += cnt;
+                ray_is_valid[r] = t1 > t0;
+                rays_n_samples[r] = 0;
+                rays_startidx[r] = 0;
             }
-            if (phase == kIdle) {
-                const std::uint32_t q = base + (unsigned)__popc(idle & lt_mask);
-                const std::uint32_t qi = queue != nullptr ? q : (((q >> 5) * n_warps + warp) << 5) + (q & 31u);
-                if (kMode == kMarchAlloc && qi < n_rays && *((volatile std::uint32_t *)next_loc) >= total_samples) {
-                    // marching.cu:135: a ray that starts after the sample buffer filled is dropped
-                    ray_is_valid[qi] = false;
-                    rays_n_samples[qi] = 0;
-                    rays_startidx[qi] = 0;
-                } else if (kMode == kMarchWrite && qi < n_rays) {
-                    // the write pass of a ray that fits (its count and start come from the scan)
-                    const std::uint32_t r = qi;
-                    n = rays_n_samples[r];
-                    if (n > 0u) {
-                        ray = r;
-                        start = rays_startidx[r];
-                        o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
-                        d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
-                        inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-                        const float t0 = t_starts[r];
-                        t1 = t_ends[r];
-                        t = t0 + calc_ds(t0, m) * noises[r];
-                        k = 0;
-                        it = 0;
-                        phase = kWrite;
-                    }
-                } else if (qi < n_rays) {
-                    const std::uint32_t r = qi;
-                    ray = r;
-                    o = {rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
-                    d = {rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
-                    const float t0 = t_starts[r];
-                    t1 = t_ends[r];
-                    if (t1 > t0 && !(coarse != nullptr && no_sample_possible(m, o, d, t0, t1, coarse))) {  // marching.cu:151
-                        inv_d = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-                        t = t0 + calc_ds(t0, m) * noises[r];
-                        n = 0;
-                        it = 0;
-                        phase = kCount;
-                    } else if (t1 > t0) {  // marching.cu:196-199: no occupied block on the way
-                        ray_is_valid[r] = true;
-                        rays_n_samples[r] = 0;
-                        rays_startidx[r] = 0;
-                    } else {
-                        ray_is_valid[r] = false;
-                        rays_n_samples[r] = 0;
-                        rays_startidx[r] = 0;
-                    }
-                }
-            }
-            // no rays left for this warp: the queue is drained, or the warp's interleaved
-            // sequence (increasing in its index) has passed the last ray
-            if (queue != nullptr)
-                exhausted = (std::uint64_t)base + cnt >= n_rays;
-            else
-                exhausted = ((((cursor >> 5) * n_warps + warp) << 5) + (cursor & 31u)) >= n_rays;
         }
-        const bool active = phase != kIdle;
-        if (__ballot_sync(0xffffffffu, active) == 0u) break;
-
-        // ---- one march iteration (marching.cu:166-191 / :231-266).  With one cascade, an
-        // occupied sample's cell is followed through: the next steps are taken in a tight loop for
-        // as long as their positions stay in that cell, whose bit they share (positions move
-        // monotonically along the ray, so it is never re-entered) -- the reference's additions and
-        // positions, without a lookup or a trip of the refill machinery per sample.
-        if (active) {
+    }
+    // ---- count pass (marching.cu:162-192)
+    if (march) {
+        std::uint32_t poll = 0;
+        while ((float)n < n_cap && t < t1 && it < kMaxMarchIters) {
+            if (kMode == kMarchCount && it >= poll) {   // do the rays before this one fill the budget?
+                if (frontier_sum(frontier) >= total_samples) break;
+                poll = it + kFrontierCheck;
+            }
             const V3 pos = at(o, d, t);
             const float ds = calc_ds(t, m);
             V3 g;
             float mb;
             if (occupied_at(m, pos, ds, bits, g, mb, expand)) {
-                const std::uint32_t key = m.K == 1 ? cell_key(m, g) : 0u;
-                if (phase == kWrite) {
-                    auto put = [&](V3 p, float dsj, float tj) {
-                        const std::uint32_t s = start + k;
-                        idcs[s] = ray;
-                        xyzs[(std::size_t)s * 3 + 0] = p.x;
-                        xyzs[(std::size_t)s * 3 + 1] = p.y;
-                        xyzs[(std::size_t)s * 3 + 2] = p.z;
-                        dirs[(std::size_t)s * 3 + 0] = d.x;
-                        dirs[(std::size_t)s * 3 + 1] = d.y;
-                        dirs[(std::size_t)s * 3 + 2] = d.z;
-                        dss[s] = dsj;
-                        z_vals[s] = tj;
-                        ++k;
-                    };
-                    put(pos, ds, t);
-                    t = t + ds;
-                    if (m.K == 1) {
-                        while (k < n && t < t1 && it < kMaxMarchIters) {   // marching.cu:231
-                            const V3 p2 = at(o, d, t);
-                            if (cell_key_at(m, p2) != key) break;
-                            const float ds2 = calc_ds(t, m);
-                            put(p2, ds2, t);
-                            t = t + ds2;
-                            ++it;
-                        }
-                    }
-                } else {
-                    if (n == 0) t_hit = t;
-                    ++n;
-                    t = t + ds;
-                    if (m.K == 1) {
-                        while ((float)n < n_cap && t < t1 && it < kMaxMarchIters) {   // marching.cu:164
-                            if (cell_key_at(m, at(o, d, t)) != key) break;
-                            ++n;
-                            t = t + calc_ds(t, m);
-                            ++it;
-                        }
+                if (n == 0) t_hit = t;
+                ++n;
+                t = t + ds;
+                if (m.K == 1) {
+                    const std::uint32_t key = cell_key(m, g);
+                    while ((float)n < n_cap && t < t1 && it < kMaxMarchIters) {
+                        if (cell_key_at(m, at(o, d, t)) != key) break;
+                        ++n;
+                        t = t + calc_ds(t, m);
+                        ++it;
                     }
                 }
             } else {
@@ -461,85 +433,191 @@ __global__ void __launch_bounds__(kMarchBlock, kMarchBlocksPerSm) march_rays_ker
             }
             ++it;
         }
-
-        // ---- phase changes
-        bool count_done = phase == kCount && !((float)n < n_cap && t < t1 && it < kMaxMarchIters);
-        if (kMode == kMarchCount && count_done) {   // the count and the ray's validity so far; the scan decides
-            ray_is_valid[ray] = true;
-            rays_n_samples[ray] = n;
-            phase = kIdle;
-            count_done = false;
+    }
+    if (kMode == kMarchCount) {
+        if (march) {
+            ray_is_valid[r] = true;   // ray_scan_fit_kernel decides
+            rays_n_samples[r] = n;
+            rays_startidx[r] = __float_as_uint(t_hit);   // for the write pass (ray_scan_fit_kernel)
         }
-        if (count_done && n == 0) {  // marching.cu:196-199
-            ray_is_valid[ray] = true;
-            rays_n_samples[ray] = 0;
-            rays_startidx[ray] = 0;
-            phase = kIdle;
-            count_done = false;
-        }
-        const bool want = count_done;  // n > 0
-        const unsigned wm = __ballot_sync(0xffffffffu, want);
-        if (kMode == kMarchAlloc && wm != 0u) {
-            const std::uint32_t incl = warp_inclusive_scan(want ? n : 0u);
-            const std::uint32_t total_w = __shfl_sync(0xffffffffu, incl, 31);
-            const int leader = __ffs(wm) - 1;
-            std::uint32_t base = 0;
-            if ((int)lane == leader) base = atomicAdd(next_loc, total_w);
-            base = __shfl_sync(0xffffffffu, base, leader);
-            bool fits = false;
-            if (want) {
-                start = base + incl - n;
-                fits = (std::uint64_t)start + n <= total_samples;
-                ray_is_valid[ray] = fits;
-                rays_n_samples[ray] = fits ? n : 0u;
-                rays_startidx[ray] = fits ? start : 0u;
-                if (fits) {  // second pass writes the samples (marching.cu:224-267)
-                    phase = kWrite;
-                    t = t_hit;
-                    k = 0;
-                    it = 0;
-                } else {
-                    phase = kIdle;
+        return march ? n : 0u;   // no warp collective follows in this mode
+    }
+    // kMarchAlloc: one atomic per warp (warp prefix sum of the counts)
+    const bool want = march && n > 0u;
+    if (march && n == 0u) {
+        ray_is_valid[r] = true;
+        rays_n_samples[r] = 0;
+        rays_startidx[r] = 0;
+    }
+    const unsigned wm = __ballot_sync(0xffffffffu, want);
+    const std::uint32_t incl = warp_inclusive_scan(want ? n : 0u);
+    const std::uint32_t total_w = __shfl_sync(0xffffffffu, incl, 31);
+    std::uint32_t base = 0;
+    if (wm != 0u) {
+        const int leader = __ffs(wm) - 1;
+        if ((int)lane_id() == leader) base = atomicAdd(next_loc, total_w);
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    bool fits = false;
+    if (want) {
+        start = base + incl - n;
+        fits = (std::uint64_t)start + n <= total_samples;
+        ray_is_valid[r] = fits;
+        rays_n_samples[r] = fits ? n : 0u;
+        rays_startidx[r] = fits ? start : 0u;
+    }
+    const std::uint32_t over = warp_sum((want && !fits) ? n : 0u);
+    if (lane_id() == 0 && over > 0u) atomicAdd(n_exceeded, over);
+    // ---- write pass (marching.cu:224-267), from the first occupied sample
+    if (want && fits) {
+        t = t_hit;
+        it = 0;
+        std::uint32_t k = 0;
+        auto put = [&](V3 p, float dsj, float tj) {
+            const std::uint32_t s = start + k;
+            idcs[s] = r;
+            xyzs[(std::size_t)s * 3 + 0] = p.x;
+            xyzs[(std::size_t)s * 3 + 1] = p.y;
+            xyzs[(std::size_t)s * 3 + 2] = p.z;
+            dirs[(std::size_t)s * 3 + 0] = d.x;
+            dirs[(std::size_t)s * 3 + 1] = d.y;
+            dirs[(std::size_t)s * 3 + 2] = d.z;
+            dss[s] = dsj;
+            z_vals[s] = tj;
+            ++k;
+        };
+        while (k < n && t < t1 && it < kMaxMarchIters) {
+            const V3 pos = at(o, d, t);
+            const float ds = calc_ds(t, m);
+            V3 g;
+            float mb;
+            if (occupied_at(m, pos, ds, bits, g, mb, expand)) {
+                put(pos, ds, t);
+                t = t + ds;
+                if (m.K == 1) {
+                    const std::uint32_t key = cell_key(m, g);
+                    while (k < n && t < t1 && it < kMaxMarchIters) {
+                        const V3 p2 = at(o, d, t);
+                        if (cell_key_at(m, p2) != key) break;
+                        const float ds2 = calc_ds(t, m);
+                        put(p2, ds2, t);
+                        t = t + ds2;
+                        ++it;
+                    }
                 }
+            } else {
+                float tb;
+                if (block_skip && skip_block(m, t, g, pos, o, d, inv_d, coarse, tb))
+                    t = tb;
+                else
+                    t = skip_empty(m, t, g, mb, pos, d, inv_d);
             }
-            const std::uint32_t over = warp_sum((want && !fits) ? n : 0u);
-            if (lane == 0 && over > 0) atomicAdd(n_exceeded, over);
+            ++it;
         }
-        if (phase == kWrite && !(k < n && t < t1 && it < kMaxMarchIters)) phase = kIdle;
     }
+    return 0u;
 }
 
-// Ray-order allocation of the training march (between its count and write passes).  Rays are
-// taken in blocks of kScanRays; block b sums the counts of rays [b kScanRays, (b+1) kScanRays).
-constexpr int kScanRays = 1024;
-
-__global__ void __launch_bounds__(kScanRays) ray_block_sums_kernel(std::uint32_t n_rays,
-                                                                   const std::uint32_t *__restrict__ counts,
-                                                                   std::uint32_t *__restrict__ sums) {
-    __shared__ std::uint32_t ws[kScanRays / 32];
-    const std::uint32_t r = blockIdx.x * kScanRays + threadIdx.x;
-    const std::uint32_t v = warp_sum(r < n_rays ? counts[r] : 0u);
-    if (lane_id() == 0) ws[threadIdx.x >> 5] = v;
+// kMarchAlloc: every ray.  kMarchCount: the chunks after the leading ones (their number from
+// `split`, the previous call's word), whose count sums start the frontier.
+template <int kMode>
+__global__ void __launch_bounds__(kThreadBlock) march_rays_kernel(
+    std::uint32_t n_rays, std::uint32_t total_samples, MarchParams m,
+    const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+    const float *__restrict__ t_starts, const float *__restrict__ t_ends,
+    const float *__restrict__ noises, const std::uint8_t *__restrict__ bits,
+    std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded, bool *__restrict__ ray_is_valid,
+    std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
+    std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
+    float *__restrict__ dss, float *__restrict__ z_vals, const std::uint8_t *__restrict__ coarse,
+    std::uint32_t *__restrict__ chunk_sums, std::uint32_t *__restrict__ chunk_done,
+    unsigned long long *__restrict__ frontier, const std::uint32_t *__restrict__ split) {
+    __shared__ std::uint32_t expand[1024];
+    __shared__ std::uint32_t red[kThreadBlock / 32];
+    __shared__ int s_full;
+    const std::uint32_t n_chunks = (n_rays + kThreadBlock - 1) / kThreadBlock;
+    const std::uint32_t c_lo = kMode == kMarchCount ? lead_chunks(*split, n_rays) : 0u;
+    if (c_lo + blockIdx.x >= n_chunks) return;
+    for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
+    if (kMode == kMarchCount) {
+        // the leading chunks are done (an earlier launch): their sum starts the frontier
+        std::uint32_t a = 0;
+        for (std::uint32_t c = threadIdx.x; c < c_lo; c += kThreadBlock) a += chunk_sums[c];
+        a = warp_sum(a);
+        if (lane_id() == 0) red[threadIdx.x >> 5] = a;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            std::uint64_t p = 0;
+            for (int w = 0; w < kThreadBlock / 32; ++w) p += red[w];
+            atomicCAS(frontier, 0ull, frontier_pack(c_lo, p));   // the first block sets it
+        }
+    }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        const std::uint32_t x = warp_sum(ws[threadIdx.x]);
-        if (threadIdx.x == 0) sums[blockIdx.x] = x;
+    const float n_cap = (float)m.dns * m.bound;
+    const bool block_skip = coarse != nullptr && m.K == 1 && m.const_ds && (m.G & 7u) == 0u;
+    // block-uniform trips: every lane of a block runs the same trips (the allocation's warp scan,
+    // the count mode's block sum)
+    for (std::uint32_t c = c_lo + blockIdx.x; c < n_chunks; c += gridDim.x) {
+        const std::uint64_t base = (std::uint64_t)c * kThreadBlock;
+        if (kMode == kMarchCount) {   // the rays before this chunk fill the budget: all are dropped
+            if (threadIdx.x == 0) s_full = frontier_sum(frontier) >= total_samples;
+            __syncthreads();
+            const bool full = s_full;
+            __syncthreads();
+            if (full) {   // no count (ray_scan_fit_kernel drops them); the chunk's sum stays 0
+                if (base + threadIdx.x < n_rays) rays_n_samples[base + threadIdx.x] = 0u;
+                continue;
+            }
+        }
+        const std::uint32_t n = march_one<kMode>(
+            (std::uint32_t)(base + threadIdx.x), n_rays, total_samples, m, n_cap, block_skip, rays_o, rays_d, t_starts,
+            t_ends, noises, bits, next_loc, n_exceeded, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs,
+            dss, z_vals, coarse, expand, frontier);
+        if (kMode == kMarchCount) {   // the sum of the chunk's counts (rays [base, base + kThreadBlock))
+            const std::uint32_t w = warp_sum(n);
+            if (lane_id() == 0) red[threadIdx.x >> 5] = w;
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                const std::uint32_t x = warp_sum(threadIdx.x < kThreadBlock / 32 ? red[threadIdx.x] : 0u);
+                if (threadIdx.x == 0) publish_chunk(c, x, n_chunks, total_samples, chunk_sums, chunk_done, frontier);
+            }
+            __syncthreads();
+        }
     }
 }
 
-// Ray r's first sample slot is the sum of the counts of the rays before it; it fits when its
-// samples end within the budget (marching.cu:206-209).  A ray with samples that does not fit is
-// invalid, with no samples; the counters receive the samples requested and those left out (their
-// difference is the samples written, as march_rays' counters give it).
+
+// The fit of the training march, in ray order (marching.cu:135, :196-209 under the one-at-a-time
+// schedule).  A block takes kScanRays rays; the sums of the counts of the chunks before it give
+// its prefix.  P(r) is the sum of the counts of the rays before r; ray r is dropped when
+// P(r) >= budget (invalid, no samples), valid without samples when its count is 0, fits when
+// P(r) + n(r) <= budget (it gets the t of its first occupied sample, which the count pass left in
+// its start word, in its first sample slot of dss, where the write pass resumes from it), and
+// otherwise is the ray that does not fit (invalid; its samples are the ones left out).  The
+// counters: the samples of the rays not dropped, and those of the ray that did not fit.  `split`
+// receives the first dropped or unfit ray (~0u when there is none).
+//
+// The counts are exact for every ray up to the first that is dropped or does not fit, q: a ray
+// stops counting only on reading a frontier sum P >= budget, and no ray up to q can (the chunks
+// before its own sum to at most P(ray) < budget).  From q on, counts may be lower bounds, but
+// each computed P(r) for r > q is at least P(q) + n(q) > budget, or at least the frontier sum
+// >= budget that stopped it: every ray after q is dropped, as in the exact result.
+constexpr int kScanRays = 1024;
+static_assert(kScanRays % kThreadBlock == 0, "a scan block takes whole count chunks");
+
 __global__ void __launch_bounds__(kScanRays) ray_scan_fit_kernel(
-    std::uint32_t n_rays, std::uint32_t total_samples, const std::uint32_t *__restrict__ sums,
+    std::uint32_t n_rays, std::uint32_t total_samples, const std::uint32_t *__restrict__ chunk_sums,
     bool *__restrict__ valid, std::uint32_t *__restrict__ counts, std::uint32_t *__restrict__ startidx,
-    std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded) {
+    float *__restrict__ dss, std::uint32_t *__restrict__ next_loc, std::uint32_t *__restrict__ n_exceeded,
+    std::uint32_t *__restrict__ split) {
     __shared__ unsigned long long s_prefix;
+    __shared__ std::uint32_t s_first;
     __shared__ std::uint32_t ws[kScanRays / 32], wt[kScanRays / 32], wo[kScanRays / 32];
+    if (threadIdx.x == 0) s_first = 0xffffffffu;
     if (threadIdx.x < 32) {
         unsigned long long a = 0;
-        for (std::uint32_t b = threadIdx.x; b < blockIdx.x; b += 32) a += sums[b];
+        const std::uint32_t chunks = blockIdx.x * (kScanRays / kThreadBlock);
+        for (std::uint32_t b = threadIdx.x; b < chunks; b += 32) a += chunk_sums[b];
         a = warp_sum(a);
         if (threadIdx.x == 0) s_prefix = a;
     }
@@ -554,15 +632,17 @@ __global__ void __launch_bounds__(kScanRays) ray_scan_fit_kernel(
     }
     __syncthreads();
     const unsigned long long start = s_prefix + ws[threadIdx.x >> 5] + (incl - n);
-    const bool fits = start + n <= (unsigned long long)total_samples;
+    const bool counted = start < (unsigned long long)total_samples;   // not dropped (marching.cu:135)
+    const bool fits = counted && n > 0u && start + n <= (unsigned long long)total_samples;
+    const bool unfit = counted && n > 0u && !fits;
     if (r < n_rays) {
-        if (n > 0u) {
-            valid[r] = fits;
-            counts[r] = fits ? n : 0u;
-        }
-        startidx[r] = (n > 0u && fits) ? (std::uint32_t)start : 0u;
+        if (!counted || n > 0u) valid[r] = fits;
+        counts[r] = fits ? n : 0u;
+        if (fits) dss[start] = __uint_as_float(startidx[r]);
+        startidx[r] = fits ? (std::uint32_t)start : 0u;
+        if (!counted || unfit) atomicMin(&s_first, r);   // shared memory: cheap
     }
-    const std::uint32_t tot = warp_sum(n), over = warp_sum((n > 0u && !fits) ? n : 0u);
+    const std::uint32_t tot = warp_sum(counted ? n : 0u), over = warp_sum(unfit ? n : 0u);
     if (lane_id() == 0) {
         wt[threadIdx.x >> 5] = tot;
         wo[threadIdx.x >> 5] = over;
@@ -573,6 +653,7 @@ __global__ void __launch_bounds__(kScanRays) ray_scan_fit_kernel(
         if (threadIdx.x == 0) {
             if (a > 0u) atomicAdd(next_loc, a);
             if (o > 0u) atomicAdd(n_exceeded, o);
+            if (s_first != 0xffffffffu) atomicMin(split, s_first);
         }
     }
 }
@@ -787,6 +868,158 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_warp_kernel(
             if (!advance(m, a, lane, k, d, inv_d, t)) break;
             if (k < 32u) ++it;
         }
+    }
+}
+
+// ------------------------------------------------- the training march's warp-per-ray passes
+
+// advance() with the coarse-block skip: lane k, on an empty cell, crosses the empty coarse block
+// it lies in at once when skip_block can (the thread march's step at the same t).
+__device__ __forceinline__ bool advance_skip(const MarchParams &m, const Lookahead &a, unsigned lane, unsigned k,
+                                             V3 o, V3 d, V3 inv_d, const std::uint8_t *__restrict__ coarse,
+                                             bool block_skip, float &t) {
+    if (k < 32u) {
+        if (!__shfl_sync(0xffffffffu, a.live, k)) return false;
+        float nt = 0.f;
+        if (lane == k) {
+            float tb;
+            nt = (block_skip && skip_block(m, a.t, a.g, a.pos, o, d, inv_d, coarse, tb))
+                     ? tb : skip_empty(m, a.t, a.g, a.mb, a.pos, d, inv_d);
+        }
+        t = __shfl_sync(0xffffffffu, nt, k);
+    } else {
+        const float nt = lane == 31u ? a.t + a.ds : 0.f;
+        t = __shfl_sync(0xffffffffu, nt, 31);
+    }
+    return true;
+}
+
+// One ray by one warp, from t: the count (kWrite false: up to n_cap samples, and t_hit, the t of
+// the first) or the writing of its n_write samples from slot `start` (kWrite true).  The steps
+// are march_rays_kernel's, 32 at a time (look_ahead); every lane returns the same count.
+template <bool kWrite>
+__device__ __forceinline__ std::uint32_t warp_march(
+    const MarchParams &m, V3 o, V3 d, V3 inv_d, float t, float t1, float n_cap, std::uint32_t n_write,
+    const std::uint8_t *__restrict__ bits, const std::uint32_t *expand, const std::uint8_t *__restrict__ coarse,
+    bool block_skip, unsigned lane, float &t_hit, std::uint32_t r, std::uint32_t start,
+    std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs, float *__restrict__ dirs,
+    float *__restrict__ dss, float *__restrict__ z_vals) {
+    std::uint32_t n = 0, it = 0;
+    for (;;) {
+        const bool cond = kWrite ? n + lane < n_write : (float)(n + lane) < n_cap;
+        Lookahead a;
+        look_ahead(m, t, lane, o, d, t1, cond && it + lane < kMaxMarchIters, bits, expand, a);
+        const unsigned stop = __ballot_sync(0xffffffffu, !a.occ);
+        const unsigned k = stop != 0u ? (unsigned)__ffs(stop) - 1u : 32u;
+        if (kWrite) {
+            if (lane < k) {
+                const std::uint32_t s = start + n + lane;
+                idcs[s] = r;
+                xyzs[(std::size_t)s * 3 + 0] = a.pos.x;
+                xyzs[(std::size_t)s * 3 + 1] = a.pos.y;
+                xyzs[(std::size_t)s * 3 + 2] = a.pos.z;
+                dirs[(std::size_t)s * 3 + 0] = d.x;
+                dirs[(std::size_t)s * 3 + 1] = d.y;
+                dirs[(std::size_t)s * 3 + 2] = d.z;
+                dss[s] = a.ds;
+                z_vals[s] = a.t;
+            }
+        } else if (n == 0u && k > 0u) {
+            t_hit = t;   // lane 0's sample: the trip starts at it
+        }
+        n += k;
+        it += k;
+        if (!advance_skip(m, a, lane, k, o, d, inv_d, coarse, block_skip, t)) break;
+        if (k < 32u) ++it;   // the skip is a step of its own
+    }
+    return n;
+}
+
+constexpr int kWarpBlock = 256;   // 8 rays at a time per block
+constexpr std::uint32_t kSmemCoarse = 4096;   // coarse grids up to 16^3 blocks (G <= 128) go to shared memory
+
+// The coarse grid in shared memory when it fits (every block of a warp kernel reads it at each
+// empty cell), else the global copy.
+__device__ __forceinline__ const std::uint8_t *stage_coarse(const MarchParams &m, const std::uint8_t *coarse,
+                                                            std::uint8_t *s_coarse) {
+    if (coarse == nullptr) return nullptr;
+    const std::uint32_t Gc = m.G >> 3, nc = Gc * Gc * Gc;
+    if (nc > kSmemCoarse) return coarse;
+    for (std::uint32_t i = threadIdx.x; i < nc; i += blockDim.x) s_coarse[i] = coarse[i];
+    return s_coarse;
+}
+
+// The leading rays of the training march, counted in full, a warp per ray: validity, count and
+// the t of the first sample (in the start word) per ray, and each chunk's count sum.
+__global__ void __launch_bounds__(kWarpBlock) march_lead_kernel(
+    std::uint32_t n_rays, MarchParams m, const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+    const float *__restrict__ t_starts, const float *__restrict__ t_ends, const float *__restrict__ noises,
+    const std::uint8_t *__restrict__ bits, const std::uint8_t *__restrict__ coarse,
+    const std::uint32_t *__restrict__ split, bool *__restrict__ ray_is_valid,
+    std::uint32_t *__restrict__ rays_n_samples, std::uint32_t *__restrict__ rays_startidx,
+    std::uint32_t *__restrict__ chunk_sums) {
+    __shared__ std::uint32_t expand[1024];
+    __shared__ std::uint8_t s_coarse[kSmemCoarse];
+    const std::uint32_t lead = min(lead_chunks(*split, n_rays) * (std::uint32_t)kThreadBlock, n_rays);
+    const std::uint32_t warp0 = blockIdx.x * (kWarpBlock / 32);
+    if (warp0 >= lead) return;
+    for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
+    coarse = stage_coarse(m, coarse, s_coarse);
+    __syncthreads();
+    const unsigned lane = lane_id();
+    const float n_cap = (float)m.dns * m.bound;
+    const bool block_skip = coarse != nullptr && m.K == 1 && m.const_ds && (m.G & 7u) == 0u;
+    for (std::uint32_t r = warp0 + (threadIdx.x >> 5); r < lead; r += gridDim.x * (kWarpBlock / 32)) {
+        const V3 o{rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
+        const V3 d{rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
+        const float t0 = t_starts[r], t1 = t_ends[r];
+        std::uint32_t n = 0;
+        float t_hit = 0.f;
+        if (t1 > t0 && !(coarse != nullptr && no_sample_possible(m, o, d, t0, t1, coarse))) {
+            const V3 inv_d{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+            n = warp_march<false>(m, o, d, inv_d, t0 + calc_ds(t0, m) * noises[r], t1, n_cap, 0u, bits, expand,
+                                  coarse, block_skip, lane, t_hit, r, 0u, nullptr, nullptr, nullptr, nullptr, nullptr);
+        }
+        if (lane == 0) {
+            ray_is_valid[r] = t1 > t0;   // marching.cu:151; ray_scan_fit_kernel decides the rest
+            rays_n_samples[r] = n;
+            rays_startidx[r] = __float_as_uint(t_hit);
+            if (n > 0u) atomicAdd(chunk_sums + r / kThreadBlock, n);
+        }
+    }
+}
+
+// The samples of the rays that fit (marching.cu:224-267), a warp per ray, from the t of each
+// ray's first sample (left in its first slot of dss); the rays that fit all come before the
+// first dropped or unfit ray (`split`).
+__global__ void __launch_bounds__(kWarpBlock) march_write_kernel(
+    std::uint32_t n_rays, MarchParams m, const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+    const float *__restrict__ t_ends, const std::uint8_t *__restrict__ bits, const std::uint8_t *__restrict__ coarse,
+    const std::uint32_t *__restrict__ split, const std::uint32_t *__restrict__ rays_n_samples,
+    const std::uint32_t *__restrict__ rays_startidx, std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs,
+    float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals) {
+    __shared__ std::uint32_t expand[1024];
+    __shared__ std::uint8_t s_coarse[kSmemCoarse];
+    const std::uint32_t end = min(*split, n_rays);
+    const std::uint32_t warp0 = blockIdx.x * (kWarpBlock / 32);
+    if (warp0 >= end) return;
+    for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
+    coarse = stage_coarse(m, coarse, s_coarse);
+    __syncthreads();
+    const unsigned lane = lane_id();
+    const bool block_skip = coarse != nullptr && m.K == 1 && m.const_ds && (m.G & 7u) == 0u;
+    for (std::uint32_t r = warp0 + (threadIdx.x >> 5); r < end; r += gridDim.x * (kWarpBlock / 32)) {
+        const std::uint32_t n = rays_n_samples[r];
+        if (n == 0u) continue;
+        const std::uint32_t start = rays_startidx[r];
+        const V3 o{rays_o[r * 3 + 0], rays_o[r * 3 + 1], rays_o[r * 3 + 2]};
+        const V3 d{rays_d[r * 3 + 0], rays_d[r * 3 + 1], rays_d[r * 3 + 2]};
+        const V3 inv_d{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+        const float t = dss[start];
+        __syncwarp();   // every lane has read the first slot before lane 0 overwrites it
+        float unused = 0.f;
+        warp_march<true>(m, o, d, inv_d, t, t_ends[r], 0.f, n, bits, expand, coarse, block_skip, lane, unused, r,
+                         start, idcs, xyzs, dirs, dss, z_vals);
     }
 }
 
@@ -1089,6 +1322,7 @@ MarchParams make_params(std::uint32_t dns, std::uint32_t K, std::uint32_t G, flo
 
 // ----------------------------------------------------------------------------- launchers
 
+
 int set_march_blocks_per_sm(int n) {
     if (n < 0 || n > kMarchBlocksPerSm) return -1;
     return g_march_blocks_per_sm.exchange(n == 0 ? kMarchBlocksPerSm : n);
@@ -1106,34 +1340,52 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
     NGP_CHECK_ARG(d.bound > 0.f && d.stepsize_portion >= 0.f, "march_rays: bound must be positive, stepsize_portion non-negative");
     NGP_CUDA_TRY(cudaMemsetAsync(next_loc, 0, sizeof(std::uint32_t), stream));
     NGP_CUDA_TRY(cudaMemsetAsync(n_exceeded, 0, sizeof(std::uint32_t), stream));
-    if (queue != nullptr) NGP_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(std::uint32_t), stream));
     const MarchParams m = make_params(d.diagonal_n_steps, d.K, d.G, d.bound, d.stepsize_portion);
     if (d.n_rays > 0) {
-        const unsigned warps_needed = (d.n_rays + 31) / 32;
-        const unsigned blocks_needed = (warps_needed + kMarchBlock / 32 - 1) / (kMarchBlock / 32);
+        // a thread per ray, at most g_march_blocks_per_sm CTAs per SM (the kernel strides over the rest)
+        const unsigned blocks_needed = (d.n_rays + kThreadBlock - 1) / kThreadBlock;
         const unsigned cap = (unsigned)sm_count() * (unsigned)g_march_blocks_per_sm.load(std::memory_order_relaxed);
         const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
-        const std::uint32_t nb = (d.n_rays + kScanRays - 1) / kScanRays;
-        if (ordered && queue != nullptr && nb <= d.total_samples) {
-            // count every ray; allocate in ray order (the block sums borrow the sample-index
-            // buffer's last nb words, which the write pass and the tail zeroing overwrite later);
-            // write the rays that fit
-            march_rays_kernel<kMarchCount><<<grid, kMarchBlock, 0, stream>>>(
-                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
-            std::uint32_t *sums = idcs + (d.total_samples - nb);
-            ray_block_sums_kernel<<<nb, kScanRays, 0, stream>>>(d.n_rays, rays_n_samples, sums);
+        const std::uint32_t n_chunks = (std::uint32_t)blocks_needed;   // count chunks of kThreadBlock rays
+        if (ordered && queue != nullptr && 2ull * n_chunks + 3u <= d.total_samples &&
+            (reinterpret_cast<std::uintptr_t>(idcs) & 3u) == 0u) {
+            // the chunk sums, the chunks' done flags and the frontier borrow the sample-index
+            // buffer's last 2 n_chunks + 3 words, which the write pass and the tail zeroing
+            // overwrite after the fit has read them
+            std::uint32_t *sums = idcs + (d.total_samples - n_chunks);
+            std::uint32_t *done = sums - n_chunks;
+            std::uint32_t *fw = done - 2;   // an 8-byte aligned pair in [done - 3, done)
+            if (reinterpret_cast<std::uintptr_t>(fw) & 7u) --fw;
+            unsigned long long *frontier = reinterpret_cast<unsigned long long *>(fw);
+            NGP_CUDA_TRY(cudaMemsetAsync(done - 3, 0, sizeof(std::uint32_t) * (2 * n_chunks + 3), stream));
+            // warp-per-ray grids: a warp per leading ray; for the writes, at most cap blocks
+            const unsigned wpb = kWarpBlock / 32;
+            const std::uint32_t lead_max = d.n_rays < kLeadMax ? d.n_rays : kLeadMax;
+            const unsigned lead_grid = (lead_max + wpb - 1) / wpb;
+            const unsigned write_need = (d.n_rays + wpb - 1) / wpb;
+            const unsigned write_grid = write_need < cap ? write_need : cap;
+            // the leading rays, then the rest (how many lead: `queue` as the previous call left it)
+            march_lead_kernel<<<lead_grid < cap ? lead_grid : cap, kWarpBlock, 0, stream>>>(
+                d.n_rays, m, rays_o, rays_d, t_starts, t_ends, noises, bits, coarse, queue, ray_is_valid,
+                rays_n_samples, rays_startidx, sums);
+            march_rays_kernel<kMarchCount><<<grid, kThreadBlock, 0, stream>>>(
+                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc, n_exceeded,
+                ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse, sums, done, frontier,
+                queue);
+            NGP_CUDA_TRY(cudaMemsetAsync(queue, 0xff, sizeof(std::uint32_t), stream));
+            const std::uint32_t nb = (d.n_rays + kScanRays - 1) / kScanRays;
             ray_scan_fit_kernel<<<nb, kScanRays, 0, stream>>>(d.n_rays, d.total_samples, sums, ray_is_valid,
-                                                               rays_n_samples, rays_startidx, next_loc, n_exceeded);
-            NGP_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(std::uint32_t), stream));
-            march_rays_kernel<kMarchWrite><<<grid, kMarchBlock, 0, stream>>>(
-                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+                                                               rays_n_samples, rays_startidx, dss, next_loc, n_exceeded,
+                                                               queue);
+            march_write_kernel<<<write_grid, kWarpBlock, 0, stream>>>(d.n_rays, m, rays_o, rays_d, t_ends, bits, coarse,
+                                                                      queue, rays_n_samples, rays_startidx, idcs, xyzs,
+                                                                      dirs, dss, z_vals);
             count_launches(4);
         } else {
-            march_rays_kernel<kMarchAlloc><<<grid, kMarchBlock, 0, stream>>>(
-                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc,
-                n_exceeded, queue, ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse);
+            march_rays_kernel<kMarchAlloc><<<grid, kThreadBlock, 0, stream>>>(
+                d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc, n_exceeded,
+                ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse, nullptr, nullptr,
+                nullptr, nullptr);
             count_launches(1);
         }
     }

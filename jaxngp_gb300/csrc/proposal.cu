@@ -75,15 +75,16 @@ __global__ void __launch_bounds__(256) proposal_rays_kernel(
     const std::uint32_t incl = warp_inclusive_scan(need);
     const std::uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     std::uint32_t base = 0;
-    if (lane_id() == 31 && total > 0) base = atomicAdd(next_loc, total);
+    if (lane_id() == 31)   // a warp without intervals reads the counter for its rays' validity
+        base = total > 0 ? atomicAdd(next_loc, total) : *((volatile std::uint32_t *)next_loc);
     base = __shfl_sync(0xffffffffu, base, 31);
     const std::uint32_t start = base + incl - need;
     const bool fits = hit && (std::uint64_t)start + spr <= total_samples;
     const unsigned over = __ballot_sync(0xffffffffu, hit && !fits);
     if (lane_id() == 0 && over != 0u) atomicAdd(n_exceeded, (std::uint32_t)__popc(over) * spr);
     if (!in) return;
-    if (!hit) {
-        ray_is_valid[r] = true;
+    if (!hit) {   // valid with no samples, unless taken up after the budget filled (marching.cu:135)
+        ray_is_valid[r] = start < total_samples;
         rays_n_samples[r] = 0;
         rays_startidx[r] = 0;
         return;

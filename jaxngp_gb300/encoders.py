@@ -216,3 +216,32 @@ class HashGridEncoder(torch.nn.Module):
         tv = _HashGridTVFn.apply(pos, self.latents, self.table, float(bound), float(self.tv_scale)) \
             if self.tv_scale > 0 else 0.0
         return enc, tv
+
+
+def spherical_harmonics_encoding(coord: torch.Tensor, degree: int) -> torch.Tensor:
+    """shjax.spherical_harmonics_encoding (deps/spherical-harmonics-encoding-jax/src/shjax/
+    __init__.py:120-134): [n, 3] unit directions -> [n, degree^2] float32, the real spherical
+    harmonics of degrees 0..degree-1 (degree in 1..8).  Like the reference's op it has no
+    gradient: directions come from the ray batch, not from parameters."""
+    if coord.dtype != torch.float32 or coord.dim() != 2 or coord.shape[-1] != 3:
+        raise ValueError("coord must be float32 [n, 3]")
+    if int(degree) < 0:
+        raise ValueError("degree must be non-negative")
+    coord = coord.contiguous()
+    n = coord.shape[0]
+    out = torch.empty(n, int(degree) ** 2, dtype=torch.float32, device=coord.device)
+    L.call("spherical_harmonics_encoding_cuda_f32", [coord, out], L.SphericalHarmonicsEncodingDescriptor(n, int(degree)))
+    return out
+
+
+class SphericalHarmonicsEncoder(torch.nn.Module):
+    """models/encoders.py:351-406 (SphericalHarmonicsEncoder and its shjax-backed twin): dirs
+    [..., 3] unit vectors -> [..., L^2]."""
+
+    def __init__(self, L: int):
+        super().__init__()
+        self.L = int(L)
+
+    def forward(self, dirs: torch.Tensor) -> torch.Tensor:
+        flat = dirs.reshape(-1, 3)
+        return spherical_harmonics_encoding(flat, self.L).view(*dirs.shape[:-1], self.L * self.L)

@@ -101,10 +101,10 @@ class CpuTrainer:
         gt = rgba[:, :3] * rgba[:, 3:] + bg * (1 - rgba[:, 3:])
         self._t("rays", t)
         t = time.perf_counter()
-        # every ray is counted before slots are taken (as the GPU marcher does; a legal schedule of
-        # the reference's kernel): rays without samples are valid, rays that do not fit are not
+        # the reference's kernel run one thread at a time in ray order (the training march's
+        # schedule): the rays before the budget filled keep their results, later rays are dropped
         m, valid, ns, st, idcs, xyzs, dirs, dss, zs = V.march_rays(S, self.dns, 1, self.G, sc.bound, 0.0, o, d, t0, t1,
-                                                                   noise, self.bits, early_exit=False)
+                                                                   noise, self.bits, early_exit=True)
         used = int(m)
         self._t("march", t)
         t = time.perf_counter()

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY; run in a container that holds the reference checkout:
 
-    python tests/golden/make_golden.py REFERENCE_ROOT [volrend] [field] [tv]
+    python tests/golden/make_golden.py REFERENCE_ROOT [volrend] [field] [tv] [sh]
 
 (REFERENCE_ROOT may be left out when the environment variable NGP_REFERENCE_ROOT names it.)
 
@@ -12,6 +12,8 @@ TEST INFRASTRUCTURE ONLY; run in a container that holds the reference checkout:
 * ``hashgrid_*.npz`` and ``field_*.npz``: outputs of the reference's ``HashGridEncoder``
   (models/encoders.py) and ``make_nerf_ngp`` field (models/nerfs.py), executed unmodified on the
   NumPy stand-in for jax/flax in ``jax_numpy_shim.py``.
+* ``sh_encodings.npz``: the reference's ``SphericalHarmonicsEncoder`` (models/encoders.py) for
+  degrees 1..8, run the same way.
 * ``tv_*.npz``: the total-variation term the same ``HashGridEncoder`` returns with tv_scale > 0.
 
 ``python tests/golden/make_golden.py REF tv`` regenerates only the ``tv_*`` files.
@@ -188,18 +190,38 @@ def total_variation(ref_root: str):
         _save(f"{case['tag']}.npz", tv=np.asarray(tv, np.float32), **{k: v for k, v in case.items() if k != "tag"})
 
 
+def spherical_harmonics(ref_root: str):
+    """The reference's SphericalHarmonicsEncoder (models/encoders.py:361-406) for every degree it
+    supports (1..8) on unit directions: random ones and the axis-aligned and diagonal ones."""
+    import jax_numpy_shim as shim
+    shim.install()
+    enc_mod = shim.load_reference_module("models.encoders", os.path.join(ref_root, "models", "encoders.py"))
+    rng = np.random.default_rng(41)
+    d = rng.normal(size=(300, 3))
+    edge = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [1, 1, 1], [-1, 1, -1],
+                     [1, -1, 0], [0, 1, 1]], np.float64)
+    d = np.concatenate([edge, d])
+    dirs = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
+    out = {"dirs": dirs}
+    for L in range(1, 9):
+        out[f"deg{L}"] = np.asarray(enc_mod.SphericalHarmonicsEncoder(L=L)(dirs), np.float32)
+    _save("sh_encodings.npz", **out)
+
+
 if __name__ == "__main__":
     args = sys.argv[1:]
-    if args and args[0] not in ("volrend", "field", "tv"):
+    if args and args[0] not in ("volrend", "field", "tv", "sh"):
         ref = args.pop(0)
     elif os.environ.get("NGP_REFERENCE_ROOT"):
         ref = os.environ["NGP_REFERENCE_ROOT"]
     else:
-        sys.exit("usage: make_golden.py REFERENCE_ROOT [volrend] [field] [tv]  (or set NGP_REFERENCE_ROOT)")
-    parts = args or ["volrend", "field", "tv"]
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [volrend] [field] [tv] [sh]  (or set NGP_REFERENCE_ROOT)")
+    parts = args or ["volrend", "field", "tv", "sh"]
     if "volrend" in parts:
         volrend(ref)
     if "field" in parts:
         field(ref)
     if "tv" in parts:
         total_variation(ref)
+    if "sh" in parts:
+        spherical_harmonics(ref)

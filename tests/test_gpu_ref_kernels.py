@@ -169,7 +169,12 @@ def test_integrate_vs_reference_gpu(R):
         m = torch.zeros(1, dtype=torch.int32, device="cuda")
         rgbd, opac = torch.empty(n, 4, device="cuda"), torch.empty(n, device="cuda")
         call("integrate_rays", [st, ns, bgs_d, dss, zs, drgbs_d, m, rgbd, opac], lib.IntegratingDescriptor(n, S))
-        g_bg, g_z, g_c = torch.empty(n, 3, device="cuda"), torch.empty(S, device="cuda"), torch.empty(S, 4, device="cuda")
+        # the reference's backward writes no gradient for the samples after a ray terminated
+        # (integrating.cu:177, its loop ends there), so its buffers start zeroed; ours start as
+        # NaN, and every sample's gradient must be written (zero after termination)
+        fill = float("nan") if call is lib.call else 0.0
+        g_bg, g_z, g_c = (torch.full((n, 3), fill, device="cuda"), torch.full((S,), fill, device="cuda"),
+                          torch.full((S, 4), fill, device="cuda"))
         call("integrate_rays_backward", [st, ns, bgs_d, dss, zs, drgbs_d, rgbd, opac, g, g_bg, g_z, g_c],
              lib.IntegratingBackwardDescriptor(n, S, 0.3))
         fw.append((int(host(m)[0]), host(rgbd), host(opac)))

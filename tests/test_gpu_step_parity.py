@@ -145,7 +145,7 @@ def test_train_step_matches_cpu_restatement(scene):
     # ---- march (bit-exact, per ray) on the GPU's rays
     G = cfg.G
     m, valid, ns, st, idcs, xyzs, dirs, dss, zs = V.march_rays(tr.S, cfg.diagonal_n_steps, 1, G, tr.bound, 0.0, o_g, d_g,
-                                                                t0_g, t1_g, noise, bits, early_exit=False)
+                                                                t0_g, t1_g, noise, bits, early_exit=True)
     valid_g, ns_g, st_g = h(tr.valid), h(tr.n_samples), h(tr.startidx)
     nv = int(valid.sum())
     assert np.array_equal(valid_g, valid) and np.array_equal(ns_g, ns)

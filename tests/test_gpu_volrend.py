@@ -287,7 +287,7 @@ def test_march_rays_inference_multiwarp_vs_oracle(vr):
         idx_h, nri_h, t_h = ref[1], ref[0], ref[3]
 
 
-def _march_train(z, total, coarse=None):
+def _march_train(z, total, coarse=None, queue=None):
     from jaxngp_gb300 import _lib as L
     n = z["rays_o"].shape[0]
     i32 = dict(dtype=torch.int32, device="cuda")
@@ -295,7 +295,7 @@ def _march_train(z, total, coarse=None):
            torch.empty(n, **i32), torch.empty(n, **i32), torch.empty(total, **i32),
            torch.empty(total, 3, device="cuda"), torch.empty(total, 3, device="cuda"), torch.empty(total, device="cuda"),
            torch.empty(total, device="cuda")]
-    queue = torch.zeros(1, **i32)
+    queue = torch.zeros(1, **i32) if queue is None else queue
     d = L.MarchingDescriptor(n, total, int(z["diagonal_n_steps"]), int(z["K"]), int(z["G"]), float(z["bound"]),
                              float(z["stepsize_portion"]))
     L.call("ngp_march_rays_train", [dev(z["rays_o"]), dev(z["rays_d"]), dev(z["t_starts"]), dev(z["t_ends"]),
@@ -303,53 +303,91 @@ def _march_train(z, total, coarse=None):
     return [host(x) for x in out]
 
 
+def _assert_sequential(z, total, got):
+    """ngp_march_rays_train's buffers and counters equal, bit for bit, the reference kernel's run
+    one thread at a time in ray order (the oracle's march with early_exit: a ray that starts
+    after the buffer filled is dropped, marching.cu:135)."""
+    (m, valid, ns, st, idcs, xyzs, dirs, dss, zs), cnt = V.march_rays(
+        total, z["diagonal_n_steps"], z["K"], z["G"], z["bound"], z["stepsize_portion"], z["rays_o"], z["rays_d"],
+        z["t_starts"], z["t_ends"], z["noises"], z["bitfield"], return_counters=True, early_exit=True)
+    c0, c1 = int(got[0][0]), int(got[1][0])
+    assert (c0, c1) == (int(cnt[0]), int(cnt[1]))
+    for name, x, y in zip(("valid", "n_samples", "startidx", "idcs", "xyzs", "dirs", "dss", "z_vals"), got[2:],
+                          (valid, ns, st, idcs, xyzs, dirs, dss, zs)):
+        assert np.array_equal(x, y), name
+    return ns, valid
+
+
+def _first_cut(full_n, live, total):
+    """The first ray the one-at-a-time schedule drops or cannot fit, or None."""
+    prefix = np.concatenate([[0], np.cumsum(full_n.astype(np.int64))[:-1]])
+    cut = (prefix >= total) | ((full_n > 0) & (prefix + full_n > total))
+    idx = np.nonzero(cut)[0]
+    return int(idx[0]) if idx.size else None
+
+
 @pytest.mark.parametrize("budget_frac", [None, 0.3, 0.02])
 def test_march_rays_train_variant(vr, budget_frac):
-    """The training marcher: without overflow it equals the oracle ray by ray; with overflow every
-    ray that fits carries its full sample run, every sample-less ray is valid, every other ray is
-    not, and the samples written are exactly next - exceeded and fill [0, measured); the rays that
-    fit are the ray-order prefix of the counts, and two runs give the same buffers."""
+    """The training marcher is the reference kernel under the one-at-a-time ray-order schedule:
+    without overflow it is the plain march, with overflow the rays before the budget filled keep
+    their results, the one that does not fit is invalid with its samples left out, and every later
+    ray is dropped.  Every buffer and both counters equal the oracle's, and two runs agree."""
     rng = np.random.default_rng(21)
     n = 6000
     o, d, t0, t1 = make_rays(rng, n, 1.0)
     noise = rng.uniform(size=n).astype(np.float32)
     bits = random_bitfield(rng, 1, 64, 0.3)
-    ref = V.march_rays(1 << 24, 1024, 1, 64, 1.0, 0.0, o, d, t0, t1, noise, bits)
-    full_n = ref[2]
+    full_n = V.march_rays(1 << 24, 1024, 1, 64, 1.0, 0.0, o, d, t0, t1, noise, bits)[2]
     total = (1 << 24) if budget_frac is None else max(1, int(full_n.sum() * budget_frac))
     z = dict(diagonal_n_steps=1024, K=1, G=64, bound=1.0, stepsize_portion=0.0, rays_o=o, rays_d=d, t_starts=t0,
              t_ends=t1, noises=noise, bitfield=bits)
-    c0, c1, valid, ns, st, idcs, xyzs, dirs, dss, zs = _march_train(z, total)
-    m = int(c0[0]) - int(c1[0])
-    assert ns.sum() == m and m <= total
-    live = t1 > t0
-    fit = ns > 0
-    assert np.array_equal(valid, (live & (full_n == 0)) | fit)
-    assert np.array_equal(ns[fit], full_n[fit])
-    assert np.all(~valid[(full_n > 0) & ~fit])
-    for r in np.nonzero(fit)[0][::7]:
-        a, b, k = st[r], ref[3][r], ns[r]
-        assert np.array_equal(xyzs[a:a + k], ref[5][b:b + k]) and np.array_equal(zs[a:a + k], ref[8][b:b + k])
-    if total < (1 << 24):
-        assert not idcs[m:].any() and not zs[m:].any()
+    got = _march_train(z, total)
+    ns, valid = _assert_sequential(z, total, got)
     if budget_frac is None:
-        assert np.array_equal(valid, ref[1]) and np.array_equal(ns, full_n)
-    # rays fit in ray order: ray r fits when the counts of the rays before it and its own fit the
-    # budget, at the start their sum gives; the result does not depend on the schedule
-    prefix = np.concatenate([[0], np.cumsum(full_n.astype(np.int64))[:-1]])
-    want_fit = (full_n > 0) & (prefix + full_n <= total)
-    assert np.array_equal(fit, want_fit)
-    assert np.array_equal(st[fit], prefix[fit].astype(np.uint32))
+        assert np.array_equal(ns, full_n)
+    else:
+        q = _first_cut(full_n, t1 > t0, total)
+        assert q is not None and not valid[q:].any() and (ns[:q] == full_n[:q]).all()
     again = _march_train(z, total)
-    for x, y in zip(again, (c0, c1, valid, ns, st, idcs, xyzs, dirs, dss, zs)):
+    for x, y in zip(again, got):
         assert np.array_equal(x, y)
+
+
+def test_march_rays_train_many_chunks(vr):
+    """A batch of many more rays than fit (2^17 rays, a budget of 1% of their samples), with the
+    leading rays' launch covering the fit, short of it, or sized by a first call: the result is
+    the one-at-a-time schedule's, bit for bit, and the call leaves its first dropped or unfit ray
+    in the queue word."""
+    rng = np.random.default_rng(23)
+    n = 1 << 17
+    o, d, t0, t1 = make_rays(rng, n, 1.0)
+    noise = rng.uniform(size=n).astype(np.float32)
+    bits = random_bitfield(rng, 1, 64, 0.3)
+    full_n = V.march_rays(1 << 26, 1024, 1, 64, 1.0, 0.0, o, d, t0, t1, noise, bits, early_exit=False)[2]
+    total = int(full_n.astype(np.int64).sum() // 100)
+    z = dict(diagonal_n_steps=1024, K=1, G=64, bound=1.0, stepsize_portion=0.0, rays_o=o, rays_d=d, t_starts=t0,
+             t_ends=t1, noises=noise, bitfield=bits)
+    q = _first_cut(full_n, t1 > t0, total)
+    assert q is not None and q > 1024
+    queue = torch.zeros(1, dtype=torch.int32, device="cuda")
+    # a first call (8192 leading rays), the word it leaves (1.25 q + 512), and a word that makes
+    # the lead fall short (513 rays: the rest find the budget full only as the frontier moves)
+    for word in (0, None, 1):
+        if word is not None:
+            queue.fill_(word)
+        got = _march_train(z, total, queue=queue)
+        assert int(queue[0]) == q
+        _assert_sequential(z, total, got)
+        print(f"queue word {word}: {int(got[0][0])} samples requested, {int((got[3] > 0).sum())} of {n} rays fit, "
+              f"first cut at ray {q}")
 
 
 @pytest.mark.parametrize("budget_frac", [None, 0.3])
 def test_march_rays_train_coarse_shortcut(vr, budget_frac):
     """With coarse occupancy blocks the training marcher finishes rays that cross no occupied
-    block at once; on a grid of a few blobs (most rays miss them) every ray's result is still the
-    oracle's, bit for bit, and the same as without the shortcut."""
+    block at once and crosses empty blocks in one step; on a grid of a few blobs (most rays miss
+    them) every buffer is still the one-at-a-time schedule's, bit for bit, and the same as without
+    the coarse grid."""
     from jaxngp_gb300 import _lib as L
     from tests.test_oracle_proposal import blob_bitfield
     rng = np.random.default_rng(22)
@@ -357,8 +395,7 @@ def test_march_rays_train_coarse_shortcut(vr, budget_frac):
     o, d, t0, t1 = make_rays(rng, n, 1.0)
     noise = rng.uniform(size=n).astype(np.float32)
     bits = blob_bitfield(G, [(0.3, -0.2, 0.1), (-0.4, 0.35, -0.3), (0.05, 0.5, -0.5)], 0.12)
-    ref = V.march_rays(1 << 24, 1024, 1, G, 1.0, 0.0, o, d, t0, t1, noise, bits, early_exit=False)
-    full_n = ref[2]
+    full_n = V.march_rays(1 << 24, 1024, 1, G, 1.0, 0.0, o, d, t0, t1, noise, bits, early_exit=False)[2]
     assert (full_n == 0).mean() > 0.3 and (full_n > 0).sum() > 100
     coarse = torch.zeros((G // 8) ** 3, dtype=torch.uint8, device="cuda")
     L.call("ngp_proposal_coarse", [dev(bits), coarse],
@@ -367,18 +404,10 @@ def test_march_rays_train_coarse_shortcut(vr, budget_frac):
     z = dict(diagonal_n_steps=1024, K=1, G=G, bound=1.0, stepsize_portion=0.0, rays_o=o, rays_d=d, t_starts=t0,
              t_ends=t1, noises=noise, bitfield=bits)
     with_c = _march_train(z, total, coarse)
-    c0, c1, valid, ns, st, idcs, xyzs, dirs, dss, zs = with_c
-    fit = ns > 0
-    assert np.array_equal(ns[fit], full_n[fit])
-    live = t1 > t0
-    assert np.array_equal(valid, (live & (full_n == 0)) | fit)
-    for r in np.nonzero(fit)[0][::5]:
-        a, b, k = st[r], ref[3][r], ns[r]
-        assert np.array_equal(xyzs[a:a + k], ref[5][b:b + k]) and np.array_equal(zs[a:a + k], ref[8][b:b + k])
-    if budget_frac is None:
-        assert np.array_equal(ns, full_n) and np.array_equal(valid, ref[1])
-        without = _march_train(z, total)
-        assert np.array_equal(without[3], ns) and np.array_equal(without[2], valid)
+    _assert_sequential(z, total, with_c)
+    without = _march_train(z, total)
+    for x, y in zip(with_c, without):
+        assert np.array_equal(x, y)
 
 
 @pytest.mark.parametrize("n_blobs,radius,cam", [(3, 0.12, 4.0), (20, 0.1, 4.0), (60, 0.08, 4.0), (20, 0.1, 2.0)])
