@@ -46,6 +46,11 @@ unsigned long long ngp_kernel_launches(void);
  * recorded a device-side error since the last call -- a tensor-core kernel whose bounded wait for
  * its MMAs ran out -- else NGP_OK, or NGP_ERR_CUDA if the synchronisation failed. */
 int ngp_device_status(void);
+/* Test hook of the failure path above: one thread waits, with the tensor-core kernels' bounded
+ * wait, on an mbarrier that nothing completes; after `polls` polls (1..2^20) it gives up and
+ * records the device error, which the next ngp_device_status() reports once.  Returns the launch
+ * status. */
+int ngp_selftest_bounded_wait(cudaStream_t stream, unsigned int polls);
 /* At most this many CTAs per SM for the marches (march_rays, ngp_march_rays_train,
  * ngp_march_rays_fallback) on every later call on any thread -- they stride over the rest of the
  * rays; 0 restores the default (10: no limit below what fits).

@@ -62,6 +62,7 @@ int launch_mlp_bf16_density(cudaStream_t, std::uint32_t, const float *, const fl
 int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                              const float *, const float *, const float *, float *, float *, unsigned *);
 int device_status();
+int launch_bounded_wait_selftest(cudaStream_t stream, std::uint32_t polls);
 int set_march_blocks_per_sm(int);
 int launch_proposal_judge(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t, float, const float *,
                           const float *, const float *, const std::uint32_t *, const float *, const float *, const float *,
@@ -207,6 +208,9 @@ const char *ngp_last_status_message(void) { return t_message; }
 int ngp_abi_version(void) { return 1; }
 unsigned long long ngp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 int ngp_device_status(void) { return device_status(); }
+int ngp_selftest_bounded_wait(cudaStream_t stream, unsigned int polls) {
+    return launch_bounded_wait_selftest(stream, polls);
+}
 int ngp_set_march_blocks_per_sm(int n) { return set_march_blocks_per_sm(n); }
 
 NGP_ENTRY(pack_density_into_bits) {

@@ -1001,6 +1001,25 @@ int launch_prop_f16_forward(cudaStream_t stream, std::uint32_t n, const std::uin
     return launch_status();
 }
 
+namespace {
+// The bounded wait of the tensor-core kernels on an mbarrier that nothing completes: it gives up
+// after `polls` polls and records the error word, as a kernel whose MMAs never finished would.
+__global__ void bounded_wait_selftest_kernel(std::uint32_t polls) {
+    __shared__ __align__(8) std::uint64_t bar;
+    if (threadIdx.x != 0) return;
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+    if (!tc::mbar_wait(&bar, 0, polls)) atomicOr(&g_device_error, 1u);
+}
+}  // namespace
+
+int launch_bounded_wait_selftest(cudaStream_t stream, std::uint32_t polls) {
+    NGP_CHECK_ARG(polls > 0 && polls <= (1u << 20), "bounded-wait self-test: polls must be in [1, 2^20]");
+    bounded_wait_selftest_kernel<<<1, 32, 0, stream>>>(polls);
+    count_launches(1);
+    return launch_status();
+}
+
 // Reads and clears the device error word (synchronises the device).
 int device_status() {
     unsigned v = 0;
