@@ -13,8 +13,11 @@ the public API with the pixel indices copied from pinned host memory and the ste
 back every step.  `forms` repeats the measurement for the BF16 tensor-core field MLP and for the
 learned proposal sampler with it (also with a 16-bit table copy and 16-bit encodings, BF16 or
 FP16 under a dynamic loss scale), each with the held-out PSNR of the trained field and 1080p
-inference FPS, and `learned_proposal_vs_plain` gives each proposal form's throughput ratio and
-PSNR difference against the plain step (with samples/s and rays-with-samples/s beside rays/s).
+inference FPS; `forms_vs_plain` gives every form's throughput ratio and PSNR difference against
+the plain step, and the time to the plain step's PSNR of the fastest form within 0.1 dB of it;
+`learned_proposal_vs_plain` adds, per proposal form, rays-with-samples/s and the proposal
+renderer's 1080p ratio.  The plain step fits its rays in ray order (the reference kernel run one
+thread at a time), so its valid rays are a prefix of the batch: about the rays the budget takes.
 The occupancy grid starts as the reference's does (mark_untrained_density_grid, then the learned
 refresh on its cadence) unless --occupancy-init analytic.  Three further blocks: `config0_encoder`
 (the hash-grid encoder alone at 2^18 points, both level tables, with its roofline and a NumPy
@@ -86,7 +89,7 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=1 << 14, help="batch of the CPU baseline's sample steps")
     p.add_argument("--cpu-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--forms", default="fp32-march,bf16-march,bf16-proposal,bf16x-proposal,fp16x-proposal,bf16x-proposal-fb",
+    p.add_argument("--forms", default="fp32-march,bf16-march,bf16x-march,bf16-proposal,bf16x-proposal,fp16x-proposal,bf16x-proposal-fb",
                    help="training forms to run, the first is the headline: fp32-march (the reference's "
                         "algorithm, FP32 SIMT field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
                         "(learned proposal sampler + BF16 MLP); the x forms (bf16x-*, fp16x-*) also gather from a "
@@ -953,8 +956,14 @@ def main():
                         for f, r in results.items()}
         if "fp32-march" in results:
             a = results["fp32-march"]
-            cmp = {}
+            cmp, allcmp = {}, {}
             for f, b in results.items():
+                if f == "fp32-march":
+                    continue
+                allcmp[f] = {"train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
+                             "e2e_ratio": round(b["e2e"]["value"] / a["e2e"]["value"], 3),
+                             "samples_per_s_ratio": round(b["batch"]["samples_per_s"] / a["batch"]["samples_per_s"], 3),
+                             "delta_psnr_db": round(b["quality"]["psnr_heldout"] - a["quality"]["psnr_heldout"], 3)}
                 if FORMS[f][1] != "proposal":
                     continue
                 cmp[f] = {"train_rays_per_s_ratio": round(b["value"] / a["value"], 3),
@@ -971,9 +980,14 @@ def main():
                         b["quality"]["psnr_heldout_proposal_renderer"] - a["quality"]["psnr_heldout"], 3)
             if cmp:
                 out["learned_proposal_vs_plain"] = {"plain": "fp32-march", **cmp}
-            if cmp and args.equal_psnr_steps > 0:
-                fastest = max(cmp, key=lambda f: results[f]["value"])
-                out["learned_proposal_vs_plain"]["at_equal_psnr"] = equal_psnr(args, data, "fp32-march", fastest)
+            if allcmp:
+                # every form against the plain FP32 step; time to the plain step's PSNR for the
+                # fastest form that trains within 0.1 dB of it at equal steps
+                out["forms_vs_plain"] = {"plain": "fp32-march", **allcmp}
+                ok = [f for f in allcmp if allcmp[f]["delta_psnr_db"] >= -0.1]
+                if ok and args.equal_psnr_steps > 0:
+                    fastest = max(ok, key=lambda f: results[f]["value"])
+                    out["forms_vs_plain"]["at_equal_psnr"] = equal_psnr(args, data, "fp32-march", fastest)
     if rank == 0 and not args.no_encoder_block:
         out["config0_encoder"] = encoder_block(args, cores)
     if args.scene == "blobs64" and args.config4_steps > 0:
