@@ -123,7 +123,12 @@ int pack_density_into_bits_status(cudaStream_t stream, void **buffers, const cha
  * occupancy_bitfield u8[K*G^3/8] -> next_sample_write_location u32[1],
  * number_of_exceeded_samples u32[1], ray_is_valid bool[R], rays_n_samples u32[R],
  * rays_sample_startidx u32[R], idcs u32[S], xyzs f32[S,3], dirs f32[S,3], dss f32[S],
- * z_vals f32[S]; opaque: MarchingDescriptor. */
+ * z_vals f32[S]; opaque: MarchingDescriptor.  The result is the reference kernel's under the
+ * schedule in which its threads run one at a time in ray order (as ngp_march_rays_train below,
+ * without a queue word or coarse blocks): deterministic, and the reference's own result whenever
+ * the budget does not overflow; with overflow the reference's result depends on its schedule.
+ * With fewer than 2 ceil(R / 256) + 3 sample slots the rays take slots in the order their warps
+ * finish counting, as in the reference. */
 void march_rays(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int march_rays_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 

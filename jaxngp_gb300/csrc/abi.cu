@@ -226,7 +226,7 @@ NGP_ENTRY(ngp_packbits_scalar) {
 NGP_ENTRY(march_rays) {
     NGP_DESC(MarchingDescriptor, d);
     return launch_march_rays(stream, d, CF32(0), CF32(1), CF32(2), CF32(3), CF32(4), CU8(5), U32(6), U32(7), B8(8),
-                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), nullptr, false, nullptr);
+                             U32(9), U32(10), U32(11), F32(12), F32(13), F32(14), F32(15), nullptr, true, nullptr);
 }
 
 NGP_ENTRY(ngp_march_rays_train) {

@@ -361,6 +361,59 @@ __device__ __forceinline__ void publish_chunk(std::uint32_t c, std::uint32_t sum
     }
 }
 
+// The write pass of one ray (marching.cu:224-267), one thread: its n samples from slot `start`,
+// marching from t, the t of its first occupied sample (the march state is t alone).
+__device__ __forceinline__ void write_ray_thread(const MarchParams &m, std::uint32_t r, std::uint32_t start,
+                                                 std::uint32_t n, float t, float t1, V3 o, V3 d, V3 inv_d,
+                                                 const std::uint8_t *__restrict__ bits, const std::uint32_t *expand,
+                                                 const std::uint8_t *__restrict__ coarse, bool block_skip,
+                                                 std::uint32_t *__restrict__ idcs, float *__restrict__ xyzs,
+                                                 float *__restrict__ dirs, float *__restrict__ dss,
+                                                 float *__restrict__ z_vals) {
+    std::uint32_t k = 0, it = 0;
+    auto put = [&](V3 p, float dsj, float tj) {
+        const std::uint32_t s = start + k;
+        idcs[s] = r;
+        xyzs[(std::size_t)s * 3 + 0] = p.x;
+        xyzs[(std::size_t)s * 3 + 1] = p.y;
+        xyzs[(std::size_t)s * 3 + 2] = p.z;
+        dirs[(std::size_t)s * 3 + 0] = d.x;
+        dirs[(std::size_t)s * 3 + 1] = d.y;
+        dirs[(std::size_t)s * 3 + 2] = d.z;
+        dss[s] = dsj;
+        z_vals[s] = tj;
+        ++k;
+    };
+    while (k < n && t < t1 && it < kMaxMarchIters) {
+        const V3 pos = at(o, d, t);
+        const float ds = calc_ds(t, m);
+        V3 g;
+        float mb;
+        if (occupied_at(m, pos, ds, bits, g, mb, expand)) {
+            put(pos, ds, t);
+            t = t + ds;
+            if (m.K == 1) {
+                const std::uint32_t key = cell_key(m, g);
+                while (k < n && t < t1 && it < kMaxMarchIters) {
+                    const V3 p2 = at(o, d, t);
+                    if (cell_key_at(m, p2) != key) break;
+                    const float ds2 = calc_ds(t, m);
+                    put(p2, ds2, t);
+                    t = t + ds2;
+                    ++it;
+                }
+            }
+        } else {
+            float tb;
+            if (block_skip && skip_block(m, t, g, pos, o, d, inv_d, coarse, tb))
+                t = tb;
+            else
+                t = skip_empty(m, t, g, mb, pos, d, inv_d);
+        }
+        ++it;
+    }
+}
+
 // One ray of march_rays_kernel (every lane of the warp calls it together; r >= n_rays idles).
 // Returns the ray's count (as far as it was counted) in kMarchCount mode, else 0.
 template <int kMode>
@@ -469,52 +522,9 @@ __device__ __forceinline__ std::uint32_t march_one(
     const std::uint32_t over = warp_sum((want && !fits) ? n : 0u);
     if (lane_id() == 0 && over > 0u) atomicAdd(n_exceeded, over);
     // ---- write pass (marching.cu:224-267), from the first occupied sample
-    if (want && fits) {
-        t = t_hit;
-        it = 0;
-        std::uint32_t k = 0;
-        auto put = [&](V3 p, float dsj, float tj) {
-            const std::uint32_t s = start + k;
-            idcs[s] = r;
-            xyzs[(std::size_t)s * 3 + 0] = p.x;
-            xyzs[(std::size_t)s * 3 + 1] = p.y;
-            xyzs[(std::size_t)s * 3 + 2] = p.z;
-            dirs[(std::size_t)s * 3 + 0] = d.x;
-            dirs[(std::size_t)s * 3 + 1] = d.y;
-            dirs[(std::size_t)s * 3 + 2] = d.z;
-            dss[s] = dsj;
-            z_vals[s] = tj;
-            ++k;
-        };
-        while (k < n && t < t1 && it < kMaxMarchIters) {
-            const V3 pos = at(o, d, t);
-            const float ds = calc_ds(t, m);
-            V3 g;
-            float mb;
-            if (occupied_at(m, pos, ds, bits, g, mb, expand)) {
-                put(pos, ds, t);
-                t = t + ds;
-                if (m.K == 1) {
-                    const std::uint32_t key = cell_key(m, g);
-                    while (k < n && t < t1 && it < kMaxMarchIters) {
-                        const V3 p2 = at(o, d, t);
-                        if (cell_key_at(m, p2) != key) break;
-                        const float ds2 = calc_ds(t, m);
-                        put(p2, ds2, t);
-                        t = t + ds2;
-                        ++it;
-                    }
-                }
-            } else {
-                float tb;
-                if (block_skip && skip_block(m, t, g, pos, o, d, inv_d, coarse, tb))
-                    t = tb;
-                else
-                    t = skip_empty(m, t, g, mb, pos, d, inv_d);
-            }
-            ++it;
-        }
-    }
+    if (want && fits)
+        write_ray_thread(m, r, start, n, t_hit, t1, o, d, inv_d, bits, expand, coarse, block_skip, idcs, xyzs, dirs,
+                         dss, z_vals);
     return 0u;
 }
 
@@ -536,10 +546,10 @@ __global__ void __launch_bounds__(kThreadBlock) march_rays_kernel(
     __shared__ std::uint32_t red[kThreadBlock / 32];
     __shared__ int s_full;
     const std::uint32_t n_chunks = (n_rays + kThreadBlock - 1) / kThreadBlock;
-    const std::uint32_t c_lo = kMode == kMarchCount ? lead_chunks(*split, n_rays) : 0u;
+    const std::uint32_t c_lo = kMode == kMarchCount ? lead_chunks(split != nullptr ? *split : 0u, n_rays) : 0u;
     if (c_lo + blockIdx.x >= n_chunks) return;
     for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
-    if (kMode == kMarchCount) {
+    if constexpr (kMode == kMarchCount) {
         // the leading chunks are done (an earlier launch): their sum starts the frontier
         std::uint32_t a = 0;
         for (std::uint32_t c = threadIdx.x; c < c_lo; c += kThreadBlock) a += chunk_sums[c];
@@ -653,7 +663,7 @@ __global__ void __launch_bounds__(kScanRays) ray_scan_fit_kernel(
         if (threadIdx.x == 0) {
             if (a > 0u) atomicAdd(next_loc, a);
             if (o > 0u) atomicAdd(n_exceeded, o);
-            if (s_first != 0xffffffffu) atomicMin(split, s_first);
+            if (s_first != 0xffffffffu && split != nullptr) atomicMin(split, s_first);
         }
     }
 }
@@ -960,7 +970,8 @@ __global__ void __launch_bounds__(kWarpBlock) march_lead_kernel(
     std::uint32_t *__restrict__ chunk_sums) {
     __shared__ std::uint32_t expand[1024];
     __shared__ std::uint8_t s_coarse[kSmemCoarse];
-    const std::uint32_t lead = min(lead_chunks(*split, n_rays) * (std::uint32_t)kThreadBlock, n_rays);
+    const std::uint32_t lead =
+        min(lead_chunks(split != nullptr ? *split : 0u, n_rays) * (std::uint32_t)kThreadBlock, n_rays);
     const std::uint32_t warp0 = blockIdx.x * (kWarpBlock / 32);
     if (warp0 >= lead) return;
     for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
@@ -990,8 +1001,10 @@ __global__ void __launch_bounds__(kWarpBlock) march_lead_kernel(
 }
 
 // The samples of the rays that fit (marching.cu:224-267), a warp per ray, from the t of each
-// ray's first sample (left in its first slot of dss); the rays that fit all come before the
-// first dropped or unfit ray (`split`).
+// ray's first sample (left in its first slot of dss); the rays that fit all come before the first
+// dropped or unfit ray (`split`, all rays when null).  (A thread per ray where many rays of a
+// chunk fit was measured slower on both a training budget and an unbounded one: the rays that fit
+// are long, ~250 samples, in both.)
 __global__ void __launch_bounds__(kWarpBlock) march_write_kernel(
     std::uint32_t n_rays, MarchParams m, const float *__restrict__ rays_o, const float *__restrict__ rays_d,
     const float *__restrict__ t_ends, const std::uint8_t *__restrict__ bits, const std::uint8_t *__restrict__ coarse,
@@ -1000,7 +1013,7 @@ __global__ void __launch_bounds__(kWarpBlock) march_write_kernel(
     float *__restrict__ dirs, float *__restrict__ dss, float *__restrict__ z_vals) {
     __shared__ std::uint32_t expand[1024];
     __shared__ std::uint8_t s_coarse[kSmemCoarse];
-    const std::uint32_t end = min(*split, n_rays);
+    const std::uint32_t end = split != nullptr ? min(*split, n_rays) : n_rays;
     const std::uint32_t warp0 = blockIdx.x * (kWarpBlock / 32);
     if (warp0 >= end) return;
     for (std::uint32_t v = threadIdx.x; v < m.G; v += blockDim.x) expand[v] = expand_bits(v);
@@ -1347,7 +1360,7 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
         const unsigned cap = (unsigned)sm_count() * (unsigned)g_march_blocks_per_sm.load(std::memory_order_relaxed);
         const unsigned grid = blocks_needed < cap ? blocks_needed : cap;
         const std::uint32_t n_chunks = (std::uint32_t)blocks_needed;   // count chunks of kThreadBlock rays
-        if (ordered && queue != nullptr && 2ull * n_chunks + 3u <= d.total_samples &&
+        if (ordered && 2ull * n_chunks + 3u <= d.total_samples &&
             (reinterpret_cast<std::uintptr_t>(idcs) & 3u) == 0u) {
             // the chunk sums, the chunks' done flags and the frontier borrow the sample-index
             // buffer's last 2 n_chunks + 3 words, which the write pass and the tail zeroing
@@ -1372,7 +1385,7 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
                 d.n_rays, d.total_samples, m, rays_o, rays_d, t_starts, t_ends, noises, bits, next_loc, n_exceeded,
                 ray_is_valid, rays_n_samples, rays_startidx, idcs, xyzs, dirs, dss, z_vals, coarse, sums, done, frontier,
                 queue);
-            NGP_CUDA_TRY(cudaMemsetAsync(queue, 0xff, sizeof(std::uint32_t), stream));
+            if (queue != nullptr) NGP_CUDA_TRY(cudaMemsetAsync(queue, 0xff, sizeof(std::uint32_t), stream));
             const std::uint32_t nb = (d.n_rays + kScanRays - 1) / kScanRays;
             ray_scan_fit_kernel<<<nb, kScanRays, 0, stream>>>(d.n_rays, d.total_samples, sums, ray_is_valid,
                                                                rays_n_samples, rays_startidx, dss, next_loc, n_exceeded,

@@ -130,8 +130,9 @@ def test_march_rays_vs_oracle(vr, seed, K, G, bound, sp, n):
 
 
 def test_march_rays_overflow(vr):
-    """A sample budget below demand: the rays that fit are exactly the warps' prefix; nothing past
-    `measured` is written; counters obey measured = next - exceeded."""
+    """A sample budget below demand: the drop-in march gives the reference kernel's result under
+    its one-at-a-time ray-order schedule (every buffer and both counters), so nothing past
+    `measured` is written and the counters obey measured = next - exceeded."""
     rng = np.random.default_rng(3)
     n = 4096
     o, d, t0, t1 = make_rays(rng, n, 1.0)
@@ -146,6 +147,11 @@ def test_march_rays_overflow(vr):
     fit = ns > 0
     assert np.array_equal(ns[fit], full[2][fit])  # rays that fit carry their full sample run
     assert not idcs[m:].any() and not zs[m:].any()
+    a, ca = V.march_rays(total, 1024, 1, 64, 1.0, 0.0, o, d, t0, t1, np.full(n, 0.5, np.float32), bits,
+                         return_counters=True, early_exit=True)
+    assert np.array_equal(counters, ca)
+    for x, y in zip((valid, ns, st, idcs, xyzs, dirs, dss, zs), a[1:]):
+        assert np.array_equal(x, y)
 
 
 def test_march_rays_inference_golden(vr):
