@@ -339,6 +339,14 @@ __device__ __forceinline__ std::uint32_t frontier_sum(const unsigned long long *
     return (std::uint32_t)*((const volatile unsigned long long *)frontier);
 }
 
+// The frontier's sum as a relaxed load that nothing waits for until its value is used (the march
+// loop uses it one poll later, so the load's latency stays off the ray's chain of steps).
+__device__ __forceinline__ std::uint32_t frontier_sum_async(const unsigned long long *frontier) {
+    std::uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(frontier));   // P: the low half
+    return v;
+}
+
 // Publishes chunk c's count sum and moves the frontier over the chunks done (one thread).  The
 // attempts are bounded; a frontier left behind is moved on by the next chunk that finishes, and
 // only ever lowers what the rays can skip.
@@ -454,10 +462,11 @@ __device__ __forceinline__ std::uint32_t march_one(
     }
     // ---- count pass (marching.cu:162-192)
     if (march) {
-        std::uint32_t poll = 0;
+        std::uint32_t poll = 0, fsum = 0;
         while ((float)n < n_cap && t < t1 && it < kMaxMarchIters) {
-            if (kMode == kMarchCount && it >= poll) {   // do the rays before this one fill the budget?
-                if (frontier_sum(frontier) >= total_samples) break;
+            if (kMode == kMarchCount && it >= poll) {   // did the rays before this one fill the budget?
+                if (fsum >= total_samples) break;       // (as of the previous poll)
+                fsum = frontier_sum_async(frontier);
                 poll = it + kFrontierCheck;
             }
             const V3 pos = at(o, d, t);
