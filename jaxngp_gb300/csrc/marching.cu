@@ -954,7 +954,7 @@ __device__ __forceinline__ std::uint32_t warp_march(
     return n;
 }
 
-constexpr int kWarpBlock = 256;   // 8 rays at a time per block
+constexpr int kWarpBlock = 64;    // 2 rays at a time per block: a block frees its registers as soon as its rays are done
 constexpr std::uint32_t kSmemCoarse = 4096;   // coarse grids up to 16^3 blocks (G <= 128) go to shared memory
 
 // The coarse grid in shared memory when it fits (every block of a warp kernel reads it at each
@@ -1380,14 +1380,16 @@ int launch_march_rays(cudaStream_t stream, const MarchingDescriptor &d, const fl
             if (reinterpret_cast<std::uintptr_t>(fw) & 7u) --fw;
             unsigned long long *frontier = reinterpret_cast<unsigned long long *>(fw);
             NGP_CUDA_TRY(cudaMemsetAsync(done - 3, 0, sizeof(std::uint32_t) * (2 * n_chunks + 3), stream));
-            // warp-per-ray grids: a warp per leading ray; for the writes, at most cap blocks
+            // warp-per-ray grids: a warp per leading ray; for the writes, at most as many threads
+            // as the thread-per-ray grid's cap
             const unsigned wpb = kWarpBlock / 32;
+            const unsigned cap_w = cap * (unsigned)(kThreadBlock / kWarpBlock);
             const std::uint32_t lead_max = d.n_rays < kLeadMax ? d.n_rays : kLeadMax;
             const unsigned lead_grid = (lead_max + wpb - 1) / wpb;
             const unsigned write_need = (d.n_rays + wpb - 1) / wpb;
-            const unsigned write_grid = write_need < cap ? write_need : cap;
+            const unsigned write_grid = write_need < cap_w ? write_need : cap_w;
             // the leading rays, then the rest (how many lead: `queue` as the previous call left it)
-            march_lead_kernel<<<lead_grid < cap ? lead_grid : cap, kWarpBlock, 0, stream>>>(
+            march_lead_kernel<<<lead_grid < cap_w ? lead_grid : cap_w, kWarpBlock, 0, stream>>>(
                 d.n_rays, m, rays_o, rays_d, t_starts, t_ends, noises, bits, coarse, queue, ray_is_valid,
                 rays_n_samples, rays_startidx, sums);
             march_rays_kernel<kMarchCount><<<grid, kThreadBlock, 0, stream>>>(
