@@ -344,8 +344,10 @@ typedef struct NgpMlpDescriptor {
 
 /* Replaces the XLA computation of NeRF.__call__ after the encoder (models/nerfs.py:64-86 with
  * make_nerf_ngp, nerfs.py:422-454): density MLP, truncated exp, SH degree 4, colour MLP, sigmoid.
+ * FP32 accuracy on the tensor cores: every operand split into three BF16 pieces, six MMAs per
+ * layer into FP32 accumulators (within FP32 rounding of the exact layer).
  * buffers: encodings f32[S,32], dirs f32[S,3], weights f32[9408], active_count u32[1] or NULL
- * -> drgbs f32[S,4].  opaque: NgpMlpDescriptor. */
+ * -> drgbs f32[S,4].  opaque: NgpMlpDescriptor.  encodings and drgbs 16-byte aligned. */
 void ngp_field_forward(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 int ngp_field_forward_status(cudaStream_t stream, void **buffers, const char *opaque, size_t opaque_len);
 

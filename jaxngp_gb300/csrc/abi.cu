@@ -48,9 +48,6 @@ int launch_integrate_rays_fp64(cudaStream_t, const IntegratingDescriptor &, cons
                                std::uint32_t *);
 int launch_hashgrid_tv(cudaStream_t, const NgpHashGridDescriptor &, float, const float *, const float *, const float *,
                        float *, float *, double *);
-int launch_mlp_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
-                       const float *, float *);
-int launch_mlp_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
 int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                         const float *, const float *, const float *, float *, float *, float *, bool);
 std::size_t mlp_partials_floats();
@@ -62,6 +59,9 @@ int launch_mlp_bf16_density(cudaStream_t, std::uint32_t, const float *, const fl
 int launch_mlp_bf16_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
                              const float *, const float *, const float *, float *, float *, unsigned *);
 int device_status();
+int launch_mlp_x6_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *, const float *,
+                          float *);
+int launch_mlp_x6_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
 int launch_bounded_wait_selftest(cudaStream_t stream, std::uint32_t polls);
 int set_march_blocks_per_sm(int);
 int launch_proposal_judge(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t, float, const float *,
@@ -355,12 +355,12 @@ NGP_ENTRY(ngp_render_blobs) {
 
 NGP_ENTRY(ngp_field_forward) {
     NGP_DESC(NgpMlpDescriptor, d);
-    return launch_mlp_forward(stream, d.n_samples, CU32(3), CF32(0), CF32(1), CF32(2), F32(4));
+    return launch_mlp_x6_forward(stream, d.n_samples, CU32(3), CF32(0), CF32(1), CF32(2), F32(4));
 }
 
 NGP_ENTRY(ngp_field_density) {
     NGP_DESC(NgpMlpDescriptor, d);
-    return launch_mlp_density(stream, d.n_samples, CF32(0), CF32(1), F32(2));
+    return launch_mlp_x6_density(stream, d.n_samples, CF32(0), CF32(1), F32(2));
 }
 
 NGP_ENTRY(ngp_field_backward) {

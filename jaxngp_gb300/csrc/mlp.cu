@@ -1,5 +1,6 @@
-// Fused density/colour MLP of the NeRF field for sm_103a, FP32: forward, density-only forward,
-// and backward with recomputation.
+// Fused density/colour MLP of the NeRF field for sm_103a, FP32 SIMT: the backward with
+// recomputation (the FP32 forward and density-only forward run on the tensor cores to FP32
+// accuracy, mlp_tc.cu), and the learned proposal's FP32 MLP.
 //
 // Replaces what XLA generates for NeRF.__call__ (models/nerfs.py:39-86) with the NGP layout of
 // make_nerf_ngp (nerfs.py:422-454): CoordinateBasedMLP layers without bias (nerfs.py:89-128),
@@ -13,7 +14,7 @@
 // Weights are one packed array of 9408 floats, each kernel in flax's [in, out] row-major layout:
 // W0 @0, W1 @2048, W2 @3072, W3 @5120, W4 @9216.
 //
-// Design: a CTA of 256 threads loops over tiles of 64 samples.  The weights (and, for the
+// Design of the backward: a CTA of 256 threads loops over tiles of 64 samples.  The weights (and, for the
 // backward, their transposes) sit in shared memory for the CTA's lifetime; per-tile activations
 // sit in shared memory; every layer is a small register-blocked SIMT GEMM (each thread owns a
 // 4-column strip, float4 weight loads, broadcast activation loads).  The backward recomputes the
@@ -292,58 +293,7 @@ __device__ __forceinline__ void tile_forward(const float *sW, float *X0, float *
 }
 
 constexpr int kActFloats = 5 * kTile * kLd + kTile * 4;      // backward: X0, H1, XC, H2, H3, O
-constexpr int kFwdActFloats = 4 * kTile * kLd + kTile * 4;   // forward: H3 reuses H1
-constexpr int kFwdThreads = 256;   // 2 CTAs per SM (108 KB of shared memory each)
 constexpr int kBwdThreads = 256;   // 1 CTA per SM (159 KB of shared memory)
-
-template <int NT>
-__global__ void __launch_bounds__(NT) mlp_forward_kernel(
-    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
-    const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ drgb) {
-    extern __shared__ __align__(16) float smem[];
-    float *sW = smem;
-    float *X0 = sW + kNW, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd, *H2 = XC + kTile * kLd;
-    float *H3 = H1, *O = H2 + kTile * kLd;
-    load_weights<NT>(weights, sW, nullptr);
-    const std::uint32_t n_act = active_count(n, count);
-    const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
-    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const std::size_t s0 = (std::size_t)tile * kTile;
-        const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
-        load_enc<NT>(enc, s0, rows, X0);
-        load_sh<NT>(dirs, s0, rows, XC);
-        __syncthreads();
-        tile_forward<NT>(sW, X0, H1, XC, H2, H3, O);
-        for (int i = threadIdx.x; i < rows; i += NT) {
-            const float4 o = *reinterpret_cast<const float4 *>(O + i * 4);
-            reinterpret_cast<float4 *>(drgb)[s0 + i] = make_float4(expf(o.x), o.y, o.z, o.w);
-        }
-        __syncthreads();
-    }
-}
-
-// sigma only (NeRF.__call__ with dir=None, nerfs.py:71-72), used by the occupancy-grid refresh.
-template <int NT>
-__global__ void __launch_bounds__(NT) mlp_density_kernel(
-    std::uint32_t n, const float *__restrict__ enc, const float *__restrict__ weights, float *__restrict__ sigma) {
-    extern __shared__ __align__(16) float smem[];
-    float *sW = smem;
-    float *X0 = sW + kNW, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd;
-    load_weights<NT>(weights, sW, nullptr);
-    const std::uint32_t n_tiles = (n + kTile - 1) / kTile;
-    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const std::size_t s0 = (std::size_t)tile * kTile;
-        const int rows = (int)min((std::uint32_t)kTile, n - (std::uint32_t)s0);
-        load_enc<NT>(enc, s0, rows, X0);
-        __syncthreads();
-        mm<NT, 32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
-        __syncthreads();
-        mm<NT, 64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
-        __syncthreads();
-        for (int i = threadIdx.x; i < rows; i += NT) sigma[s0 + i] = expf(XC[i * kLd]);
-        __syncthreads();
-    }
-}
 
 // Backward.  dL_ddrgb rows past the active count are ignored; dL_denc rows past it are zeroed.
 // `grad_scale` multiplies the incoming gradient (loss normalisation); `partials` receives one
@@ -584,9 +534,7 @@ __global__ void reduce_partials_n_kernel(std::uint32_t n_parts, std::uint32_t n,
 constexpr std::size_t kPropFwdSmem = (std::size_t)(kP2 + 256 + 3 * kTile * kLd + kTile * 4) * sizeof(float);
 constexpr std::size_t kPropBwdSmem = (std::size_t)(kP2 + 256 + 4608 + 3 * kTile * kLd + kTile) * sizeof(float);
 
-constexpr std::size_t kFwdSmem = (std::size_t)(kNW + kFwdActFloats) * sizeof(float);
 constexpr std::size_t kBwdSmem = (std::size_t)(kNW + kNT + kActFloats) * sizeof(float);
-constexpr std::size_t kDensSmem = (std::size_t)(kNW + 3 * kTile * kLd) * sizeof(float);
 
 }  // namespace
 
@@ -614,29 +562,6 @@ int mlp_partials_count() { return sm_count(); }
 std::size_t mlp_partials_floats() { return (std::size_t)mlp_partials_count() * kNW; }
 
 static bool aligned16(const void *p) { return ((std::uintptr_t)p & 15u) == 0; }
-
-int launch_mlp_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
-                       const float *enc, const float *dirs, const float *weights, float *drgb) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(drgb), "mlp: enc, weights and drgb must be 16-byte aligned");
-    NGP_SMEM_LIMIT((mlp_forward_kernel<kFwdThreads>), kFwdSmem);
-    if (n == 0) return launch_status();
-    const unsigned tiles = (n + kTile - 1) / kTile;
-    const unsigned grid = tiles < (unsigned)sm_count() * 2 ? tiles : (unsigned)sm_count() * 2;
-    mlp_forward_kernel<kFwdThreads><<<grid, kFwdThreads, kFwdSmem, stream>>>(n, count, enc, dirs, weights, drgb);
-    count_launches(1);
-    return launch_status();
-}
-
-int launch_mlp_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights), "mlp: enc and weights must be 16-byte aligned");
-    NGP_SMEM_LIMIT((mlp_density_kernel<kFwdThreads>), kDensSmem);
-    if (n == 0) return launch_status();
-    const unsigned tiles = (n + kTile - 1) / kTile;
-    const unsigned grid = tiles < (unsigned)sm_count() * 3 ? tiles : (unsigned)sm_count() * 3;
-    mlp_density_kernel<kFwdThreads><<<grid, kFwdThreads, kDensSmem, stream>>>(n, enc, weights, sigma);
-    count_launches(1);
-    return launch_status();
-}
 
 // `partials` must hold mlp_partials_floats() floats (scratch).
 int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,

@@ -725,6 +725,174 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     if (threadIdx.x < 32) tc::tmem_free(tbase, 512);
 }
 
+// ------------------------------------------------- FP32-accurate forward on the tensor cores
+//
+// The FP32 field forward (ngp_field_forward, ngp_field_density) with BF16 operands: every operand x
+// is split into three BF16 pieces x1 + x2 + x3 (x1 = bf16(x), x2 = bf16(x - x1), x3 = bf16(x - x1 -
+// x2); both differences exact in FP32), and each layer accumulates the six products of pieces whose
+// orders add up to at most 4 -- a3 b1, a2 b2, a1 b3, a2 b1, a1 b2, a1 b1, smallest first -- in the
+// FP32 accumulator.  The dropped products and the pieces' remainders are below 2^-24 relative:
+// within FP32 rounding of the exact layer (5e-8 against FP64 in the CPU emulation of this scheme,
+// against 1.4e-7 for the SIMT kernel).  Three warpgroups per CTA, each with one 128-row activation
+// buffer of three pieces that every layer reads and the next layer's input then overwrites (the
+// layer's MMAs have completed by then); the weights' three pieces stay in shared memory.
+constexpr int kX6Piece = kRows * 64;                     // elements of one piece of an activation tile
+constexpr int kX6WgAct = 3 * kX6Piece;                   // per warpgroup: three pieces
+constexpr int kX6Wgs = 3;
+constexpr std::size_t kX6Smem = (std::size_t)(3 * kFwdW + kX6Wgs * kX6WgAct) * 2;   // 204 KB
+
+__device__ __forceinline__ void split3(float v, float &a, float &b, float &c) {
+    a = __bfloat162float(__float2bfloat16_rn(v));
+    const float r = v - a;   // exact
+    b = __bfloat162float(__float2bfloat16_rn(r));
+    c = r - b;               // exact; rounded to BF16 when stored
+}
+
+// Row r of a tile with N columns (N % 8 == 0) as three BF16 pieces `piece` elements apart.
+template <int N>
+__device__ __forceinline__ void store_row3(__nv_bfloat16 *buf, int piece, int r, const float *v) {
+#pragma unroll
+    for (int c = 0; c < N; c += 8) {
+        float a[8], b[8], e[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) split3(v[c + j], a[j], b[j], e[j]);
+        const float *src[3] = {a, b, e};
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            uint4 q;
+            q.x = Bf16Op::pack(src[p][0], src[p][1]);
+            q.y = Bf16Op::pack(src[p][2], src[p][3]);
+            q.z = Bf16Op::pack(src[p][4], src[p][5]);
+            q.w = Bf16Op::pack(src[p][6], src[p][7]);
+            *reinterpret_cast<uint4 *>(buf + p * piece + rb(r, c, N)) = q;
+        }
+    }
+}
+
+// The forward weight operands (W^T, layout of load_weights_tc) in three pieces, kFwdW elements apart.
+__device__ void load_weights_x6(const float *__restrict__ w, __nv_bfloat16 *sw) {
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+    for (int i = threadIdx.x; i < 3 * kFwdW; i += blockDim.x) sw[i] = zero;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kNW; i += blockDim.x) {
+        int off;
+        if (i < kW1) { const int in = i / 64, out = i % 64; off = kF0 + rb(out, in, 32); }
+        else if (i < kW2) { const int j = i - kW1, in = j / 16, out = j % 16; off = kF1 + rb(out, in, 64); }
+        else if (i < kW3) { const int j = i - kW2, in = j / 64, out = j % 64; off = kF2 + rb(out, in, 32); }
+        else if (i < kW4) { const int j = i - kW3, in = j / 64, out = j % 64; off = kF3 + rb(out, in, 64); }
+        else { const int j = i - kW4, in = j / 3, out = j % 3; off = kF4 + rb(out, in, 64); }
+        float a, b, c;
+        split3(w[i], a, b, c);
+        sw[off] = __float2bfloat16_rn(a);
+        sw[kFwdW + off] = __float2bfloat16_rn(b);
+        sw[2 * kFwdW + off] = __float2bfloat16_rn(c);
+    }
+}
+
+// D (tmem) = A @ B^T to FP32 accuracy: the six piece products, smallest first.
+__device__ __forceinline__ void mma_kk_x6(std::uint32_t d, const __nv_bfloat16 *a, int a_piece, const __nv_bfloat16 *b,
+                                          int K, int N) {
+    const int ap[6] = {2, 1, 0, 1, 0, 0}, bp[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) mma_kk<Bf16Op>(d, a + ap[k] * a_piece, b + bp[k] * kFwdW, K, N, k > 0);
+}
+
+template <bool kDensity>
+__global__ void __launch_bounds__(kX6Wgs * 128, 1) mlp_x6_forward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ dirs, const float *__restrict__ weights, float *__restrict__ out) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ std::uint64_t bars[kX6Wgs];
+    __shared__ std::uint32_t tbase;
+    __shared__ int fails[kX6Wgs];
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    const int g = threadIdx.x / 128, r = threadIdx.x % 128, q = (threadIdx.x / 32) % 4;
+    __nv_bfloat16 *act = sw + 3 * kFwdW + g * kX6WgAct;
+    load_weights_x6(weights, sw);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kX6Wgs; ++k) {
+            tc::mbar_init(&bars[k], 1);
+            fails[k] = 0;
+        }
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(&tbase, 256);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    WarpGroup wg{g, r, tbase + (std::uint32_t)g * 64u + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
+    const bool leader = r == 0;
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
+    for (std::uint32_t tile = blockIdx.x * kX6Wgs + g; tile < n_tiles; tile += gridDim.x * kX6Wgs) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n_act;
+        float v[64];
+        {
+            EncRow<Bf16Op, false> row;
+            row.load(enc, s, valid);
+            store_row3<32>(act, kX6Piece, r, row.v);
+        }
+        // layer 0: h1 = relu(enc W0)
+        wg.sync();
+        if (leader) { mma_kk_x6(wg.tm, act, kX6Piece, sw + kF0, 32, 64); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld64(wg.tm, v);
+#pragma unroll
+        for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+        store_row3<64>(act, kX6Piece, r, v);
+        // layer 1: x = h1 W1
+        wg.sync();
+        if (leader) { mma_kk_x6(wg.tm, act, kX6Piece, sw + kF1, 64, 16); tc::commit(wg.bar); }
+        wg.wait();
+        tc::ld16(wg.tm, v);
+        if (kDensity) {
+            if (valid) out[s] = expf(v[0]);
+        } else {
+            const float x0 = v[0];
+            float dir[3] = {0.f, 0.f, 1.f};
+            if (valid) {
+                dir[0] = dirs[s * 3 + 0];
+                dir[1] = dirs[s * 3 + 1];
+                dir[2] = dirs[s * 3 + 2];
+            }
+            sh4(dir[0], dir[1], dir[2], v + 16);
+            store_row3<32>(act, kX6Piece, r, v);
+            // layer 2: h2 = relu([x, sh] W2)
+            wg.sync();
+            if (leader) { mma_kk_x6(wg.tm, act, kX6Piece, sw + kF2, 32, 64); tc::commit(wg.bar); }
+            wg.wait();
+            tc::ld64(wg.tm, v);
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+            store_row3<64>(act, kX6Piece, r, v);
+            // layer 3: h3 = relu(h2 W3)
+            wg.sync();
+            if (leader) { mma_kk_x6(wg.tm, act, kX6Piece, sw + kF3, 64, 64); tc::commit(wg.bar); }
+            wg.wait();
+            tc::ld64(wg.tm, v);
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i], 0.f);
+            store_row3<64>(act, kX6Piece, r, v);
+            // layer 4: rgb = sigmoid(h3 W4)
+            wg.sync();
+            if (leader) { mma_kk_x6(wg.tm, act, kX6Piece, sw + kF4, 64, 16); tc::commit(wg.bar); }
+            wg.wait();
+            tc::ld16(wg.tm, v);
+            if (valid) {
+                reinterpret_cast<float4 *>(out)[s] =
+                    make_float4(expf(x0), 1.f / (1.f + expf(-v[0])), 1.f / (1.f + expf(-v[1])), 1.f / (1.f + expf(-v[2])));
+            }
+        }
+        tc::bar_sync(1 + g, 128);   // every thread has read the last layer before the next tile's rows
+        if (*wg.fail) break;
+    }
+    if (*wg.fail && r == 0) atomicOr(&g_device_error, 1u);
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(tbase, 256);
+}
+
 // ------------------------------------------------------------------ proposal network (FP16)
 //
 // The learned proposal's MLP x = relu(relu(enc @ P0) @ P1) @ P2 (enc 8 features; P0 [8][64],
@@ -987,6 +1155,32 @@ int launch_mlp_tc_backward(cudaStream_t stream, std::uint32_t operand, bool half
 #undef NGP_CALL
 }
 #undef NGP_TC_DISPATCH
+
+// The FP32 field forward and density on the tensor cores (mlp_x6_forward_kernel).
+int launch_mlp_x6_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                          const float *dirs, const float *weights, float *drgb) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(drgb), "mlp: enc and drgb must be 16-byte aligned");
+    NGP_SMEM_LIMIT((mlp_x6_forward_kernel<false>), kX6Smem);
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kRows - 1) / kRows;
+    const unsigned want = (tiles + kX6Wgs - 1) / kX6Wgs;
+    const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
+    mlp_x6_forward_kernel<false><<<grid, kX6Wgs * 128, kX6Smem, stream>>>(n, count, enc, dirs, weights, drgb);
+    count_launches(1);
+    return launch_status();
+}
+
+int launch_mlp_x6_density(cudaStream_t stream, std::uint32_t n, const float *enc, const float *weights, float *sigma) {
+    NGP_CHECK_ARG(aligned16(enc), "mlp: enc must be 16-byte aligned");
+    NGP_SMEM_LIMIT((mlp_x6_forward_kernel<true>), kX6Smem);
+    if (n == 0) return launch_status();
+    const unsigned tiles = (n + kRows - 1) / kRows;
+    const unsigned want = (tiles + kX6Wgs - 1) / kX6Wgs;
+    const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
+    mlp_x6_forward_kernel<true><<<grid, kX6Wgs * 128, kX6Smem, stream>>>(n, nullptr, enc, nullptr, weights, sigma);
+    count_launches(1);
+    return launch_status();
+}
 
 int launch_prop_f16_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
                             const float *weights, float *x) {
