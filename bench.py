@@ -14,7 +14,8 @@ back every step.  `forms` repeats the measurement for the BF16 tensor-core field
 learned proposal sampler with it (also with a 16-bit table copy and 16-bit encodings, BF16 or
 FP16 under a dynamic loss scale), each with the held-out PSNR of the trained field and 1080p
 inference FPS; `forms_vs_plain` gives every form's throughput ratio and PSNR difference against
-the plain step, and the time to the plain step's PSNR of the fastest form within 0.1 dB of it;
+the plain step, and the time to the plain step's PSNR of the fastest form within 0.5 dB of it at
+equal steps (held-out PSNR moves by a few tenths of a dB between runs);
 `learned_proposal_vs_plain` adds, per proposal form, rays-with-samples/s and the proposal
 renderer's 1080p ratio.  The plain step fits its rays in ray order (the reference kernel run one
 thread at a time), so its valid rays are a prefix of the batch: about the rays the budget takes.
@@ -982,9 +983,10 @@ def main():
                 out["learned_proposal_vs_plain"] = {"plain": "fp32-march", **cmp}
             if allcmp:
                 # every form against the plain FP32 step; time to the plain step's PSNR for the
-                # fastest form that trains within 0.1 dB of it at equal steps
+                # fastest form within 0.5 dB of it at equal steps (held-out PSNR after 920 steps moves
+                # by a few tenths of a dB from run to run; the equal-PSNR run then decides)
                 out["forms_vs_plain"] = {"plain": "fp32-march", **allcmp}
-                ok = [f for f in allcmp if allcmp[f]["delta_psnr_db"] >= -0.1]
+                ok = [f for f in allcmp if allcmp[f]["delta_psnr_db"] >= -0.5]
                 if ok and args.equal_psnr_steps > 0:
                     fastest = max(ok, key=lambda f: results[f]["value"])
                     out["forms_vs_plain"]["at_equal_psnr"] = equal_psnr(args, data, "fp32-march", fastest)
