@@ -892,23 +892,42 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_warp_kernel(
 
 // ------------------------------------------------- the training march's warp-per-ray passes
 
-// advance() with the coarse-block skip: lane k, on an empty cell, crosses the empty coarse block
-// it lies in at once when skip_block can (the thread march's step at the same t).
+// advance() with the coarse-block skip, for warp_march: lane k, on an empty cell, crosses the
+// empty coarse block it lies in at once when skip_block can (the thread march's step at the same
+// t), else the cell (skip_empty); and it goes on crossing empty cells by itself -- the thread
+// march's steps, its occupancy test and its step count -- up to kSkipRun of them, so that a run of
+// empty cells costs one lookahead trip, not one each.  `it` advances by the skips taken.
+constexpr std::uint32_t kSkipRun = 32;
+
 __device__ __forceinline__ bool advance_skip(const MarchParams &m, const Lookahead &a, unsigned lane, unsigned k,
-                                             V3 o, V3 d, V3 inv_d, const std::uint8_t *__restrict__ coarse,
-                                             bool block_skip, float &t) {
+                                             V3 o, V3 d, V3 inv_d, float t1, const std::uint8_t *__restrict__ bits,
+                                             const std::uint32_t *expand, const std::uint8_t *__restrict__ coarse,
+                                             bool block_skip, std::uint32_t it_k, float &t, std::uint32_t &skips) {
     if (k < 32u) {
         if (!__shfl_sync(0xffffffffu, a.live, k)) return false;
         float nt = 0.f;
+        std::uint32_t ns = 0;
         if (lane == k) {
-            float tb;
-            nt = (block_skip && skip_block(m, a.t, a.g, a.pos, o, d, inv_d, coarse, tb))
-                     ? tb : skip_empty(m, a.t, a.g, a.mb, a.pos, d, inv_d);
+            float tt = a.t;
+            V3 g = a.g, pos = a.pos;
+            float mb = a.mb;
+            for (;;) {   // it_k + ns: the step count before this skip
+                float tb;
+                tt = (block_skip && skip_block(m, tt, g, pos, o, d, inv_d, coarse, tb))
+                         ? tb : skip_empty(m, tt, g, mb, pos, d, inv_d);
+                ++ns;
+                if (ns >= kSkipRun || !(tt < t1) || it_k + ns >= kMaxMarchIters) break;
+                pos = at(o, d, tt);
+                if (occupied_at(m, pos, calc_ds(tt, m), bits, g, mb, expand)) break;   // the next trip samples here
+            }
+            nt = tt;
         }
         t = __shfl_sync(0xffffffffu, nt, k);
+        skips = __shfl_sync(0xffffffffu, ns, k);
     } else {
         const float nt = lane == 31u ? a.t + a.ds : 0.f;
         t = __shfl_sync(0xffffffffu, nt, 31);
+        skips = 0;
     }
     return true;
 }
@@ -948,8 +967,9 @@ __device__ __forceinline__ std::uint32_t warp_march(
         }
         n += k;
         it += k;
-        if (!advance_skip(m, a, lane, k, o, d, inv_d, coarse, block_skip, t)) break;
-        if (k < 32u) ++it;   // the skip is a step of its own
+        std::uint32_t skips = 0;
+        if (!advance_skip(m, a, lane, k, o, d, inv_d, t1, bits, expand, coarse, block_skip, it, t, skips)) break;
+        it += skips;   // each skip is a step of its own
     }
     return n;
 }

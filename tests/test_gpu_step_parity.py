@@ -164,12 +164,14 @@ def test_train_step_matches_cpu_restatement(scene):
     drgb_g = h(tr.drgbs)[:used]
     drgb64, _ = Fd.forward(enc, dirs_g[:used], w0, dtype=np.float64)
     assert col_err(drgb_g, drgb64) <= 1e-5
+    # a float32 evaluation of the field (explicit FMA chains): the forward kernel (three BF16 pieces
+    # per operand on the tensor cores, FP32 accumulation) is another float32 evaluation of the
+    # same layers, a few ulps away in each layer's sum
     drgb32, cache = Fd.forward_fma32(enc, dirs_g[:used], w0)
-    assert col_err(drgb_g, drgb32) <= 1e-6
-    same = (drgb_g == drgb32).mean(axis=0)
-    print(f"\nstep parity: {cfg.n_rays} rays, {used} samples, {nv} valid rays; field outputs bit-identical to the "
-          f"FP32-kernel emulation (CUDA's expf against the C library's in sigma and the sigmoid): "
-          f"sigma {same[0]:.4f} rgb {same[1]:.4f} {same[2]:.4f} {same[3]:.4f}")
+    e32 = col_err(drgb_g, drgb32)
+    assert e32 <= 5e-6
+    print(f"\nstep parity: {cfg.n_rays} rays, {used} samples, {nv} valid rays; field outputs {col_err(drgb_g, drgb64):.2e} "
+          f"from FP64 and {e32:.2e} from the float32 FMA-chain evaluation (column scale)")
 
     # ---- integrate + masked Huber loss + integrate backward (on the GPU's field values)
     drgbs_full = np.zeros((tr.S, 4), np.float32)
