@@ -717,17 +717,43 @@ __device__ __forceinline__ void look_ahead(const MarchParams &m, float t, unsign
 }
 
 // After a lookahead that accepted k occupied steps: the t the sequential march reaches next, or
-// false when its loop ends at lane k (k < 32 and the condition fails there).  An empty cell at
-// lane k is skipped by that lane exactly as marching.cu:182-189 skips it.
-__device__ __forceinline__ bool advance(const MarchParams &m, const Lookahead &a, unsigned lane, unsigned k, V3 d,
-                                        V3 inv_d, float &t) {
+// false when its loop ends at lane k (k < 32 and the condition fails there).  Lane k, on an empty
+// cell, crosses the empty coarse block it lies in at once when skip_block can (the thread march's
+// step at the same t), else the cell (skip_empty, marching.cu:182-189); and it goes on crossing
+// empty cells by itself -- the thread march's steps, its occupancy test and its step count -- up
+// to kSkipRun of them, so that a run of empty cells costs one lookahead trip, not one each.
+// `skips` receives the steps taken.
+constexpr std::uint32_t kSkipRun = 32;
+
+__device__ __forceinline__ bool advance_skip(const MarchParams &m, const Lookahead &a, unsigned lane, unsigned k,
+                                             V3 o, V3 d, V3 inv_d, float t1, const std::uint8_t *__restrict__ bits,
+                                             const std::uint32_t *expand, const std::uint8_t *__restrict__ coarse,
+                                             bool block_skip, std::uint32_t it_k, float &t, std::uint32_t &skips) {
     if (k < 32u) {
         if (!__shfl_sync(0xffffffffu, a.live, k)) return false;
-        const float nt = lane == k ? skip_empty(m, a.t, a.g, a.mb, a.pos, d, inv_d) : 0.f;
+        float nt = 0.f;
+        std::uint32_t ns = 0;
+        if (lane == k) {
+            float tt = a.t;
+            V3 g = a.g, pos = a.pos;
+            float mb = a.mb;
+            for (;;) {   // it_k + ns: the step count before this skip
+                float tb;
+                tt = (block_skip && skip_block(m, tt, g, pos, o, d, inv_d, coarse, tb))
+                         ? tb : skip_empty(m, tt, g, mb, pos, d, inv_d);
+                ++ns;
+                if (ns >= kSkipRun || !(tt < t1) || it_k + ns >= kMaxMarchIters) break;
+                pos = at(o, d, tt);
+                if (occupied_at(m, pos, calc_ds(tt, m), bits, g, mb, expand)) break;   // the next trip samples here
+            }
+            nt = tt;
+        }
         t = __shfl_sync(0xffffffffu, nt, k);
+        skips = __shfl_sync(0xffffffffu, ns, k);
     } else {
         const float nt = lane == 31u ? a.t + a.ds : 0.f;
         t = __shfl_sync(0xffffffffu, nt, 31);
+        skips = 0;
     }
     return true;
 }
@@ -804,9 +830,10 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_warp_kernel(
             const std::uint32_t n0 = n;
             n += k;
             it += k;
-            const bool more = advance(m, a, lane, k, d, inv_d, t);
+            std::uint32_t skips = 0;
+            const bool more = advance_skip(m, a, lane, k, o, d, inv_d, t1, bits, expand, nullptr, false, it, t, skips);
             if (!more) break;
-            if (k < 32u) ++it;   // the skip is a step of its own
+            it += skips;   // each skip is a step of its own
             // a sample numbered 1, 17, 33, ... was taken in this trip: probe the budget (lane 0
             // reads the counter, so the whole warp takes the same decision)
             if (k > 0 && ((n0 + 15u) >> 4) != ((n + 15u) >> 4)) {
@@ -884,53 +911,14 @@ __global__ void __launch_bounds__(kMarchBlock) march_rays_warp_kernel(
             }
             w += k;
             it += k;
-            if (!advance(m, a, lane, k, d, inv_d, t)) break;
-            if (k < 32u) ++it;
+            std::uint32_t skips = 0;
+            if (!advance_skip(m, a, lane, k, o, d, inv_d, t1, bits, expand, nullptr, false, it, t, skips)) break;
+            it += skips;
         }
     }
 }
 
 // ------------------------------------------------- the training march's warp-per-ray passes
-
-// advance() with the coarse-block skip, for warp_march: lane k, on an empty cell, crosses the
-// empty coarse block it lies in at once when skip_block can (the thread march's step at the same
-// t), else the cell (skip_empty); and it goes on crossing empty cells by itself -- the thread
-// march's steps, its occupancy test and its step count -- up to kSkipRun of them, so that a run of
-// empty cells costs one lookahead trip, not one each.  `it` advances by the skips taken.
-constexpr std::uint32_t kSkipRun = 32;
-
-__device__ __forceinline__ bool advance_skip(const MarchParams &m, const Lookahead &a, unsigned lane, unsigned k,
-                                             V3 o, V3 d, V3 inv_d, float t1, const std::uint8_t *__restrict__ bits,
-                                             const std::uint32_t *expand, const std::uint8_t *__restrict__ coarse,
-                                             bool block_skip, std::uint32_t it_k, float &t, std::uint32_t &skips) {
-    if (k < 32u) {
-        if (!__shfl_sync(0xffffffffu, a.live, k)) return false;
-        float nt = 0.f;
-        std::uint32_t ns = 0;
-        if (lane == k) {
-            float tt = a.t;
-            V3 g = a.g, pos = a.pos;
-            float mb = a.mb;
-            for (;;) {   // it_k + ns: the step count before this skip
-                float tb;
-                tt = (block_skip && skip_block(m, tt, g, pos, o, d, inv_d, coarse, tb))
-                         ? tb : skip_empty(m, tt, g, mb, pos, d, inv_d);
-                ++ns;
-                if (ns >= kSkipRun || !(tt < t1) || it_k + ns >= kMaxMarchIters) break;
-                pos = at(o, d, tt);
-                if (occupied_at(m, pos, calc_ds(tt, m), bits, g, mb, expand)) break;   // the next trip samples here
-            }
-            nt = tt;
-        }
-        t = __shfl_sync(0xffffffffu, nt, k);
-        skips = __shfl_sync(0xffffffffu, ns, k);
-    } else {
-        const float nt = lane == 31u ? a.t + a.ds : 0.f;
-        t = __shfl_sync(0xffffffffu, nt, 31);
-        skips = 0;
-    }
-    return true;
-}
 
 // One ray by one warp, from t: the count (kWrite false: up to n_cap samples, and t_hit, the t of
 // the first) or the writing of its n_write samples from slot `start` (kWrite true).  The steps
