@@ -682,6 +682,30 @@ def kernels_vs_reference(tr) -> dict:
         "pack_density_into_bits": (lambda: [thr, tr.density] + pk_out(), L.PackbitsDescriptor(n_cells // 8),
                                    "packbits.cu:9-34"),
     }
+    # the inference pair, one refill iteration: every slot takes a new ray of the batch, marches up
+    # to `cap` samples, and the integrator continues the rays (a field drawn at random)
+    n_slots, cap = 1 << 16, 8
+    term = torch.ones(n_slots, dtype=torch.bool, device="cuda")
+    idx0 = torch.zeros(n_slots, **i32)
+    nri0 = torch.zeros(1, **i32)
+    mi_desc = L.MarchingInferenceDescriptor(R, n_slots, tr.cfg.diagonal_n_steps, tr.K, tr.cfg.G, cap, tr.bound, tr.sp)
+    mi_out = lambda: [torch.empty(1, **i32), torch.empty(n_slots, **i32), torch.empty(n_slots, **i32),
+                      torch.empty(n_slots, device="cuda"), torch.empty(n_slots, cap, 3, device="cuda"),
+                      torch.empty(n_slots, cap, device="cuda"), torch.empty(n_slots, cap, device="cuda")]
+    mi_in = [tr.rays_o, tr.rays_d, tr.t0, tr.t1, tr.bitfield, nri0, term, idx0]
+    m_ref = mi_out()
+    RG.call("march_rays_inference", mi_in + m_ref, mi_desc)
+    drgb_i = torch.rand(n_slots, cap, 4, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
+    drgb_i[..., 0] *= 40.0
+    bg_i, rgbd_i = torch.ones(R, 3, device="cuda"), torch.zeros(R, 4, device="cuda")
+    T_i = torch.ones(R, device="cuda")
+    ii_out = lambda: [torch.zeros(1, **i32), torch.empty(n_slots, dtype=torch.bool, device="cuda"),
+                      torch.empty(n_slots, 4, device="cuda"), torch.empty(n_slots, device="cuda")]
+    cases["march_rays_inference"] = (lambda: mi_in + mi_out(), mi_desc,
+                                     "marching.cu:271-397 (its launcher synchronises the stream, :562: included)")
+    cases["integrate_rays_inference"] = (
+        lambda: [bg_i, rgbd_i, T_i, m_ref[2], m_ref[1], m_ref[5], m_ref[6], drgb_i] + ii_out(),
+        L.IntegratingInferenceDescriptor(R, n_slots, cap), "integrating.cu:242-322")
     for name, (mk, desc, where) in cases.items():
         b_ours, b_ref = mk(), mk()
         ms_o = _event_ms(lambda: L.call(name, b_ours, desc))
