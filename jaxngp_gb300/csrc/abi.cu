@@ -48,8 +48,6 @@ int launch_integrate_rays_fp64(cudaStream_t, const IntegratingDescriptor &, cons
                                std::uint32_t *);
 int launch_hashgrid_tv(cudaStream_t, const NgpHashGridDescriptor &, float, const float *, const float *, const float *,
                        float *, float *, double *);
-int launch_mlp_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
-                        const float *, const float *, const float *, float *, float *, float *, bool);
 std::size_t mlp_partials_floats();
 int launch_mlp_partials_reduce(cudaStream_t, unsigned, const float *, float *, bool, std::uint32_t, const std::uint32_t *,
                                float *, unsigned);
@@ -62,6 +60,8 @@ int device_status();
 int launch_mlp_x6_forward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *, const float *,
                           float *);
 int launch_mlp_x6_density(cudaStream_t, std::uint32_t, const float *, const float *, float *);
+int launch_mlp_x6_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                           const float *, const float *, const float *, float *, float *, unsigned, unsigned *);
 int launch_bounded_wait_selftest(cudaStream_t stream, std::uint32_t polls);
 int set_march_blocks_per_sm(int);
 int launch_proposal_judge(cudaStream_t, std::uint32_t, const std::uint32_t *, std::uint32_t, float, const float *,
@@ -365,8 +365,11 @@ NGP_ENTRY(ngp_field_density) {
 
 NGP_ENTRY(ngp_field_backward) {
     NGP_DESC(NgpMlpDescriptor, d);
-    return launch_mlp_backward(stream, d.n_samples, CU32(4), CF32(0), CF32(1), CF32(2), CF32(3), CF32(5), F32(7),
-                               F32(8), F32(6), d.accumulate != 0);
+    unsigned parts = 0;
+    const int st = launch_mlp_x6_backward(stream, d.n_samples, CU32(4), CF32(0), CF32(1), CF32(2), CF32(3), CF32(5),
+                                          F32(7), F32(6), ~0u, &parts);
+    if (st != NGP_OK) return st;
+    return launch_mlp_partials_reduce(stream, parts, CF32(6), F32(8), d.accumulate != 0, d.n_samples, CU32(4), F32(7), 32u);
 }
 
 size_t ngp_field_backward_scratch_floats(void) { return mlp_partials_floats(); }

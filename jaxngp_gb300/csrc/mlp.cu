@@ -1,27 +1,18 @@
-// Fused density/colour MLP of the NeRF field for sm_103a, FP32 SIMT: the backward with
-// recomputation (the FP32 forward and density-only forward run on the tensor cores to FP32
-// accuracy, mlp_tc.cu), and the learned proposal's FP32 MLP.
+// SIMT parts of the MLPs for sm_103a: the learned proposal's FP32 MLP (forward and backward), the
+// fixed-order sum of the field backward's per-CTA dL/dW partials, and the allocation-free entry
+// point of the field backward.  The field MLP itself (NeRF.__call__, models/nerfs.py:39-86, with
+// the NGP layout of make_nerf_ngp, nerfs.py:422-454) runs on the tensor cores in mlp_tc.cu, to
+// FP32 accuracy for ngp_field_forward/_density/_backward and in BF16/FP16 for the mixed forms.
 //
-// Replaces what XLA generates for NeRF.__call__ (models/nerfs.py:39-86) with the NGP layout of
-// make_nerf_ngp (nerfs.py:422-454): CoordinateBasedMLP layers without bias (nerfs.py:89-128),
-// truncated exponential on density (nerfs.py:221-238), degree-4 spherical harmonics of the view
-// direction (models/encoders.py:375-406), sigmoid on colour:
+// Field weights are one packed array of 9408 floats, each kernel in flax's [in, out] row-major
+// layout: W0 @0, W1 @2048, W2 @3072, W3 @5120, W4 @9216.
 //
-//   h1 = relu(enc @ W0)  [32->64]     x = h1 @ W1  [64->16]       sigma = exp(x[0])
-//   h2 = relu([x, SH4(dir)] @ W2)  [32->64]   h3 = relu(h2 @ W3)  [64->64]
-//   rgb = sigmoid(h3 @ W4)  [64->3]           drgb = [sigma, rgb]
-//
-// Weights are one packed array of 9408 floats, each kernel in flax's [in, out] row-major layout:
-// W0 @0, W1 @2048, W2 @3072, W3 @5120, W4 @9216.
-//
-// Design of the backward: a CTA of 256 threads loops over tiles of 64 samples.  The weights (and, for the
-// backward, their transposes) sit in shared memory for the CTA's lifetime; per-tile activations
-// sit in shared memory; every layer is a small register-blocked SIMT GEMM (each thread owns a
-// 4-column strip, float4 weight loads, broadcast activation loads).  The backward recomputes the
-// forward activations of its tile from the encodings (nothing per-layer is stored in HBM),
-// accumulates each thread's share of dL/dW in registers across all its tiles, and writes one
-// partial per CTA; a second kernel sums the partials in a fixed order, so weight gradients are
-// deterministic.  FP32 throughout (the parity path); the BF16 tensor-core path is separate.
+// The proposal MLP: a CTA of 256 threads loops over tiles of 64 points with the weights (and, for
+// the backward, their transposes) in shared memory; every layer is a small register-blocked SIMT
+// GEMM (each thread owns a 4-column strip, float4 weight loads, broadcast activation loads).  The
+// backward recomputes the tile's activations, accumulates each thread's share of dL/dP in
+// registers across all its tiles, and writes one partial per CTA; a second kernel sums the
+// partials in a fixed order, so weight gradients are deterministic.
 #include <mutex>
 
 #include "common.cuh"
@@ -31,34 +22,7 @@ namespace {
 
 constexpr int kTile = 64;
 constexpr int kW0 = 0, kW1 = 2048, kW2 = 3072, kW3 = 5120, kW4 = 9216, kNW = 9408;
-// transposed copies (backward only)
-constexpr int kT0 = 0;      // W0^T [64][32]
-constexpr int kT1 = 2048;   // W1^T [16][64]
-constexpr int kT2 = 3072;   // W2[:16]^T [64][16]
-constexpr int kT3 = 4096;   // W3^T [64][64]
-constexpr int kT4 = 8192;   // W4^T [3][64]
-constexpr int kNT = 8384;
 constexpr int kLd = 68;     // activation row stride (floats): 16-byte aligned rows
-
-__device__ __forceinline__ void sh4(float x, float y, float z, float *o) {
-    const float xy = x * y, xz = x * z, yz = y * z, x2 = x * x, y2 = y * y, z2 = z * z;
-    o[0] = 0.28209479177387814f;
-    o[1] = -0.48860251190291987f * y;
-    o[2] = 0.48860251190291987f * z;
-    o[3] = -0.48860251190291987f * x;
-    o[4] = 1.0925484305920792f * xy;
-    o[5] = -1.0925484305920792f * yz;
-    o[6] = 0.94617469575755997f * z2 - 0.31539156525251999f;
-    o[7] = -1.0925484305920792f * xz;
-    o[8] = 0.54627421529603959f * x2 - 0.54627421529603959f * y2;
-    o[9] = 0.59004358992664352f * y * (-3.0f * x2 + y2);
-    o[10] = 2.8906114426405538f * xy * z;
-    o[11] = 0.45704579946446572f * y * (1.0f - 5.0f * z2);
-    o[12] = 0.3731763325901154f * z * (5.0f * z2 - 3.0f);
-    o[13] = 0.45704579946446572f * x * (1.0f - 5.0f * z2);
-    o[14] = 1.4453057213202769f * z * (x2 - y2);
-    o[15] = 0.59004358992664352f * x * (-x2 + 3.0f * y2);
-}
 
 // Thread layout of a [ROWS x N] result over NT threads: each thread owns a 4-wide column strip
 // and RPT rows spaced R apart; when there are more row groups than rows the extra threads idle.
@@ -208,188 +172,6 @@ __device__ __forceinline__ std::uint32_t active_count(std::uint32_t n, const std
     return count != nullptr ? min(n, *count) : n;
 }
 
-// Stage the packed weights (and optionally their transposes) into shared memory.
-template <int NT>
-__device__ __forceinline__ void load_weights(const float *__restrict__ w, float *sW, float *sT) {
-    for (int i = threadIdx.x; i < kNW / 4; i += NT)
-        reinterpret_cast<float4 *>(sW)[i] = reinterpret_cast<const float4 *>(w)[i];
-    if (sT != nullptr) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < 2048; i += NT) {  // W0 [32][64] -> [64][32]
-            const int r = i / 64, c = i % 64;
-            sT[kT0 + c * 32 + r] = sW[kW0 + i];
-        }
-        for (int i = threadIdx.x; i < 1024; i += NT) {  // W1 [64][16] -> [16][64]
-            const int r = i / 16, c = i % 16;
-            sT[kT1 + c * 64 + r] = sW[kW1 + i];
-        }
-        for (int i = threadIdx.x; i < 1024; i += NT) {  // W2[:16] [16][64] -> [64][16]
-            const int r = i / 64, c = i % 64;
-            sT[kT2 + c * 16 + r] = sW[kW2 + i];
-        }
-        for (int i = threadIdx.x; i < 4096; i += NT) {  // W3 [64][64] -> [64][64]
-            const int r = i / 64, c = i % 64;
-            sT[kT3 + c * 64 + r] = sW[kW3 + i];
-        }
-        for (int i = threadIdx.x; i < 192; i += NT) {  // W4 [64][3] -> [3][64]
-            const int r = i / 3, c = i % 3;
-            sT[kT4 + c * 64 + r] = sW[kW4 + i];
-        }
-    }
-    __syncthreads();
-}
-
-// Loads the tile's encodings into X[:, 0:32] (zero rows past `rows`).
-template <int NT>
-__device__ __forceinline__ void load_enc(const float *__restrict__ enc, std::size_t s0, int rows, float *X) {
-    for (int i = threadIdx.x; i < kTile * 8; i += NT) {
-        const int r = i / 8, c = (i % 8) * 4;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (r < rows) v = *reinterpret_cast<const float4 *>(enc + (s0 + r) * 32 + c);
-        *reinterpret_cast<float4 *>(X + r * kLd + c) = v;
-    }
-}
-
-// XC[s][16:32] = SH4(dir_s); rows past `rows` get a unit +z direction.
-template <int NT>
-__device__ __forceinline__ void load_sh(const float *__restrict__ dirs, std::size_t s0, int rows, float *XC) {
-    for (int r = threadIdx.x; r < kTile; r += NT) {
-        float dx = 0.f, dy = 0.f, dz = 1.f;
-        if (r < rows) {
-            dx = dirs[(s0 + r) * 3 + 0];
-            dy = dirs[(s0 + r) * 3 + 1];
-            dz = dirs[(s0 + r) * 3 + 2];
-        }
-        float o[16];
-        sh4(dx, dy, dz, o);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) XC[r * kLd + 16 + j] = o[j];
-    }
-}
-
-// Forward through the tile; leaves X0=enc, H1, XC=[x, sh], H2, H3 in shared memory and writes
-// sigma/rgb into O (O[s][0] = x0 (pre-activation), O[s][1..3] = rgb).  H3 may alias H1 when the
-// caller does not need H1 afterwards (the forward-only kernel).
-template <int NT>
-__device__ __forceinline__ void tile_forward(const float *sW, float *X0, float *H1, float *XC, float *H2,
-                                             float *H3, float *O) {
-    mm<NT, 32, 64, true>(X0, kLd, sW + kW0, H1, kLd);
-    __syncthreads();
-    mm<NT, 64, 16, false>(H1, kLd, sW + kW1, XC, kLd);
-    __syncthreads();
-    mm<NT, 32, 64, true>(XC, kLd, sW + kW2, H2, kLd);
-    __syncthreads();
-    mm<NT, 64, 64, true>(H2, kLd, sW + kW3, H3, kLd);
-    __syncthreads();
-    for (int i = threadIdx.x; i < kTile * 3; i += NT) {
-        const int r = i / 3, c = i % 3;
-        float a = 0.f;
-#pragma unroll 16
-        for (int k = 0; k < 64; ++k) a += H3[r * kLd + k] * sW[kW4 + k * 3 + c];
-        O[r * 4 + 1 + c] = 1.f / (1.f + expf(-a));
-    }
-    for (int r = threadIdx.x; r < kTile; r += NT) O[r * 4] = XC[r * kLd];
-    __syncthreads();
-}
-
-constexpr int kActFloats = 5 * kTile * kLd + kTile * 4;      // backward: X0, H1, XC, H2, H3, O
-constexpr int kBwdThreads = 256;   // 1 CTA per SM (159 KB of shared memory)
-
-// Backward.  dL_ddrgb rows past the active count are ignored; dL_denc rows past it are zeroed.
-// `grad_scale` multiplies the incoming gradient (loss normalisation); `partials` receives one
-// [9408] dL/dW partial per CTA.
-template <int NT>
-__global__ void __launch_bounds__(NT) mlp_backward_kernel(
-    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
-    const float *__restrict__ dirs, const float *__restrict__ weights,
-    const float *__restrict__ dL_ddrgb, const float *__restrict__ grad_scale,
-    float *__restrict__ dL_denc, float *__restrict__ partials) {
-    extern __shared__ __align__(16) float smem[];
-    float *sW = smem, *sT = sW + kNW;
-    float *X0 = sT + kNT, *H1 = X0 + kTile * kLd, *XC = H1 + kTile * kLd, *H2 = XC + kTile * kLd;
-    float *H3 = H2 + kTile * kLd, *O = H3 + kTile * kLd;
-    load_weights<NT>(weights, sW, sT);
-    const float gs = grad_scale != nullptr ? *grad_scale : 1.f;
-
-    WGrad<NT, 32, 64> g0;  // dW0 = enc^T dA1
-    WGrad<NT, 64, 16> g1;  // dW1 = h1^T dx
-    WGrad<NT, 32, 64> g2;  // dW2 = [x, sh]^T dA2
-    WGrad<NT, 64, 64> g3;  // dW3 = h2^T dA3
-    float g4 = 0.f;    // dW4 = h3^T dA4: thread t < 192 owns element t
-    g0.zero();
-    g1.zero();
-    g2.zero();
-    g3.zero();
-
-    const std::uint32_t n_act = active_count(n, count);
-    const std::uint32_t n_tiles = (n_act + kTile - 1) / kTile;
-    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const std::size_t s0 = (std::size_t)tile * kTile;
-        const int rows = (int)min((std::uint32_t)kTile, n_act - (std::uint32_t)s0);
-        load_enc<NT>(enc, s0, rows, X0);
-        load_sh<NT>(dirs, s0, rows, XC);
-        __syncthreads();
-        tile_forward<NT>(sW, X0, H1, XC, H2, H3, O);
-
-        // O[s] <- [dL/dx0, dL/da4 (3)]; rows past `rows` get zero gradient
-        for (int r = threadIdx.x; r < kTile; r += NT) {
-            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r < rows) g = reinterpret_cast<const float4 *>(dL_ddrgb)[s0 + r];
-            const float4 o = *reinterpret_cast<const float4 *>(O + r * 4);
-            const float x0 = fminf(fmaxf(o.x, -15.f), 15.f);
-            *reinterpret_cast<float4 *>(O + r * 4) =
-                make_float4(gs * g.x * expf(x0), gs * g.y * o.y * (1.f - o.y), gs * g.z * o.z * (1.f - o.z),
-                            gs * g.w * o.w * (1.f - o.w));
-        }
-        __syncthreads();
-        if (threadIdx.x < 192) {  // dW4[m][c] += sum_s h3[s][m] * dA4[s][c]
-            const int m = threadIdx.x / 3, c = threadIdx.x % 3;
-            float a = 0.f;
-            for (int s = 0; s < kTile; ++s) a += H3[s * kLd + m] * O[s * 4 + 1 + c];
-            g4 += a;
-        }
-        __syncthreads();
-        // dA3 = (dA4 @ W4^T) * (h3 > 0), over H3
-        for (int i = threadIdx.x; i < kTile * 64; i += NT) {
-            const int r = i / 64, c = i % 64;
-            const float h = H3[r * kLd + c];
-            const float v = O[r * 4 + 1] * sT[kT4 + c] + O[r * 4 + 2] * sT[kT4 + 64 + c] + O[r * 4 + 3] * sT[kT4 + 128 + c];
-            H3[r * kLd + c] = h > 0.f ? v : 0.f;
-        }
-        __syncthreads();
-        g3.add(H2, kLd, H3, kLd, kTile);
-        __syncthreads();
-        mm_mask_inplace<NT, 64, 64>(H3, kLd, sT + kT3, H2, kLd);  // dA2 over H2
-        __syncthreads();
-        g2.add(XC, kLd, H2, kLd, kTile);
-        __syncthreads();
-        // dx = dA2 @ W2[:16]^T (+ dL/dx0 on column 0), over XC[:, 0:16]
-        mm<NT, 64, 16, false>(H2, kLd, sT + kT2, XC, kLd);
-        __syncthreads();
-        for (int r = threadIdx.x; r < kTile; r += NT) XC[r * kLd] += O[r * 4];
-        __syncthreads();
-        g1.add(H1, kLd, XC, kLd, kTile);
-        __syncthreads();
-        mm_mask_inplace<NT, 16, 64>(XC, kLd, sT + kT1, H1, kLd);  // dA1 over H1
-        __syncthreads();
-        g0.add(X0, kLd, H1, kLd, kTile);
-        __syncthreads();
-        mm<NT, 64, 32, false>(H1, kLd, sT + kT0, X0, kLd);  // dL/denc over X0
-        __syncthreads();
-        for (int i = threadIdx.x; i < kTile * 8; i += NT) {
-            const int r = i / 8, c = (i % 8) * 4;
-            if (r < rows) *reinterpret_cast<float4 *>(dL_denc + (s0 + r) * 32 + c) = *reinterpret_cast<const float4 *>(X0 + r * kLd + c);
-        }
-        __syncthreads();
-    }
-    float *p = partials + (std::size_t)blockIdx.x * kNW;
-    g0.store(p + kW0);
-    g1.store(p + kW1);
-    g2.store(p + kW2);
-    g3.store(p + kW3);
-    if (threadIdx.x < 192) p[kW4 + threadIdx.x] = g4;
-}
-
 // dW[j] = sum over CTAs c (in order) of partials[c][j]; accumulate into dW when requested.
 __global__ void reduce_partials_kernel(std::uint32_t n_parts, const float *__restrict__ partials,
                                        float *__restrict__ dW, int accumulate) {
@@ -534,8 +316,6 @@ __global__ void reduce_partials_n_kernel(std::uint32_t n_parts, std::uint32_t n,
 constexpr std::size_t kPropFwdSmem = (std::size_t)(kP2 + 256 + 3 * kTile * kLd + kTile * 4) * sizeof(float);
 constexpr std::size_t kPropBwdSmem = (std::size_t)(kP2 + 256 + 4608 + 3 * kTile * kLd + kTile) * sizeof(float);
 
-constexpr std::size_t kBwdSmem = (std::size_t)(kNW + kNT + kActFloats) * sizeof(float);
-
 }  // namespace
 
 // ------------------------------------------------------------- allocation-free backward
@@ -546,8 +326,9 @@ constexpr std::size_t kBwdSmem = (std::size_t)(kNW + kNT + kActFloats) * sizeof(
 // pre-reserved memory budget may not call cudaMalloc or any allocating library routine -- use
 // ngp_field_backward_noalloc instead, whose partials live in the array below: room for
 // kNoAllocMaxParts partials (256 x 9408 floats = 9.6 MB), held by every GPU that loads the library
-// until the process exits.  The kernel strides its CTAs over the batch's tiles, so a call launches
-// min(SM count, kNoAllocMaxParts, tiles) CTAs and any batch would fit the array; the batch limit
+// until the process exits.  The kernel (the tensor-core backward of ngp_field_backward) strides its
+// CTAs over the batch's tiles, so a call launches min(SM count, kNoAllocMaxParts) CTAs, each of
+// which writes its partial, and any batch would fit the array; the batch limit
 // NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES is a deliberate, published bound of this entry point (a
 // caller sizes its batches against it), not a property of the array.  Each call overwrites every
 // partial it later reads, so nothing has to be cleared between calls; but all calls share the one
@@ -562,26 +343,6 @@ int mlp_partials_count() { return sm_count(); }
 std::size_t mlp_partials_floats() { return (std::size_t)mlp_partials_count() * kNW; }
 
 static bool aligned16(const void *p) { return ((std::uintptr_t)p & 15u) == 0; }
-
-// `partials` must hold mlp_partials_floats() floats (scratch).
-int launch_mlp_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
-                        const float *enc, const float *dirs, const float *weights,
-                        const float *dL_ddrgb, const float *grad_scale, float *dL_denc,
-                        float *dL_dweights, float *partials, bool accumulate) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
-                  "mlp: buffers must be 16-byte aligned");
-    NGP_SMEM_LIMIT((mlp_backward_kernel<kBwdThreads>), kBwdSmem);
-    const unsigned grid = (unsigned)mlp_partials_count();
-    mlp_backward_kernel<kBwdThreads><<<grid, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, partials);
-    count_launches(1);
-    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(grid, partials, dL_dweights, accumulate ? 1 : 0);
-    count_launches(1);
-    if (count != nullptr && n > 0) {
-        zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
-        count_launches(1);
-    }
-    return launch_status();
-}
 
 int launch_prop_forward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
                         const float *weights, float *x) {
@@ -646,12 +407,13 @@ static int noalloc_scratch(float **out) {
     return NGP_OK;
 }
 
+int launch_mlp_x6_backward(cudaStream_t, std::uint32_t, const std::uint32_t *, const float *, const float *,
+                           const float *, const float *, const float *, float *, float *, unsigned, unsigned *);
+
 int launch_mlp_backward_noalloc(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count,
                                 const float *enc, const float *dirs, const float *weights,
                                 const float *dL_ddrgb, const float *grad_scale, float *dL_denc,
                                 float *dL_dweights, bool accumulate) {
-    NGP_CHECK_ARG(aligned16(enc) && aligned16(weights) && aligned16(dL_ddrgb) && aligned16(dL_denc),
-                  "mlp: buffers must be 16-byte aligned");
     if (n > kNoAllocMaxSamples) {
         set_last_status(NGP_ERR_CAPACITY,
                         "ngp_field_backward_noalloc: n_samples exceeds 524288, the published limit of this entry "
@@ -661,23 +423,11 @@ int launch_mlp_backward_noalloc(cudaStream_t stream, std::uint32_t n, const std:
     float *scratch = nullptr;
     int st = noalloc_scratch(&scratch);
     if (st != NGP_OK) return st;
-    NGP_SMEM_LIMIT((mlp_backward_kernel<kBwdThreads>), kBwdSmem);
-    const std::uint32_t tiles = (n + kTile - 1) / kTile;
-    std::uint32_t parts = (std::uint32_t)sm_count();
-    if (parts > kNoAllocMaxParts) parts = kNoAllocMaxParts;
-    if (parts > tiles) parts = tiles;
-    if (parts > 0) {
-        mlp_backward_kernel<kBwdThreads><<<parts, kBwdThreads, kBwdSmem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb,
-                                                                                   grad_scale, dL_denc, scratch);
-        count_launches(1);
-    }
-    reduce_partials_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(parts, scratch, dL_dweights, accumulate ? 1 : 0);
-    count_launches(1);
-    if (count != nullptr && n > 0) {
-        zero_rows_kernel<<<grid_for((std::size_t)n * 32, 256, 4), 256, 0, stream>>>(n, count, dL_denc, 32);
-        count_launches(1);
-    }
-    return launch_status();
+    unsigned parts = 0;
+    st = launch_mlp_x6_backward(stream, n, count, enc, dirs, weights, dL_ddrgb, grad_scale, dL_denc, scratch,
+                                kNoAllocMaxParts, &parts);
+    if (st != NGP_OK) return st;
+    return launch_mlp_partials_reduce(stream, parts, scratch, dL_dweights, accumulate, n, count, dL_denc, 32u);
 }
 
 }  // namespace ngp

@@ -748,25 +748,36 @@ __device__ __forceinline__ void split3(float v, float &a, float &b, float &c) {
     c = r - b;               // exact; rounded to BF16 when stored
 }
 
+// The three pieces of (x, y) as packed BF16 pairs: the same values as split3, two at a time.
+__device__ __forceinline__ void split3_pair(float x, float y, std::uint32_t &p1, std::uint32_t &p2, std::uint32_t &p3) {
+    p1 = Bf16Op::pack(x, y);
+    const float2 f1 = Bf16Op::unpack(p1);
+    const float rx = x - f1.x, ry = y - f1.y;   // exact
+    p2 = Bf16Op::pack(rx, ry);
+    const float2 f2 = Bf16Op::unpack(p2);
+    p3 = Bf16Op::pack(rx - f2.x, ry - f2.y);    // the differences exact, then rounded
+}
+
+// Columns [c0, c0 + C) of row r of a tile with N columns (c0, C multiples of 8) as three BF16
+// pieces `piece` elements apart; v holds the C values.
+template <int N, int C>
+__device__ __forceinline__ void store_cols3(__nv_bfloat16 *buf, int piece, int r, int c0, const float *v) {
+#pragma unroll
+    for (int c = 0; c < C; c += 8) {
+        uint4 q[3];
+        split3_pair(v[c + 0], v[c + 1], q[0].x, q[1].x, q[2].x);
+        split3_pair(v[c + 2], v[c + 3], q[0].y, q[1].y, q[2].y);
+        split3_pair(v[c + 4], v[c + 5], q[0].z, q[1].z, q[2].z);
+        split3_pair(v[c + 6], v[c + 7], q[0].w, q[1].w, q[2].w);
+#pragma unroll
+        for (int p = 0; p < 3; ++p) *reinterpret_cast<uint4 *>(buf + p * piece + rb(r, c0 + c, N)) = q[p];
+    }
+}
+
 // Row r of a tile with N columns (N % 8 == 0) as three BF16 pieces `piece` elements apart.
 template <int N>
 __device__ __forceinline__ void store_row3(__nv_bfloat16 *buf, int piece, int r, const float *v) {
-#pragma unroll
-    for (int c = 0; c < N; c += 8) {
-        float a[8], b[8], e[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) split3(v[c + j], a[j], b[j], e[j]);
-        const float *src[3] = {a, b, e};
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-            uint4 q;
-            q.x = Bf16Op::pack(src[p][0], src[p][1]);
-            q.y = Bf16Op::pack(src[p][2], src[p][3]);
-            q.z = Bf16Op::pack(src[p][4], src[p][5]);
-            q.w = Bf16Op::pack(src[p][6], src[p][7]);
-            *reinterpret_cast<uint4 *>(buf + p * piece + rb(r, c, N)) = q;
-        }
-    }
+    store_cols3<N, N>(buf, piece, r, 0, v);
 }
 
 // The forward weight operands (W^T, layout of load_weights_tc) in three pieces, kFwdW elements apart.
@@ -789,12 +800,22 @@ __device__ void load_weights_x6(const float *__restrict__ w, __nv_bfloat16 *sw) 
     }
 }
 
-// D (tmem) = A @ B^T to FP32 accuracy: the six piece products, smallest first.
+// D (tmem) = A @ B^T to FP32 accuracy: the six piece products, smallest first -- a3 b1, a2 b2,
+// a1 b3, a2 b1, a1 b2, a1 b1 (A's pieces `a_piece`, B's `b_piece` elements apart).
 __device__ __forceinline__ void mma_kk_x6(std::uint32_t d, const __nv_bfloat16 *a, int a_piece, const __nv_bfloat16 *b,
-                                          int K, int N) {
+                                          int K, int N, int b_piece = kFwdW) {
     const int ap[6] = {2, 1, 0, 1, 0, 0}, bp[6] = {0, 1, 2, 0, 1, 0};
 #pragma unroll
-    for (int k = 0; k < 6; ++k) mma_kk<Bf16Op>(d, a + ap[k] * a_piece, b + bp[k] * kFwdW, K, N, k > 0);
+    for (int k = 0; k < 6; ++k) mma_kk<Bf16Op>(d, a + ap[k] * a_piece, b + bp[k] * b_piece, K, N, k > 0);
+}
+
+// D (tmem, M = 64) (+)= A^T @ B over the tile's 128 samples to FP32 accuracy (mma_mn on the six
+// piece products; both operands' pieces kX6Piece elements apart).
+__device__ __forceinline__ void mma_mn_x6(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int N,
+                                          bool acc) {
+    const int ap[6] = {2, 1, 0, 1, 0, 0}, bp[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) mma_mn<Bf16Op>(d, a + ap[k] * kX6Piece, b + bp[k] * kX6Piece, N, acc || k > 0);
 }
 
 template <bool kDensity>
@@ -891,6 +912,300 @@ __global__ void __launch_bounds__(kX6Wgs * 128, 1) mlp_x6_forward_kernel(
     tc::fence_before();
     __syncthreads();
     if (threadIdx.x < 32) tc::tmem_free(tbase, 256);
+}
+
+// ------------------------------------------------ FP32-accurate backward on the tensor cores
+//
+// ngp_field_backward with the same three-piece BF16 products as the forward above.  A CTA (one per
+// SM) works on one tile of 128 samples at a time with 256 threads, two per sample row: thread
+// (r, h) owns columns [w h, w (h + 1)) of a layer of width 2w.  The recomputed forward leaves each
+// thread's share of the layer inputs the backward needs again in registers (h1 and h2 values, x or
+// the SH features, the encodings, and the relu decisions of h1, h2, h3 as bit masks), so tensor
+// memory holds only the current layer's result and the dW accumulators, and shared memory only the
+// operands of the layer at hand: two three-piece buffers P and Q, 48 KB each, beside the weights'
+// three pieces in both layouts (W^T for the forward, W for the data gradients).  Each adjoint step
+// issues the weight-gradient MMA (M = 64, the tile's samples as the contraction, accumulated in
+// tensor memory across all tiles of the CTA) and the data-gradient MMA on the same operands; the
+// next step's gradient and layer input then overwrite P and Q, whose MMAs have completed.
+constexpr int kB6Threads = 256;
+constexpr int kB6Weights = 3 * kAllW;                                               // pieces kAllW apart
+constexpr std::size_t kB6Smem = (std::size_t)(kB6Weights + 2 * kX6WgAct) * 2;      // 210 KB
+// Tensor-memory columns: every layer's result, then the dW accumulators.
+constexpr std::uint32_t kTD = 0;
+constexpr std::uint32_t kTA0 = 64, kTA1 = 96, kTA2 = 112, kTA3 = 144, kTA4 = 208, kTCols = 256;
+static_assert(kTA4 + 16 <= kTCols, "tensor-memory columns");
+
+// The weights' three pieces in the forward (W^T) and backward (W) operand layouts of load_weights_tc.
+__device__ void load_weights_x6b(const float *__restrict__ w, __nv_bfloat16 *sw) {
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+    for (int i = threadIdx.x; i < kB6Weights; i += blockDim.x) sw[i] = zero;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kNW; i += blockDim.x) {
+        int f, b = -1;
+        if (i < kW1) { const int in = i / 64, out = i % 64; f = kF0 + rb(out, in, 32); b = kG0 + rb(in, out, 64); }
+        else if (i < kW2) { const int j = i - kW1, in = j / 16, out = j % 16; f = kF1 + rb(out, in, 64); b = kG1 + rb(in, out, 16); }
+        else if (i < kW3) {
+            const int j = i - kW2, in = j / 64, out = j % 64;
+            f = kF2 + rb(out, in, 32);
+            if (in < 16) b = kG2 + rb(in, out, 64);   // the data gradient needs the x rows only
+        }
+        else if (i < kW4) { const int j = i - kW3, in = j / 64, out = j % 64; f = kF3 + rb(out, in, 64); b = kG3 + rb(in, out, 64); }
+        else { const int j = i - kW4, in = j / 3, out = j % 3; f = kF4 + rb(out, in, 64); b = kG4 + rb(in, out, 16); }
+        float p[3];
+        split3(w[i], p[0], p[1], p[2]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const __nv_bfloat16 v = __float2bfloat16_rn(p[k]);
+            sw[k * kAllW + f] = v;
+            if (b >= 0) sw[k * kAllW + b] = v;
+        }
+    }
+}
+
+// relu over 32 values in place; bit i of the result is the decision v[i] > 0.
+__device__ __forceinline__ std::uint32_t relu_bits32(float *v) {
+    std::uint32_t m = 0;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        m |= (v[i] > 0.f ? 1u : 0u) << i;
+        v[i] = fmaxf(v[i], 0.f);
+    }
+    return m;
+}
+
+// The relu adjoint: v[i] where bit i of m is set, else 0.
+__device__ __forceinline__ void mask_bits32(float *v, std::uint32_t m) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = (m >> i) & 1u ? v[i] : 0.f;
+}
+
+// `grad_scale` multiplies dL/ddrgb; `partials` receives one [9408] dL/dW partial per CTA (grid =
+// the SM count), zero for a CTA without tiles.  dL/denc rows past the active count are not written.
+__global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
+    std::uint32_t n, const std::uint32_t *__restrict__ count, const float *__restrict__ enc,
+    const float *__restrict__ dirs, const float *__restrict__ weights, const float *__restrict__ dL_ddrgb,
+    const float *__restrict__ grad_scale, float *__restrict__ dL_denc, float *__restrict__ partials) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ std::uint64_t bar;
+    __shared__ std::uint32_t tbase;
+    __shared__ int fail;
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    __nv_bfloat16 *P = sw + kB6Weights, *Q = P + kX6WgAct;
+    const int r = threadIdx.x % kRows, h = threadIdx.x / kRows;   // h is uniform over a warp
+    load_weights_x6b(weights, sw);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        fail = 0;
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(&tbase, kTCols);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const std::uint32_t t0 = tbase;                                            // for the MMAs (lane 0)
+    const std::uint32_t tm = tbase + ((std::uint32_t)((r / 32) * 32) << 16);   // this warp's lanes
+    const bool leader = threadIdx.x == 0;
+    std::uint32_t phase = 0;
+    auto sync = [&] {
+        tc::fence_async_smem();
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+    };
+    auto wait = [&] {
+        if (!tc::mbar_wait(&bar, phase, kWaitLimit)) fail = 1;
+        phase ^= 1u;
+        tc::fence_after();
+    };
+
+    const float gs = grad_scale != nullptr ? *grad_scale : 1.f;
+    const std::uint32_t n_act = active_count(n, count);
+    const std::uint32_t n_tiles = (n_act + kRows - 1) / kRows;
+    // This thread's inputs of a tile: encoding columns [16h, 16h + 16), and dL/ddrgb (h = 0) or the
+    // direction (h = 1), fetched one tile ahead.
+    float ne[16];
+    float4 nx;
+    auto fetch = [&](std::uint32_t tile) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n_act;
+#pragma unroll
+        for (int c = 0; c < 16; c += 4) {
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) q = *reinterpret_cast<const float4 *>(enc + s * 32 + 16 * h + c);
+            ne[c] = q.x;
+            ne[c + 1] = q.y;
+            ne[c + 2] = q.z;
+            ne[c + 3] = q.w;
+        }
+        if (h == 0) nx = valid ? reinterpret_cast<const float4 *>(dL_ddrgb)[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        else nx = valid ? make_float4(dirs[s * 3 + 0], dirs[s * 3 + 1], dirs[s * 3 + 2], 0.f) : make_float4(0.f, 0.f, 1.f, 0.f);
+    };
+    bool first = true;
+    fetch(blockIdx.x);
+    for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const std::size_t s = (std::size_t)tile * kRows + r;
+        const bool valid = s < n_act;
+        float e[16], v[32], h1[32], h2[32], xs[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) e[i] = ne[i];
+        const float4 x4 = nx;
+        fetch(tile + gridDim.x);
+
+        // forward: h1 = relu(enc W0), x = h1 W1, h2 = relu([x, sh] W2), h3 = relu(h2 W3), a4 = h3 W4
+        store_cols3<32, 16>(P, kX6Piece, r, 16 * h, e);
+        sync();
+        if (leader) { mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kF0, 32, 64, kAllW); tc::commit(&bar); }
+        wait();
+        tc::ld32(tm + kTD + 32 * h, h1);
+        const std::uint32_t m1 = relu_bits32(h1);
+        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h1);
+        sync();
+        if (leader) { mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kF1, 64, 16, kAllW); tc::commit(&bar); }
+        wait();
+        if (h == 0) tc::ld16(tm + kTD, xs);     // x
+        else sh4(x4.x, x4.y, x4.z, xs);          // SH of the direction
+        store_cols3<32, 16>(P, kX6Piece, r, 16 * h, xs);
+        sync();
+        if (leader) { mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kF2, 32, 64, kAllW); tc::commit(&bar); }
+        wait();
+        tc::ld32(tm + kTD + 32 * h, h2);
+        const std::uint32_t m2 = relu_bits32(h2);
+        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h2);
+        sync();
+        if (leader) { mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kF3, 64, 64, kAllW); tc::commit(&bar); }
+        wait();
+        tc::ld32(tm + kTD + 32 * h, v);
+        const std::uint32_t m3 = relu_bits32(v);
+        store_cols3<64, 32>(P, kX6Piece, r, 32 * h, v);   // P = h3
+        sync();
+        if (leader) { mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kF4, 64, 16, kAllW); tc::commit(&bar); }
+        wait();
+
+        // output layer: dL/da4 (3 columns, padded to 16) and dL/dx0 through the truncated exponential
+        float dx0 = 0.f;
+        if (h == 0) {
+            tc::ld16(tm + kTD, v);
+            float d[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) d[i] = 0.f;
+            const float g[3] = {x4.y, x4.z, x4.w};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float rgb = 1.f / (1.f + expf(-v[c]));
+                d[c] = gs * g[c] * rgb * (1.f - rgb);
+            }
+            dx0 = gs * x4.x * expf(fminf(fmaxf(xs[0], -15.f), 15.f));
+            store_cols3<16, 16>(Q, kX6Piece, r, 0, d);   // Q = dA4
+        }
+        // layer 4: dW4 += h3^T dA4;  dh3 = dA4 W4^T
+        sync();
+        if (leader) {
+            mma_mn_x6(t0 + kTA4, P, Q, 16, !first);
+            mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG4, 16, 64, kAllW);
+            tc::commit(&bar);
+        }
+        wait();
+        tc::ld32(tm + kTD + 32 * h, v);
+        mask_bits32(v, m3);
+        store_cols3<64, 32>(P, kX6Piece, r, 32 * h, v);   // P = dA3
+        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h2);  // Q = h2
+        // layer 3: dW3^T += dA3^T h2;  dh2 = dA3 W3^T
+        sync();
+        if (leader) {
+            mma_mn_x6(t0 + kTA3, P, Q, 64, !first);
+            mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kG3, 64, 64, kAllW);
+            tc::commit(&bar);
+        }
+        wait();
+        tc::ld32(tm + kTD + 32 * h, v);
+        mask_bits32(v, m2);
+        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, v);   // Q = dA2
+        store_cols3<32, 16>(P, kX6Piece, r, 16 * h, xs);  // P = [x, sh]
+        // layer 2: dW2^T += dA2^T [x, sh];  dx = dA2 W2[:16]^T
+        sync();
+        if (leader) {
+            mma_mn_x6(t0 + kTA2, Q, P, 32, !first);
+            mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG2, 64, 16, kAllW);
+            tc::commit(&bar);
+        }
+        wait();
+        if (h == 0) {
+            tc::ld16(tm + kTD, v);
+            v[0] += dx0;
+            store_cols3<16, 16>(P, kX6Piece, r, 0, v);    // P = dx
+        }
+        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h1);  // Q = h1
+        // layer 1: dW1 += h1^T dx;  dh1 = dx W1^T
+        sync();
+        if (leader) {
+            mma_mn_x6(t0 + kTA1, Q, P, 16, !first);
+            mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kG1, 16, 64, kAllW);
+            tc::commit(&bar);
+        }
+        wait();
+        tc::ld32(tm + kTD + 32 * h, v);
+        mask_bits32(v, m1);
+        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, v);   // Q = dA1
+        store_cols3<32, 16>(P, kX6Piece, r, 16 * h, e);   // P = enc
+        // layer 0: dW0^T += dA1^T enc;  denc = dA1 W0^T
+        sync();
+        if (leader) {
+            mma_mn_x6(t0 + kTA0, Q, P, 32, !first);
+            mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG0, 64, 32, kAllW);
+            tc::commit(&bar);
+        }
+        wait();
+        tc::ld16(tm + kTD + 16 * h, v);
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < 16; c += 4)
+                *reinterpret_cast<float4 *>(dL_denc + s * 32 + 16 * h + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+        }
+        first = false;
+        tc::fence_before();
+        __syncthreads();   // every thread has read the tile's results before the next tile's MMAs
+        if (fail) break;
+    }
+    if (fail && threadIdx.x == 0) atomicOr(&g_device_error, 1u);
+
+    // dW, in the packed [in][out] layout: row m of an M = 64 accumulator sits in TMEM lane
+    // m64_lane(m); the two threads of a lane read different accumulators.
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    float *p = partials + (std::size_t)blockIdx.x * kNW;
+    if (first) {
+        for (int i = threadIdx.x; i < kNW; i += blockDim.x) p[i] = 0.f;
+    } else {
+        const int m = (r & 31) < 16 ? (r >> 5) * 16 + (r & 15) : -1;
+        float a[64];
+        if (h == 0) {
+            tc::ld32(tm + kTA0, a);   // dW0^T: row = out, 32 columns = in
+            if (m >= 0)
+#pragma unroll
+                for (int i = 0; i < 32; ++i) p[kW0 + i * 64 + m] = a[i];
+            tc::ld16(tm + kTA1, a);   // dW1: row = in, 16 columns = out
+            if (m >= 0)
+#pragma unroll
+                for (int o = 0; o < 16; ++o) p[kW1 + m * 16 + o] = a[o];
+            tc::ld16(tm + kTA4, a);   // dW4: row = in, columns 0..2 = out
+            if (m >= 0)
+#pragma unroll
+                for (int o = 0; o < 3; ++o) p[kW4 + m * 3 + o] = a[o];
+        } else {
+            tc::ld32(tm + kTA2, a);   // dW2^T: row = out, 32 columns = in
+            if (m >= 0)
+#pragma unroll
+                for (int i = 0; i < 32; ++i) p[kW2 + i * 64 + m] = a[i];
+            tc::ld64(tm + kTA3, a);   // dW3^T: row = out, 64 columns = in
+            if (m >= 0)
+#pragma unroll
+                for (int i = 0; i < 64; ++i) p[kW3 + i * 64 + m] = a[i];
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_free(tbase, kTCols);
 }
 
 // ------------------------------------------------------------------ proposal network (FP16)
@@ -1179,6 +1494,24 @@ int launch_mlp_x6_density(cudaStream_t stream, std::uint32_t n, const float *enc
     const unsigned grid = want < (unsigned)sm_count() ? want : (unsigned)sm_count();
     mlp_x6_forward_kernel<true><<<grid, kX6Wgs * 128, kX6Smem, stream>>>(n, nullptr, enc, nullptr, weights, sigma);
     count_launches(1);
+    return launch_status();
+}
+
+// The FP32 field backward on the tensor cores (mlp_x6_backward_kernel): one CTA per SM, at most
+// `max_parts`, each writing one dL/dW partial to `partials` (that many x 9408 floats); their count
+// in *grid_out.
+int launch_mlp_x6_backward(cudaStream_t stream, std::uint32_t n, const std::uint32_t *count, const float *enc,
+                           const float *dirs, const float *weights, const float *dL_ddrgb, const float *grad_scale,
+                           float *dL_denc, float *partials, unsigned max_parts, unsigned *grid_out) {
+    NGP_CHECK_ARG(aligned16(enc) && aligned16(dL_ddrgb) && aligned16(dL_denc) && aligned16(partials),
+                  "mlp: buffers must be 16-byte aligned");
+    NGP_CHECK_ARG(max_parts > 0, "mlp: no room for a dL/dW partial");
+    NGP_SMEM_LIMIT(mlp_x6_backward_kernel, kB6Smem);
+    const unsigned grid = (unsigned)sm_count() < max_parts ? (unsigned)sm_count() : max_parts;
+    mlp_x6_backward_kernel<<<grid, kB6Threads, kB6Smem, stream>>>(n, count, enc, dirs, weights, dL_ddrgb, grad_scale,
+                                                                   dL_denc, partials);
+    count_launches(1);
+    *grid_out = grid;
     return launch_status();
 }
 

@@ -113,6 +113,33 @@ def backward(dL_ddrgb: np.ndarray, cache, w: Dict[str, np.ndarray], dtype=np.flo
     return denc, grads
 
 
+def kink_flip_tolerance(dL_ddrgb: np.ndarray, cache, w: Dict[str, np.ndarray], rel: float = 1e-6):
+    """What ReLU decisions within rounding of a kink can move in the backward.  A pre-activation a
+    with |a| <= rel * sum_k |x_k w_k| (x its layer input, w its weight column) may come out on either
+    side of 0 in any float32-accurate evaluation of the layer; for every such entry the bound adds
+    |backward of that one sample with the decision flipped - backward without| (FP64, one flip at a
+    time; `cache` from forward(..., dtype=np.float64)).  Returns (dict of per-element bounds on
+    dL/dW, per-element bounds on dL/denc [S, 32], number of such entries)."""
+    w64 = {k: np.asarray(v, np.float64) for k, v in w.items()}
+    g = np.asarray(dL_ddrgb, np.float64)
+    tol_w = {k: np.zeros_like(v) for k, v in w64.items()}
+    tol_enc = np.zeros((g.shape[0], w64["W0"].shape[0]))
+    n_near = 0
+    for a_key, x_key, w_key in (("a1", "enc", "W0"), ("a2", "c", "W2"), ("a3", "h2", "W3")):
+        a = np.asarray(cache[a_key], np.float64)
+        absum = np.abs(np.asarray(cache[x_key], np.float64)) @ np.abs(w64[w_key])
+        for s, u in np.argwhere(np.abs(a) <= rel * absum):
+            n_near += 1
+            one = {k: np.array(v[s:s + 1], np.float64) for k, v in cache.items()}
+            enc0, gw0 = backward(g[s:s + 1], one, w64)
+            one[a_key][0, u] = -a[s, u] if a[s, u] != 0 else 1e-300
+            enc1, gw1 = backward(g[s:s + 1], one, w64)
+            for k in tol_w:
+                tol_w[k] += np.abs(gw1[k] - gw0[k])
+            tol_enc[s] += np.abs(enc1 - enc0)[0]
+    return tol_w, tol_enc, n_near
+
+
 def round_bf16(x) -> np.ndarray:
     """float32 values rounded to bfloat16 (nearest, ties to even), returned as float32."""
     a = np.ascontiguousarray(x, np.float32)

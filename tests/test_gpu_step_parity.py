@@ -18,8 +18,11 @@ Bars:
 * loss: 1e-5 relative; dL/ddrgbs: 1e-5 of each column's scale, plus the float32 uncertainty of
   the loss residual (pred - gt) propagated to each sample, on rays away from the T = 1e-4 stopping
   threshold;
-* dL/dW and dL/dlatents: 1e-5 of each matrix's scale against FP64 sums taken with the FP32
-  kernel's own ReLU decisions (oracle.field.forward_fma32 reproduces its pre-activations);
+* dL/dW and dL/dlatents: 1e-5 of each matrix's scale against FP64 sums with FP64 ReLU decisions,
+  plus, per element, what the decisions within float32-accurate rounding of a kink can move (every
+  pre-activation within 1e-6 of its terms' absolute sum, flipped one at a time in FP64: the field
+  kernels evaluate each layer to FP32 accuracy on the tensor cores, whose pre-activations no
+  float32 restatement reproduces to the bit);
 * the parameter update: the optax chain on the step's own gradients, 1e-6 relative.
 """
 import numpy as np
@@ -219,14 +222,22 @@ def test_train_step_matches_cpu_restatement(scene):
           f"(bar 1e-5 plus the residual's propagated float32 uncertainty); samples over the bar {int(over.sum())}")
     assert not over.any()
 
-    # ---- field backward (FP64 with the kernel's ReLU decisions) and table scatter
-    denc64, gw64 = Fd.backward(g_drgbs_g, cache, w0, dtype=np.float64)
+    # ---- field backward (FP64, FP64 ReLU decisions, plus what decisions at a kink can move) and
+    # table scatter
+    _, cache64 = Fd.forward(enc, dirs_g[:used], w0, dtype=np.float64)
+    denc64, gw64 = Fd.backward(g_drgbs_g, cache64, w0, dtype=np.float64)
+    tol_w, tol_enc, n_near = Fd.kink_flip_tolerance(g_drgbs_g, cache64, w0)
     gw_g = {k: v.cpu().numpy() for k, v in unpack_weights(spy.rec["w_in"][1]).items()}
+    print(f"dL/dW vs FP64: {max(mat_err(gw_g[k], gw64[k]) for k in gw64):.2e} of the matrix scale; "
+          f"{n_near} pre-activations within 1e-6 of a kink")
     for k in gw64:
-        assert mat_err(gw_g[k], gw64[k]) <= 1e-5, (k, mat_err(gw_g[k], gw64[k]))
+        over = np.abs(gw_g[k] - gw64[k]) > 1e-5 * np.abs(gw64[k]).max() + tol_w[k]
+        assert not over.any(), (k, mat_err(gw_g[k], gw64[k]), int(over.sum()))
     glat64 = H.encode_backward(xyz_g[:used], denc64, tr.bound, tab, dtype=np.float64)
+    tol_lat = H.encode_backward(xyz_g[:used], tol_enc, tr.bound, tab, dtype=np.float64)   # weights >= 0
     glat_g = h(spy.rec["lat_in"][1])
-    assert mat_err(glat_g, glat64) <= 1e-5, mat_err(glat_g, glat64)
+    over = np.abs(glat_g - glat64) > 1e-5 * np.abs(glat64).max() + tol_lat
+    assert not over.any(), (mat_err(glat_g, glat64), int(over.sum()))
 
     # ---- optimiser: the optax chain on the step's own gradients
     lr = OP.reference_lr(count0, cfg.lr)
