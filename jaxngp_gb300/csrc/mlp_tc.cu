@@ -50,6 +50,7 @@ constexpr std::uint32_t kWaitLimit = 1u << 22;
 // gradients: B[n = in][k = out] (= W).  Layer 4 has 3 outputs, padded to 16 with zeros.
 constexpr int kF0 = 0, kF1 = 2048, kF2 = 3072, kF3 = 5120, kF4 = 9216, kFwdW = 10240;
 constexpr int kG4 = 10240, kG3 = 11264, kG2 = 15360, kG1 = 16384, kG0 = 17408, kAllW = 19456;
+static_assert(kFwdW % 8 == 0 && kAllW % 8 == 0, "weight pieces start on 16-byte boundaries");
 
 // Per-warpgroup activation rows (element offsets): layer inputs of the tile, and the output-layer
 // gradient for the backward.
@@ -170,20 +171,19 @@ __device__ void load_weights_tc(const float *__restrict__ w, typename E::T *sw, 
 template <class E>
 __device__ __forceinline__ void mma_kk(std::uint32_t d, const typename E::T *a, const typename E::T *b, int K, int N,
                                        bool acc) {
-    const std::uint32_t id = tc::idesc_kf16(128, N, E::kFmt, false, false);
-    const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), sbo = (std::uint32_t)K * 16;
-    for (int j = 0; j < K / 16; ++j)
-        tc::mma_bf16(d, tc::sdesc(sa + j * 256, 128, sbo), tc::sdesc(sb + j * 256, 128, sbo), id, acc || j > 0);
+    const std::uint32_t id = tc::idesc_kf16(128, N, E::kFmt, false, false), sbo = (std::uint32_t)K * 16;
+    const tc::SDesc da = tc::sdesc2(smem_addr(a), 128, sbo), db = tc::sdesc2(smem_addr(b), 128, sbo);
+    for (int j = 0; j < K / 16; ++j) tc::mma_bf16(d, da, 16u * j, db, 16u * j, id, acc || j > 0);   // +256 bytes of K
 }
 
 // D (tmem, M = 64) += A^T @ B over the tile's 128 samples: A = buffer with 64 columns, B = buffer
 // with N columns, both read MN-major (the sample index is the contraction).
 template <class E>
 __device__ __forceinline__ void mma_mn(std::uint32_t d, const typename E::T *a, const typename E::T *b, int N, bool acc) {
-    const std::uint32_t id = tc::idesc_kf16(64, N, E::kFmt, true, true);
-    const std::uint32_t sa = smem_addr(a), sb = smem_addr(b), la = 64 * 16, lb = (std::uint32_t)N * 16;
-    for (int j = 0; j < kRows / 16; ++j)
-        tc::mma_bf16(d, tc::sdesc(sa + j * 2 * la, la, 128), tc::sdesc(sb + j * 2 * lb, lb, 128), id, acc || j > 0);
+    const std::uint32_t id = tc::idesc_kf16(64, N, E::kFmt, true, true), la = 64 * 16, lb = (std::uint32_t)N * 16;
+    const tc::SDesc da = tc::sdesc2(smem_addr(a), la, 128), db = tc::sdesc2(smem_addr(b), lb, 128);
+    for (int j = 0; j < kRows / 16; ++j)   // 16 rows of K: +2 LBO
+        tc::mma_bf16(d, da, j * 2 * la / 16, db, j * 2 * lb / 16, id, acc || j > 0);
 }
 
 // TMEM lane that holds row m of an M = 64 result: rows 16j..16j+15 sit in lanes 32j..32j+15
@@ -805,8 +805,15 @@ __device__ void load_weights_x6(const float *__restrict__ w, __nv_bfloat16 *sw) 
 __device__ __forceinline__ void mma_kk_x6(std::uint32_t d, const __nv_bfloat16 *a, int a_piece, const __nv_bfloat16 *b,
                                           int K, int N, int b_piece = kFwdW) {
     const int ap[6] = {2, 1, 0, 1, 0, 0}, bp[6] = {0, 1, 2, 0, 1, 0};
+    const std::uint32_t id = tc::idesc_kf16(128, N, Bf16Op::kFmt, false, false), sbo = (std::uint32_t)K * 16;
+    const tc::SDesc da = tc::sdesc2(smem_addr(a), 128, sbo), db = tc::sdesc2(smem_addr(b), 128, sbo);
+    // pieces are a_piece / b_piece elements (2 bytes each) apart: a_piece / 8 in 16-byte units
 #pragma unroll
-    for (int k = 0; k < 6; ++k) mma_kk<Bf16Op>(d, a + ap[k] * a_piece, b + bp[k] * b_piece, K, N, k > 0);
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int j = 0; j < K / 16; ++j)
+            tc::mma_bf16(d, da, (std::uint32_t)(ap[k] * (a_piece / 8) + 16 * j), db,
+                         (std::uint32_t)(bp[k] * (b_piece / 8) + 16 * j), id, k > 0 || j > 0);
 }
 
 // D (tmem, M = 64) (+)= A^T @ B over the tile's 128 samples to FP32 accuracy (mma_mn on the six
@@ -814,8 +821,15 @@ __device__ __forceinline__ void mma_kk_x6(std::uint32_t d, const __nv_bfloat16 *
 __device__ __forceinline__ void mma_mn_x6(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int N,
                                           bool acc) {
     const int ap[6] = {2, 1, 0, 1, 0, 0}, bp[6] = {0, 1, 2, 0, 1, 0};
+    const std::uint32_t id = tc::idesc_kf16(64, N, Bf16Op::kFmt, true, true), la = 64 * 16, lb = (std::uint32_t)N * 16;
+    const tc::SDesc da = tc::sdesc2(smem_addr(a), la, 128), db = tc::sdesc2(smem_addr(b), lb, 128);
+    static_assert(kX6Piece % 8 == 0, "pieces start on 16-byte boundaries");
 #pragma unroll
-    for (int k = 0; k < 6; ++k) mma_mn<Bf16Op>(d, a + ap[k] * kX6Piece, b + bp[k] * kX6Piece, N, acc || k > 0);
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int j = 0; j < kRows / 16; ++j)
+            tc::mma_bf16(d, da, (std::uint32_t)(ap[k] * (kX6Piece / 8)) + j * 2 * la / 16, db,
+                         (std::uint32_t)(bp[k] * (kX6Piece / 8)) + j * 2 * lb / 16, id, acc || k > 0 || j > 0);
 }
 
 template <bool kDensity>
@@ -986,7 +1000,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
     const float *__restrict__ dirs, const float *__restrict__ weights, const float *__restrict__ dL_ddrgb,
     const float *__restrict__ grad_scale, float *__restrict__ dL_denc, float *__restrict__ partials) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ std::uint64_t bar;
+    __shared__ std::uint64_t bar, wbar;   // data-path MMAs; weight-gradient MMAs
     __shared__ std::uint32_t tbase;
     __shared__ int fail;
     __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
@@ -995,6 +1009,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
     load_weights_x6b(weights, sw);
     if (threadIdx.x == 0) {
         tc::mbar_init(&bar, 1);
+        tc::mbar_init(&wbar, 1);
         fail = 0;
         tc::fence_mbar_init();
     }
@@ -1015,6 +1030,16 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
     auto wait = [&] {
         if (!tc::mbar_wait(&bar, phase, kWaitLimit)) fail = 1;
         phase ^= 1u;
+        tc::fence_after();
+    };
+    // A backward layer commits its data gradient (which the next layer waits for) to `bar` and its
+    // weight gradient, issued after it, to `wbar`: the data gradient's epilogue reads tensor memory
+    // while the weight-gradient MMAs still run, and waits for them only before it overwrites the
+    // P/Q rows they read.
+    std::uint32_t wphase = 0;
+    auto wait_w = [&] {
+        if (!tc::mbar_wait(&wbar, wphase, kWaitLimit)) fail = 1;
+        wphase ^= 1u;
         tc::fence_after();
     };
 
@@ -1100,59 +1125,70 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         // layer 4: dW4 += h3^T dA4;  dh3 = dA4 W4^T
         sync();
         if (leader) {
-            mma_mn_x6(t0 + kTA4, P, Q, 16, !first);
             mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG4, 16, 64, kAllW);
             tc::commit(&bar);
+            mma_mn_x6(t0 + kTA4, P, Q, 16, !first);
+            tc::commit(&wbar);
         }
         wait();
         tc::ld32(tm + kTD + 32 * h, v);
         mask_bits32(v, m3);
+        wait_w();
         store_cols3<64, 32>(P, kX6Piece, r, 32 * h, v);   // P = dA3
         store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h2);  // Q = h2
         // layer 3: dW3^T += dA3^T h2;  dh2 = dA3 W3^T
         sync();
         if (leader) {
-            mma_mn_x6(t0 + kTA3, P, Q, 64, !first);
             mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kG3, 64, 64, kAllW);
             tc::commit(&bar);
+            mma_mn_x6(t0 + kTA3, P, Q, 64, !first);
+            tc::commit(&wbar);
         }
         wait();
         tc::ld32(tm + kTD + 32 * h, v);
         mask_bits32(v, m2);
+        wait_w();
         store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, v);   // Q = dA2
         store_cols3<32, 16>(P, kX6Piece, r, 16 * h, xs);  // P = [x, sh]
         // layer 2: dW2^T += dA2^T [x, sh];  dx = dA2 W2[:16]^T
         sync();
         if (leader) {
-            mma_mn_x6(t0 + kTA2, Q, P, 32, !first);
             mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG2, 64, 16, kAllW);
             tc::commit(&bar);
+            mma_mn_x6(t0 + kTA2, Q, P, 32, !first);
+            tc::commit(&wbar);
         }
         wait();
         if (h == 0) {
             tc::ld16(tm + kTD, v);
             v[0] += dx0;
+        }
+        wait_w();
+        if (h == 0) {
             store_cols3<16, 16>(P, kX6Piece, r, 0, v);    // P = dx
         }
         store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h1);  // Q = h1
         // layer 1: dW1 += h1^T dx;  dh1 = dx W1^T
         sync();
         if (leader) {
-            mma_mn_x6(t0 + kTA1, Q, P, 16, !first);
             mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kG1, 16, 64, kAllW);
             tc::commit(&bar);
+            mma_mn_x6(t0 + kTA1, Q, P, 16, !first);
+            tc::commit(&wbar);
         }
         wait();
         tc::ld32(tm + kTD + 32 * h, v);
         mask_bits32(v, m1);
+        wait_w();
         store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, v);   // Q = dA1
         store_cols3<32, 16>(P, kX6Piece, r, 16 * h, e);   // P = enc
         // layer 0: dW0^T += dA1^T enc;  denc = dA1 W0^T
         sync();
         if (leader) {
-            mma_mn_x6(t0 + kTA0, Q, P, 32, !first);
             mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG0, 64, 32, kAllW);
             tc::commit(&bar);
+            mma_mn_x6(t0 + kTA0, Q, P, 32, !first);
+            tc::commit(&wbar);
         }
         wait();
         tc::ld16(tm + kTD + 16 * h, v);
@@ -1161,6 +1197,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
             for (int c = 0; c < 16; c += 4)
                 *reinterpret_cast<float4 *>(dL_denc + s * 32 + 16 * h + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
         }
+        wait_w();   // the next tile overwrites P and Q
         first = false;
         tc::fence_before();
         __syncthreads();   // every thread has read the tile's results before the next tile's MMAs

@@ -31,6 +31,19 @@ __device__ __forceinline__ std::uint64_t sdesc(std::uint32_t saddr, std::uint32_
            ((std::uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((std::uint64_t)1 << 46);
 }
 
+// A shared-memory descriptor as its two 32-bit halves.  The low half holds the start address (bits
+// 0-13, in 16-byte units) and the LBO; the descriptor of an offset of `b` bytes into the same buffer
+// is the low half plus b / 16 (shared addresses stay below 2^18 bytes, so the address field never
+// carries into the LBO), which makes a run of MMAs over one buffer one add per operand each.
+struct SDesc {
+    std::uint32_t lo, hi;
+};
+
+__device__ __forceinline__ SDesc sdesc2(std::uint32_t saddr, std::uint32_t lbo, std::uint32_t sbo) {
+    const std::uint64_t v = sdesc(saddr, lbo, sbo);
+    return {static_cast<std::uint32_t>(v), static_cast<std::uint32_t>(v >> 32)};
+}
+
 // Instruction descriptor of kind::f16 with an FP32 accumulator; `fmt` is the operand format of
 // both A and B (0 = FP16, 1 = BF16: one instruction never mixes them).
 __host__ __device__ constexpr std::uint32_t idesc_kf16(int M, int N, std::uint32_t fmt, bool a_mn, bool b_mn) {
@@ -55,6 +68,19 @@ __device__ __forceinline__ void mma_bf16(std::uint32_t d_tmem, std::uint64_t a, 
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
         :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate ? 1u : 0u) : "memory");
+}
+
+// The same MMA with the operand descriptors given as halves: (a_lo + a_off, a_hi) and (b_lo + b_off,
+// b_hi), the offsets in 16-byte units (see SDesc).
+__device__ __forceinline__ void mma_bf16(std::uint32_t d_tmem, SDesc a, std::uint32_t a_off, SDesc b,
+                                         std::uint32_t b_off, std::uint32_t idesc, bool accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t.reg .b64 da, db;\n\t"
+        "mov.b64 da, {%1, %2};\n\tmov.b64 db, {%3, %4};\n\t"
+        "setp.ne.b32 p, %6, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %5, p;\n\t}"
+        :: "r"(d_tmem), "r"(a.lo + a_off), "r"(a.hi), "r"(b.lo + b_off), "r"(b.hi), "r"(idesc),
+           "r"(accumulate ? 1u : 0u) : "memory");
 }
 
 // Arrive on `bar` once every MMA issued so far by this thread has completed.
