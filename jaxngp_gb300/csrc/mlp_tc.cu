@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     static_assert(!kTma || kHalf, "TMA tiles carry 16-bit encodings");
     using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ std::uint64_t bars[NWG], tbars[NWG][2];
+    __shared__ std::uint64_t bars[NWG], wbars[NWG], tbars[NWG][2];
     __shared__ std::uint32_t tbase;
     __shared__ int fails[NWG];
     __shared__ int tiles_done[NWG];
@@ -516,6 +516,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     if (threadIdx.x == 0) {
         for (int k = 0; k < NWG; ++k) {
             tc::mbar_init(&bars[k], 1);
+            tc::mbar_init(&wbars[k], 1);
             tc::mbar_init(&tbars[k][0], 1);
             tc::mbar_init(&tbars[k][1], 1);
             fails[k] = 0;
@@ -529,7 +530,17 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
     tc::fence_after();
     const std::uint32_t tm0 = tbase + (std::uint32_t)g * 256u;
     WarpGroup wg{g, r, tm0 + ((std::uint32_t)(q * 32) << 16), &bars[g], 0u, &fails[g]};
-    const bool leader = r == 0;
+    // In the backward layers the warpgroup's thread 0 issues the data-gradient MMAs (completing on
+    // bars[g]) and its thread 32, in another warp, the weight-gradient MMAs (completing on
+    // wbars[g]), side by side; the epilogue reads the data gradient while the weight gradient still
+    // runs and waits for it only before overwriting the rows it reads.
+    const bool leader = r == 0, wleader = r == 32;
+    std::uint32_t wphase = 0;
+    auto wait_w = [&] {
+        if (!tc::mbar_wait(&wbars[g], wphase, kWaitLimit)) *wg.fail = 1;
+        wphase ^= 1u;
+        tc::fence_after();
+    };
     float gs = grad_scale != nullptr ? *grad_scale : 1.f;
     if (ls != nullptr) gs *= ls->scale;
     bool fits = true;
@@ -594,9 +605,11 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
         // layer 4: dW4 += h3^T dA4;  dh3 = dA4 @ W4^T
         wg.sync();
         if (leader) {
-            mma_mn<E>(tm0 + kA4, act + kH3, act + kDY, 16, !first);
             mma_kk<E>(tm0 + kDA, act + kDY, sw + kG4, 16, 64, false);
             tc::commit(wg.bar);
+        } else if (wleader) {
+            mma_mn<E>(tm0 + kA4, act + kH3, act + kDY, 16, !first);
+            tc::commit(&wbars[g]);
         }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
@@ -607,13 +620,16 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
             for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
         }
         if (check) fits &= row_fits<E, 64>(v);
+        wait_w();
         store_row<E, 64>(act + kH3, r, v);  // dA3 over h3
         // layer 3: dW3^T += dA3^T h2;  dh2 = dA3 @ W3^T
         wg.sync();
         if (leader) {
-            mma_mn<E>(tm0 + kA3, act + kH3, act + kH2, 64, !first);
             mma_kk<E>(tm0 + kDA, act + kH3, sw + kG3, 64, 64, false);
             tc::commit(wg.bar);
+        } else if (wleader) {
+            mma_mn<E>(tm0 + kA3, act + kH3, act + kH2, 64, !first);
+            tc::commit(&wbars[g]);
         }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
@@ -624,25 +640,31 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
             for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
         }
         if (check) fits &= row_fits<E, 64>(v);
+        wait_w();
         store_row<E, 64>(act + kH2, r, v);  // dA2 over h2
         // layer 2: dW2^T += dA2^T [x, sh];  dx = dA2 @ W2[:16]^T
         wg.sync();
         if (leader) {
-            mma_mn<E>(tm0 + kA2, act + kH2, act + kX2, 32, !first);
             mma_kk<E>(tm0 + kDB, act + kH2, sw + kG2, 64, 16, false);
             tc::commit(wg.bar);
+        } else if (wleader) {
+            mma_mn<E>(tm0 + kA2, act + kH2, act + kX2, 32, !first);
+            tc::commit(&wbars[g]);
         }
         wg.wait();
         tc::ld16(wg.tm + kDB, v);
         v[0] += dx0;
         if (check) fits &= row_fits<E, 16>(v);
+        wait_w();
         store_row<E, 16>(act + kX2, r, v);  // dx (16 columns) over [x, sh]
         // layer 1: dW1 += h1^T dx;  dh1 = dx @ W1^T
         wg.sync();
         if (leader) {
-            mma_mn<E>(tm0 + kA1, act + kH1, act + kX2, 16, !first);
             mma_kk<E>(tm0 + kDA, act + kX2, sw + kG1, 16, 64, false);
             tc::commit(wg.bar);
+        } else if (wleader) {
+            mma_mn<E>(tm0 + kA1, act + kH1, act + kX2, 16, !first);
+            tc::commit(&wbars[g]);
         }
         wg.wait();
         tc::ld64(wg.tm + kDA, v);
@@ -653,13 +675,16 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
             for (int i = 0; i < 64; ++i) v[i] = h[i] > 0.f ? v[i] : 0.f;
         }
         if (check) fits &= row_fits<E, 64>(v);
+        wait_w();
         store_row<E, 64>(act + kH1, r, v);  // dA1 over h1
         // layer 0: dW0^T += dA1^T enc;  denc = dA1 @ W0^T
         wg.sync();
         if (leader) {
-            mma_mn<E>(tm0 + kA0, act + kH1, X0, 32, !first);
             mma_kk<E>(tm0 + kDA, act + kH1, sw + kG0, 64, 32, false);
             tc::commit(wg.bar);
+        } else if (wleader) {
+            mma_mn<E>(tm0 + kA0, act + kH1, X0, 32, !first);
+            tc::commit(&wbars[g]);
         }
         wg.wait();
         tc::ld32(wg.tm + kDA, v);
@@ -667,6 +692,7 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
             if (check) fits &= kHalf ? row_fits<E, 32>(v) : row_fits<F32Op, 32>(v);
             write_denc<E>(dL_denc, s, v);
         }
+        wait_w();   // the next tiles overwrite H1 and the encoding buffer
         first = false;
         tc::bar_sync(1 + g, 128);
         if (*wg.fail) break;
@@ -1019,7 +1045,10 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
     tc::fence_after();
     const std::uint32_t t0 = tbase;                                            // for the MMAs (lane 0)
     const std::uint32_t tm = tbase + ((std::uint32_t)((r / 32) * 32) << 16);   // this warp's lanes
-    const bool leader = threadIdx.x == 0;
+    // Thread 0 issues the data path's MMAs and commits them to `bar`; thread 32 (another warp, so
+    // the two issue streams run side by side) issues the weight gradients' MMAs and commits them to
+    // `wbar`.  The two streams write different tensor-memory columns and only read shared memory.
+    const bool leader = threadIdx.x == 0, wleader = threadIdx.x == 32;
     std::uint32_t phase = 0;
     auto sync = [&] {
         tc::fence_async_smem();
@@ -1032,10 +1061,10 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         phase ^= 1u;
         tc::fence_after();
     };
-    // A backward layer commits its data gradient (which the next layer waits for) to `bar` and its
-    // weight gradient, issued after it, to `wbar`: the data gradient's epilogue reads tensor memory
-    // while the weight-gradient MMAs still run, and waits for them only before it overwrites the
-    // P/Q rows they read.
+    // A backward layer's data gradient (which the next layer waits for) completes on `bar`, its
+    // weight gradient on `wbar`: the data gradient's epilogue reads tensor memory while the
+    // weight-gradient MMAs still run, and waits for them only before it overwrites the P/Q rows
+    // they read.
     std::uint32_t wphase = 0;
     auto wait_w = [&] {
         if (!tc::mbar_wait(&wbar, wphase, kWaitLimit)) fail = 1;
@@ -1127,6 +1156,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         if (leader) {
             mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG4, 16, 64, kAllW);
             tc::commit(&bar);
+        } else if (wleader) {
             mma_mn_x6(t0 + kTA4, P, Q, 16, !first);
             tc::commit(&wbar);
         }
@@ -1141,6 +1171,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         if (leader) {
             mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kG3, 64, 64, kAllW);
             tc::commit(&bar);
+        } else if (wleader) {
             mma_mn_x6(t0 + kTA3, P, Q, 64, !first);
             tc::commit(&wbar);
         }
@@ -1155,6 +1186,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         if (leader) {
             mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG2, 64, 16, kAllW);
             tc::commit(&bar);
+        } else if (wleader) {
             mma_mn_x6(t0 + kTA2, Q, P, 32, !first);
             tc::commit(&wbar);
         }
@@ -1173,6 +1205,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         if (leader) {
             mma_kk_x6(t0 + kTD, P, kX6Piece, sw + kG1, 16, 64, kAllW);
             tc::commit(&bar);
+        } else if (wleader) {
             mma_mn_x6(t0 + kTA1, Q, P, 16, !first);
             tc::commit(&wbar);
         }
@@ -1187,6 +1220,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
         if (leader) {
             mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG0, 64, 32, kAllW);
             tc::commit(&bar);
+        } else if (wleader) {
             mma_mn_x6(t0 + kTA0, Q, P, 32, !first);
             tc::commit(&wbar);
         }
