@@ -92,7 +92,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--forms", default="fp32-march,bf16-march,bf16x-march,bf16-proposal,bf16x-proposal,fp16x-proposal,bf16x-proposal-fb",
                    help="training forms to run, the first is the headline: fp32-march (the reference's "
-                        "algorithm, FP32 SIMT field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
+                        "algorithm, FP32-accurate field MLP), bf16-march (tensor-core BF16 MLP), bf16-proposal "
                         "(learned proposal sampler + BF16 MLP); the x forms (bf16x-*, fp16x-*) also gather from a "
                         "16-bit copy of the table and keep the encodings in 16 bits (fp16 under a dynamic loss scale)")
     p.add_argument("--occupancy-init", default="reference", choices=["reference", "analytic"],
@@ -758,7 +758,7 @@ def config4_block(args, cores: int) -> dict:
 
 def fp64_errors(tr) -> dict:
     """Errors of the form's colours against FP64 on a whole training batch (the last one trained,
-    at the trained weights).  The reference is the FP32 field (FP32 table, FP32 SIMT MLP)
+    at the trained weights).  The reference is the FP32 field (FP32 table, FP32-accurate MLP)
     composited in FP64 on the GPU (ngp_integrate_rays_fp64).  `chain`: the form's own encoder and
     field composited by the float integrator.  `integrator`: the FP32 field's samples composited
     in float.  Norm-relative over the batch's rays with samples (rgb, then opacity); rays whose

@@ -43,8 +43,9 @@ PRECISIONS = ("fp32", "bf16", "fp16")
 
 
 def entry(name: str, precision: str) -> str:
-    """Entry point of a field op for "fp32" (SIMT, the parity path) or "bf16" (tensor cores, BF16
-    operands with FP32 accumulation, FP32 encodings).  FP16 and 16-bit encodings go through the
+    """Entry point of a field op for "fp32" (the parity path: tensor cores at FP32 accuracy, three
+    BF16 pieces per operand) or "bf16" (tensor cores, BF16 operands with FP32 accumulation, FP32
+    encodings).  FP16 and 16-bit encodings go through the
     ``*_mixed`` entries (FieldOps)."""
     if precision not in ("fp32", "bf16"):
         raise ValueError(f"entry() covers fp32 and bf16; use FieldOps for {precision!r}")

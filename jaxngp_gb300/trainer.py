@@ -48,7 +48,7 @@ class TrainConfig:
     near: float = 0.3
     huber_delta: float = 0.1
     seed: int = 0
-    mlp_precision: str = "fp32"        # "fp32" (SIMT parity path), "bf16" or "fp16" (tensor cores)
+    mlp_precision: str = "fp32"        # "fp32" (parity path, FP32 accuracy), "bf16" or "fp16"
     table_precision: str = "fp32"      # "bf16"/"fp16": the encoder gathers from a 16-bit copy of the
                                        # FP32 table, which the table's Adam update rewrites
     half_activations: bool = False     # encodings and their gradient in the MLP's 16-bit type
