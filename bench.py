@@ -67,6 +67,11 @@ SCENES = {"blobs64": (64, 0, 100, 800, 1 << 18, WORKLOAD, METRIC),
                       "train rays/s (plain FP32 hash-grid NeRF step, 512 blobs + 8 shells, 2^20 samples)")}
 
 
+def empty_space_decay(args, sampler: str) -> float:
+    """The learned-proposal forms' empty-space density term (TrainConfig.empty_space_decay)."""
+    return float(args.empty_space_decay) if sampler == "proposal" else 0.0
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -100,6 +105,9 @@ def parse():
                         "refresh on its cadence, utils/types.py:1149-1392) before the untimed pretraining; analytic: "
                         "the grid starts from the scene's analytic density (a converged grid's stand-in)")
     p.add_argument("--psnr-views", type=int, default=8, help="held-out views the PSNR is averaged over")
+    p.add_argument("--empty-space-decay", type=float, default=0.0,
+                   help="learned-proposal forms: weight of the L1 density term at uniform random points of the box "
+                        "(TrainConfig.empty_space_decay; 0: off)")
     p.add_argument("--no-encoder-block", action="store_true", help="skip the standalone encoder block (config 0)")
     p.add_argument("--no-kernels-vs-reference", action="store_true",
                    help="skip timing the drop-in kernels against the reference's own sm_103a build")
@@ -333,7 +341,7 @@ def run_ours(args, data, form: str, with_render: bool, on_trainer=None) -> dict:
     precision, sampler, table, half_act = FORMS[form]
     cfg = TrainConfig(total_samples=args.samples, seed=rank, mlp_precision=precision, sampler=sampler,
                       table_precision=table, half_activations=half_act, proposal_fallback=form in FALLBACK_FORMS,
-                      pipeline=form in PIPELINE_FORMS)
+                      pipeline=form in PIPELINE_FORMS, empty_space_decay=empty_space_decay(args, sampler))
     tr = NGPTrainer(data, cfg)
     if args.occupancy_init == "analytic":
         tr.init_occupancy_analytic()
@@ -515,7 +523,9 @@ def run_ours(args, data, form: str, with_render: bool, on_trainer=None) -> dict:
     if tr.prop is not None:
         out["proposal"] = {"slots_per_step": tr.prop.slots, "samples_per_ray": tr.prop.spr,
                            "fallback_rays_per_proposal_step": round(tr.prop.fallback_rate(), 1)
-                           if cfg.proposal_fallback else None, "march_every": cfg.march_every}
+                           if cfg.proposal_fallback else None, "march_every": cfg.march_every,
+                           "empty_space_decay": cfg.empty_space_decay,
+                           "empty_space_points": cfg.empty_space_points if cfg.empty_space_decay > 0 else 0}
     if render is not None:
         out["render_1080p"] = render
     if render_prop is not None:
@@ -862,7 +872,8 @@ def equal_psnr(args, data, plain: str, fast: str) -> dict:
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
                                           table_precision=table, half_activations=half_act,
-                                          proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS))
+                                          proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS,
+                                          empty_space_decay=empty_space_decay(args, sampler)))
         if args.occupancy_init == "analytic":
             tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()
@@ -900,7 +911,8 @@ def convergence(args, data, forms) -> dict:
         precision, sampler, table, half_act = FORMS[f]
         tr = NGPTrainer(data, TrainConfig(total_samples=args.samples, seed=0, mlp_precision=precision, sampler=sampler,
                                           table_precision=table, half_activations=half_act,
-                                          proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS))
+                                          proposal_fallback=f in FALLBACK_FORMS, pipeline=f in PIPELINE_FORMS,
+                                          empty_space_decay=empty_space_decay(args, sampler)))
         if args.occupancy_init == "analytic":
             tr.init_occupancy_analytic()
         stream = torch.cuda.current_stream()

@@ -68,6 +68,11 @@ class TrainConfig:
                                        # rays that cross no occupied block at once (exact: the same samples)
     tv_scale: float = 0.0              # the encoder's total-variation term (encoders.py:236-254), added to
                                        # the loss and its gradient to the table's (0: off, the reference's default)
+    empty_space_decay: float = 0.0     # proposal sampler: weight of an L1 term on the density at uniform random
+                                       # points of the box, added to the step's gradients (0: off).  Space the
+                                       # proposal's samples never visit gets no photometric gradient and keeps
+                                       # its initial density, which the march renderer then shows as fog.
+    empty_space_points: int = 1 << 14  # random points per step of that term
 
 
 def cascades_for(bound: float) -> int:
@@ -180,6 +185,19 @@ class NGPTrainer:
             self.enc_d = torch.empty(self.prop.M, 32, **f32)
         elif cfg.sampler != "march":
             raise ValueError(f"sampler must be 'march' or 'proposal', got {cfg.sampler!r}")
+        self.empty = None
+        if cfg.empty_space_decay > 0 and self.prop is not None:
+            M = int(cfg.empty_space_points)
+            g_rows = torch.zeros(M, 4, **f32)
+            g_rows[:, 0] = float(cfg.empty_space_decay) / M   # d(decay * mean density)/d density
+            dirs = torch.zeros(M, 3, **f32)
+            dirs[:, 2] = 1.0                                   # no colour gradient: any unit direction
+            gen = torch.Generator(device=self.dev)
+            gen.manual_seed(cfg.seed + 0x9E3779B9)
+            genc = torch.empty(M, 32, dtype=act, device=self.dev)
+            self.empty = dict(M=M, xyz=torch.empty(M, 3, **f32), enc=torch.empty(M, 32, dtype=act, device=self.dev),
+                              genc=genc, dirs=dirs, g=g_rows, gen=gen,
+                              bwd=backward_call(self.table.descriptor(M, bound, accumulate=True), genc))
         self.mark_untrained_grid()
 
     # ---------------------------------------------------------------------------- helpers
@@ -429,6 +447,8 @@ class NGPTrainer:
             gs = self.loss_scale.state[0:1].view(torch.float32) if self.loss_scale is not None else None
             L.call("ngp_hashgrid_tv", [self.xyzs, self.latents, gs, self.tv, self.g_lat, self.tv_acc], self._d_tv)
             self.stats[0:1] += self.tv
+        if self.empty is not None:
+            self._empty_space_decay()
         count = self.step_count
         lr = lr_at(cfg.lr, count)
         d_lat = L.NgpAdamDescriptor(self.latents.numel(), count + 1, lr, 0.9, 0.99, 1e-15, 1e-15, 0.0, 1)
@@ -447,6 +467,19 @@ class NGPTrainer:
         self.step_count += 1
         if self.ogrid_due(self.step_count + self.cadence_offset):
             self.update_ogrid()
+
+    def _empty_space_decay(self):
+        """Adds the gradient of empty_space_decay * mean(sigma) over uniform random points of the box
+        to the field's gradients: the encoder forward at the points, the field backward with a
+        density-only upstream gradient (accumulated into dL/dW, under the loss scale when there is
+        one), and the encoder's scatter into the table gradient."""
+        e = self.empty
+        torch.rand(e["xyz"].shape, generator=e["gen"], out=e["xyz"])
+        e["xyz"].mul_(2.0 * self.bound).sub_(self.bound)
+        self._encode(e["xyz"], None, e["enc"], e["M"])
+        self.field.backward(e["enc"], e["dirs"], self.weights, e["g"], None, None, self.mlp_scratch, e["genc"],
+                            self.g_w, accumulate=True, loss_scale=self.loss_scale, n=e["M"])
+        L.call(e["bwd"][0], [e["xyz"], e["genc"], None, self.g_lat], e["bwd"][1])
 
     # -------------------------------------------------------------------------- rendering
     @torch.no_grad()
