@@ -843,9 +843,9 @@ __device__ __forceinline__ void mma_kk_x6(std::uint32_t d, const __nv_bfloat16 *
 }
 
 // D (tmem, M = 64) (+)= A^T @ B over the tile's 128 samples to FP32 accuracy (mma_mn on the six
-// piece products; both operands' pieces kX6Piece elements apart).
+// piece products; A's pieces kX6Piece elements apart, B's b_piece).
 __device__ __forceinline__ void mma_mn_x6(std::uint32_t d, const __nv_bfloat16 *a, const __nv_bfloat16 *b, int N,
-                                          bool acc) {
+                                          bool acc, int b_piece = kX6Piece) {
     const int ap[6] = {2, 1, 0, 1, 0, 0}, bp[6] = {0, 1, 2, 0, 1, 0};
     const std::uint32_t id = tc::idesc_kf16(64, N, Bf16Op::kFmt, true, true), la = 64 * 16, lb = (std::uint32_t)N * 16;
     const tc::SDesc da = tc::sdesc2(smem_addr(a), la, 128), db = tc::sdesc2(smem_addr(b), lb, 128);
@@ -855,7 +855,7 @@ __device__ __forceinline__ void mma_mn_x6(std::uint32_t d, const __nv_bfloat16 *
 #pragma unroll
         for (int j = 0; j < kRows / 16; ++j)
             tc::mma_bf16(d, da, (std::uint32_t)(ap[k] * (kX6Piece / 8)) + j * 2 * la / 16, db,
-                         (std::uint32_t)(bp[k] * (kX6Piece / 8)) + j * 2 * lb / 16, id, acc || k > 0 || j > 0);
+                         (std::uint32_t)(bp[k] * (b_piece / 8)) + j * 2 * lb / 16, id, acc || k > 0 || j > 0);
 }
 
 template <bool kDensity>
@@ -969,7 +969,9 @@ __global__ void __launch_bounds__(kX6Wgs * 128, 1) mlp_x6_forward_kernel(
 // next step's gradient and layer input then overwrite P and Q, whose MMAs have completed.
 constexpr int kB6Threads = 256;
 constexpr int kB6Weights = 3 * kAllW;                                               // pieces kAllW apart
-constexpr std::size_t kB6Smem = (std::size_t)(kB6Weights + 2 * kX6WgAct) * 2;      // 210 KB
+constexpr int kD4Piece = kRows * 16;                                                // one piece of dL/da4 [128][16]
+constexpr std::size_t kB6Smem = (std::size_t)(kB6Weights + 2 * kX6WgAct + 3 * kD4Piece) * 2;   // 222 KB
+static_assert(kB6Smem + 128 <= 232448, "the backward's shared memory fits one CTA per SM");
 // Tensor-memory columns: every layer's result, then the dW accumulators.
 constexpr std::uint32_t kTD = 0;
 constexpr std::uint32_t kTA0 = 64, kTA1 = 96, kTA2 = 112, kTA3 = 144, kTA4 = 208, kTCols = 256;
@@ -1030,7 +1032,9 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
     __shared__ std::uint32_t tbase;
     __shared__ int fail;
     __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
-    __nv_bfloat16 *P = sw + kB6Weights, *Q = P + kX6WgAct;
+    // P, Q: activation rows (three pieces); D4: dL/da4 (three pieces), apart from them so that Q
+    // keeps h2 from the forward until layer 3's weight gradient reads it.
+    __nv_bfloat16 *P = sw + kB6Weights, *Q = P + kX6WgAct, *D4 = Q + kX6WgAct;
     const int r = threadIdx.x % kRows, h = threadIdx.x / kRows;   // h is uniform over a warp
     load_weights_x6b(weights, sw);
     if (threadIdx.x == 0) {
@@ -1099,7 +1103,7 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
     for (std::uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const std::size_t s = (std::size_t)tile * kRows + r;
         const bool valid = s < n_act;
-        float e[16], v[32], h1[32], h2[32], xs[16];
+        float e[16], v[32], h1[32], h2[32], xs[16];   // h2 is dead once stored in Q
 #pragma unroll
         for (int i = 0; i < 16; ++i) e[i] = ne[i];
         const float4 x4 = nx;
@@ -1149,23 +1153,22 @@ __global__ void __launch_bounds__(kB6Threads, 1) mlp_x6_backward_kernel(
                 d[c] = gs * g[c] * rgb * (1.f - rgb);
             }
             dx0 = gs * x4.x * expf(fminf(fmaxf(xs[0], -15.f), 15.f));
-            store_cols3<16, 16>(Q, kX6Piece, r, 0, d);   // Q = dA4
+            store_cols3<16, 16>(D4, kD4Piece, r, 0, d);   // D4 = dA4
         }
         // layer 4: dW4 += h3^T dA4;  dh3 = dA4 W4^T
         sync();
         if (leader) {
-            mma_kk_x6(t0 + kTD, Q, kX6Piece, sw + kG4, 16, 64, kAllW);
+            mma_kk_x6(t0 + kTD, D4, kD4Piece, sw + kG4, 16, 64, kAllW);
             tc::commit(&bar);
         } else if (wleader) {
-            mma_mn_x6(t0 + kTA4, P, Q, 16, !first);
+            mma_mn_x6(t0 + kTA4, P, D4, 16, !first, kD4Piece);
             tc::commit(&wbar);
         }
         wait();
         tc::ld32(tm + kTD + 32 * h, v);
         mask_bits32(v, m3);
         wait_w();
-        store_cols3<64, 32>(P, kX6Piece, r, 32 * h, v);   // P = dA3
-        store_cols3<64, 32>(Q, kX6Piece, r, 32 * h, h2);  // Q = h2
+        store_cols3<64, 32>(P, kX6Piece, r, 32 * h, v);   // P = dA3; Q still holds h2
         // layer 3: dW3^T += dA3^T h2;  dh2 = dA3 W3^T
         sync();
         if (leader) {
