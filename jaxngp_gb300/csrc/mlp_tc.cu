@@ -758,8 +758,8 @@ __global__ void __launch_bounds__(NWG * 128, 1) mlp_tc_backward_kernel(
 // x2); both differences exact in FP32), and each layer accumulates the six products of pieces whose
 // orders add up to at most 4 -- a3 b1, a2 b2, a1 b3, a2 b1, a1 b2, a1 b1, smallest first -- in the
 // FP32 accumulator.  The dropped products and the pieces' remainders are below 2^-24 relative:
-// within FP32 rounding of the exact layer (5e-8 against FP64 in the CPU emulation of this scheme,
-// against 1.4e-7 for the SIMT kernel).  Three warpgroups per CTA, each with one 128-row activation
+// within FP32 rounding of the exact layer (1.3e-7 against FP64 in the CPU restatement of this scheme,
+// about what a plain FP32 evaluation of the field gives).  Three warpgroups per CTA, each with one 128-row activation
 // buffer of three pieces that every layer reads and the next layer's input then overwrites (the
 // layer's MMAs have completed by then); the weights' three pieces stay in shared memory.
 constexpr int kX6Piece = kRows * 64;                     // elements of one piece of an activation tile

@@ -312,3 +312,83 @@ def kink_distance(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray]) -
         a = np.abs(c[k])
         out = np.minimum(out, (a / a.max()).min(axis=1))
     return out
+
+
+# ------------------------------------------------------------------ FP32 accuracy from BF16 pieces
+#
+# Restatement, as a checker, of the operand split the FP32 field kernels use on the tensor cores
+# (jaxngp_gb300/csrc/mlp_tc.cu: split3, mma_kk_x6, mma_mn_x6): every matmul operand x becomes BF16
+# pieces x1 = bf16(x), x2 = bf16(x - x1), x3 = bf16(x - x1 - x2), the differences taken in float32
+# (exact there), and a matmul sums a chosen set of piece products.  Products are summed exactly
+# (float64) and the result rounded once to float32, so these functions measure the error of the
+# split itself, without the FP32 accumulator's own rounding.  No counterpart in the reference,
+# whose MLP runs in FP32 (models/nerfs.py:39-128).
+
+SPLIT_SCHEMES = {
+    # name: (pieces per operand, (i, j) piece products, smallest first)
+    "x6": (3, ((2, 0), (1, 1), (0, 2), (1, 0), (0, 1), (0, 0))),   # the kernels' scheme
+    "x4": (2, ((1, 1), (1, 0), (0, 1), (0, 0))),
+    "x3": (2, ((1, 0), (0, 1), (0, 0))),
+}
+
+
+def split_bf16(x, pieces: int = 3):
+    """The BF16 pieces of float32 `x` (as float64 arrays), first piece first."""
+    r = np.asarray(x, np.float32)
+    out = []
+    for _ in range(pieces):
+        p = round_bf16(r)
+        out.append(p.astype(np.float64))
+        r = (r - p).astype(np.float32)
+    return out
+
+
+def matmul_split(A, B, scheme: str = "x6") -> np.ndarray:
+    """A @ B from the scheme's products of BF16 pieces, summed exactly, rounded to float32."""
+    n, prods = SPLIT_SCHEMES[scheme]
+    a, b = split_bf16(A, n), split_bf16(B, n)
+    return sum(a[i] @ b[j] for i, j in prods).astype(np.float32)
+
+
+def forward_split(enc: np.ndarray, dirs: np.ndarray, w: Dict[str, np.ndarray], scheme: str = "x6"):
+    """forward() with every matmul in split form and float32 in between (as the kernel: FP32
+    layer outputs, ReLU, exp and sigmoid in float32).  Returns (drgb [S,4], cache)."""
+    mm = lambda a, b: matmul_split(a, b, scheme)
+    w = {k: np.asarray(v, np.float32) for k, v in w.items()}
+    enc = np.asarray(enc, np.float32)
+    a1 = mm(enc, w["W0"])
+    h1 = np.maximum(a1, 0)
+    x = mm(h1, w["W1"])
+    sigma = np.exp(x[:, :1])
+    c = np.concatenate([x, sh4(np.asarray(dirs, np.float32))], axis=-1)
+    a2 = mm(c, w["W2"])
+    h2 = np.maximum(a2, 0)
+    a3 = mm(h2, w["W3"])
+    h3 = np.maximum(a3, 0)
+    a4 = mm(h3, w["W4"])
+    rgb = (1 / (1 + np.exp(-a4))).astype(np.float32)
+    drgb = np.concatenate([sigma, rgb], axis=-1).astype(np.float32)
+    return drgb, dict(enc=enc, a1=a1, h1=h1, x=x, c=c, a2=a2, h2=h2, a3=a3, h3=h3, rgb=rgb)
+
+
+def backward_split(dL_ddrgb: np.ndarray, cache, w: Dict[str, np.ndarray], scheme: str = "x6"):
+    """backward() with every matmul (data and weight gradients) in split form, float32 in between;
+    `cache` from forward_split.  Returns (dL_denc [S,32], dict of dL_dW)."""
+    mm = lambda a, b: matmul_split(a, b, scheme)
+    w = {k: np.asarray(v, np.float32) for k, v in w.items()}
+    c = cache
+    g = np.asarray(dL_ddrgb, np.float32)
+    dx0 = (g[:, 0] * np.exp(np.clip(c["x"][:, 0], -15, 15))).astype(np.float32)
+    rgb = c["rgb"]
+    da4 = (g[:, 1:] * rgb * (1 - rgb)).astype(np.float32)
+    grads = {"W4": mm(c["h3"].T, da4)}
+    da3 = mm(da4, w["W4"].T) * (c["a3"] > 0)
+    grads["W3"] = mm(c["h2"].T, da3)
+    da2 = mm(da3, w["W3"].T) * (c["a2"] > 0)
+    grads["W2"] = mm(c["c"].T, da2)
+    dx = mm(da2, w["W2"][:16].T)
+    dx[:, 0] += dx0
+    grads["W1"] = mm(c["h1"].T, dx)
+    da1 = mm(dx, w["W1"].T) * (c["a1"] > 0)
+    grads["W0"] = mm(c["enc"].T, da1)
+    return mm(da1, w["W0"].T), grads
