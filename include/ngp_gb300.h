@@ -369,9 +369,10 @@ size_t ngp_field_backward_scratch_floats(void);
  * memory: an XLA custom call bound through the legacy signature receives only its operand and
  * result buffers, and an embedder running inside a fixed, pre-reserved memory budget may not call
  * cudaMalloc or any allocating library routine.  The per-CTA dL/dW partials live in a static
- * array inside the library (9.6 MB, held by every GPU that loads the library until exit) instead
- * of a caller-provided scratch buffer, so the batch is bounded by
- * NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES; larger batches return NGP_ERR_CAPACITY.  The first call
+ * array inside the library (9.6 MB, room for the partials of 256 CTAs whatever the batch, held by
+ * every GPU that loads the library until exit) instead of a caller-provided scratch buffer.  A call
+ * takes at most NGP_FIELD_BACKWARD_NOALLOC_MAX_SAMPLES samples, a published bound of this entry
+ * point; larger batches return NGP_ERR_CAPACITY.  The first call
  * on each device looks up the array's device address (cudaGetSymbolAddress); make that first call
  * before any stream capture.  All calls share the array: calls that overlap on the GPU (different
  * streams) race on it and must be ordered by the caller.  Nothing has to be cleared between calls.
