@@ -959,14 +959,15 @@ __global__ void __launch_bounds__(kX6Wgs * 128, 1) mlp_x6_forward_kernel(
 // ngp_field_backward with the same three-piece BF16 products as the forward above.  A CTA (one per
 // SM) works on one tile of 128 samples at a time with 256 threads, two per sample row: thread
 // (r, h) owns columns [w h, w (h + 1)) of a layer of width 2w.  The recomputed forward leaves each
-// thread's share of the layer inputs the backward needs again in registers (h1 and h2 values, x or
-// the SH features, the encodings, and the relu decisions of h1, h2, h3 as bit masks), so tensor
-// memory holds only the current layer's result and the dW accumulators, and shared memory only the
-// operands of the layer at hand: two three-piece buffers P and Q, 48 KB each, beside the weights'
-// three pieces in both layouts (W^T for the forward, W for the data gradients).  Each adjoint step
-// issues the weight-gradient MMA (M = 64, the tile's samples as the contraction, accumulated in
-// tensor memory across all tiles of the CTA) and the data-gradient MMA on the same operands; the
-// next step's gradient and layer input then overwrite P and Q, whose MMAs have completed.
+// thread's share of the layer inputs the backward needs again in registers (h1 values, x or the
+// SH features, the encodings, and the relu decisions of h1, h2, h3 as bit masks; h2 stays in Q), so
+// tensor memory holds only the current layer's result and the dW accumulators, and shared memory
+// only the operands of the layer at hand: two three-piece buffers P and Q, 48 KB each, and dL/da4
+// (D4, 12 KB), beside the weights' three pieces in both layouts (W^T for the forward, W for the
+// data gradients).  Each adjoint step issues the data-gradient MMA (thread 0) and the
+// weight-gradient MMA (thread 32; M = 64, the tile's samples as the contraction, accumulated in
+// tensor memory across all tiles of the CTA) on the same operands; the next step's gradient and
+// layer input then overwrite P and Q once both have completed.
 constexpr int kB6Threads = 256;
 constexpr int kB6Weights = 3 * kAllW;                                               // pieces kAllW apart
 constexpr int kD4Piece = kRows * 16;                                                // one piece of dL/da4 [128][16]
