@@ -67,6 +67,19 @@ SCENES = {"blobs64": (64, 0, 100, 800, 1 << 18, WORKLOAD, METRIC),
                       "train rays/s (plain FP32 hash-grid NeRF step, 512 blobs + 8 shells, 2^20 samples)")}
 
 
+def guarded(fn, *a, **kw):
+    """Runs a secondary measurement block (the forms after the headline's, the equal-PSNR run, the
+    encoder and config-4 blocks, the reference's kernels, the CPU baseline).  A failure there is
+    reported in the JSON line (and its traceback on stderr) instead of ending the run, so the
+    headline measurement taken before it is still printed."""
+    try:
+        return fn(*a, **kw)
+    except Exception as e:
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(e).__name__}: {e}"[:500]}
+
+
 def empty_space_decay(args, sampler: str) -> float:
     """The learned-proposal forms' empty-space density term (TrainConfig.empty_space_decay)."""
     return float(args.empty_space_decay) if sampler == "proposal" else 0.0
@@ -976,13 +989,20 @@ def main():
     for i, f in enumerate(forms):
         cb = None
         if i == 0 and args.scene == "blobs64" and not args.no_kernels_vs_reference:
-            cb = lambda tr: extra.__setitem__("kernels_vs_reference", kernels_vs_reference(tr))
-        results[f] = run_ours(args, data, f, with_render=True, on_trainer=cb)
+            cb = lambda tr: extra.__setitem__("kernels_vs_reference", guarded(kernels_vs_reference, tr))
+        if i == 0:   # the headline form: a failure ends the run
+            results[f] = run_ours(args, data, f, with_render=True, on_trainer=cb)
+            continue
+        r = guarded(run_ours, args, data, f, with_render=True, on_trainer=cb)
+        if "error" in r and "value" not in r:
+            extra.setdefault("form_errors", {})[f] = r["error"]
+        else:
+            results[f] = r
     head = results[forms[0]]
     out = dict(head)
     out.update(extra)
     out["config"] = dict(head["config"])
-    if len(forms) > 1:
+    if len(results) > 1:
         out["forms"] = {f: {k: r[k] for k in ("value", "ms_per_step", "dtype", "e2e", "gpu_launches", "quality",
                                                "roofline", "clocks") if k in r} | {"proposal": r.get("proposal")} | {
                             "batch": r["batch"],
@@ -1026,21 +1046,21 @@ def main():
                 ok = [f for f in allcmp if allcmp[f]["delta_psnr_db"] >= -0.5]
                 if ok and args.equal_psnr_steps > 0:
                     fastest = max(ok, key=lambda f: results[f]["value"])
-                    out["forms_vs_plain"]["at_equal_psnr"] = equal_psnr(args, data, "fp32-march", fastest)
+                    out["forms_vs_plain"]["at_equal_psnr"] = guarded(equal_psnr, args, data, "fp32-march", fastest)
     if rank == 0 and not args.no_encoder_block:
-        out["config0_encoder"] = encoder_block(args, cores)
+        out["config0_encoder"] = guarded(encoder_block, args, cores)
     if args.scene == "blobs64" and args.config4_steps > 0:
         del data
         import torch
         torch.cuda.empty_cache()
-        out["config4_learned_proposal"] = config4_block(args, cores)
+        out["config4_learned_proposal"] = guarded(config4_block, args, cores)
     if rank == 0:
         if not args.no_cpu_baseline:
             from jaxngp_gb300.scene import BlobScene, PinholeCamera, hemisphere_poses, poses_to_transforms
             blob = BlobScene.random(args.n_blobs, args.n_shells, 0)
             cam = PinholeCamera.from_fov(args.res, args.res, 40.0)
             transforms = poses_to_transforms(hemisphere_poses(args.views, 4.0, np.random.default_rng(1)))
-            out["cpu_baseline"] = cpu_baseline(args, (blob.blobs, cam, transforms, 1.0), cores)
+            out["cpu_baseline"] = guarded(cpu_baseline, args, (blob.blobs, cam, transforms, 1.0), cores)
         print(json.dumps(out))
     return 0
 
