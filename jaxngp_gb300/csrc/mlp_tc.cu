@@ -1387,8 +1387,8 @@ namespace {
 
 // Tensor map of 16-bit encodings enc [n][32] (n a multiple of 8) as the 4-D view [n/8][4][8][8]
 // (row group, column chunk, row, column; byte strides 512, 16, 64) with a box of one 128-row tile:
-// the box lands in shared memory in the MMA operand's core-matrix layout.  False when the driver
-// entry point is unavailable or n does not qualify (the caller then loads the rows itself).
+// the box lands in shared memory in the MMA operand's core-matrix layout.  False when the CUDA
+// driver entry point is unavailable or n does not qualify (the caller then loads the rows itself).
 template <class E>
 int encode_enc_map(CUtensorMap *map, const void *enc, std::uint32_t n, bool *ok) {
     *ok = false;

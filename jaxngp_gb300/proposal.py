@@ -14,8 +14,8 @@ Per training step:
 Every k-th training step (TrainConfig.march_every, 8 by default) marches the occupancy grid instead
 -- the sampler's fallback for whole steps: its evenly spread samples train the field's empty
 space, which the proposal's concentrated samples rarely visit, and teach the proposal where its
-density is wrong.  Without it the field keeps density the occupancy-grid renderer (the judge) then
-shows.  Per ray (TrainConfig.proposal_fallback), rays on which the proposal misses more than 1% of
+density is wrong.  Without it the field keeps density that the occupancy-grid renderer, against
+which the proposal's PSNR is measured, then shows.  Per ray (TrainConfig.proposal_fallback), rays on which the proposal misses more than 1% of
 the transmittance the occupancy grid implies are marched within the step (sample()).
 
 Everything stays on the device; the sample count of a step is read by the kernels from `counts`.
